@@ -1,0 +1,114 @@
+// Shared helpers for the fegb CUDA library: status/last-error handling,
+// launch geometry, stream-ordered scratch allocation and small device utilities.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+namespace fegb {
+
+// ---------------------------------------------------------------------------
+// Status and last-error text (one buffer per host thread, like the reference
+// runtime's thread_local message at src/gpu/fe_gpu_runtime.cu:26).
+// ---------------------------------------------------------------------------
+int set_ok();
+int set_error(const char* fmt, ...);
+int set_cuda_error(cudaError_t err, const char* context);
+const char* last_error();
+
+#define FEGB_TRY(expr)              \
+    do {                            \
+        int _st = (expr);           \
+        if (_st != 0) return _st;   \
+    } while (0)
+
+#define FEGB_CUDA(call, ctx)                                                   \
+    do {                                                                       \
+        cudaError_t _e = (call);                                               \
+        if (_e != cudaSuccess) return ::fegb::set_cuda_error(_e, (ctx));       \
+    } while (0)
+
+#define FEGB_LAUNCH_CHECK(ctx) FEGB_CUDA(cudaPeekAtLastError(), (ctx))
+
+int num_sms();
+
+inline unsigned grid_1d(long long n, int threads, long long max_blocks = 1LL << 30) {
+    long long b = (n + threads - 1) / threads;
+    if (b < 1) b = 1;
+    if (b > max_blocks) b = max_blocks;
+    return (unsigned)b;
+}
+
+// Grid-stride launch size: a few waves of resident blocks.
+inline unsigned grid_stride_blocks(long long n, int threads) {
+    long long want = (n + threads - 1) / threads;
+    long long cap = (long long)num_sms() * 8;
+    if (want < 1) want = 1;
+    return (unsigned)(want < cap ? want : cap);
+}
+
+// ---------------------------------------------------------------------------
+// Stream-ordered scratch: a list of cudaMallocAsync blocks freed together.
+// ---------------------------------------------------------------------------
+class Scratch {
+  public:
+    explicit Scratch(cudaStream_t s) : stream_(s) {}
+    ~Scratch() { release(); }
+    Scratch(const Scratch&) = delete;
+    Scratch& operator=(const Scratch&) = delete;
+
+    template <typename T>
+    int alloc(T** out, size_t count, const char* what) {
+        void* p = nullptr;
+        size_t bytes = count * sizeof(T);
+        if (bytes == 0) bytes = 16;
+        bytes = (bytes + 255) & ~size_t(255);
+        cudaError_t e = cudaMallocAsync(&p, bytes, stream_);
+        if (e != cudaSuccess) {
+            *out = nullptr;
+            return set_cuda_error(e, what);
+        }
+        ptrs_.push_back(p);
+        *out = static_cast<T*>(p);
+        return 0;
+    }
+    void release() {
+        for (void* p : ptrs_) cudaFreeAsync(p, stream_);
+        ptrs_.clear();
+    }
+    cudaStream_t stream() const { return stream_; }
+
+  private:
+    cudaStream_t stream_;
+    std::vector<void*> ptrs_;
+};
+
+// Keep the default memory pool's freed blocks cached across calls.
+void configure_mem_pool();
+
+// ---------------------------------------------------------------------------
+// Device helpers
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ unsigned long long dbl_bits(double v) {
+    return (unsigned long long)__double_as_longlong(v);
+}
+__device__ __forceinline__ double bits_dbl(unsigned long long b) { return __longlong_as_double((long long)b); }
+
+// atomicMax on a non-negative double stored as its bit pattern (the order of
+// the bit patterns of non-negative doubles is the numeric order). Max is order
+// independent, so the result is deterministic.
+__device__ __forceinline__ void atomic_max_nonneg(unsigned long long* slot, double v) {
+    atomicMax(slot, dbl_bits(v));
+}
+
+__device__ __forceinline__ double warp_max(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+
+}  // namespace fegb

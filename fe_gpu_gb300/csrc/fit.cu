@@ -1,0 +1,1431 @@
+// Whole-fit estimator: device preparation, within-transform (plain FP64 and
+// FP32-correction refinement), normal equations / 2SLS, clustered SEs.
+//
+// Host-side control mirrors the reference estimation driver
+// (src/core/fe_pipeline.f90:516-1896) and within-transform
+// (src/gpu/fe_gpu_demean.f90:63-311); all per-row work runs in this library's
+// kernels on one stream.
+#include "fegb.h"
+#include "common.cuh"
+#include "linalg.cuh"
+#include "prep.cuh"
+#include "sweep.cuh"
+
+#include <algorithm>
+#include <cfloat>
+#include <chrono>
+#include <climits>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+namespace fegb {
+
+namespace {
+
+using Clock = std::chrono::steady_clock;
+inline double seconds_since(Clock::time_point t0) {
+    return std::chrono::duration<double>(Clock::now() - t0).count();
+}
+
+constexpr int MODE_CONTIG = 0;
+constexpr int MODE_GATHER = 1;
+constexpr int MODE_SMALLG = 2;
+constexpr int CHUNK_R = 256;
+constexpr int MAX_CLUSTER_DIMS = 3;  // src/core/fe_pipeline.f90:20
+
+struct Dim {
+    int G = 0;
+    int mode = MODE_GATHER;
+    int32_t* gid = nullptr;   // storage order, 0-based
+    int32_t* perm = nullptr;  // traversal position -> storage row (gather mode)
+    int32_t* gseq = nullptr;  // group id at traversal position (contig: = gid)
+    int32_t* off = nullptr;   // G + 1 (contig / gather)
+    int32_t* counts = nullptr;
+    std::vector<int32_t*> gid_at_perm;  // [e] gid of dim e at traversal positions (gather)
+    double* prev = nullptr;
+    double* pend64 = nullptr;
+    float* pend32 = nullptr;
+    double* alpha = nullptr;
+    double* mu = nullptr;
+};
+
+struct Problem {
+    cudaStream_t s = nullptr;
+    Scratch* scr = nullptr;
+    long long n = 0;
+    int k = 0, l = 0, C = 0, n_fe = 0;
+    double* X = nullptr;  // n x C FP64, storage order
+    float* Xc = nullptr;  // n x C FP32 correction (mixed form)
+    int32_t* row_of = nullptr;
+    int primary = -1;
+    std::vector<Dim> dims;
+    std::vector<int> order;
+    double* relax = nullptr;
+    double* prev_change = nullptr;
+    unsigned long long* change_bits = nullptr;  // n_fe
+    unsigned long long* max_bits = nullptr;     // [0] iteration max, [1] mu max
+    unsigned* done = nullptr;
+    double* sums = nullptr;
+    double* head = nullptr;
+    double* tail = nullptr;
+    double* partials = nullptr;
+    int smallg_nb = 0;
+    int projections = 0;
+    double demean_bytes = 0.0;
+};
+
+// ----------------------------- small kernels ------------------------------
+
+__global__ void build_x_kernel(const double* __restrict__ y, const double* __restrict__ W,
+                               const double* __restrict__ Z, int k, int l, long long ld, const int32_t* __restrict__ row_of,
+                               long long n, int C, int TR, double* __restrict__ X) {
+    extern __shared__ double tile[];
+    const long long r0 = (long long)blockIdx.x * TR;
+    const int rows = (int)min((long long)TR, n - r0);
+    for (int e = threadIdx.x; e < rows * C; e += blockDim.x) {
+        int r = e % rows, c = e / rows;
+        long long src_row = row_of ? (long long)row_of[r0 + r] : r0 + r;
+        double v;
+        if (c == 0)
+            v = y[src_row];
+        else if (c <= k)
+            v = W[(long long)(c - 1) * ld + src_row];
+        else
+            v = Z[(long long)(c - 1 - k) * ld + src_row];
+        tile[r * C + c] = v;
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < rows * C; e += blockDim.x) X[r0 * C + e] = tile[e];
+}
+
+__global__ void scatter_x_kernel(const double* __restrict__ X, const int32_t* __restrict__ row_of, long long n, int C,
+                                 int k, int l, long long ld, int TR, double* __restrict__ y, double* __restrict__ W,
+                                 double* __restrict__ Z) {
+    extern __shared__ double tile[];
+    const long long r0 = (long long)blockIdx.x * TR;
+    const int rows = (int)min((long long)TR, n - r0);
+    for (int e = threadIdx.x; e < rows * C; e += blockDim.x) tile[e] = X[r0 * C + e];
+    __syncthreads();
+    for (int e = threadIdx.x; e < rows * C; e += blockDim.x) {
+        int r = e % rows, c = e / rows;
+        long long dst = row_of ? (long long)row_of[r0 + r] : r0 + r;
+        double v = tile[r * C + c];
+        if (c == 0)
+            y[dst] = v;
+        else if (c <= k)
+            W[(long long)(c - 1) * ld + dst] = v;
+        else
+            Z[(long long)(c - 1 - k) * ld + dst] = v;
+    }
+}
+
+__global__ void gather_gid_kernel(const int32_t* __restrict__ ids, const int32_t* __restrict__ rows, long long n,
+                                  int32_t* __restrict__ out) {
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long st = (long long)gridDim.x * blockDim.x;
+    for (; i < n; i += st) out[i] = ids[rows ? rows[i] : i] - 1;
+}
+
+__global__ void gather_keys_kernel(const int32_t* __restrict__ ids, const int32_t* __restrict__ rows, long long n,
+                                   uint32_t* __restrict__ keys, int32_t* __restrict__ vals) {
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long st = (long long)gridDim.x * blockDim.x;
+    for (; i < n; i += st) {
+        long long r = rows ? rows[i] : i;
+        keys[i] = (uint32_t)(ids[r] - 1);
+        vals[i] = (int32_t)r;
+    }
+}
+
+__global__ void gather_i32_kernel(const int32_t* __restrict__ src, const int32_t* __restrict__ idx, long long n,
+                                  int32_t* __restrict__ out) {
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long st = (long long)gridDim.x * blockDim.x;
+    for (; i < n; i += st) out[i] = src[idx[i]];
+}
+
+__global__ void counts_from_offsets_kernel(const int32_t* __restrict__ off, int G, int32_t* __restrict__ counts) {
+    int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g < G) counts[g] = off[g + 1] - off[g];
+}
+
+__global__ void count_ids_kernel(const int32_t* __restrict__ gid, long long n, int32_t* __restrict__ counts) {
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long st = (long long)gridDim.x * blockDim.x;
+    for (; i < n; i += st) atomicAdd(&counts[gid[i]], 1);
+}
+
+__global__ void reset_relax_kernel(double* relax, double* prev_change, unsigned long long* change_bits, unsigned* done,
+                                   int n) {
+    int d = threadIdx.x;
+    if (d < n) {
+        relax[d] = 1.5;
+        prev_change[d] = DBL_MAX;
+        change_bits[d] = 0ull;
+        done[d] = 0u;
+    }
+}
+
+__global__ void keep_flags_kernel(const uint8_t* __restrict__ keep, long long n, uint32_t* __restrict__ flags) {
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long st = (long long)gridDim.x * blockDim.x;
+    for (; i < n; i += st) flags[i] = keep[i] ? 1u : 0u;
+}
+
+__global__ void compact_rows_kernel(const uint8_t* __restrict__ keep, const uint32_t* __restrict__ excl, long long n,
+                                    int32_t* __restrict__ rows) {
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long st = (long long)gridDim.x * blockDim.x;
+    for (; i < n; i += st)
+        if (keep[i]) rows[excl[i]] = (int32_t)i;
+}
+
+__global__ void deinterleave_ids_kernel(const int32_t* __restrict__ ids, int n_fe, long long n, int32_t* __restrict__ out) {
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long st = (long long)gridDim.x * blockDim.x;
+    for (; i < n * n_fe; i += st) {
+        long long row = i / n_fe;
+        int d = (int)(i - row * n_fe);
+        out[(long long)d * n + row] = ids[i];
+    }
+}
+
+// ------------------------------ helpers -----------------------------------
+
+template <typename T>
+int dalloc(Scratch& scr, T** p, size_t count, const char* what) {
+    return scr.alloc(p, count, what);
+}
+
+int d2h_sync(void* dst, const void* src, size_t bytes, cudaStream_t s, const char* what) {
+    FEGB_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, s), what);
+    FEGB_CUDA(cudaStreamSynchronize(s), what);
+    return 0;
+}
+
+int h2d_sync(void* dst, const void* src, size_t bytes, cudaStream_t s, const char* what) {
+    FEGB_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, s), what);
+    FEGB_CUDA(cudaStreamSynchronize(s), what);
+    return 0;
+}
+
+double bits_to_double(unsigned long long b) {
+    double v;
+    std::memcpy(&v, &b, sizeof(v));
+    return v;
+}
+
+// ---------------------------- preparation ---------------------------------
+
+// Builds the storage-order problem from device inputs in the reference layout.
+int build_problem(Problem& P, long long n_in, int k, int l, int n_fe, const double* y, const double* W, const double* Z,
+                  const int32_t* const* ids, const int* G_in, bool drop_singletons, bool mixed, long long* n_single) {
+    cudaStream_t s = P.s;
+    Scratch& scr = *P.scr;
+    P.k = k;
+    P.l = l;
+    P.C = 1 + k + l;
+    P.n_fe = n_fe;
+    if (n_fe > SWEEP_MAXP) return set_error("at most %d FE dimensions are supported (got %d)", SWEEP_MAXP, n_fe);
+    *n_single = 0;
+    std::vector<int> G(n_fe, 0);
+    for (int d = 0; d < n_fe; ++d) {
+        int mn = 0, mx = 0;
+        FEGB_TRY(ids_min_max(ids[d], n_in, &mn, &mx, s, scr));
+        if (n_in > 0 && mn < 1)
+            return set_error("FE indices must be positive and contiguous (dimension %d)", d + 1);
+        G[d] = n_in > 0 ? mx : 0;
+        if (G_in && G_in[d] > 0) {
+            if (G_in[d] < G[d]) return set_error("group size %d below max id %d (dimension %d)", G_in[d], G[d], d + 1);
+            G[d] = G_in[d];
+        }
+    }
+    // rows kept (singleton removal) in original order
+    const int32_t* rows = nullptr;
+    long long n = n_in;
+    if (drop_singletons && n_fe > 0 && n_in > 0) {
+        std::vector<int32_t*> g0(n_fe);
+        for (int d = 0; d < n_fe; ++d) {
+            FEGB_TRY(dalloc(scr, &g0[d], (size_t)n_in, "singleton gid"));
+            gather_gid_kernel<<<grid_stride_blocks(n_in, 256), 256, 0, s>>>(ids[d], nullptr, n_in, g0[d]);
+            FEGB_LAUNCH_CHECK("singleton gid");
+        }
+        uint8_t* keep = nullptr;
+        FEGB_TRY(dalloc(scr, &keep, (size_t)n_in, "keep mask"));
+        long long dropped = 0;
+        FEGB_TRY(fegb::drop_singletons(g0.data(), G.data(), n_fe, n_in, keep, &dropped, s, scr));
+        *n_single = dropped;
+        if (dropped > 0) {
+            uint32_t *flags = nullptr, *excl = nullptr;
+            int32_t* kept = nullptr;
+            FEGB_TRY(dalloc(scr, &flags, (size_t)n_in, "keep flags"));
+            FEGB_TRY(dalloc(scr, &excl, (size_t)n_in, "keep scan"));
+            FEGB_TRY(dalloc(scr, &kept, (size_t)n_in, "kept rows"));
+            keep_flags_kernel<<<grid_stride_blocks(n_in, 256), 256, 0, s>>>(keep, n_in, flags);
+            FEGB_TRY(scan_exclusive_u32(flags, excl, n_in, nullptr, s, scr));
+            compact_rows_kernel<<<grid_stride_blocks(n_in, 256), 256, 0, s>>>(keep, excl, n_in, kept);
+            FEGB_LAUNCH_CHECK("compact rows");
+            rows = kept;
+            n = n_in - dropped;
+        }
+    }
+    P.n = n;
+    const int C = P.C;
+    // primary dimension: the one with most groups (first on ties)
+    P.primary = -1;
+    for (int d = 0; d < n_fe; ++d)
+        if (P.primary < 0 || G[d] > G[P.primary]) P.primary = d;
+    P.dims.assign(n_fe, Dim());
+    for (int d = 0; d < n_fe; ++d) P.dims[d].G = G[d];
+    // storage order: stable sort by the primary id
+    int32_t* row_of = nullptr;
+    if (P.primary >= 0 && n > 0) {
+        uint32_t *keys = nullptr, *sorted = nullptr;
+        int32_t* vals = nullptr;
+        FEGB_TRY(dalloc(scr, &keys, (size_t)n, "primary keys"));
+        FEGB_TRY(dalloc(scr, &vals, (size_t)n, "primary rows"));
+        FEGB_TRY(dalloc(scr, &sorted, (size_t)n, "primary sorted"));
+        FEGB_TRY(dalloc(scr, &row_of, (size_t)n, "row_of"));
+        gather_keys_kernel<<<grid_stride_blocks(n, 256), 256, 0, s>>>(ids[P.primary], rows, n, keys, vals);
+        FEGB_LAUNCH_CHECK("primary keys");
+        FEGB_TRY(radix_sort_u32(keys, vals, sorted, row_of, n, bits_for((unsigned long long)G[P.primary]), s, scr));
+        P.dims[P.primary].gid = reinterpret_cast<int32_t*>(sorted);
+    } else if (rows) {
+        row_of = const_cast<int32_t*>(rows);
+    }
+    P.row_of = row_of;
+    // AoS data block
+    FEGB_TRY(dalloc(scr, &P.X, (size_t)n * C, "data block"));
+    if (n > 0) {
+        int TR = std::max(1, std::min(64, 24576 / (8 * C)));
+        size_t smem = sizeof(double) * (size_t)TR * C;
+        build_x_kernel<<<(unsigned)((n + TR - 1) / TR), 256, smem, s>>>(y, W, Z, k, l, n_in, row_of, n, C, TR, P.X);
+        FEGB_LAUNCH_CHECK("build data block");
+    }
+    if (mixed) FEGB_TRY(dalloc(scr, &P.Xc, (size_t)n * C, "correction block"));
+    // per-dimension structures
+    int gmax = 1, gmax_small = 0;
+    for (int d = 0; d < n_fe; ++d) {
+        Dim& D = P.dims[d];
+        if (d != P.primary) {
+            FEGB_TRY(dalloc(scr, &D.gid, (size_t)n, "gid"));
+            if (n > 0) {
+                gather_gid_kernel<<<grid_stride_blocks(n, 256), 256, 0, s>>>(ids[d], row_of, n, D.gid);
+                FEGB_LAUNCH_CHECK("gid gather");
+            }
+        }
+        FEGB_TRY(dalloc(scr, &D.counts, (size_t)std::max(1, D.G), "counts"));
+        if (d == P.primary) {
+            D.mode = MODE_CONTIG;
+            D.gseq = D.gid;
+        } else if (smallg_eligible(D.G, C)) {
+            D.mode = MODE_SMALLG;
+        } else {
+            D.mode = MODE_GATHER;
+        }
+        if (D.mode == MODE_GATHER && n > 0) {
+            uint32_t* sorted = nullptr;
+            FEGB_TRY(dalloc(scr, &sorted, (size_t)n, "gather gseq"));
+            FEGB_TRY(dalloc(scr, &D.perm, (size_t)n, "gather perm"));
+            FEGB_TRY(radix_sort_u32(reinterpret_cast<const uint32_t*>(D.gid), nullptr, sorted, D.perm, n,
+                                    bits_for((unsigned long long)D.G), s, scr));
+            D.gseq = reinterpret_cast<int32_t*>(sorted);
+        }
+        if (D.mode != MODE_SMALLG) {
+            FEGB_TRY(dalloc(scr, &D.off, (size_t)D.G + 1, "offsets"));
+            if (n > 0) {
+                FEGB_TRY(segment_offsets(reinterpret_cast<const uint32_t*>(D.gseq), n, D.G, D.off, s));
+            } else {
+                FEGB_CUDA(cudaMemsetAsync(D.off, 0, sizeof(int32_t) * ((size_t)D.G + 1), s), "offsets zero");
+            }
+            if (D.G > 0) {
+                counts_from_offsets_kernel<<<(D.G + 255) / 256, 256, 0, s>>>(D.off, D.G, D.counts);
+                FEGB_LAUNCH_CHECK("counts");
+            }
+        } else {
+            FEGB_CUDA(cudaMemsetAsync(D.counts, 0, sizeof(int32_t) * (size_t)D.G, s), "counts zero");
+            if (n > 0) {
+                count_ids_kernel<<<grid_stride_blocks(n, 256), 256, 0, s>>>(D.gid, n, D.counts);
+                FEGB_LAUNCH_CHECK("count ids");
+            }
+            gmax_small = std::max(gmax_small, D.G);
+        }
+        gmax = std::max(gmax, D.G);
+        size_t gc = (size_t)std::max(1, D.G) * C;
+        FEGB_TRY(dalloc(scr, &D.prev, gc, "prev means"));
+        FEGB_TRY(dalloc(scr, &D.pend64, gc, "pending means"));
+        if (mixed) {
+            FEGB_TRY(dalloc(scr, &D.pend32, gc, "pending means fp32"));
+            FEGB_TRY(dalloc(scr, &D.alpha, gc, "fe increments"));
+            FEGB_TRY(dalloc(scr, &D.mu, gc, "fp64 group means"));
+        }
+    }
+    for (int d = 0; d < n_fe; ++d) {
+        Dim& D = P.dims[d];
+        D.gid_at_perm.assign(n_fe, nullptr);
+        if (D.mode != MODE_GATHER || n == 0) continue;
+        for (int e = 0; e < n_fe; ++e) {
+            if (e == d) continue;
+            FEGB_TRY(dalloc(scr, &D.gid_at_perm[e], (size_t)n, "gid at perm"));
+            gather_i32_kernel<<<grid_stride_blocks(n, 256), 256, 0, s>>>(P.dims[e].gid, D.perm, n, D.gid_at_perm[e]);
+            FEGB_LAUNCH_CHECK("gid at perm");
+        }
+    }
+    long long nchunks = std::max(1LL, seg_nchunks(n, CHUNK_R));
+    FEGB_TRY(dalloc(scr, &P.sums, (size_t)gmax * C, "group sums"));
+    FEGB_TRY(dalloc(scr, &P.head, (size_t)nchunks * C, "chunk heads"));
+    FEGB_TRY(dalloc(scr, &P.tail, (size_t)nchunks * C, "chunk tails"));
+    P.smallg_nb = smallg_nblocks(std::max(1LL, n));
+    if (gmax_small > 0) FEGB_TRY(dalloc(scr, &P.partials, (size_t)P.smallg_nb * gmax_small * C, "small-G partials"));
+    FEGB_TRY(dalloc(scr, &P.relax, (size_t)std::max(1, n_fe), "relaxation"));
+    FEGB_TRY(dalloc(scr, &P.prev_change, (size_t)std::max(1, n_fe), "prev change"));
+    FEGB_TRY(dalloc(scr, &P.change_bits, (size_t)std::max(1, n_fe), "change"));
+    FEGB_TRY(dalloc(scr, &P.max_bits, 2, "max update"));
+    FEGB_TRY(dalloc(scr, &P.done, (size_t)std::max(1, n_fe), "done counters"));
+    // sweep order: ascending group count, exchange sort of fe_gpu_demean.f90:104-114
+    P.order.resize(n_fe);
+    for (int d = 0; d < n_fe; ++d) P.order[d] = d;
+    for (int a = 0; a < n_fe - 1; ++a)
+        for (int b = a + 1; b < n_fe; ++b)
+            if (G[P.order[b]] < G[P.order[a]]) std::swap(P.order[a], P.order[b]);
+    return 0;
+}
+
+// ------------------------------- sweeps -----------------------------------
+
+struct PendingList {
+    std::vector<int> dims;
+    bool has(int d) const { return std::find(dims.begin(), dims.end(), d) != dims.end(); }
+};
+
+template <typename T>
+const T* pend_table(const Dim& D);
+template <>
+const double* pend_table<double>(const Dim& D) {
+    return D.pend64;
+}
+template <>
+const float* pend_table<float>(const Dim& D) {
+    return D.pend32;
+}
+
+template <typename T>
+PendingSet<T> make_pending(const Problem& P, int d, const PendingList& pl) {
+    PendingSet<T> ps{};
+    ps.n = 0;
+    const Dim& D = P.dims[d];
+    for (int e : pl.dims) {
+        const int32_t* g;
+        if (D.mode == MODE_GATHER)
+            g = (e == d) ? D.gseq : D.gid_at_perm[e];
+        else
+            g = P.dims[e].gid;
+        ps.gid[ps.n] = g;
+        ps.tab[ps.n] = pend_table<T>(P.dims[e]);
+        ++ps.n;
+    }
+    return ps;
+}
+
+struct ProjectionOpts {
+    const double* bias = nullptr;
+    bool alpha = false;
+    bool mixing = true;
+};
+
+// Group sums of dimension d over the current residual of `data`, with all
+// pending tables applied; then the finalize epilogue.
+template <typename T>
+int sweep_sums(Problem& P, int d, T* data, const PendingSet<T>& ps, bool writeback) {
+    Dim& D = P.dims[d];
+    if (D.mode == MODE_SMALLG) {
+        SmallGParams<T> sp{};
+        sp.X = data;
+        sp.C = P.C;
+        sp.n = P.n;
+        sp.gid = D.gid;
+        sp.G = D.G;
+        sp.pend = ps;
+        sp.writeback = writeback ? 1 : 0;
+        sp.rows_per_block = (P.n + P.smallg_nb - 1) / P.smallg_nb;
+        sp.partials = P.partials;
+        return launch_smallg_sweep<T>(sp, P.smallg_nb, P.s);
+    }
+    SegSweepParams<T> sp{};
+    sp.X = data;
+    sp.rs = P.C;
+    sp.cs = 1;
+    sp.C = P.C;
+    sp.n = P.n;
+    sp.perm = D.mode == MODE_GATHER ? D.perm : nullptr;
+    sp.gseq = D.gseq;
+    sp.pend = ps;
+    sp.writeback = (writeback && D.mode == MODE_CONTIG) ? 1 : 0;
+    sp.R = CHUNK_R;
+    sp.sums = P.sums;
+    sp.head = P.head;
+    sp.tail = P.tail;
+    return launch_seg_sweep<T>(sp, P.s);
+}
+
+FinalizeParams finalize_base(const Problem& P, int d) {
+    const Dim& D = P.dims[d];
+    FinalizeParams f{};
+    f.G = D.G;
+    f.C = P.C;
+    if (D.mode == MODE_SMALLG) {
+        f.partials = P.partials;
+        f.nblocks = P.smallg_nb;
+    } else {
+        f.off = D.off;
+        f.sums = P.sums;
+        f.head = P.head;
+        f.tail = P.tail;
+        f.R = CHUNK_R;
+    }
+    f.counts = D.counts;
+    return f;
+}
+
+// One AP projection of dimension d (symmetric relaxed scheme).
+template <typename T>
+int project(Problem& P, int d, T* data, PendingList& pl, const ProjectionOpts& o) {
+    if (P.n == 0 || P.dims[d].G <= 0) return 0;
+    Dim& D = P.dims[d];
+    PendingSet<T> ps = make_pending<T>(P, d, pl);
+    const bool wb = D.mode != MODE_GATHER;
+    FEGB_TRY(sweep_sums<T>(P, d, data, ps, wb));
+    bool accumulate = false;
+    if (wb) {
+        pl.dims.clear();
+        pl.dims.push_back(d);
+    } else {
+        accumulate = pl.has(d);
+        if (!accumulate) pl.dims.push_back(d);
+    }
+    FinalizeParams f = finalize_base(P, d);
+    f.bias = o.bias;
+    if (o.mixing) {
+        f.prev = D.prev;
+        f.relax = P.relax + d;
+    }
+    f.pend64 = D.pend64;
+    f.pend32 = D.pend32;
+    f.pend_accumulate = accumulate ? 1 : 0;
+    f.alpha = o.alpha ? D.alpha : nullptr;
+    f.change_bits = P.change_bits + d;
+    f.do_relax_update = 1;
+    f.done_counter = P.done + d;
+    f.relax_rw = P.relax + d;
+    f.prev_change = P.prev_change + d;
+    f.max_update_bits = P.max_bits;
+    FEGB_TRY(launch_finalize(f, P.s));
+    P.projections += 1;
+    P.demean_bytes += (double)P.n * (4.0 + 2.0 * P.C * sizeof(T));
+    return 0;
+}
+
+template <typename T>
+int apply_all_pending(Problem& P, T* data, PendingList& pl) {
+    if (pl.dims.empty() || P.n == 0) return 0;
+    PendingSet<T> ps{};
+    ps.n = 0;
+    for (int e : pl.dims) {
+        ps.gid[ps.n] = P.dims[e].gid;
+        ps.tab[ps.n] = pend_table<T>(P.dims[e]);
+        ++ps.n;
+    }
+    FEGB_TRY(launch_apply_pending<T>(data, P.C, P.n, ps, P.s));
+    pl.dims.clear();
+    return 0;
+}
+
+int reset_ap_state(Problem& P, bool alpha) {
+    for (int d = 0; d < P.n_fe; ++d) {
+        size_t gc = (size_t)std::max(1, P.dims[d].G) * P.C;
+        FEGB_CUDA(cudaMemsetAsync(P.dims[d].prev, 0, gc * sizeof(double), P.s), "reset prev");
+        if (alpha && P.dims[d].alpha)
+            FEGB_CUDA(cudaMemsetAsync(P.dims[d].alpha, 0, gc * sizeof(double), P.s), "reset alpha");
+    }
+    if (P.n_fe > 0) {
+        reset_relax_kernel<<<1, 32 * ((P.n_fe + 31) / 32), 0, P.s>>>(P.relax, P.prev_change, P.change_bits, P.done,
+                                                                    P.n_fe);
+        FEGB_LAUNCH_CHECK("reset relaxation");
+    }
+    return 0;
+}
+
+// One iteration = two symmetric sweeps (forward then backward over the dims),
+// as in fe_gpu_demean.f90:144-292. Returns the max |mixed mean| on the host.
+template <typename T>
+int ap_iteration(Problem& P, T* data, PendingList& pl, const ProjectionOpts& o, double* max_update) {
+    FEGB_CUDA(cudaMemsetAsync(P.max_bits, 0, sizeof(unsigned long long), P.s), "reset max");
+    for (int sweep = 0; sweep < 2; ++sweep) {
+        for (int sidx = 0; sidx < P.n_fe; ++sidx) FEGB_TRY(project<T>(P, P.order[sidx], data, pl, o));
+        for (int sidx = P.n_fe - 1; sidx >= 0; --sidx) FEGB_TRY(project<T>(P, P.order[sidx], data, pl, o));
+    }
+    unsigned long long b = 0;
+    FEGB_TRY(d2h_sync(&b, P.max_bits, sizeof(b), P.s, "max update copy"));
+    *max_update = bits_to_double(b);
+    return 0;
+}
+
+int demean_plain(Problem& P, double tol, int max_iter, int* iterations, int* converged, double* max_update) {
+    *iterations = 0;
+    *converged = 1;
+    *max_update = 0.0;
+    if (P.n_fe == 0 || P.n == 0) return 0;
+    FEGB_TRY(reset_ap_state(P, false));
+    PendingList pl;
+    ProjectionOpts o;
+    int hit = 0;
+    double mu = 0.0;
+    for (int iter = 1; iter <= max_iter; ++iter) {
+        FEGB_TRY(ap_iteration<double>(P, P.X, pl, o, &mu));
+        *iterations = iter;
+        if (mu < tol) {
+            hit = 1;
+            break;
+        }
+    }
+    FEGB_TRY(apply_all_pending<double>(P, P.X, pl));
+    *converged = hit;
+    *max_update = mu;
+    return 0;
+}
+
+// FP64 group means of the current FP64 residual for every dimension; the
+// first (primary, storage-order) pass also subtracts the FE increments of the
+// previous refinement round and writes the rows back. Returns max |mean|.
+int fp64_mean_pass(Problem& P, bool apply_alpha, double* mu_max) {
+    FEGB_CUDA(cudaMemsetAsync(P.max_bits + 1, 0, sizeof(unsigned long long), P.s), "reset mu max");
+    // storage-order pass first
+    std::vector<int> seq;
+    seq.push_back(P.primary);
+    for (int d = 0; d < P.n_fe; ++d)
+        if (d != P.primary) seq.push_back(d);
+    bool first = true;
+    for (int d : seq) {
+        Dim& D = P.dims[d];
+        PendingSet<double> ps{};
+        ps.n = 0;
+        if (first && apply_alpha) {
+            for (int e = 0; e < P.n_fe; ++e) {
+                ps.gid[ps.n] = P.dims[e].gid;
+                ps.tab[ps.n] = P.dims[e].alpha;
+                ++ps.n;
+            }
+        }
+        if (D.G > 0 && P.n > 0) {
+            FEGB_TRY(sweep_sums<double>(P, d, P.X, ps, first && apply_alpha));
+            FinalizeParams f = finalize_base(P, d);
+            f.mean_out = D.mu;
+            f.change_bits = P.max_bits + 1;
+            FEGB_TRY(launch_finalize(f, P.s));
+            bool rw = first && apply_alpha;
+            P.demean_bytes += (double)P.n * ((rw ? 4.0 * (1 + P.n_fe) : 4.0) + (rw ? 16.0 : 8.0) * P.C);
+        }
+        first = false;
+    }
+    unsigned long long b = 0;
+    FEGB_TRY(d2h_sync(&b, P.max_bits + 1, sizeof(b), P.s, "mu max copy"));
+    *mu_max = bits_to_double(b);
+    return 0;
+}
+
+// Mixed form: FP64 residual r (P.X) and FP64 FE increments alpha; the inner
+// alternating projections run on an FP32 correction block c with the FP64 group
+// means of r as a per-group bias (group means of r + c = mu + means of c).
+int demean_mixed(Problem& P, double tol, int max_iter, int* iterations, int* converged, double* max_update,
+                 int* outer) {
+    *iterations = 0;
+    *converged = 1;
+    *max_update = 0.0;
+    *outer = 0;
+    if (P.n_fe == 0 || P.n == 0) return 0;
+    const int max_outer = 12;
+    double mu = 0.0, mu_prev = DBL_MAX;
+    int total_iter = 0;
+    bool apply_alpha = false;
+    int hit = 0;
+    for (int round = 0; round < max_outer; ++round) {
+        FEGB_TRY(fp64_mean_pass(P, apply_alpha, &mu));
+        *outer = round + 1;
+        if (mu < tol) {
+            hit = 1;
+            break;
+        }
+        if (total_iter >= max_iter) break;
+        if (round > 2 && mu > 0.5 * mu_prev) break;  // refinement stalled
+        mu_prev = mu;
+        // inner FP32 correction sweeps
+        FEGB_CUDA(cudaMemsetAsync(P.Xc, 0, sizeof(float) * (size_t)P.n * P.C, P.s), "zero correction");
+        FEGB_TRY(reset_ap_state(P, true));
+        PendingList pl;
+        double inner_tol = std::max(0.25 * tol, 1e-5 * mu);
+        double upd = 0.0;
+        for (int it = 0; it < max_iter - total_iter; ++it) {
+            // per-dimension bias = FP64 means of r
+            ProjectionOpts o;
+            o.alpha = true;
+            // the bias differs per dimension: run the iteration projection by projection
+            FEGB_CUDA(cudaMemsetAsync(P.max_bits, 0, sizeof(unsigned long long), P.s), "reset max");
+            for (int sweep = 0; sweep < 2; ++sweep) {
+                for (int pass = 0; pass < 2; ++pass) {
+                    for (int sidx = 0; sidx < P.n_fe; ++sidx) {
+                        int d = pass == 0 ? P.order[sidx] : P.order[P.n_fe - 1 - sidx];
+                        o.bias = P.dims[d].mu;
+                        FEGB_TRY(project<float>(P, d, P.Xc, pl, o));
+                    }
+                }
+            }
+            unsigned long long b = 0;
+            FEGB_TRY(d2h_sync(&b, P.max_bits, sizeof(b), P.s, "inner max copy"));
+            upd = bits_to_double(b);
+            ++total_iter;
+            if (upd < inner_tol) break;
+        }
+        apply_alpha = true;
+    }
+    *iterations = total_iter;
+    *converged = hit;
+    *max_update = mu;
+    return 0;
+}
+
+// ------------------------------ estimator ---------------------------------
+
+struct Stats {
+    double rss = 0, tss_total = 0, tss_within = 0;
+};
+
+// fe_pipeline.f90:1963-2008
+void finalize_stats(fegb_result* r, long long n_obs) {
+    const double EPS = 1e-12;
+    double n = (double)std::max(1LL, n_obs);
+    double df_model = (double)std::max(0, r->dof_model);
+    double df_resid = (double)std::max(1LL, r->dof_resid);
+    double dev = r->rss;
+    double dev0 = std::max(EPS, r->tss_total);
+    if (dev0 > EPS) {
+        r->r2 = std::max(0.0, std::min(1.0, 1.0 - dev / dev0));
+    } else {
+        r->r2 = 0.0;
+    }
+    if (r->tss_within > EPS)
+        r->r2_within = std::max(0.0, std::min(1.0, 1.0 - dev / r->tss_within));
+    else
+        r->r2_within = r->r2;
+    double k_total = (double)(r->dof_model + r->dof_fes + 1);
+    double denom = std::max(n - k_total, 1.0);
+    if (n > 1.0 && dev0 > EPS)
+        r->r2_adj = std::max(0.0, std::min(1.0, 1.0 - (dev * (n - 1.0)) / (dev0 * denom)));
+    else
+        r->r2_adj = r->r2;
+    double ssr = std::max(0.0, dev0 - dev);
+    if (df_model > 0.0 && df_resid > 0.0 && dev > EPS)
+        r->f_stat = (ssr / df_model) / (dev / df_resid);
+    else
+        r->f_stat = 0.0;
+}
+
+__global__ void tss_partials_kernel(const double* __restrict__ y, long long n, double mean, double* partials,
+                                    double* sums) {
+    __shared__ double red[256 / 32];
+    double a = 0.0;
+    long long i = (long long)blockIdx.x * 256 + threadIdx.x;
+    const long long st = (long long)gridDim.x * 256;
+    for (; i < n; i += st) a += sums ? y[i] : (y[i] - mean) * (y[i] - mean);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = a;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double v = 0.0;
+        for (int w = 0; w < 8; ++w) v += red[w];
+        (sums ? sums : partials)[blockIdx.x] = v;
+    }
+}
+
+// Total sum of squares around the mean of the raw y (compute_tss,
+// fe_pipeline.f90:1935-1955), with a fixed reduction order.
+int compute_tss_dev(const double* y, long long n, double* out, cudaStream_t s, Scratch& scr) {
+    *out = 0.0;
+    if (n <= 0) return 0;
+    int nb = (int)std::min<long long>((long long)num_sms() * 4, (n + 255) / 256);
+    double* part = nullptr;
+    FEGB_TRY(scr.alloc(&part, (size_t)nb, "tss partials"));
+    std::vector<double> h(nb);
+    tss_partials_kernel<<<nb, 256, 0, s>>>(y, n, 0.0, nullptr, part);
+    FEGB_LAUNCH_CHECK("tss sum");
+    FEGB_TRY(d2h_sync(h.data(), part, sizeof(double) * nb, s, "tss sum copy"));
+    double sum = 0.0;
+    for (double v : h) sum += v;
+    double mean = sum / (double)n;
+    tss_partials_kernel<<<nb, 256, 0, s>>>(y, n, mean, part, nullptr);
+    FEGB_LAUNCH_CHECK("tss");
+    FEGB_TRY(d2h_sync(h.data(), part, sizeof(double) * nb, s, "tss copy"));
+    double t = 0.0;
+    for (double v : h) t += v;
+    *out = t;
+    return 0;
+}
+
+// Cluster-score sums of S (n x ns AoS, storage order) over the groups of one
+// cluster subset; writes Sc (n_cl x ns).
+int cluster_score_sums(Problem& P, const double* S, int ns, const int32_t* perm, const int32_t* gseq,
+                       const int32_t* off, int n_cl, double* Sc, Scratch& scr) {
+    SegSweepParams<double> sp{};
+    sp.X = const_cast<double*>(S);
+    sp.rs = ns;
+    sp.cs = 1;
+    sp.C = ns;
+    sp.n = P.n;
+    sp.perm = perm;
+    sp.gseq = gseq;
+    sp.pend.n = 0;
+    sp.writeback = 0;
+    sp.R = CHUNK_R;
+    long long nchunks = std::max(1LL, seg_nchunks(P.n, CHUNK_R));
+    double *sums = nullptr, *head = nullptr, *tail = nullptr;
+    int32_t* cnt = nullptr;
+    FEGB_TRY(scr.alloc(&sums, (size_t)std::max(1, n_cl) * ns, "score sums"));
+    FEGB_TRY(scr.alloc(&head, (size_t)nchunks * ns, "score heads"));
+    FEGB_TRY(scr.alloc(&tail, (size_t)nchunks * ns, "score tails"));
+    FEGB_TRY(scr.alloc(&cnt, (size_t)std::max(1, n_cl), "score counts"));
+    sp.sums = sums;
+    sp.head = head;
+    sp.tail = tail;
+    FEGB_TRY(launch_seg_sweep<double>(sp, P.s));
+    counts_from_offsets_kernel<<<(n_cl + 255) / 256, 256, 0, P.s>>>(off, n_cl, cnt);
+    FEGB_LAUNCH_CHECK("score counts");
+    FinalizeParams f{};
+    f.G = n_cl;
+    f.C = ns;
+    f.off = off;
+    f.sums = sums;
+    f.head = head;
+    f.tail = tail;
+    f.R = CHUNK_R;
+    f.counts = cnt;
+    f.sum_out = Sc;
+    return launch_finalize(f, P.s);
+}
+
+struct FitTimes {
+    double prep = 0, demean = 0, regression = 0, se = 0;
+};
+
+int estimate_on_problem(Problem& P, const fegb_config& cfg, const int* G_all, long long n_raw, double tss_total,
+                        double* beta_out, double* se_out, fegb_result* res, FitTimes& tm) {
+    cudaStream_t s = P.s;
+    Scratch& scr = *P.scr;
+    const int k = P.k, l = P.l, C = P.C, n_fe = P.n_fe;
+    const long long n = P.n;
+    const bool cpu_conv = cfg.se_convention == FEGB_SE_CPU;
+    for (int j = 0; j < k; ++j) {
+        beta_out[j] = 0.0;
+        se_out[j] = 0.0;
+    }
+    res->tss_total = tss_total;
+    int dof_fes = 0;
+    for (int d = 0; d < n_fe; ++d) dof_fes += std::max(0, G_all[d] - 1);
+    res->dof_fes = dof_fes;
+    // cluster dims: valid, unique, first three (fe_pipeline.f90:1553-1599, 305-346)
+    std::vector<int> cdims;
+    for (int i = 0; i < cfg.n_cluster_dims; ++i) {
+        int v = cfg.cluster_dims[i];
+        if (v < 1 || v > n_fe) continue;
+        if (std::find(cdims.begin(), cdims.end(), v) != cdims.end()) continue;
+        if ((int)cdims.size() == MAX_CLUSTER_DIMS) break;
+        cdims.push_back(v);
+    }
+    int nested = 0;
+    for (int v : cdims) nested += std::max(0, G_all[v - 1] - 1);
+
+    // ---------------- within-transform ----------------
+    auto t0 = Clock::now();
+    int iters = 0, conv = 1, outer = 0;
+    double mu = 0.0;
+    if (cfg.precision == FEGB_PREC_MIXED)
+        FEGB_TRY(demean_mixed(P, cfg.fe_tol, cfg.fe_max_iter, &iters, &conv, &mu, &outer));
+    else
+        FEGB_TRY(demean_plain(P, cfg.fe_tol, cfg.fe_max_iter, &iters, &conv, &mu));
+    FEGB_CUDA(cudaStreamSynchronize(s), "demean sync");
+    tm.demean = seconds_since(t0);
+    res->converged = conv;
+    res->fe_iterations = iters;
+    res->max_update = mu;
+    res->outer_iterations = outer;
+    res->projections = P.projections;
+    res->demean_bytes = P.demean_bytes;
+    if (k <= 0) return 0;
+
+    // ---------------- normal equations ----------------
+    t0 = Clock::now();
+    double* gram = nullptr;
+    FEGB_TRY(scr.alloc(&gram, (size_t)C * C, "gram"));
+    MatView xv{P.X, C, 1, C};
+    FEGB_TRY(crossprod(xv, xv, n, true, false, 1.0, 0.0, gram, C, s, scr));
+    std::vector<double> hg((size_t)C * C);
+    FEGB_TRY(d2h_sync(hg.data(), gram, sizeof(double) * C * C, s, "gram copy"));
+    auto Gm = [&](int i, int j) { return hg[(size_t)i + (size_t)j * C]; };
+    res->tss_within = Gm(0, 0);
+    std::vector<double> vdiag(k);
+    for (int j = 0; j < k; ++j) vdiag[j] = Gm(1 + j, 1 + j);
+
+    // endogenous / instruments (fe_pipeline.f90:672-746)
+    std::vector<int> is_endog(k, 0);
+    if (!cpu_conv)
+        for (int i = 0; i < cfg.n_iv_regressors; ++i) {
+            int v = cfg.iv_regressors[i];
+            if (v >= 1 && v <= k) is_endog[v - 1] = 1;
+        }
+    int n_endog = 0;
+    for (int v : is_endog) n_endog += v;
+    std::vector<int> sel;
+    if (l > 0 && !cpu_conv) {
+        for (int i = 0; i < cfg.n_iv_instruments; ++i) {
+            int v = cfg.iv_instruments[i];
+            if (v >= 1 && v <= l) sel.push_back(v);
+        }
+        if (sel.empty())
+            for (int i = 1; i <= l; ++i) sel.push_back(i);
+    }
+    bool use_iv = n_endog > 0 && (int)sel.size() >= n_endog;
+    std::vector<int> za;  // X columns of Z_aug = [exogenous W, selected Z]
+    if (use_iv) {
+        for (int j = 0; j < k; ++j)
+            if (!is_endog[j]) za.push_back(1 + j);
+        for (int v : sel) za.push_back(1 + k + (v - 1));
+    }
+    const int na = (int)za.size();
+    res->is_iv = use_iv ? 1 : 0;
+    res->n_instruments = use_iv ? na : 0;
+
+    int kmax = std::max(k, std::max(na, 1));
+    double *Q = nullptr, *b = nullptr, *work = nullptr, *Pi = nullptr;
+    int* info_dev = nullptr;
+    FEGB_TRY(scr.alloc(&Q, (size_t)k * k, "Q"));
+    FEGB_TRY(scr.alloc(&b, (size_t)k, "b"));
+    FEGB_TRY(scr.alloc(&work, (size_t)4 * kmax * kmax, "dense work"));
+    FEGB_TRY(scr.alloc(&info_dev, 4, "info"));
+    // Q = W'W, b = W'y from the Gram block
+    {
+        std::vector<double> hQ((size_t)k * k), hb(k);
+        for (int i = 0; i < k; ++i) {
+            hb[i] = Gm(1 + i, 0);
+            for (int j = 0; j < k; ++j) hQ[(size_t)i + (size_t)j * k] = Gm(1 + i, 1 + j);
+        }
+        FEGB_TRY(h2d_sync(Q, hQ.data(), sizeof(double) * k * k, s, "Q upload"));
+        FEGB_TRY(h2d_sync(b, hb.data(), sizeof(double) * k, s, "b upload"));
+    }
+    if (use_iv) {
+        // build_iv_normal_equations (fe_pipeline.f90:947-1032)
+        double *Qzz = nullptr, *Qzy = nullptr, *Qzx = nullptr, *rhs = nullptr, *Qinv_zz = nullptr;
+        FEGB_TRY(scr.alloc(&Qzz, (size_t)na * na, "Qzz"));
+        FEGB_TRY(scr.alloc(&Qzy, (size_t)na, "Qzy"));
+        FEGB_TRY(scr.alloc(&Qzx, (size_t)na * k, "Qzx"));
+        FEGB_TRY(scr.alloc(&rhs, (size_t)na, "iv rhs"));
+        FEGB_TRY(scr.alloc(&Qinv_zz, (size_t)na * na, "Qzz inverse"));
+        FEGB_TRY(scr.alloc(&Pi, (size_t)na * k, "projection"));
+        std::vector<double> hzz((size_t)na * na), hzy(na), hzx((size_t)na * k);
+        for (int i = 0; i < na; ++i) {
+            hzy[i] = Gm(za[i], 0);
+            for (int j = 0; j < na; ++j) hzz[(size_t)i + (size_t)j * na] = Gm(za[i], za[j]);
+            for (int j = 0; j < k; ++j) hzx[(size_t)i + (size_t)j * na] = Gm(za[i], 1 + j);
+        }
+        FEGB_TRY(h2d_sync(Qzz, hzz.data(), sizeof(double) * na * na, s, "Qzz upload"));
+        FEGB_TRY(h2d_sync(Qzy, hzy.data(), sizeof(double) * na, s, "Qzy upload"));
+        FEGB_TRY(h2d_sync(Qzx, hzx.data(), sizeof(double) * na * k, s, "Qzx upload"));
+        FEGB_TRY(dense_chol_solve_inv(na, Qzz, na, nullptr, Qzy, rhs, Qinv_zz, info_dev, work, s));
+        int info = 0;
+        FEGB_TRY(d2h_sync(&info, info_dev, sizeof(int), s, "iv info"));
+        if (info != 0) {
+            res->solver_info = info;
+            return 0;
+        }
+        FEGB_TRY(dense_gemm(false, false, na, k, na, 1.0, Qinv_zz, na, Qzx, na, 0.0, Pi, na, s));
+        // Q = 0.5 (T + T^T)
+        FEGB_TRY(dense_gemm(true, false, k, k, na, 0.5, Qzx, na, Pi, na, 0.0, Q, k, s));
+        FEGB_TRY(dense_gemm(true, false, k, k, na, 0.5, Pi, na, Qzx, na, 1.0, Q, k, s));
+        FEGB_TRY(dense_gemm(true, false, k, 1, na, 1.0, Qzx, na, rhs, na, 0.0, b, k, s));
+    }
+    // column filter (fe_pipeline.f90:1034-1107); the CPU path keeps every column
+    std::vector<int> kept;
+    {
+        double dmax = 0.0;
+        for (int j = 0; j < k; ++j) dmax = std::max(dmax, std::fabs(vdiag[j]));
+        dmax = std::max(dmax, 1.0);
+        double tol = 1.0e-10 * dmax;
+        for (int j = 0; j < k; ++j)
+            if (cpu_conv || !(std::fabs(vdiag[j]) <= tol)) kept.push_back(j);
+    }
+    const int kk = (int)kept.size();
+    res->dof_model = kk;
+    if (kk == 0) {
+        res->solver_info = -1;
+        return 0;
+    }
+    int* idx_dev = nullptr;
+    double *beta_sel = nullptr, *Qinv = nullptr, *beta_full = nullptr;
+    FEGB_TRY(scr.alloc(&idx_dev, (size_t)kk, "kept idx"));
+    FEGB_TRY(scr.alloc(&beta_sel, (size_t)kk, "beta sel"));
+    FEGB_TRY(scr.alloc(&Qinv, (size_t)kk * kk, "Qinv"));
+    FEGB_TRY(scr.alloc(&beta_full, (size_t)k, "beta"));
+    FEGB_TRY(h2d_sync(idx_dev, kept.data(), sizeof(int) * kk, s, "idx upload"));
+    FEGB_TRY(dense_chol_solve_inv(kk, Q, k, idx_dev, b, beta_sel, Qinv, info_dev, work, s));
+    int info = 0;
+    FEGB_TRY(d2h_sync(&info, info_dev, sizeof(int), s, "solve info"));
+    res->solver_info = info;
+    if (info != 0) return 0;
+    std::vector<double> hbeta(kk);
+    FEGB_TRY(d2h_sync(hbeta.data(), beta_sel, sizeof(double) * kk, s, "beta copy"));
+    for (int t = 0; t < kk; ++t) beta_out[kept[t]] = hbeta[t];
+    res->rank = kk;
+    FEGB_TRY(h2d_sync(beta_full, beta_out, sizeof(double) * k, s, "beta upload"));
+    tm.regression = seconds_since(t0);
+
+    // ---------------- residual, scores and SEs ----------------
+    t0 = Clock::now();
+    const bool clusters = !cdims.empty();
+    std::vector<int> score_cols;
+    if (use_iv)
+        score_cols = za;
+    else
+        for (int j = 0; j < k; ++j) score_cols.push_back(1 + j);
+    const int ns = (int)score_cols.size();
+    int* score_cols_dev = nullptr;
+    double *S = nullptr, *rss_dev = nullptr;
+    FEGB_TRY(scr.alloc(&score_cols_dev, (size_t)ns, "score cols"));
+    FEGB_TRY(scr.alloc(&rss_dev, 1, "rss"));
+    FEGB_TRY(h2d_sync(score_cols_dev, score_cols.data(), sizeof(int) * ns, s, "score cols upload"));
+    if (clusters) FEGB_TRY(scr.alloc(&S, (size_t)n * ns, "score rows"));
+    FEGB_TRY(residual_scores(P.X, C, n, beta_full, k, score_cols_dev, ns, S, nullptr, rss_dev, s, scr));
+    double rss = 0.0;
+    FEGB_TRY(d2h_sync(&rss, rss_dev, sizeof(double), s, "rss copy"));
+    res->rss = rss;
+    long long df;
+    if (cpu_conv) {
+        df = n - k;  // fe_pipeline.f90:187
+    } else {
+        long long pc = (long long)std::max(0, res->dof_model) + std::max(0, res->dof_fes) + 1;
+        df = std::max(1LL, n - pc);  // fe_pipeline.f90:1171-1176
+    }
+    res->dof_resid = df;
+    double sigma2 = cpu_conv ? rss / std::max(1.0, (double)(n - k)) : rss / (double)df;
+    bool cluster_ok = false;
+    if (clusters) {
+        cluster_ok = true;
+        double* acc = nullptr;
+        double* meat = nullptr;
+        double* meat_k = nullptr;
+        double* se_sel = nullptr;
+        int* psd_dev = nullptr;
+        FEGB_TRY(scr.alloc(&acc, (size_t)kk * kk, "cov acc"));
+        FEGB_TRY(scr.alloc(&meat, (size_t)ns * ns, "meat"));
+        FEGB_TRY(scr.alloc(&meat_k, (size_t)k * k, "meat k"));
+        FEGB_TRY(scr.alloc(&se_sel, (size_t)kk, "se sel"));
+        FEGB_TRY(scr.alloc(&psd_dev, 1, "psd"));
+        FEGB_CUDA(cudaMemsetAsync(acc, 0, sizeof(double) * kk * kk, s), "acc zero");
+        const int ncd = (int)cdims.size();
+        long long min_single = LLONG_MAX;
+        for (int mask = 1; mask < (1 << ncd) && cluster_ok; ++mask) {
+            std::vector<int> sd;
+            for (int j = 0; j < ncd; ++j)
+                if (mask & (1 << j)) sd.push_back(cdims[j] - 1);
+            const int m = (int)sd.size();
+            Scratch sub(s);
+            const int32_t *perm = nullptr, *gseq = nullptr, *off = nullptr;
+            int n_cl = 0;
+            if (m == 1 && P.dims[sd[0]].mode != MODE_SMALLG) {
+                const Dim& D = P.dims[sd[0]];
+                perm = D.mode == MODE_GATHER ? D.perm : nullptr;
+                gseq = D.gseq;
+                off = D.off;
+                n_cl = D.G;
+            } else {
+                // intersection (or small-G single) clusters: sort rows by key
+                std::vector<const int32_t*> ptrs;
+                std::vector<unsigned long long> strides;
+                unsigned long long stride = 1;
+                bool fits = true;
+                for (int d : sd) {
+                    ptrs.push_back(P.dims[d].gid);
+                    strides.push_back(stride);
+                    unsigned long long Gd = (unsigned long long)std::max(1, P.dims[d].G);
+                    if (stride > (1ULL << 62) / Gd) fits = false;
+                    stride *= Gd;
+                }
+                if (!fits) {
+                    set_error("cluster key span exceeds 2^62 for a %d-way subset", m);
+                    cluster_ok = false;
+                    break;
+                }
+                int32_t *pm = nullptr, *gs = nullptr, *of = nullptr;
+                FEGB_TRY(sub.alloc(&pm, (size_t)n, "cluster perm"));
+                FEGB_TRY(sub.alloc(&gs, (size_t)n, "cluster gseq"));
+                FEGB_TRY(sub.alloc(&of, (size_t)n + 1, "cluster offsets"));
+                FEGB_TRY(cluster_ids_by_key(ptrs.data(), strides.data(), m, n, bits_for(stride), nullptr, &n_cl, pm,
+                                            of, s, sub, true, gs));
+                perm = pm;
+                gseq = gs;
+                off = of;
+                if (m == 1 && !cpu_conv) n_cl = P.dims[sd[0]].G;  // ids equal FE ids; empty groups add nothing
+                if (m == 1 && !cpu_conv) {
+                    // offsets must cover G groups: rebuild from the FE counts when groups are empty
+                    int32_t* of2 = nullptr;
+                    FEGB_TRY(sub.alloc(&of2, (size_t)n_cl + 1, "cluster offsets G"));
+                    uint32_t* gsu = reinterpret_cast<uint32_t*>(gs);
+                    // gseq holds ranks; for a single dim the FE id order equals rank order, so
+                    // recompute the sorted FE ids and offsets over all G groups
+                    gather_i32_kernel<<<grid_stride_blocks(n, 256), 256, 0, s>>>(P.dims[sd[0]].gid, pm, n, gs);
+                    FEGB_LAUNCH_CHECK("single cluster ids");
+                    FEGB_TRY(segment_offsets(gsu, n, n_cl, of2, s));
+                    off = of2;
+                }
+            }
+            if (n_cl <= 0) {
+                cluster_ok = false;
+                break;
+            }
+            if (m == 1) {
+                long long nc1 = n_cl;
+                if (cpu_conv && P.dims[sd[0]].mode != MODE_SMALLG) {
+                    // the CPU path counts distinct ids (cluster_id_builder ranks)
+                    std::vector<int32_t> hc(P.dims[sd[0]].G);
+                    FEGB_TRY(d2h_sync(hc.data(), P.dims[sd[0]].counts, sizeof(int32_t) * hc.size(), s, "counts copy"));
+                    nc1 = 0;
+                    for (int32_t c : hc) nc1 += c > 0;
+                }
+                min_single = std::min(min_single, nc1);
+            }
+            double* Sc = nullptr;
+            FEGB_TRY(sub.alloc(&Sc, (size_t)n_cl * ns, "cluster scores"));
+            FEGB_TRY(cluster_score_sums(P, S, ns, perm, gseq, off, n_cl, Sc, sub));
+            MatView sv{Sc, ns, 1, ns};
+            FEGB_TRY(crossprod(sv, sv, n_cl, true, false, 1.0, 0.0, meat, ns, s, sub));
+            const double* Mk = meat;
+            int ldm = ns;
+            if (use_iv) {
+                // meat of the projected regressors: Pi^T meat_Z Pi
+                FEGB_TRY(dense_gemm(false, false, ns, k, ns, 1.0, meat, ns, Pi, na, 0.0, work, ns, s));
+                FEGB_TRY(dense_gemm(true, false, k, k, ns, 1.0, Pi, na, work, ns, 0.0, meat_k, k, s));
+                Mk = meat_k;
+                ldm = k;
+            }
+            double w = (m % 2 == 1) ? 1.0 : -1.0;
+            FEGB_TRY(dense_sandwich_acc(kk, Qinv, Mk, ldm, idx_dev, w, acc, work, s));
+            FEGB_CUDA(cudaStreamSynchronize(s), "subset sync");
+        }
+        if (cluster_ok) {
+            double scalar;
+            long long ms = min_single == LLONG_MAX ? 0 : min_single;
+            if (cpu_conv) {
+                // fe_pipeline.f90:466-472
+                double denom = (double)std::max(1LL, n - (long long)k);
+                scalar = (double)std::max(1LL, n - 1) / denom;
+                if (ms > 1) scalar *= (double)ms / (double)(ms - 1);
+            } else {
+                // fe_pipeline.f90:1348-1360
+                int nested_adj = nested > 0 ? 1 : 0;
+                long long pce = (long long)std::max(0, res->dof_model) + nested_adj;
+                double denom = (double)std::max(1LL, n - pce);
+                scalar = (double)std::max(1LL, n - 1) / denom;
+                if (ms > 1) scalar *= (double)ms / (double)(ms - 1);
+            }
+            FEGB_TRY(dense_finalize_cov(kk, acc, scalar, cpu_conv ? 0 : 1, se_sel, psd_dev, work, s));
+            std::vector<double> hse(kk);
+            int psd = 0;
+            FEGB_TRY(d2h_sync(hse.data(), se_sel, sizeof(double) * kk, s, "se copy"));
+            FEGB_TRY(d2h_sync(&psd, psd_dev, sizeof(int), s, "psd copy"));
+            for (int t = 0; t < kk; ++t) se_out[kept[t]] = hse[t];
+            res->psd_fix_applied = psd;
+            if (ms > 0) res->dof_resid = std::max(1LL, ms - 1);
+            res->n_cluster_dims_used = ncd;
+            res->min_single_cluster = (int)ms;
+        }
+    }
+    if (!cluster_ok) {
+        std::vector<double> hq((size_t)kk * kk);
+        FEGB_TRY(d2h_sync(hq.data(), Qinv, sizeof(double) * kk * kk, s, "Qinv copy"));
+        for (int t = 0; t < kk; ++t)
+            se_out[kept[t]] = std::sqrt(std::max(0.0, sigma2 * hq[(size_t)t + (size_t)t * kk]));
+    }
+    tm.se = seconds_since(t0);
+    finalize_stats(res, n);
+    (void)n_raw;
+    return 0;
+}
+
+class StreamHolder {
+  public:
+    explicit StreamHolder(void* user) {
+        if (user) {
+            s_ = static_cast<cudaStream_t>(user);
+        } else {
+            cudaStreamCreateWithFlags(&s_, cudaStreamNonBlocking);
+            own_ = true;
+        }
+    }
+    ~StreamHolder() {
+        if (own_) cudaStreamDestroy(s_);
+    }
+    cudaStream_t get() const { return s_; }
+
+  private:
+    cudaStream_t s_ = nullptr;
+    bool own_ = false;
+};
+
+int estimate_device_impl(const fegb_config* cfg_in, long long n, int k, int l, int n_fe, const double* y,
+                         const double* W, const double* Z, const int32_t* const* ids, const int* group_sizes,
+                         double* beta, double* se, fegb_result* result, double t_h2d, cudaStream_t s) {
+    auto t_start = Clock::now();
+    fegb_config cfg;
+    if (cfg_in)
+        cfg = *cfg_in;
+    else
+        fegb_config_init(&cfg);
+    fegb_result local{};
+    fegb_result* res = result ? result : &local;
+    std::memset(res, 0, sizeof(*res));
+    if (n < 0 || k < 0 || l < 0 || n_fe < 0) return set_error("invalid sizes n=%lld k=%d l=%d n_fe=%d", n, k, l, n_fe);
+    if (n > 0x7fffffffLL) return set_error("n=%lld exceeds the int32 row index range", n);
+    if (k > 0 && (!beta || !se)) return set_error("beta/se output arrays are required");
+    if (cfg.demean_method != FEGB_DEMEAN_AP && cfg.demean_method != FEGB_DEMEAN_CG)
+        return set_error("unknown demean method %d", cfg.demean_method);
+    configure_mem_pool();
+    Scratch scr(s);
+    Problem P;
+    P.s = s;
+    P.scr = &scr;
+    FitTimes tm;
+    auto t0 = Clock::now();
+    long long n_single = 0;
+    FEGB_TRY(build_problem(P, n, k, l, n_fe, y, W, Z, ids, group_sizes, cfg.drop_singletons != 0,
+                           cfg.precision == FEGB_PREC_MIXED, &n_single));
+    std::vector<int> G(n_fe);
+    for (int d = 0; d < n_fe; ++d) G[d] = P.dims[d].G;
+    // TSS of the raw y over the rows used
+    double tss = 0.0;
+    {
+        double* ycol = nullptr;
+        FEGB_TRY(scr.alloc(&ycol, (size_t)std::max(1LL, P.n), "y column"));
+        // copy the strided column 0 of the data block into a contiguous vector
+        if (P.n > 0) {
+            FEGB_CUDA(cudaMemcpy2DAsync(ycol, sizeof(double), P.X, sizeof(double) * P.C, sizeof(double), (size_t)P.n,
+                                        cudaMemcpyDeviceToDevice, s),
+                      "y column copy");
+        }
+        FEGB_TRY(compute_tss_dev(ycol, P.n, &tss, s, scr));
+    }
+    FEGB_CUDA(cudaStreamSynchronize(s), "prep sync");
+    tm.prep = seconds_since(t0);
+    res->n_obs_used = P.n;
+    res->n_singletons = n_single;
+    int st = estimate_on_problem(P, cfg, G.data(), n, tss, beta, se, res, tm);
+    FEGB_CUDA(cudaStreamSynchronize(s), "fit sync");
+    res->time_h2d = t_h2d;
+    res->time_prep = tm.prep;
+    res->time_demean = tm.demean;
+    res->time_regression = tm.regression;
+    res->time_se = tm.se;
+    res->time_total = seconds_since(t_start) + t_h2d;
+    if (st != 0) return st;
+    return set_ok();
+}
+
+}  // namespace
+
+}  // namespace fegb
+
+using namespace fegb;
+
+extern "C" {
+
+void fegb_config_init(fegb_config* cfg) {
+    if (!cfg) return;
+    std::memset(cfg, 0, sizeof(*cfg));
+    cfg->fe_tol = 1.0e-6;  // src/core/fe_config.f90:55
+    cfg->fe_max_iter = 500;
+    cfg->precision = FEGB_PREC_FP64;
+    cfg->demean_method = FEGB_DEMEAN_AP;
+    cfg->se_convention = FEGB_SE_GPU;
+}
+
+int fegb_estimate_device(const fegb_config* cfg, long long n, int k, int l, int n_fe, const double* d_y,
+                         const double* d_W, const double* d_Z, const int* const* d_fe_ids, const int* group_sizes,
+                         double* beta, double* se, fegb_result* result) {
+    StreamHolder sh(cfg ? cfg->stream : nullptr);
+    std::vector<const int32_t*> ids(n_fe);
+    for (int d = 0; d < n_fe; ++d) ids[d] = d_fe_ids[d];
+    return estimate_device_impl(cfg, n, k, l, n_fe, d_y, d_W, d_Z, ids.data(), group_sizes, beta, se, result, 0.0,
+                                sh.get());
+}
+
+int fegb_estimate_host(const fegb_config* cfg, long long n, int k, int l, int n_fe, const double* y,
+                       const double* W, const double* Z, const int* fe_ids, const int* group_sizes, double* beta,
+                       double* se, fegb_result* result) {
+    if (n < 0 || k < 0 || l < 0 || n_fe < 0) return set_error("invalid sizes");
+    StreamHolder sh(cfg ? cfg->stream : nullptr);
+    cudaStream_t s = sh.get();
+    configure_mem_pool();
+    auto t0 = Clock::now();
+    Scratch scr(s);
+    double *dy = nullptr, *dW = nullptr, *dZ = nullptr;
+    int32_t *dids = nullptr, *dint = nullptr;
+    size_t nn = (size_t)std::max(1LL, n);
+    FEGB_TRY(scr.alloc(&dy, nn, "y upload"));
+    FEGB_TRY(scr.alloc(&dW, nn * std::max(1, k), "W upload"));
+    FEGB_TRY(scr.alloc(&dZ, nn * std::max(1, l), "Z upload"));
+    FEGB_TRY(scr.alloc(&dint, nn * std::max(1, n_fe), "ids upload"));
+    FEGB_TRY(scr.alloc(&dids, nn * std::max(1, n_fe), "ids"));
+    if (n > 0) {
+        FEGB_CUDA(cudaMemcpyAsync(dy, y, sizeof(double) * n, cudaMemcpyHostToDevice, s), "y H2D");
+        if (k > 0) FEGB_CUDA(cudaMemcpyAsync(dW, W, sizeof(double) * n * k, cudaMemcpyHostToDevice, s), "W H2D");
+        if (l > 0) FEGB_CUDA(cudaMemcpyAsync(dZ, Z, sizeof(double) * n * l, cudaMemcpyHostToDevice, s), "Z H2D");
+        if (n_fe > 0) {
+            FEGB_CUDA(cudaMemcpyAsync(dint, fe_ids, sizeof(int32_t) * n * n_fe, cudaMemcpyHostToDevice, s), "ids H2D");
+            deinterleave_ids_kernel<<<grid_stride_blocks(n * n_fe, 256), 256, 0, s>>>(dint, n_fe, n, dids);
+            FEGB_LAUNCH_CHECK("ids deinterleave");
+        }
+    }
+    FEGB_CUDA(cudaStreamSynchronize(s), "H2D sync");
+    double t_h2d = seconds_since(t0);
+    std::vector<const int32_t*> ids(n_fe);
+    for (int d = 0; d < n_fe; ++d) ids[d] = dids + (size_t)d * n;
+    return estimate_device_impl(cfg, n, k, l, n_fe, dy, dW, dZ, ids.data(), group_sizes, beta, se, result, t_h2d, s);
+}
+
+int fegb_within_transform(const fegb_config* cfg_in, long long n, int k, int l, int n_fe, double* d_y, double* d_W,
+                          double* d_Z, const int* const* d_fe_ids, const int* group_sizes, int* converged,
+                          int* iterations, double* max_update) {
+    fegb_config cfg;
+    if (cfg_in)
+        cfg = *cfg_in;
+    else
+        fegb_config_init(&cfg);
+    StreamHolder sh(cfg.stream);
+    cudaStream_t s = sh.get();
+    configure_mem_pool();
+    Scratch scr(s);
+    Problem P;
+    P.s = s;
+    P.scr = &scr;
+    std::vector<const int32_t*> ids(n_fe);
+    for (int d = 0; d < n_fe; ++d) ids[d] = d_fe_ids[d];
+    long long n_single = 0;
+    FEGB_TRY(build_problem(P, n, k, l, n_fe, d_y, d_W, d_Z, ids.data(), group_sizes, false,
+                           cfg.precision == FEGB_PREC_MIXED, &n_single));
+    int it = 0, conv = 1, outer = 0;
+    double mu = 0.0;
+    if (cfg.precision == FEGB_PREC_MIXED)
+        FEGB_TRY(demean_mixed(P, cfg.fe_tol, cfg.fe_max_iter, &it, &conv, &mu, &outer));
+    else
+        FEGB_TRY(demean_plain(P, cfg.fe_tol, cfg.fe_max_iter, &it, &conv, &mu));
+    if (n > 0) {
+        int TR = std::max(1, std::min(64, 24576 / (8 * P.C)));
+        size_t smem = sizeof(double) * (size_t)TR * P.C;
+        scatter_x_kernel<<<(unsigned)((n + TR - 1) / TR), 256, smem, s>>>(P.X, P.row_of, n, P.C, k, l, n, TR, d_y, d_W,
+                                                                         d_Z);
+        FEGB_LAUNCH_CHECK("scatter data block");
+    }
+    FEGB_CUDA(cudaStreamSynchronize(s), "within sync");
+    if (converged) *converged = conv;
+    if (iterations) *iterations = it;
+    if (max_update) *max_update = mu;
+    return set_ok();
+}
+
+int fegb_cluster_ids(const int* const* d_fe_ids, const int* sizes, int n_dims, long long n, int* d_out_ids,
+                     int* n_clusters) {
+    if (!d_fe_ids || !sizes || !d_out_ids || !n_clusters || n_dims <= 0) return set_error("invalid cluster-id arguments");
+    if (n_dims > 4) return set_error("at most 4 cluster dimensions (got %d)", n_dims);
+    if (n <= 0) {
+        *n_clusters = 0;
+        return set_ok();
+    }
+    StreamHolder sh(nullptr);
+    cudaStream_t s = sh.get();
+    configure_mem_pool();
+    Scratch scr(s);
+    std::vector<const int32_t*> ptrs(n_dims);
+    std::vector<unsigned long long> strides(n_dims);
+    unsigned long long span = 1;
+    bool sort_ok = true;
+    for (int j = 0; j < n_dims; ++j) {
+        ptrs[j] = d_fe_ids[j];
+        strides[j] = span;
+        unsigned long long sz = (unsigned long long)(sizes[j] > 0 ? sizes[j] : 0);
+        if (sz == 0 || sz > ~0ULL / span) {
+            sort_ok = false;
+            break;
+        }
+        span *= sz;
+        if (span > (1ULL << 62)) {
+            sort_ok = false;
+            break;
+        }
+    }
+    int nc = 0;
+    if (sort_ok) {
+        FEGB_TRY(cluster_ids_by_key(ptrs.data(), strides.data(), n_dims, n, bits_for(span), d_out_ids, &nc, nullptr,
+                                    nullptr, s, scr));
+    } else {
+        FEGB_TRY(cluster_ids_first_appearance(ptrs.data(), sizes, n_dims, n, d_out_ids, &nc, s, scr));
+    }
+    FEGB_CUDA(cudaStreamSynchronize(s), "cluster ids sync");
+    *n_clusters = nc;
+    return set_ok();
+}
+
+int fegb_compact_ids(const int* d_raw, long long n, int* d_out, int* n_levels) {
+    if (n > 0 && (!d_raw || !d_out)) return set_error("invalid compaction arguments");
+    StreamHolder sh(nullptr);
+    configure_mem_pool();
+    Scratch scr(sh.get());
+    FEGB_TRY(compact_ids(d_raw, n, d_out, n_levels, sh.get(), scr));
+    FEGB_CUDA(cudaStreamSynchronize(sh.get()), "compact sync");
+    return set_ok();
+}
+
+int fegb_group_sizes(const int* const* d_fe_ids, int n_fe, long long n, int* sizes) {
+    StreamHolder sh(nullptr);
+    configure_mem_pool();
+    Scratch scr(sh.get());
+    for (int d = 0; d < n_fe; ++d) {
+        if (n <= 0) {
+            sizes[d] = 0;
+            continue;
+        }
+        int mn = 0, mx = 0;
+        FEGB_TRY(ids_min_max(d_fe_ids[d], n, &mn, &mx, sh.get(), scr));
+        if (mn < 1) return set_error("FE indices must be positive and contiguous (dimension %d)", d + 1);
+        sizes[d] = std::max(0, mx);
+    }
+    return set_ok();
+}
+
+int fegb_drop_singletons(const int* const* d_fe_ids, const int* sizes, int n_fe, long long n, unsigned char* d_keep,
+                         long long* n_dropped) {
+    StreamHolder sh(nullptr);
+    cudaStream_t s = sh.get();
+    configure_mem_pool();
+    Scratch scr(s);
+    std::vector<int32_t*> g0(n_fe);
+    for (int d = 0; d < n_fe; ++d) {
+        FEGB_TRY(scr.alloc(&g0[d], (size_t)std::max(1LL, n), "singleton gid"));
+        if (n > 0) {
+            gather_gid_kernel<<<grid_stride_blocks(n, 256), 256, 0, s>>>(d_fe_ids[d], nullptr, n, g0[d]);
+            FEGB_LAUNCH_CHECK("singleton gid");
+        }
+    }
+    std::vector<int> G(sizes, sizes + n_fe);
+    FEGB_TRY(drop_singletons(g0.data(), G.data(), n_fe, n, d_keep, n_dropped, s, scr));
+    FEGB_CUDA(cudaStreamSynchronize(s), "singleton sync");
+    return set_ok();
+}
+
+}  // extern "C"

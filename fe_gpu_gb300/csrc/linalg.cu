@@ -1,0 +1,564 @@
+// Tall-skinny reductions and small dense kernels (see linalg.cuh).
+#include "linalg.cuh"
+
+#include <cmath>
+
+namespace fegb {
+
+namespace {
+
+constexpr int CP_THREADS = 256;
+constexpr int CP_TR = 16;
+constexpr int CP_MAXPAIRS_LAUNCH = 8192;
+
+struct CPParams {
+    const double* A;
+    long long ars, acs;
+    int a;
+    const double* B;
+    long long brs, bcs;
+    int b;
+    long long n;
+    int gram;
+    long long p0;      // first pair index of this launch
+    int npairs;        // pairs in this launch
+    int phases;        // row phases (PPT == 1 mode)
+    long long rows_per_block;
+    double* partials;  // nblocks x npairs
+};
+
+__device__ __forceinline__ void pair_ij(long long p, int gram, int a, int& i, int& j) {
+    if (gram) {
+        int jj = (int)((sqrt(8.0 * (double)p + 1.0) - 1.0) * 0.5);
+        while ((long long)(jj + 1) * (jj + 2) / 2 <= p) ++jj;
+        while ((long long)jj * (jj + 1) / 2 > p) --jj;
+        j = jj;
+        i = (int)(p - (long long)jj * (jj + 1) / 2);
+    } else {
+        i = (int)(p % a);
+        j = (int)(p / a);
+    }
+}
+
+__device__ __forceinline__ void load_tile(double* dst, const double* src, long long rs, long long cs, int width,
+                                          long long row0, int rows) {
+    const int total = rows * width;
+    if (rs == 1) {
+        for (int e = threadIdx.x; e < total; e += blockDim.x) {
+            int r = e % rows, c = e / rows;
+            dst[r * width + c] = src[(row0 + r) + (long long)c * cs];
+        }
+    } else {
+        for (int e = threadIdx.x; e < total; e += blockDim.x) {
+            int r = e / width, c = e % width;
+            dst[r * width + c] = src[(row0 + r) * rs + (long long)c * cs];
+        }
+    }
+}
+
+template <int PPT>
+__global__ void __launch_bounds__(CP_THREADS) crossprod_kernel(CPParams p) {
+    extern __shared__ double sm[];
+    double* sA = sm;
+    double* sB = p.gram ? sm : sm + CP_TR * p.a;
+    const int t = threadIdx.x;
+    int pi[PPT], pj[PPT];
+    bool pv[PPT];
+    double acc[PPT];
+    int phase = 0;
+    if (PPT == 1) {
+        int local = t % p.npairs;
+        phase = t / p.npairs;
+        pv[0] = phase < p.phases;
+        pair_ij(p.p0 + local, p.gram, p.a, pi[0], pj[0]);
+        acc[0] = 0.0;
+    } else {
+#pragma unroll
+        for (int s = 0; s < PPT; ++s) {
+            int local = t + s * CP_THREADS;
+            pv[s] = local < p.npairs;
+            pair_ij(p.p0 + (pv[s] ? local : 0), p.gram, p.a, pi[s], pj[s]);
+            acc[s] = 0.0;
+        }
+    }
+    const long long r0 = (long long)blockIdx.x * p.rows_per_block;
+    const long long r1 = min(p.n, r0 + p.rows_per_block);
+    for (long long tile = r0; tile < r1; tile += CP_TR) {
+        const int rows = (int)min((long long)CP_TR, r1 - tile);
+        load_tile(sA, p.A, p.ars, p.acs, p.a, tile, rows);
+        if (!p.gram) load_tile(sB, p.B, p.brs, p.bcs, p.b, tile, rows);
+        __syncthreads();
+        if (PPT == 1) {
+            if (pv[0])
+                for (int r = phase; r < rows; r += p.phases) acc[0] += sA[r * p.a + pi[0]] * sB[r * p.b + pj[0]];
+        } else {
+            for (int r = 0; r < rows; ++r) {
+#pragma unroll
+                for (int s = 0; s < PPT; ++s)
+                    if (pv[s]) acc[s] += sA[r * p.a + pi[s]] * sB[r * p.b + pj[s]];
+            }
+        }
+        __syncthreads();
+    }
+    if (PPT == 1) {
+        // fold row phases in a fixed order
+        __shared__ double fold[CP_THREADS];
+        fold[t] = pv[0] ? acc[0] : 0.0;
+        __syncthreads();
+        if (t < p.npairs) {
+            double v = 0.0;
+            for (int ph = 0; ph < p.phases; ++ph) v += fold[ph * p.npairs + t];
+            p.partials[(long long)blockIdx.x * p.npairs + t] = v;
+        }
+    } else {
+#pragma unroll
+        for (int s = 0; s < PPT; ++s)
+            if (pv[s]) p.partials[(long long)blockIdx.x * p.npairs + t + s * CP_THREADS] = acc[s];
+    }
+}
+
+__global__ void crossprod_reduce_kernel(const double* __restrict__ partials, int nblocks, int npairs, long long p0,
+                                        int gram, int upper_only, int a, double alpha, double beta, double* out,
+                                        int ldo) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= npairs) return;
+    double v = 0.0;
+    for (int b = 0; b < nblocks; ++b) v += partials[(long long)b * npairs + t];
+    int i, j;
+    pair_ij(p0 + t, gram, a, i, j);
+    double* o = out + i + (long long)j * ldo;
+    *o = alpha * v + (beta != 0.0 ? beta * (*o) : 0.0);
+    if (gram && !upper_only && i != j) {
+        double* o2 = out + j + (long long)i * ldo;
+        *o2 = alpha * v + (beta != 0.0 ? beta * (*o2) : 0.0);
+    }
+}
+
+constexpr int RS_THREADS = 256;
+
+__global__ void __launch_bounds__(RS_THREADS)
+    residual_scores_kernel(const double* __restrict__ X, int C, long long n, const double* __restrict__ beta, int k,
+                           const int* __restrict__ score_cols, int n_score, double* __restrict__ S,
+                           double* __restrict__ resid, double* __restrict__ partials) {
+    __shared__ double red[RS_THREADS / 32];
+    double local = 0.0;
+    long long i = (long long)blockIdx.x * RS_THREADS + threadIdx.x;
+    const long long stride = (long long)gridDim.x * RS_THREADS;
+    for (; i < n; i += stride) {
+        const double* row = X + i * C;
+        double r = row[0];
+        for (int j = 0; j < k; ++j) r -= row[1 + j] * beta[j];
+        if (resid) resid[i] = r;
+        if (S)
+            for (int t = 0; t < n_score; ++t) S[i * n_score + t] = r * row[score_cols[t]];
+        local += r * r;
+    }
+    // fixed-shape tree: warp then block
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) local += __shfl_xor_sync(0xffffffffu, local, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = local;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double v = 0.0;
+        for (int w = 0; w < RS_THREADS / 32; ++w) v += red[w];
+        partials[blockIdx.x] = v;
+    }
+}
+
+__global__ void sum_partials_kernel(const double* __restrict__ partials, int nb, double* out) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        double v = 0.0;
+        for (int b = 0; b < nb; ++b) v += partials[b];
+        *out = v;
+    }
+}
+
+// ---------------------------- dense kernels ------------------------------
+
+constexpr int DN_THREADS = 256;
+
+__global__ void __launch_bounds__(DN_THREADS)
+    chol_solve_inv_kernel(int k, const double* __restrict__ Q, int ldq, const int* __restrict__ idx,
+                          const double* __restrict__ b, double* __restrict__ beta, double* __restrict__ Qinv,
+                          int* __restrict__ info, double* __restrict__ work) {
+    double* U = work;
+    double* Ui = work + (size_t)k * k;
+    __shared__ int s_info;
+    __shared__ double s_d;
+    const int t = threadIdx.x;
+    for (int e = t; e < k * k; e += DN_THREADS) {
+        int i = e % k, j = e / k;
+        int qi = idx ? idx[i] : i, qj = idx ? idx[j] : j;
+        U[e] = Q[qi + (long long)qj * ldq];
+    }
+    if (t == 0) s_info = 0;
+    __syncthreads();
+    for (int j = 0; j < k; ++j) {
+        for (int c = j + t; c < k; c += DN_THREADS) {
+            double v = U[j + c * k];
+            for (int p = 0; p < j; ++p) v -= U[p + j * k] * U[p + c * k];
+            U[j + c * k] = v;
+        }
+        __syncthreads();
+        if (t == 0) {
+            double d = U[j + j * k];
+            if (!(d > 0.0)) {
+                s_info = j + 1;
+            } else {
+                s_d = sqrt(d);
+                U[j + j * k] = s_d;
+            }
+        }
+        __syncthreads();
+        if (s_info) break;
+        for (int c = j + 1 + t; c < k; c += DN_THREADS) U[j + c * k] /= s_d;
+        __syncthreads();
+    }
+    if (s_info) {
+        if (t == 0) *info = s_info;
+        return;
+    }
+    // U^{-1}: column j by thread j (back substitution on the upper factor)
+    for (int j = t; j < k; j += DN_THREADS) {
+        for (int i = 0; i < k; ++i) Ui[i + j * k] = 0.0;
+        Ui[j + j * k] = 1.0 / U[j + j * k];
+        for (int i = j - 1; i >= 0; --i) {
+            double s = 0.0;
+            for (int p = i + 1; p <= j; ++p) s += U[i + p * k] * Ui[p + j * k];
+            Ui[i + j * k] = -s / U[i + i * k];
+        }
+    }
+    __syncthreads();
+    // beta = U^{-1} U^{-T} b_sel, Qinv = U^{-1} U^{-T}
+    for (int e = t; e < k * k; e += DN_THREADS) {
+        int i = e % k, j = e / k;
+        if (i > j) continue;
+        double s = 0.0;
+        for (int p = j; p < k; ++p) s += Ui[i + p * k] * Ui[j + p * k];
+        Qinv[i + j * k] = s;
+        Qinv[j + i * k] = s;
+    }
+    __syncthreads();
+    if (t == 0) {
+        // forward then backward substitution (dpotrs order)
+        for (int i = 0; i < k; ++i) {
+            double v = b[idx ? idx[i] : i];
+            for (int p = 0; p < i; ++p) v -= U[p + i * k] * beta[p];
+            beta[i] = v / U[i + i * k];
+        }
+        for (int i = k - 1; i >= 0; --i) {
+            double v = beta[i];
+            for (int p = i + 1; p < k; ++p) v -= U[i + p * k] * beta[p];
+            beta[i] = v / U[i + i * k];
+        }
+        *info = 0;
+    }
+}
+
+__global__ void gemm_small_kernel(int ta, int tb, int m, int n, int k, double alpha, const double* __restrict__ A,
+                                  int lda, const double* __restrict__ B, int ldb, double beta, double* __restrict__ C,
+                                  int ldc) {
+    long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= (long long)m * n) return;
+    int i = (int)(e % m), j = (int)(e / m);
+    double s = 0.0;
+    for (int p = 0; p < k; ++p) {
+        double av = ta ? A[p + (long long)i * lda] : A[i + (long long)p * lda];
+        double bv = tb ? B[j + (long long)p * ldb] : B[p + (long long)j * ldb];
+        s += av * bv;
+    }
+    double* o = C + i + (long long)j * ldc;
+    *o = alpha * s + (beta != 0.0 ? beta * (*o) : 0.0);
+}
+
+__global__ void select_kernel(int k, const double* __restrict__ M, int ldm, const int* __restrict__ idx,
+                              double* __restrict__ out) {
+    int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= k * k) return;
+    int i = e % k, j = e / k;
+    int mi = idx ? idx[i] : i, mj = idx ? idx[j] : j;
+    out[e] = M[mi + (long long)mj * ldm];
+}
+
+// Parallel cyclic Jacobi on a k x k symmetric matrix A (in place; global
+// memory), eigenvectors accumulated in V; the round-robin pairing makes all
+// rotations of one round touch disjoint rows/columns.
+__device__ void block_jacobi(int k, double* A, double* V) {
+    __shared__ int sp[DN_THREADS], sq[DN_THREADS];
+    __shared__ double sc[DN_THREADS], ss[DN_THREADS];
+    __shared__ double s_off, s_tot;
+    __shared__ double red[DN_THREADS / 32];
+    const int t = threadIdx.x;
+    for (int e = t; e < k * k; e += DN_THREADS) V[e] = (e % k == e / k) ? 1.0 : 0.0;
+    const int kk = (k % 2) ? k + 1 : k;
+    const int m = kk / 2;
+    __syncthreads();
+    for (int sweep = 0; sweep < 60; ++sweep) {
+        double off = 0.0, tot = 0.0;
+        for (int e = t; e < k * k; e += DN_THREADS) {
+            double a = A[e] * A[e];
+            tot += a;
+            if (e % k != e / k) off += a;
+        }
+        for (int pass = 0; pass < 2; ++pass) {
+            double v = pass == 0 ? off : tot;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+            if ((t & 31) == 0) red[t >> 5] = v;
+            __syncthreads();
+            if (t == 0) {
+                double s = 0.0;
+                for (int w = 0; w < DN_THREADS / 32; ++w) s += red[w];
+                if (pass == 0)
+                    s_off = s;
+                else
+                    s_tot = s;
+            }
+            __syncthreads();
+        }
+        if (s_off == 0.0 || s_off <= 1e-30 * (s_tot > 0.0 ? s_tot : 1.0)) break;
+        for (int round = 0; round < kk - 1; ++round) {
+            for (int i = t; i < m; i += DN_THREADS) {
+                int p, q;
+                if (i == 0) {
+                    p = round;
+                    q = kk - 1;
+                } else {
+                    p = (round + i) % (kk - 1);
+                    q = (round - i + (kk - 1)) % (kk - 1);
+                }
+                if (p > q) {
+                    int tmp = p;
+                    p = q;
+                    q = tmp;
+                }
+                double c = 1.0, s = 0.0;
+                if (q < k) {
+                    double apq = A[p + q * k];
+                    if (apq != 0.0) {
+                        double app = A[p + p * k], aqq = A[q + q * k];
+                        double theta = (aqq - app) / (2.0 * apq);
+                        double tt = (theta >= 0.0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
+                        c = 1.0 / sqrt(tt * tt + 1.0);
+                        s = tt * c;
+                    }
+                }
+                sp[i] = p;
+                sq[i] = q;
+                sc[i] = c;
+                ss[i] = s;
+            }
+            __syncthreads();
+            // columns: A <- A J, V <- V J
+            for (int e = t; e < m * k; e += DN_THREADS) {
+                int i = e / k, r = e % k;
+                int p = sp[i], q = sq[i];
+                if (q >= k || ss[i] == 0.0) continue;
+                double c = sc[i], s = ss[i];
+                double arp = A[r + p * k], arq = A[r + q * k];
+                A[r + p * k] = c * arp - s * arq;
+                A[r + q * k] = s * arp + c * arq;
+                double vrp = V[r + p * k], vrq = V[r + q * k];
+                V[r + p * k] = c * vrp - s * vrq;
+                V[r + q * k] = s * vrp + c * vrq;
+            }
+            __syncthreads();
+            // rows: A <- J^T A
+            for (int e = t; e < m * k; e += DN_THREADS) {
+                int i = e / k, col = e % k;
+                int p = sp[i], q = sq[i];
+                if (q >= k || ss[i] == 0.0) continue;
+                double c = sc[i], s = ss[i];
+                double apc = A[p + col * k], aqc = A[q + col * k];
+                A[p + col * k] = c * apc - s * aqc;
+                A[q + col * k] = s * apc + c * aqc;
+            }
+            __syncthreads();
+        }
+    }
+}
+
+__global__ void __launch_bounds__(DN_THREADS)
+    finalize_cov_kernel(int k, double* __restrict__ acc, double scalar, int do_psd, double* __restrict__ se,
+                        int* __restrict__ psd_applied, double* __restrict__ work) {
+    const int t = threadIdx.x;
+    double* A = work;
+    double* V = work + (size_t)k * k;
+    __shared__ int s_applied;
+    if (t == 0) s_applied = 0;
+    for (int e = t; e < k * k; e += DN_THREADS) acc[e] *= scalar;
+    __syncthreads();
+    if (!do_psd) {
+        // 0.5 (A + A^T), as the CPU path does (fe_pipeline.f90:476)
+        for (int e = t; e < k * k; e += DN_THREADS) {
+            int i = e % k, j = e / k;
+            A[e] = 0.5 * (acc[i + j * k] + acc[j + i * k]);
+        }
+        __syncthreads();
+        for (int e = t; e < k * k; e += DN_THREADS) acc[e] = A[e];
+        __syncthreads();
+        for (int i = t; i < k; i += DN_THREADS) se[i] = sqrt(fmax(0.0, acc[i + i * k]));
+        if (t == 0) *psd_applied = 0;
+        return;
+    }
+    // mirror the upper triangle to the lower (fe_pipeline.f90:1366, 1802-1811)
+    for (int e = t; e < k * k; e += DN_THREADS) {
+        int i = e % k, j = e / k;
+        if (i > j) acc[e] = acc[j + i * k];
+    }
+    __syncthreads();
+    for (int e = t; e < k * k; e += DN_THREADS) A[e] = acc[e];
+    __syncthreads();
+    block_jacobi(k, A, V);
+    __syncthreads();
+    // lambda_j = A[j,j]; scale eigenvector columns by sqrt(max(lambda,0))
+    for (int e = t; e < k * k; e += DN_THREADS) {
+        int j = e / k;
+        double lam = A[j + j * k];
+        if (lam < 0.0) {
+            s_applied = 1;
+            lam = 0.0;
+        }
+        V[e] *= lam > 0.0 ? sqrt(lam) : 0.0;
+    }
+    __syncthreads();
+    for (int e = t; e < k * k; e += DN_THREADS) {
+        int i = e % k, j = e / k;
+        double s = 0.0;
+        for (int p = 0; p < k; ++p) s += V[i + p * k] * V[j + p * k];
+        acc[e] = s;
+    }
+    __syncthreads();
+    for (int i = t; i < k; i += DN_THREADS) se[i] = sqrt(fmax(0.0, acc[i + i * k]));
+    if (t == 0) *psd_applied = s_applied;
+}
+
+}  // namespace
+
+int crossprod(const MatView& A, const MatView& B, long long n, bool gram, bool upper_only, double alpha, double beta,
+              double* out, int ldo, cudaStream_t s, Scratch& scr) {
+    const int a = A.cols, b = gram ? A.cols : B.cols;
+    if (a <= 0 || b <= 0) return 0;
+    const long long total_pairs = gram ? (long long)a * (a + 1) / 2 : (long long)a * b;
+    if (n <= 0) {
+        // A^T B over zero rows is the zero matrix
+        for (long long p0 = 0; p0 < total_pairs; p0 += CP_MAXPAIRS_LAUNCH) {
+            int np = (int)std::min<long long>(CP_MAXPAIRS_LAUNCH, total_pairs - p0);
+            double* zeros = nullptr;
+            FEGB_TRY(scr.alloc(&zeros, (size_t)np, "crossprod zeros"));
+            FEGB_CUDA(cudaMemsetAsync(zeros, 0, sizeof(double) * np, s), "crossprod zero");
+            crossprod_reduce_kernel<<<(np + 255) / 256, 256, 0, s>>>(zeros, 1, np, p0, gram, upper_only, a, alpha,
+                                                                      beta, out, ldo);
+            FEGB_LAUNCH_CHECK("crossprod zero reduce");
+        }
+        return 0;
+    }
+    long long nb = std::min<long long>((n + CP_TR - 1) / CP_TR, (long long)num_sms() * 4);
+    long long rpb = (n + nb - 1) / nb;
+    rpb = ((rpb + CP_TR - 1) / CP_TR) * CP_TR;
+    nb = (n + rpb - 1) / rpb;
+    size_t smem = sizeof(double) * CP_TR * (gram ? a : a + b);
+    if (smem > 200 * 1024) return set_error("crossprod: %d x %d columns exceed the shared-memory tile", a, b);
+    static bool attr_done = false;
+    if (!attr_done) {
+        FEGB_CUDA(cudaFuncSetAttribute(crossprod_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024),
+                  "crossprod attr");
+        FEGB_CUDA(cudaFuncSetAttribute(crossprod_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024),
+                  "crossprod attr");
+        FEGB_CUDA(cudaFuncSetAttribute(crossprod_kernel<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024),
+                  "crossprod attr");
+        FEGB_CUDA(cudaFuncSetAttribute(crossprod_kernel<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024),
+                  "crossprod attr");
+        FEGB_CUDA(cudaFuncSetAttribute(crossprod_kernel<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024),
+                  "crossprod attr");
+        attr_done = true;
+    }
+    for (long long p0 = 0; p0 < total_pairs; p0 += CP_MAXPAIRS_LAUNCH) {
+        const int np = (int)std::min<long long>(CP_MAXPAIRS_LAUNCH, total_pairs - p0);
+        double* partials = nullptr;
+        FEGB_TRY(scr.alloc(&partials, (size_t)nb * np, "crossprod partials"));
+        CPParams p;
+        p.A = A.ptr;
+        p.ars = A.rs;
+        p.acs = A.cs;
+        p.a = a;
+        p.B = gram ? A.ptr : B.ptr;
+        p.brs = gram ? A.rs : B.rs;
+        p.bcs = gram ? A.cs : B.cs;
+        p.b = b;
+        p.n = n;
+        p.gram = gram ? 1 : 0;
+        p.p0 = p0;
+        p.npairs = np;
+        p.phases = np <= 128 ? CP_THREADS / np : 1;
+        p.rows_per_block = rpb;
+        p.partials = partials;
+        if (np <= 128)
+            crossprod_kernel<1><<<(unsigned)nb, CP_THREADS, smem, s>>>(p);
+        else if (np <= 4 * CP_THREADS)
+            crossprod_kernel<4><<<(unsigned)nb, CP_THREADS, smem, s>>>(p);
+        else if (np <= 8 * CP_THREADS)
+            crossprod_kernel<8><<<(unsigned)nb, CP_THREADS, smem, s>>>(p);
+        else if (np <= 16 * CP_THREADS)
+            crossprod_kernel<16><<<(unsigned)nb, CP_THREADS, smem, s>>>(p);
+        else
+            crossprod_kernel<32><<<(unsigned)nb, CP_THREADS, smem, s>>>(p);
+        FEGB_LAUNCH_CHECK("crossprod");
+        crossprod_reduce_kernel<<<(np + 255) / 256, 256, 0, s>>>(partials, (int)nb, np, p0, gram, upper_only, a, alpha,
+                                                                  beta, out, ldo);
+        FEGB_LAUNCH_CHECK("crossprod reduce");
+    }
+    return 0;
+}
+
+int residual_scores(const double* X, int C, long long n, const double* beta, int k, const int* score_cols_dev,
+                    int n_score, double* S, double* resid, double* rss_dev, cudaStream_t s, Scratch& scr) {
+    int nb = (int)std::min<long long>((long long)num_sms() * 8, std::max(1LL, (n + RS_THREADS - 1) / RS_THREADS));
+    double* partials = nullptr;
+    FEGB_TRY(scr.alloc(&partials, (size_t)nb, "rss partials"));
+    residual_scores_kernel<<<nb, RS_THREADS, 0, s>>>(X, C, n, beta, k, score_cols_dev, n_score, S, resid, partials);
+    FEGB_LAUNCH_CHECK("residual/scores");
+    sum_partials_kernel<<<1, 32, 0, s>>>(partials, nb, rss_dev);
+    FEGB_LAUNCH_CHECK("rss sum");
+    return 0;
+}
+
+int dense_chol_solve_inv(int k, const double* Q, int ldq, const int* idx_dev, const double* b, double* beta_out,
+                         double* Qinv, int* info_dev, double* work, cudaStream_t s) {
+    if (k <= 0) return 0;
+    chol_solve_inv_kernel<<<1, DN_THREADS, 0, s>>>(k, Q, ldq, idx_dev, b, beta_out, Qinv, info_dev, work);
+    FEGB_LAUNCH_CHECK("cholesky");
+    return 0;
+}
+
+int dense_gemm(bool ta, bool tb, int m, int n, int k, double alpha, const double* A, int lda, const double* B, int ldb,
+               double beta, double* C, int ldc, cudaStream_t s) {
+    long long tot = (long long)m * n;
+    if (tot <= 0) return 0;
+    gemm_small_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C,
+                                                                     ldc);
+    FEGB_LAUNCH_CHECK("small gemm");
+    return 0;
+}
+
+int dense_sandwich_acc(int k, const double* Qinv, const double* M, int ldm, const int* idx_dev, double w, double* acc,
+                       double* work, cudaStream_t s) {
+    if (k <= 0) return 0;
+    double* Ms = work;
+    double* T = work + (size_t)k * k;
+    select_kernel<<<(k * k + 255) / 256, 256, 0, s>>>(k, M, ldm, idx_dev, Ms);
+    FEGB_LAUNCH_CHECK("meat select");
+    FEGB_TRY(dense_gemm(false, false, k, k, k, 1.0, Ms, k, Qinv, k, 0.0, T, k, s));
+    FEGB_TRY(dense_gemm(false, false, k, k, k, w, Qinv, k, T, k, 1.0, acc, k, s));
+    return 0;
+}
+
+int dense_finalize_cov(int k, double* acc, double scalar, int do_psd, double* se_out, int* psd_applied, double* work,
+                       cudaStream_t s) {
+    if (k <= 0) return 0;
+    finalize_cov_kernel<<<1, DN_THREADS, 0, s>>>(k, acc, scalar, do_psd, se_out, psd_applied, work);
+    FEGB_LAUNCH_CHECK("covariance finalize");
+    return 0;
+}
+
+}  // namespace fegb

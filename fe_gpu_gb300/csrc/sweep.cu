@@ -1,0 +1,377 @@
+// Alternating-projection sweep kernels (see sweep.cuh for the scheme).
+#include "sweep.cuh"
+
+#include <type_traits>
+
+namespace fegb {
+
+namespace {
+
+constexpr int SW_THREADS = 256;
+
+struct Geometry {
+    int L;   // lanes per chunk slot (columns handled at once)
+    int P;   // chunk slots per warp
+    int CT;  // column tiles per chunk
+};
+
+inline Geometry geometry(int C) {
+    Geometry g;
+    g.L = C <= 32 ? C : 32;
+    g.P = 32 / g.L;
+    g.CT = (C + g.L - 1) / g.L;
+    return g;
+}
+
+template <typename T>
+struct SweepUnroll {
+    static constexpr int U = sizeof(T) == 4 ? 8 : 4;
+};
+
+template <typename T>
+__global__ void __launch_bounds__(SW_THREADS)
+    seg_sweep_kernel(SegSweepParams<T> p, int L, int P, int CT, long long n_items) {
+    constexpr int U = SweepUnroll<T>::U;
+    constexpr bool kF32 = sizeof(T) == 4;
+    const int lane = threadIdx.x & 31;
+    const long long warp = ((long long)blockIdx.x * SW_THREADS + threadIdx.x) >> 5;
+    const int slot = lane / L;
+    if (slot >= P) return;
+    const long long item = warp * P + slot;
+    if (item >= n_items) return;
+    const int cl = lane - slot * L;
+    const long long q = item / CT;
+    const int C = p.C;
+    const int col = (int)(item - q * CT) * L + cl;
+    const bool col_ok = col < C;
+    const int colc = col_ok ? col : C - 1;
+    const long long j0 = q * (long long)p.R;
+    const long long j1 = min(j0 + (long long)p.R, p.n);
+    const int32_t* __restrict__ gseq = p.gseq;
+    const int32_t* __restrict__ perm = p.perm;
+    T* __restrict__ X = p.X;
+    const int first_g = gseq[j0];
+    const bool before = j0 > 0 && gseq[j0 - 1] == first_g;
+    const int last_g = gseq[j1 - 1];
+    const bool after = j1 < p.n && gseq[j1] == last_g;
+    const int np = p.pend.n;
+
+    int cur = first_g;
+    bool first_run = true;
+    double acc = 0.0;
+    T part = T(0);
+
+    for (long long j = j0; j < j1; j += U) {
+        int g[U];
+        long long row[U];
+        T v[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const long long jj = j + u;
+            const bool ok = jj < j1;
+            g[u] = ok ? gseq[jj] : cur;
+            row[u] = ok ? (perm ? (long long)perm[jj] : jj) : -1;
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) v[u] = row[u] >= 0 ? X[row[u] * p.rs + colc * p.cs] : T(0);
+        for (int e = 0; e < np; ++e) {
+            const int32_t* __restrict__ pg = p.pend.gid[e];
+            const T* __restrict__ tb = p.pend.tab[e];
+#pragma unroll
+            for (int u = 0; u < U; ++u)
+                if (row[u] >= 0) v[u] -= tb[(long long)pg[j + u] * C + colc];
+        }
+        if (p.writeback && col_ok) {
+#pragma unroll
+            for (int u = 0; u < U; ++u)
+                if (row[u] >= 0) X[row[u] * p.rs + col * p.cs] = v[u];
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            if (row[u] < 0) continue;
+            if (g[u] != cur) {
+                if (kF32) {
+                    acc += (double)part;
+                    part = T(0);
+                }
+                if (col_ok) {
+                    const bool is_head = first_run && before;
+                    if (is_head)
+                        p.head[q * C + col] = acc;
+                    else
+                        p.sums[(long long)cur * C + col] = acc;
+                }
+                acc = 0.0;
+                first_run = false;
+                cur = g[u];
+            }
+            if (kF32)
+                part += v[u];
+            else
+                acc += (double)v[u];
+        }
+        if (kF32) {
+            acc += (double)part;
+            part = T(0);
+        }
+    }
+    if (col_ok) {
+        const bool is_head = first_run && before;
+        if (is_head)
+            p.head[q * C + col] = acc;
+        else if (after)
+            p.tail[q * C + col] = acc;
+        else
+            p.sums[(long long)cur * C + col] = acc;
+    }
+}
+
+template <typename T>
+__global__ void smallg_sweep_kernel(SmallGParams<T> p, int P) {
+    constexpr int U = SweepUnroll<T>::U;
+    extern __shared__ double tabs[];
+    const int C = p.C;  // C <= 32, one column per lane
+    const int nwarps = blockDim.x >> 5;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int nslots = nwarps * P;
+    const int GC = p.G * C;
+    for (int i = threadIdx.x; i < nslots * GC; i += blockDim.x) tabs[i] = 0.0;
+    __syncthreads();
+    const int slot = lane / C;
+    if (slot < P) {
+        const int s = warp * P + slot;
+        double* tab = tabs + (long long)s * GC;
+        const int col = lane - slot * C;
+        const long long rb0 = (long long)blockIdx.x * p.rows_per_block;
+        const long long rb1 = min(p.n, rb0 + p.rows_per_block);
+        const long long sc = (p.rows_per_block + nslots - 1) / nslots;
+        const long long r0 = rb0 + (long long)s * sc;
+        const long long r1 = min(rb1, r0 + sc);
+        const int32_t* __restrict__ gid = p.gid;
+        T* __restrict__ X = p.X;
+        const int np = p.pend.n;
+        for (long long j = r0; j < r1; j += U) {
+            int g[U];
+            T v[U];
+            bool ok[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                ok[u] = (j + u) < r1;
+                g[u] = ok[u] ? gid[j + u] : 0;
+                v[u] = ok[u] ? X[(j + u) * C + col] : T(0);
+            }
+            for (int e = 0; e < np; ++e) {
+                const int32_t* __restrict__ pg = p.pend.gid[e];
+                const T* __restrict__ tb = p.pend.tab[e];
+#pragma unroll
+                for (int u = 0; u < U; ++u)
+                    if (ok[u]) v[u] -= tb[(long long)pg[j + u] * C + col];
+            }
+            if (p.writeback) {
+#pragma unroll
+                for (int u = 0; u < U; ++u)
+                    if (ok[u]) X[(j + u) * C + col] = v[u];
+            }
+#pragma unroll
+            for (int u = 0; u < U; ++u)
+                if (ok[u]) tab[g[u] * C + col] += (double)v[u];
+        }
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < GC; e += blockDim.x) {
+        double t = 0.0;
+        for (int s = 0; s < nslots; ++s) t += tabs[(long long)s * GC + e];
+        p.partials[(long long)blockIdx.x * GC + e] = t;
+    }
+}
+
+constexpr int FIN_THREADS = 256;
+
+__global__ void __launch_bounds__(FIN_THREADS) finalize_kernel(FinalizeParams p) {
+    __shared__ double red[FIN_THREADS / 32];
+    __shared__ bool am_last;
+    const long long idx = (long long)blockIdx.x * FIN_THREADS + threadIdx.x;
+    const long long total = (long long)p.G * p.C;
+    double amax = 0.0;
+    if (idx < total) {
+        const int g = (int)(idx / p.C);
+        const int c = (int)(idx - (long long)g * p.C);
+        double sum = 0.0;
+        if (p.partials) {
+            for (int b = 0; b < p.nblocks; ++b) sum += p.partials[(long long)b * total + idx];
+        } else {
+            const int s = p.off[g], e = p.off[g + 1];
+            if (e > s) {
+                const long long qs = s / p.R, qe = (e - 1) / p.R;
+                if (qs == qe) {
+                    sum = p.sums[idx];
+                } else {
+                    sum = p.tail[qs * p.C + c];
+                    for (long long q = qs + 1; q <= qe; ++q) sum += p.head[q * p.C + c];
+                }
+            }
+        }
+        const int cnt = p.counts ? p.counts[g] : 0;
+        if (p.sum_out) p.sum_out[idx] = sum;
+        // reciprocal multiply, as in src/gpu/fe_gpu_runtime.cu:195-200
+        double mean = cnt > 0 ? sum * (1.0 / (double)cnt) : 0.0;
+        if (p.bias) mean += p.bias[idx];
+        if (p.mean_out) p.mean_out[idx] = mean;
+        double mixed = mean;
+        if (p.prev) {
+            const double pv = p.prev[idx];
+            mixed = pv + (*p.relax) * (mean - pv);
+            p.prev[idx] = mixed;
+        }
+        if (p.pend64) {
+            const double np = (p.pend_accumulate ? p.pend64[idx] : 0.0) + mixed;
+            p.pend64[idx] = np;
+            if (p.pend32) p.pend32[idx] = (float)np;
+        } else if (p.pend32) {
+            p.pend32[idx] = (p.pend_accumulate ? p.pend32[idx] : 0.0f) + (float)mixed;
+        }
+        if (p.alpha) p.alpha[idx] += mixed;
+        amax = fabs(mixed);
+    }
+    if (p.change_bits) {
+        amax = warp_max(amax);
+        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = amax;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double m = red[0];
+            for (int w = 1; w < FIN_THREADS / 32; ++w) m = fmax(m, red[w]);
+            atomic_max_nonneg(p.change_bits, m);
+        }
+    }
+    if (p.do_relax_update) {
+        if (threadIdx.x == 0) {
+            __threadfence();
+            unsigned ticket = atomicAdd(p.done_counter, 1u);
+            am_last = (ticket == gridDim.x - 1);
+        }
+        __syncthreads();
+        if (am_last && threadIdx.x == 0) {
+            __threadfence();
+            volatile unsigned long long* cb = p.change_bits;
+            const double cd = bits_dbl(*cb);
+            const double pc = *p.prev_change;
+            double r = *p.relax_rw;
+            if (cd > pc * 1.05)
+                r = fmax(0.4, r * 0.5);
+            else if (cd < pc * 0.8)
+                r = fmin(2.0, r * 1.10);
+            *p.relax_rw = r;
+            *p.prev_change = cd;
+            atomic_max_nonneg(p.max_update_bits, cd);
+            *cb = 0ull;
+            *p.done_counter = 0u;
+        }
+    }
+}
+
+template <typename T>
+__global__ void apply_pending_kernel(T* __restrict__ X, int C, long long n, PendingSet<T> pend) {
+    const long long total = n * (long long)C;
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (; i < total; i += stride) {
+        const long long row = i / C;
+        const int col = (int)(i - row * C);
+        T v = X[i];
+        for (int e = 0; e < pend.n; ++e) v -= pend.tab[e][(long long)pend.gid[e][row] * C + col];
+        X[i] = v;
+    }
+}
+
+__global__ void convert_kernel(const double* __restrict__ src, float* __restrict__ dst, long long n) {
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (; i < n; i += stride) dst[i] = (float)src[i];
+}
+
+constexpr int SMALLG_SMEM_BUDGET = 96 * 1024;
+
+}  // namespace
+
+template <typename T>
+int launch_seg_sweep(const SegSweepParams<T>& p, cudaStream_t s) {
+    if (p.n <= 0) return 0;
+    Geometry g = geometry(p.C);
+    long long nchunks = seg_nchunks(p.n, p.R);
+    long long n_items = nchunks * g.CT;
+    long long warps = (n_items + g.P - 1) / g.P;
+    long long blocks = (warps * 32 + SW_THREADS - 1) / SW_THREADS;
+    seg_sweep_kernel<T><<<(unsigned)blocks, SW_THREADS, 0, s>>>(p, g.L, g.P, g.CT, n_items);
+    FEGB_LAUNCH_CHECK("segment sweep");
+    return 0;
+}
+
+bool smallg_eligible(int G, int C) {
+    if (C > 32 || G <= 0) return false;
+    const int P = 32 / C;
+    return (long long)P * G * C * (long long)sizeof(double) <= SMALLG_SMEM_BUDGET;
+}
+
+int smallg_nblocks(long long n) {
+    long long nb = (long long)num_sms() * 4;
+    long long min_rows = 4096;
+    if (n / nb < min_rows) nb = (n + min_rows - 1) / min_rows;
+    if (nb < 1) nb = 1;
+    return (int)nb;
+}
+
+template <typename T>
+int launch_smallg_sweep(const SmallGParams<T>& p, int nblocks, cudaStream_t s) {
+    if (p.n <= 0) return 0;
+    if (!smallg_eligible(p.G, p.C)) return set_error("small-G sweep: G=%d C=%d not eligible", p.G, p.C);
+    const int P = 32 / p.C;
+    const long long per_warp = (long long)P * p.G * p.C * sizeof(double);
+    int nwarps = (int)(SMALLG_SMEM_BUDGET / per_warp);
+    if (nwarps > 8) nwarps = 8;
+    if (nwarps < 1) nwarps = 1;
+    size_t smem = (size_t)nwarps * per_warp;
+    static bool attr_set[2] = {false, false};
+    const int which = sizeof(T) == 4 ? 1 : 0;
+    if (!attr_set[which]) {
+        FEGB_CUDA(cudaFuncSetAttribute(smallg_sweep_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       SMALLG_SMEM_BUDGET),
+                  "small-G smem attribute");
+        attr_set[which] = true;
+    }
+    smallg_sweep_kernel<T><<<nblocks, nwarps * 32, smem, s>>>(p, P);
+    FEGB_LAUNCH_CHECK("small-G sweep");
+    return 0;
+}
+
+int launch_finalize(const FinalizeParams& p, cudaStream_t s) {
+    long long total = (long long)p.G * p.C;
+    if (total <= 0) return 0;
+    unsigned blocks = (unsigned)((total + FIN_THREADS - 1) / FIN_THREADS);
+    finalize_kernel<<<blocks, FIN_THREADS, 0, s>>>(p);
+    FEGB_LAUNCH_CHECK("finalize");
+    return 0;
+}
+
+template <typename T>
+int launch_apply_pending(T* X, int C, long long n, const PendingSet<T>& pend, cudaStream_t s) {
+    if (pend.n == 0 || n <= 0) return 0;
+    apply_pending_kernel<T><<<grid_stride_blocks(n * C, 256), 256, 0, s>>>(X, C, n, pend);
+    FEGB_LAUNCH_CHECK("apply pending");
+    return 0;
+}
+
+int launch_convert_f64_f32(const double* src, float* dst, long long n, cudaStream_t s) {
+    if (n <= 0) return 0;
+    convert_kernel<<<grid_stride_blocks(n, 256), 256, 0, s>>>(src, dst, n);
+    FEGB_LAUNCH_CHECK("convert");
+    return 0;
+}
+
+template int launch_seg_sweep<double>(const SegSweepParams<double>&, cudaStream_t);
+template int launch_seg_sweep<float>(const SegSweepParams<float>&, cudaStream_t);
+template int launch_smallg_sweep<double>(const SmallGParams<double>&, int, cudaStream_t);
+template int launch_smallg_sweep<float>(const SmallGParams<float>&, int, cudaStream_t);
+template int launch_apply_pending<double>(double*, int, long long, const PendingSet<double>&, cudaStream_t);
+template int launch_apply_pending<float>(float*, int, long long, const PendingSet<float>&, cudaStream_t);
+
+}  // namespace fegb

@@ -1,0 +1,140 @@
+/*
+ * fegb.h -- whole-fit C ABI of the GB300 estimation library (libfegb.so).
+ *
+ * These entry points replace, as one call, the estimation driver that the
+ * reference runs on top of its kernel-level ABI:
+ *   fegb_estimate_host    <- fe_gpu_estimate(cfg, header, host, group_sizes, result)
+ *                            (src/core/fe_pipeline.f90:516-1896) including the
+ *                            upload of src/gpu/fe_gpu_data.f90:41-120
+ *   fegb_estimate_device  <- the same with the dataset already resident on the
+ *                            device (fe_gpu_dataset, src/gpu/fe_gpu_data.f90:23-32)
+ *   fegb_within_transform <- fe_gpu_within_transform (src/gpu/fe_gpu_demean.f90:63-311)
+ *   fegb_cluster_ids      <- fe_build_cluster_ids (src/core/cluster_id_builder.c:271-278)
+ *                            and fe_gpu_build_multi_cluster_ids
+ *                            (src/gpu/fe_gpu_runtime.cu:700-886), bit-identical ids
+ *   fegb_compact_ids      <- relabel_ids (tools/dataframe_to_fe_binary.py:87-94)
+ *   fegb_group_sizes      <- compute_fe_group_sizes (src/core/fe_grouping.f90:11-37)
+ *
+ * Conventions follow the kernel-level ABI in fe_gpu_runtime.h: every call
+ * returns 0 on success or a nonzero status and leaves a message readable with
+ * fe_gpu_runtime_get_last_error(); matrices are column-major FP64 with leading
+ * dimension n; FE and cluster ids are int32 and 1-based. Host FE ids use the
+ * reference host layout fe_ids(n_fe, n): dimension index fastest.
+ */
+#ifndef FEGB_H
+#define FEGB_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FEGB_PREC_FP64 0   /* plain form: FP64 storage and arithmetic throughout */
+#define FEGB_PREC_MIXED 1  /* FP32 correction sweeps inside an FP64 refinement loop */
+
+#define FEGB_DEMEAN_AP 0   /* symmetric over-relaxed alternating projections */
+#define FEGB_DEMEAN_CG 1   /* conjugate gradients on the FE normal equations (--demean-cg) */
+
+#define FEGB_SE_GPU 0      /* conventions of the reference GPU estimator */
+#define FEGB_SE_CPU 1      /* conventions of the reference CPU estimator */
+
+typedef struct fegb_config {
+    double fe_tol;            /* stop when the max group-mean update is below this (default 1e-6) */
+    int fe_max_iter;          /* iteration cap (default 500) */
+    int precision;            /* FEGB_PREC_* */
+    int demean_method;        /* FEGB_DEMEAN_* */
+    int se_convention;        /* FEGB_SE_* */
+    int drop_singletons;      /* 1: drop rows in singleton groups, iterated (off by default) */
+    int n_cluster_dims;       /* entries in cluster_dims */
+    const int* cluster_dims;  /* 1-based FE dimensions for clustered SEs (at most 3 used) */
+    int n_iv_regressors;      /* entries in iv_regressors */
+    const int* iv_regressors; /* 1-based endogenous regressor columns */
+    int n_iv_instruments;     /* entries in iv_instruments (0 = all instrument columns) */
+    const int* iv_instruments;/* 1-based instrument columns */
+    int verbose;
+    void* stream;             /* cudaStream_t to run on; NULL = the library's own stream */
+} fegb_config;
+
+typedef struct fegb_result {
+    int converged;
+    int fe_iterations;        /* iterations of the within-transform */
+    int solver_info;          /* 0 ok; Cholesky minor that failed; -1 all columns dropped */
+    int rank;
+    int dof_model;
+    int dof_fes;
+    long long dof_resid;
+    int is_iv;
+    int n_instruments;
+    int n_cluster_dims_used;
+    int psd_fix_applied;
+    int min_single_cluster;
+    long long n_obs_used;     /* rows after singleton removal */
+    long long n_singletons;   /* rows dropped as singletons */
+    double max_update;        /* final convergence measure */
+    double rss;
+    double tss_total;
+    double tss_within;
+    double r2;
+    double r2_adj;
+    double r2_within;
+    double f_stat;
+    /* instrumentation */
+    int projections;          /* FE projections executed (all precisions) */
+    int outer_iterations;     /* FP64 refinement passes (mixed form) */
+    double demean_bytes;      /* algorithmic bytes of the sweeps: sum over projections of n*(4 + 2*C*s) */
+    double time_h2d;          /* seconds */
+    double time_prep;
+    double time_demean;
+    double time_regression;
+    double time_se;
+    double time_total;
+} fegb_result;
+
+/* Default configuration (tolerance 1e-6, 500 iterations, FP64, AP, GPU conventions). */
+void fegb_config_init(fegb_config* cfg);
+
+/* Whole fit from host arrays: y[n], W[n*k] and Z[n*l] column-major,
+ * fe_ids[n_fe*n] in the reference host layout (dimension fastest).
+ * group_sizes may be NULL (computed as the max id per dimension).
+ * beta and se receive k values. */
+int fegb_estimate_host(const fegb_config* cfg, long long n, int k, int l, int n_fe, const double* y,
+                       const double* W, const double* Z, const int* fe_ids, const int* group_sizes, double* beta,
+                       double* se, fegb_result* result);
+
+/* Whole fit from device arrays: d_y[n], d_W[n*k], d_Z[n*l] (column-major,
+ * leading dimension n) and d_fe_ids[d] = device pointer to n 1-based ids of
+ * dimension d. Device inputs are not modified. beta and se are host arrays. */
+int fegb_estimate_device(const fegb_config* cfg, long long n, int k, int l, int n_fe, const double* d_y,
+                         const double* d_W, const double* d_Z, const int* const* d_fe_ids, const int* group_sizes,
+                         double* beta, double* se, fegb_result* result);
+
+/* Within-transform of device columns in place: d_y[n], d_W[n*k], d_Z[n*l]
+ * (column-major, leading dimension n) against the FE ids d_fe_ids[d].
+ * *converged and *iterations are written on the host. */
+int fegb_within_transform(const fegb_config* cfg, long long n, int k, int l, int n_fe, double* d_y, double* d_W,
+                          double* d_Z, const int* const* d_fe_ids, const int* group_sizes, int* converged,
+                          int* iterations, double* max_update);
+
+/* Multi-way cluster-intersection ids on the device, identical to the
+ * reference builder: d_fe_ids[j] (device, 1-based) for the subset dims,
+ * sizes[j] their group counts. d_out_ids (device, n) receives 1-based ids,
+ * *n_clusters the count. */
+int fegb_cluster_ids(const int* const* d_fe_ids, const int* sizes, int n_dims, long long n, int* d_out_ids,
+                     int* n_clusters);
+
+/* 1-based dense relabelling of raw device codes (rank among sorted distinct values). */
+int fegb_compact_ids(const int* d_raw, long long n, int* d_out, int* n_levels);
+
+/* G_d = max id per dimension over device id arrays; status 1 if an id < 1. */
+int fegb_group_sizes(const int* const* d_fe_ids, int n_fe, long long n, int* sizes);
+
+/* Iterated singleton removal: d_keep (device, n bytes) gets 1 for kept rows. */
+int fegb_drop_singletons(const int* const* d_fe_ids, const int* sizes, int n_fe, long long n, unsigned char* d_keep,
+                         long long* n_dropped);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FEGB_H */

@@ -1,0 +1,377 @@
+#!/usr/bin/env python3
+"""Benchmark of the fixed-effects estimation path on GB300.
+
+One step = one whole fit (FE preparation, within-transform to fe-tol 1e-8,
+normal equations, 3-way clustered SEs) of the workload below, with its inputs
+already resident in HBM. The default workload is the 20M-row worker-firm panel
+(1,000,000 workers x 20 periods, 100,000 firms with Pareto(1.5) sizes, 10%
+switching per period, 8 regressors, FEs worker/firm/time, 3-way clustering),
+fitted in the mixed-precision form; the plain FP64 form is timed beside it.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints one JSON line (rank 0). Under torchrun each rank fits its own replica
+of the panel (weak scaling, no collective on the data path).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+METRIC = "fit time & demean GB/s (of ~8 TB/s): FP32-mixed+batched vs plain FP64 @ tol 1e-8"
+UNIT = "rows/s"
+
+WORKLOADS = {
+    "worker_firm_20M": dict(n_workers=1_000_000, n_firms=100_000, n_periods=20, switch_prob=0.1, n_reg=8,
+                            seed=20261204, desc="1M workers x 20 periods, 100k Pareto(1.5) firms, 10% switching, "
+                                               "8 regressors, FEs worker/firm/time, 3-way clustered SEs"),
+    "worker_firm_150M": dict(n_workers=5_000_000, n_firms=1_000_000, n_periods=30, switch_prob=0.05, n_reg=8,
+                             tenure_sick=True, seed=20261206,
+                             desc="5M workers x 30 periods, 1M Pareto(1.5) firms, 5% mobility, tenure/sick + 6 "
+                                  "regressors, FEs worker/firm/time, 3-way clustered SEs"),
+    "worker_firm_2M": dict(n_workers=100_000, n_firms=10_000, n_periods=20, switch_prob=0.1, n_reg=8,
+                           seed=20261204, desc="small case of the 20M panel for profiling"),
+}
+
+
+def dist_env():
+    return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(
+        os.environ.get("LOCAL_RANK", "0"))
+
+
+def make_panel(name):
+    from fe_gpu_gb300.synth import worker_firm_panel
+
+    w = dict(WORKLOADS[name])
+    w.pop("desc")
+    return worker_firm_panel(**w)
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index: int):
+        self.idx = device_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                                          "-lms", "200", "-i", str(self.idx)], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, power, reasons = [], None, [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+                power.append(float(parts[3]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm), "power_w_max": max(power) if power else None}
+
+
+def measured_hbm_peak():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            v = json.load(f).get("hbm_gbs")
+        if v:
+            return float(v), "measured"
+    except (OSError, ValueError):
+        pass
+    return 6800.0, "fallback"
+
+
+def cpu_baseline(name, threads):
+    """The oracle (C restatement of the reference CPU estimator) on a bounded
+    sample of the workload: the same panel design with 1/5 of the workers and
+    firms (4M rows), fitted with the CPU path's conventions."""
+    from fe_gpu_gb300.synth import worker_firm_panel
+    from oracle import oracle as O
+
+    w = dict(WORKLOADS[name])
+    w.pop("desc")
+    w["n_workers"] = max(1000, w["n_workers"] // 5)
+    w["n_firms"] = max(100, w["n_firms"] // 5)
+    hdr, host = worker_firm_panel(**w)
+    os.environ["OMP_NUM_THREADS"] = str(threads)
+    t0 = time.perf_counter()
+    r = O.cpu_estimate(host.y, host.W, host.fe_ids, tol=1e-8, max_iter=100000, cluster_dims=[1, 2, 3])
+    dt = time.perf_counter() - t0
+    n = host.y.shape[0]
+    return {"value": n / dt, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{n} rows ({w['n_workers']} workers x {w['n_periods']} periods, {w['n_firms']} firms), "
+                      f"whole fit with the reference CPU conventions, {r.stats['fe_iterations']} AP iterations, "
+                      f"{dt:.2f} s", "seconds": dt}
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    threads = os.cpu_count() or 1
+    os.environ["OMP_NUM_THREADS"] = str(threads)
+    vals = []
+    cb = None
+    for i in range(args.warmup + args.steps):
+        cb = cpu_baseline(args.workload, threads)
+        if i >= args.warmup:
+            vals.append(cb["value"])
+    value = float(np.median(vals)) if vals else cb["value"]
+    w = WORKLOADS[args.workload]
+    rows = w["n_workers"] * w["n_periods"]
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": rows / value * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+        "config": {"workload": args.workload, "description": w["desc"], "rows": rows, "fe_tol": 1e-8},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": cb["sample"]},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="worker_firm_20M")
+    ap.add_argument("--precision", choices=["mixed", "fp64"], default="mixed")
+    ap.add_argument("--method", choices=["cg", "ap"], default="cg",
+                    help="within-transform of the headline form (the FP64 comparison always uses AP)")
+    ap.add_argument("--fp64-steps", type=int, default=2, help="timed steps of the plain FP64 form")
+    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile-case", action="store_true",
+                    help="one fit per (precision, method) and exit (for ncu captures)")
+    ap.add_argument("--case", default="all", help="with --profile-case: mixed-cg, fp64-cg, mixed-ap, fp64-ap or all")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+
+    from fe_gpu_gb300 import _native
+    from fe_gpu_gb300.estimator import fe_gpu_estimate, fe_gpu_estimate_device, fe_runtime_config
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    _native.check(_native.lib().fe_gpu_runtime_is_available(), "no CUDA device")
+    stream = torch.cuda.Stream()
+
+    hdr, host = make_panel(args.workload)
+    n, k = host.W.shape
+    n_fe = host.fe_ids.shape[0]
+    dev = torch.device("cuda", local)
+    d_y = torch.from_numpy(host.y).to(dev)
+    d_W = torch.from_numpy(np.ascontiguousarray(host.W.T)).to(dev)  # column-major n x k
+    d_ids = [torch.from_numpy(np.ascontiguousarray(host.fe_ids[d])).to(dev) for d in range(n_fe)]
+    torch.cuda.synchronize()
+
+    def cfg_for(precision, method=None):
+        method = args.method if method is None else method
+        return fe_runtime_config(fe_tolerance=1e-8, fe_max_iterations=100000, cluster_fe_dims=[1, 2, 3],
+                                 precision=precision, demean_cg=(method == "cg"))
+
+    def fit(precision, profile=False, method=None):
+        return fe_gpu_estimate_device(cfg_for(precision, method), n, k, 0, d_y.data_ptr(), d_W.data_ptr(), None,
+                                      [t.data_ptr() for t in d_ids], stream=stream.cuda_stream, profile=profile)
+
+    if args.profile_case:
+        for p, m in (("mixed", "cg"), ("fp64", "cg"), ("mixed", "ap"), ("fp64", "ap")):
+            if args.case != "all" and args.case != f"{p}-{m}":
+                continue
+            r = fit(p, method=m)
+            print(p, m, r.fe_iterations, r.stats["outer_iterations"], r.stats["time_total"], flush=True)
+        return 0
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+
+            dist.barrier()
+
+    def timed(precision, steps, profile, method=None):
+        res = None
+        barrier()
+        torch.cuda.synchronize()
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        launches0 = _native.lib().fegb_kernel_launches()
+        ev0.record(stream)
+        results = []
+        for _ in range(steps):
+            res = fit(precision, profile, method)
+            results.append(res)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        barrier()
+        launches = _native.lib().fegb_kernel_launches() - launches0
+        ms = ev0.elapsed_time(ev1) / steps
+        if world > 1:
+            import torch.distributed as dist
+
+            t = torch.tensor([ms], device=dev)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms = float(t.item())
+        return ms, results, launches
+
+    for _ in range(args.warmup):
+        fit(args.precision)
+    sampler = ClockSampler(local)
+    sampler.start()
+    ms, results, launches = timed(args.precision, args.steps, True)
+    clocks = sampler.stop()
+    last = results[-1]
+
+    # plain FP64 form beside it
+    fp64_ms = None
+    fp64_res = None
+    if args.fp64_steps > 0:
+        fit("fp64", method="ap")
+        fp64_ms, fr, _ = timed("fp64", args.fp64_steps, False, method="ap")
+        fp64_res = fr[-1]
+
+    # end to end through the host-buffer C ABI, inputs in pinned host memory
+    pin_y = torch.empty(n, dtype=torch.float64, pin_memory=True).numpy()
+    pin_y[:] = host.y
+    pin_W = torch.empty(n * k, dtype=torch.float64, pin_memory=True).numpy().reshape(k, n).T
+    pin_W[:] = host.W
+    pin_ids = torch.empty(n * n_fe, dtype=torch.int32, pin_memory=True).numpy().reshape(n, n_fe).T
+    pin_ids[:] = host.fe_ids
+    from fe_gpu_gb300.bin_io import fe_host_arrays
+
+    hp = fe_host_arrays(y=pin_y, W=pin_W, Z=np.zeros((n, 0), order="F"), fe_ids=pin_ids)
+    fe_gpu_estimate(cfg_for(args.precision), hdr, hp, stream=stream.cuda_stream)
+    barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.e2e_steps):
+        er = fe_gpu_estimate(cfg_for(args.precision), hdr, hp, stream=stream.cuda_stream)
+    torch.cuda.synchronize()
+    e2e_s = (time.perf_counter() - t0) / args.e2e_steps
+    if world > 1:
+        import torch.distributed as dist
+
+        t = torch.tensor([e2e_s], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    h2d = pin_y.nbytes + n * k * 8 + n * n_fe * 4
+    d2h = 2 * k * 8
+
+    # roofline of the dominant sweep-kernel family, timed live in the timed steps
+    fam = ["segment sweep fp64", "segment sweep fp32", "small-G sweep fp64", "small-G sweep fp32"]
+    secs = [sum(r.stats["prof_seconds"][i] for r in results) for i in range(4)]
+    nlaunch = [sum(r.stats["prof_launches"][i] for r in results) for i in range(4)]
+    nbytes = [sum(r.stats["prof_bytes"][i] for r in results) for i in range(4)]
+    top = int(np.argmax(secs))
+    peak, peak_kind = measured_hbm_peak()
+    achieved = nbytes[top] / secs[top] / 1e9 if secs[top] > 0 else 0.0
+    traffic_per_launch = TRAFFIC_PER_LAUNCH.get((args.workload, fam[top]))
+    demean_gbs = last.stats["demean_bytes"] / last.stats["time_demean"] / 1e9 if last.stats["time_demean"] else None
+
+    value = world * n / (ms / 1e3)
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32-sweeps+f64" if args.precision == "mixed" else "f64", "data": "synthetic (seeded)",
+        "config": {"workload": args.workload, "description": WORKLOADS[args.workload]["desc"], "rows": n,
+                   "columns": 1 + k, "fe_tol": 1e-8, "precision": args.precision, "within_transform": args.method,
+                   "l2": "inputs larger than L2 (%.2f GB of FP64 data per fit)" % (n * (1 + k) * 8 / 1e9),
+                   "parallelism": f"replicas x{world}"},
+        "fit_time_s": ms / 1e3,
+        "fit_breakdown_s": {key: last.stats[key] for key in ("time_prep", "time_demean", "time_regression",
+                                                              "time_se")},
+        "fe_iterations": last.fe_iterations, "outer_iterations": last.stats["outer_iterations"],
+        "projections": last.stats["projections"],
+        "demean_gbs_algorithmic": demean_gbs,
+        "rows_x_cols_demeaned_per_s": (last.stats["projections"] * n * (1 + k) / last.stats["time_demean"]
+                                       if last.stats["time_demean"] else None),
+        "fp64_ap_fit_time_s": fp64_ms / 1e3 if fp64_ms else None,
+        "fp64_fe_iterations": fp64_res.fe_iterations if fp64_res else None,
+        "speedup_vs_plain_fp64_ap": (fp64_ms / ms) if fp64_ms else None,
+        "beta_max_rel_diff_mixed_vs_fp64": (float(np.max(np.abs(last.beta - fp64_res.beta) /
+                                                         np.abs(fp64_res.beta))) if fp64_res else None),
+        "se_max_rel_diff_mixed_vs_fp64": (float(np.max(np.abs(last.se - fp64_res.se) / np.abs(fp64_res.se)))
+                                          if fp64_res else None),
+        "e2e": {"value": world * n / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "seconds_per_step": e2e_s},
+        "gpu_launches": int(launches / args.steps) * args.steps,
+        "roofline": {"bound": "hbm", "kernel": fam[top], "achieved": achieved, "peak": peak,
+                     "peak_source": peak_kind, "unit": "GB/s", "frac": achieved / peak if peak else None,
+                     "traffic": traffic_per_launch, "launches": nlaunch[top],
+                     "avg_launch_ms": secs[top] / max(1, nlaunch[top]) * 1e3,
+                     "alg_bytes_per_launch": nbytes[top] / max(1, nlaunch[top]),
+                     "all_families": {fam[i]: {"launches": nlaunch[i], "seconds": secs[i],
+                                               "gbs": (nbytes[i] / secs[i] / 1e9) if secs[i] else None}
+                                      for i in range(4)}},
+        "clocks": clocks,
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = {k2: v for k2, v in cpu_baseline(args.workload, os.cpu_count() or 1).items()
+                                if k2 != "seconds"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+    return 0
+
+
+# DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) from
+# the ncu captures summarised under profiles/, scaled to the workload.
+TRAFFIC_PER_LAUNCH: dict = {}
+
+
+if __name__ == "__main__":
+    sys.exit(main())

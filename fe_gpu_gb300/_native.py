@@ -41,6 +41,7 @@ class FegbConfig(C.Structure):
         ("iv_instruments", C.POINTER(C.c_int)),
         ("verbose", C.c_int),
         ("stream", C.c_void_p),
+        ("profile", C.c_int),
     ]
 
 
@@ -77,10 +78,17 @@ class FegbResult(C.Structure):
         ("time_regression", C.c_double),
         ("time_se", C.c_double),
         ("time_total", C.c_double),
+        ("prof_launches", C.c_int * 4),
+        ("prof_seconds", C.c_double * 4),
+        ("prof_bytes", C.c_double * 4),
     ]
 
     def as_dict(self) -> dict:
-        return {name: getattr(self, name) for name, _ in self._fields_}
+        out = {}
+        for name, _ in self._fields_:
+            v = getattr(self, name)
+            out[name] = list(v) if name.startswith("prof_") else v
+        return out
 
 
 class FeGpuDeviceInfo(C.Structure):
@@ -144,6 +152,7 @@ SIGNATURES = {
     "fegb_compact_ids": (_I, [_P, _LL, _P, _IP]),
     "fegb_group_sizes": (_I, [C.POINTER(C.c_void_p), _I, _LL, _IP]),
     "fegb_drop_singletons": (_I, [C.POINTER(C.c_void_p), _IP, _I, _LL, _P, C.POINTER(C.c_longlong)]),
+    "fegb_kernel_launches": (_LL, []),
 }
 
 

@@ -32,9 +32,17 @@ const char* last_error();
         if (_e != cudaSuccess) return ::fegb::set_cuda_error(_e, (ctx));       \
     } while (0)
 
-#define FEGB_LAUNCH_CHECK(ctx) FEGB_CUDA(cudaPeekAtLastError(), (ctx))
+// Counts every kernel launch of the library (each launch site is followed by
+// exactly one FEGB_LAUNCH_CHECK).
+void count_launch();
+#define FEGB_LAUNCH_CHECK(ctx)                                   \
+    do {                                                         \
+        ::fegb::count_launch();                                  \
+        FEGB_CUDA(cudaPeekAtLastError(), (ctx));                 \
+    } while (0)
 
 int num_sms();
+long long launches();
 
 inline unsigned grid_1d(long long n, int threads, long long max_blocks = 1LL << 30) {
     long long b = (n + threads - 1) / threads;

@@ -43,6 +43,8 @@ struct Dim {
     int32_t* off = nullptr;   // G + 1 (contig / gather)
     int32_t* counts = nullptr;
     std::vector<int32_t*> gid_at_perm;  // [e] gid of dim e at traversal positions (gather)
+    int32_t* long_list = nullptr;       // groups spanning more than SEG_LONG_SPAN chunks
+    int n_long = 0;
     double* prev = nullptr;
     double* pend64 = nullptr;
     float* pend32 = nullptr;
@@ -70,10 +72,47 @@ struct Problem {
     double* head = nullptr;
     double* tail = nullptr;
     double* partials = nullptr;
+    // concatenated G-space storage of all dimensions (element (g, c) of dim d at (goff[d] + g) * C + c)
+    long long Gt = 0;
+    std::vector<long long> goff;
+    int32_t* counts_all = nullptr;
+    double* alpha_all = nullptr;
+    double* mu_all = nullptr;
     int smallg_nb = 0;
     int projections = 0;
     double demean_bytes = 0.0;
+    // optional per-launch CUDA-event timing of the sweep kernels
+    bool profile = false;
+    struct Timed {
+        cudaEvent_t a, b;
+        int kind;
+        double bytes;
+    };
+    std::vector<Timed> timed;
+    ~Problem() {
+        for (auto& t : timed) {
+            cudaEventDestroy(t.a);
+            cudaEventDestroy(t.b);
+        }
+    }
 };
+
+// Sums the recorded sweep-launch durations into the result (kind 0..3).
+int collect_profile(Problem& P, fegb_result* res) {
+    if (!P.profile || P.timed.empty()) return 0;
+    FEGB_CUDA(cudaStreamSynchronize(P.s), "profile sync");
+    for (auto& t : P.timed) {
+        float ms = 0.f;
+        FEGB_CUDA(cudaEventElapsedTime(&ms, t.a, t.b), "profile elapsed");
+        res->prof_launches[t.kind] += 1;
+        res->prof_seconds[t.kind] += ms * 1e-3;
+        res->prof_bytes[t.kind] += t.bytes;
+        cudaEventDestroy(t.a);
+        cudaEventDestroy(t.b);
+    }
+    P.timed.clear();
+    return 0;
+}
 
 // ----------------------------- small kernels ------------------------------
 
@@ -304,10 +343,21 @@ int build_problem(Problem& P, long long n_in, int k, int l, int n_fe, const doub
         FEGB_LAUNCH_CHECK("build data block");
     }
     if (mixed) FEGB_TRY(dalloc(scr, &P.Xc, (size_t)n * C, "correction block"));
-    // per-dimension structures
+    // per-dimension structures; group-indexed tables are slices of concatenated arrays
+    P.goff.assign(n_fe + 1, 0);
+    for (int d = 0; d < n_fe; ++d) P.goff[d + 1] = P.goff[d] + std::max(1, G[d]);
+    P.Gt = P.goff[n_fe];
+    FEGB_TRY(dalloc(scr, &P.counts_all, (size_t)std::max(1LL, P.Gt), "counts"));
+    FEGB_TRY(dalloc(scr, &P.alpha_all, (size_t)std::max(1LL, P.Gt) * C, "fe coefficients"));
+    FEGB_TRY(dalloc(scr, &P.mu_all, (size_t)std::max(1LL, P.Gt) * C, "fp64 group means"));
+    FEGB_CUDA(cudaMemsetAsync(P.counts_all, 0, sizeof(int32_t) * (size_t)std::max(1LL, P.Gt), s), "counts zero");
+    FEGB_CUDA(cudaMemsetAsync(P.alpha_all, 0, sizeof(double) * (size_t)std::max(1LL, P.Gt) * C, s), "alpha zero");
     int gmax = 1, gmax_small = 0;
     for (int d = 0; d < n_fe; ++d) {
         Dim& D = P.dims[d];
+        D.counts = P.counts_all + P.goff[d];
+        D.alpha = P.alpha_all + P.goff[d] * C;
+        D.mu = P.mu_all + P.goff[d] * C;
         if (d != P.primary) {
             FEGB_TRY(dalloc(scr, &D.gid, (size_t)n, "gid"));
             if (n > 0) {
@@ -315,7 +365,6 @@ int build_problem(Problem& P, long long n_in, int k, int l, int n_fe, const doub
                 FEGB_LAUNCH_CHECK("gid gather");
             }
         }
-        FEGB_TRY(dalloc(scr, &D.counts, (size_t)std::max(1, D.G), "counts"));
         if (d == P.primary) {
             D.mode = MODE_CONTIG;
             D.gseq = D.gid;
@@ -342,6 +391,8 @@ int build_problem(Problem& P, long long n_in, int k, int l, int n_fe, const doub
             if (D.G > 0) {
                 counts_from_offsets_kernel<<<(D.G + 255) / 256, 256, 0, s>>>(D.off, D.G, D.counts);
                 FEGB_LAUNCH_CHECK("counts");
+                FEGB_TRY(dalloc(scr, &D.long_list, (size_t)D.G, "long groups"));
+                FEGB_TRY(find_long_groups(D.off, D.G, CHUNK_R, D.long_list, &D.n_long, s));
             }
         } else {
             FEGB_CUDA(cudaMemsetAsync(D.counts, 0, sizeof(int32_t) * (size_t)D.G, s), "counts zero");
@@ -355,11 +406,7 @@ int build_problem(Problem& P, long long n_in, int k, int l, int n_fe, const doub
         size_t gc = (size_t)std::max(1, D.G) * C;
         FEGB_TRY(dalloc(scr, &D.prev, gc, "prev means"));
         FEGB_TRY(dalloc(scr, &D.pend64, gc, "pending means"));
-        if (mixed) {
-            FEGB_TRY(dalloc(scr, &D.pend32, gc, "pending means fp32"));
-            FEGB_TRY(dalloc(scr, &D.alpha, gc, "fe increments"));
-            FEGB_TRY(dalloc(scr, &D.mu, gc, "fp64 group means"));
-        }
+        if (mixed) FEGB_TRY(dalloc(scr, &D.pend32, gc, "pending means fp32"));
     }
     for (int d = 0; d < n_fe; ++d) {
         Dim& D = P.dims[d];
@@ -437,7 +484,27 @@ struct ProjectionOpts {
 // Group sums of dimension d over the current residual of `data`, with all
 // pending tables applied; then the finalize epilogue.
 template <typename T>
+int sweep_sums_impl(Problem& P, int d, T* data, const PendingSet<T>& ps, bool writeback);
+
+// One sweep launch (segment or small-G), timed with CUDA events on the fit's
+// stream when profiling is on. Algorithmic bytes per launch: n (4 + 2 C s).
+template <typename T>
 int sweep_sums(Problem& P, int d, T* data, const PendingSet<T>& ps, bool writeback) {
+    if (!P.profile) return sweep_sums_impl<T>(P, d, data, ps, writeback);
+    Problem::Timed t;
+    t.kind = (P.dims[d].mode == MODE_SMALLG ? 2 : 0) + (sizeof(T) == 4 ? 1 : 0);
+    t.bytes = (double)P.n * (4.0 + 2.0 * P.C * sizeof(T));
+    FEGB_CUDA(cudaEventCreate(&t.a), "profile event");
+    FEGB_CUDA(cudaEventCreate(&t.b), "profile event");
+    FEGB_CUDA(cudaEventRecord(t.a, P.s), "profile record");
+    int st = sweep_sums_impl<T>(P, d, data, ps, writeback);
+    FEGB_CUDA(cudaEventRecord(t.b, P.s), "profile record");
+    P.timed.push_back(t);
+    return st;
+}
+
+template <typename T>
+int sweep_sums_impl(Problem& P, int d, T* data, const PendingSet<T>& ps, bool writeback) {
     Dim& D = P.dims[d];
     if (D.mode == MODE_SMALLG) {
         SmallGParams<T> sp{};
@@ -450,7 +517,8 @@ int sweep_sums(Problem& P, int d, T* data, const PendingSet<T>& ps, bool writeba
         sp.writeback = writeback ? 1 : 0;
         sp.rows_per_block = (P.n + P.smallg_nb - 1) / P.smallg_nb;
         sp.partials = P.partials;
-        return launch_smallg_sweep<T>(sp, P.smallg_nb, P.s);
+        FEGB_TRY(launch_smallg_sweep<T>(sp, P.smallg_nb, P.s));
+        return launch_fold_smallg(P.partials, P.smallg_nb, D.G, P.C, P.sums, P.s);
     }
     SegSweepParams<T> sp{};
     sp.X = data;
@@ -466,7 +534,8 @@ int sweep_sums(Problem& P, int d, T* data, const PendingSet<T>& ps, bool writeba
     sp.sums = P.sums;
     sp.head = P.head;
     sp.tail = P.tail;
-    return launch_seg_sweep<T>(sp, P.s);
+    FEGB_TRY(launch_seg_sweep<T>(sp, P.s));
+    return launch_long_sums(D.off, P.head, P.tail, CHUNK_R, P.C, D.long_list, D.n_long, P.sums, P.s);
 }
 
 FinalizeParams finalize_base(const Problem& P, int d) {
@@ -475,8 +544,7 @@ FinalizeParams finalize_base(const Problem& P, int d) {
     f.G = D.G;
     f.C = P.C;
     if (D.mode == MODE_SMALLG) {
-        f.partials = P.partials;
-        f.nblocks = P.smallg_nb;
+        f.sums = P.sums;  // folded by launch_fold_smallg
     } else {
         f.off = D.off;
         f.sums = P.sums;
@@ -694,6 +762,180 @@ int demean_mixed(Problem& P, double tol, int max_iter, int* iterations, int* con
     return 0;
 }
 
+
+// ----------------------- conjugate gradients (alpha space) -----------------------
+
+// Scratch of the CG solve in storage type T.
+template <typename T>
+struct CGBuffers {
+    T *r = nullptr, *z = nullptr, *p = nullptr, *q = nullptr;
+    double *rz = nullptr, *rz_new = nullptr, *pq = nullptr;
+    double *rz_part = nullptr, *pq_part = nullptr;
+    unsigned long long* zmax = nullptr;
+    int rz_blocks = 0, pq_blocks = 0;
+    std::vector<int> pq_block_off;
+};
+
+template <typename T>
+int cg_alloc(Problem& P, CGBuffers<T>& B) {
+    Scratch& scr = *P.scr;
+    const size_t n = (size_t)std::max(1LL, P.Gt) * P.C;
+    FEGB_TRY(dalloc(scr, &B.r, n, "cg r"));
+    FEGB_TRY(dalloc(scr, &B.z, n, "cg z"));
+    FEGB_TRY(dalloc(scr, &B.p, n, "cg p"));
+    FEGB_TRY(dalloc(scr, &B.q, n, "cg q"));
+    FEGB_TRY(dalloc(scr, &B.rz, (size_t)P.C, "cg rz"));
+    FEGB_TRY(dalloc(scr, &B.rz_new, (size_t)P.C, "cg rz new"));
+    FEGB_TRY(dalloc(scr, &B.pq, (size_t)P.C, "cg pq"));
+    FEGB_TRY(dalloc(scr, &B.zmax, 1, "cg zmax"));
+    B.rz_blocks = cg_partial_blocks(P.Gt * P.C);
+    B.pq_block_off.assign(P.n_fe + 1, 0);
+    for (int d = 0; d < P.n_fe; ++d)
+        B.pq_block_off[d + 1] = B.pq_block_off[d] + cg_partial_blocks((long long)std::max(1, P.dims[d].G) * P.C);
+    B.pq_blocks = B.pq_block_off[P.n_fe];
+    FEGB_TRY(dalloc(scr, &B.rz_part, (size_t)B.rz_blocks * P.C, "cg rz partials"));
+    FEGB_TRY(dalloc(scr, &B.pq_part, (size_t)std::max(1, B.pq_blocks) * P.C, "cg pq partials"));
+    FEGB_CUDA(cudaMemsetAsync(B.pq_part, 0, sizeof(double) * (size_t)std::max(1, B.pq_blocks) * P.C, P.s),
+              "cg pq partials zero");
+    return 0;
+}
+
+// q = D'D p, dimension by dimension: a no-data sweep over d's traversal with
+// the other dimensions' p as pending tables, then q_d = counts_d p_d - sums.
+template <typename T>
+int cg_apply(Problem& P, CGBuffers<T>& B) {
+    const int C = P.C;
+    for (int d = 0; d < P.n_fe; ++d) {
+        Dim& D = P.dims[d];
+        if (D.G <= 0) continue;
+        PendingSet<T> ps{};
+        ps.n = 0;
+        for (int e = 0; e < P.n_fe; ++e) {
+            if (e == d) continue;
+            ps.gid[ps.n] = D.mode == MODE_GATHER ? D.gid_at_perm[e] : P.dims[e].gid;
+            ps.tab[ps.n] = B.p + P.goff[e] * C;
+            ++ps.n;
+        }
+        if (D.mode == MODE_SMALLG) {
+            SmallGParams<T> sp{};
+            sp.X = nullptr;
+            sp.C = C;
+            sp.n = P.n;
+            sp.gid = D.gid;
+            sp.G = D.G;
+            sp.pend = ps;
+            sp.writeback = 0;
+            sp.no_data = 1;
+            sp.rows_per_block = (P.n + P.smallg_nb - 1) / P.smallg_nb;
+            sp.partials = P.partials;
+            FEGB_TRY(launch_smallg_sweep<T>(sp, P.smallg_nb, P.s));
+            FEGB_TRY(launch_fold_smallg(P.partials, P.smallg_nb, D.G, C, P.sums, P.s));
+        } else {
+            SegSweepParams<T> sp{};
+            sp.X = nullptr;
+            sp.rs = C;
+            sp.cs = 1;
+            sp.C = C;
+            sp.n = P.n;
+            sp.perm = D.mode == MODE_GATHER ? D.perm : nullptr;
+            sp.gseq = D.gseq;
+            sp.pend = ps;
+            sp.writeback = 0;
+            sp.no_data = 1;
+            sp.R = CHUNK_R;
+            sp.sums = P.sums;
+            sp.head = P.head;
+            sp.tail = P.tail;
+            FEGB_TRY(launch_seg_sweep<T>(sp, P.s));
+            FEGB_TRY(launch_long_sums(D.off, P.head, P.tail, CHUNK_R, C, D.long_list, D.n_long, P.sums, P.s));
+        }
+        FinalizeParams src = finalize_base(P, d);
+        FEGB_TRY(launch_cg_q<T>(src, B.p + P.goff[d] * C, B.q + P.goff[d] * C, B.pq_part + (size_t)B.pq_block_off[d] * C,
+                                P.s));
+        P.projections += 1;
+        P.demean_bytes += (double)P.n * 4.0 * (P.n_fe + (D.mode == MODE_GATHER ? 1 : 0));
+    }
+    return launch_fold_partials(B.pq_part, B.pq_blocks, C, B.pq, P.s);
+}
+
+// Preconditioned (group-count) CG on D'D delta = D'r, r = current FP64
+// residual whose group means are in mu_all; delta accumulates into alpha_all.
+template <typename T>
+int cg_solve(Problem& P, CGBuffers<T>& B, double inner_tol, int max_it, int* iters, double* zmax_out) {
+    const int C = P.C;
+    FEGB_CUDA(cudaMemsetAsync(B.zmax, 0, sizeof(unsigned long long), P.s), "cg zmax reset");
+    FEGB_TRY(launch_cg_init<T>(P.Gt, C, P.counts_all, P.mu_all, B.r, B.z, B.p, B.rz_part, B.zmax, P.s));
+    FEGB_TRY(launch_fold_partials(B.rz_part, B.rz_blocks, C, B.rz, P.s));
+    double best = DBL_MAX;
+    int since_best = 0;
+    int it = 0;
+    double zm = 0.0;
+    for (; it < max_it; ++it) {
+        FEGB_TRY(cg_apply<T>(P, B));
+        FEGB_CUDA(cudaMemsetAsync(B.zmax, 0, sizeof(unsigned long long), P.s), "cg zmax reset");
+        FEGB_TRY(launch_cg_update<T>(P.Gt, C, P.counts_all, B.rz, B.pq, B.p, B.q, P.alpha_all, B.r, B.z, B.rz_part,
+                                     B.zmax, P.s));
+        FEGB_TRY(launch_fold_partials(B.rz_part, B.rz_blocks, C, B.rz_new, P.s));
+        unsigned long long bits = 0;
+        FEGB_TRY(d2h_sync(&bits, B.zmax, sizeof(bits), P.s, "cg zmax copy"));
+        zm = bits_to_double(bits);
+        if (zm < inner_tol) {
+            ++it;
+            break;
+        }
+        if (zm < 0.9 * best) {
+            best = zm;
+            since_best = 0;
+        } else if (++since_best > 60) {
+            ++it;
+            break;  // the recursive residual stopped improving at this precision
+        }
+        FEGB_TRY(launch_cg_direction<T>(P.Gt, C, B.rz, B.rz_new, B.z, B.p, P.s));
+    }
+    *iters = it;
+    *zmax_out = zm;
+    return 0;
+}
+
+// FP64 refinement loop around a CG inner solve in storage type T.
+template <typename T>
+int demean_cg(Problem& P, double tol, int max_iter, int* iterations, int* converged, double* max_update, int* outer) {
+    *iterations = 0;
+    *converged = 1;
+    *max_update = 0.0;
+    *outer = 0;
+    if (P.n_fe == 0 || P.n == 0) return 0;
+    CGBuffers<T> B;
+    FEGB_TRY(cg_alloc<T>(P, B));
+    const int max_outer = 12;
+    double mu = 0.0, mu_prev = DBL_MAX;
+    int total = 0, hit = 0;
+    bool apply_alpha = false;
+    for (int round = 0; round < max_outer; ++round) {
+        FEGB_TRY(fp64_mean_pass(P, apply_alpha, &mu));
+        *outer = round + 1;
+        if (mu < tol) {
+            hit = 1;
+            break;
+        }
+        if (total >= max_iter) break;
+        if (round > 2 && mu > 0.5 * mu_prev) break;
+        mu_prev = mu;
+        FEGB_CUDA(cudaMemsetAsync(P.alpha_all, 0, sizeof(double) * (size_t)P.Gt * P.C, P.s), "alpha zero");
+        const double inner_tol =
+            sizeof(T) == 4 ? std::max(0.5 * tol, 2e-6 * mu) : std::max(0.5 * tol, 1e-12 * mu);
+        int it = 0;
+        double zm = 0.0;
+        FEGB_TRY(cg_solve<T>(P, B, inner_tol, max_iter - total, &it, &zm));
+        total += it;
+        apply_alpha = true;
+    }
+    *iterations = total;
+    *converged = hit;
+    *max_update = mu;
+    return 0;
+}
+
 // ------------------------------ estimator ---------------------------------
 
 struct Stats {
@@ -798,6 +1040,11 @@ int cluster_score_sums(Problem& P, const double* S, int ns, const int32_t* perm,
     sp.head = head;
     sp.tail = tail;
     FEGB_TRY(launch_seg_sweep<double>(sp, P.s));
+    int32_t* long_list = nullptr;
+    int n_long = 0;
+    FEGB_TRY(scr.alloc(&long_list, (size_t)std::max(1, n_cl), "score long groups"));
+    FEGB_TRY(find_long_groups(off, n_cl, CHUNK_R, long_list, &n_long, P.s));
+    FEGB_TRY(launch_long_sums(off, head, tail, CHUNK_R, ns, long_list, n_long, sums, P.s));
     counts_from_offsets_kernel<<<(n_cl + 255) / 256, 256, 0, P.s>>>(off, n_cl, cnt);
     FEGB_LAUNCH_CHECK("score counts");
     FinalizeParams f{};
@@ -848,12 +1095,19 @@ int estimate_on_problem(Problem& P, const fegb_config& cfg, const int* G_all, lo
     auto t0 = Clock::now();
     int iters = 0, conv = 1, outer = 0;
     double mu = 0.0;
-    if (cfg.precision == FEGB_PREC_MIXED)
+    if (cfg.demean_method == FEGB_DEMEAN_CG) {
+        if (cfg.precision == FEGB_PREC_MIXED)
+            FEGB_TRY(demean_cg<float>(P, cfg.fe_tol, cfg.fe_max_iter, &iters, &conv, &mu, &outer));
+        else
+            FEGB_TRY(demean_cg<double>(P, cfg.fe_tol, cfg.fe_max_iter, &iters, &conv, &mu, &outer));
+    } else if (cfg.precision == FEGB_PREC_MIXED) {
         FEGB_TRY(demean_mixed(P, cfg.fe_tol, cfg.fe_max_iter, &iters, &conv, &mu, &outer));
-    else
+    } else {
         FEGB_TRY(demean_plain(P, cfg.fe_tol, cfg.fe_max_iter, &iters, &conv, &mu));
+    }
     FEGB_CUDA(cudaStreamSynchronize(s), "demean sync");
     tm.demean = seconds_since(t0);
+    FEGB_TRY(collect_profile(P, res));
     res->converged = conv;
     res->fe_iterations = iters;
     res->max_update = mu;
@@ -1201,11 +1455,12 @@ int estimate_device_impl(const fegb_config* cfg_in, long long n, int k, int l, i
     Problem P;
     P.s = s;
     P.scr = &scr;
+    P.profile = cfg.profile != 0;
     FitTimes tm;
     auto t0 = Clock::now();
     long long n_single = 0;
     FEGB_TRY(build_problem(P, n, k, l, n_fe, y, W, Z, ids, group_sizes, cfg.drop_singletons != 0,
-                           cfg.precision == FEGB_PREC_MIXED, &n_single));
+                           cfg.precision == FEGB_PREC_MIXED && cfg.demean_method == FEGB_DEMEAN_AP, &n_single));
     std::vector<int> G(n_fe);
     for (int d = 0; d < n_fe; ++d) G[d] = P.dims[d].G;
     // TSS of the raw y over the rows used
@@ -1318,13 +1573,19 @@ int fegb_within_transform(const fegb_config* cfg_in, long long n, int k, int l, 
     for (int d = 0; d < n_fe; ++d) ids[d] = d_fe_ids[d];
     long long n_single = 0;
     FEGB_TRY(build_problem(P, n, k, l, n_fe, d_y, d_W, d_Z, ids.data(), group_sizes, false,
-                           cfg.precision == FEGB_PREC_MIXED, &n_single));
+                           cfg.precision == FEGB_PREC_MIXED && cfg.demean_method == FEGB_DEMEAN_AP, &n_single));
     int it = 0, conv = 1, outer = 0;
     double mu = 0.0;
-    if (cfg.precision == FEGB_PREC_MIXED)
+    if (cfg.demean_method == FEGB_DEMEAN_CG) {
+        if (cfg.precision == FEGB_PREC_MIXED)
+            FEGB_TRY(demean_cg<float>(P, cfg.fe_tol, cfg.fe_max_iter, &it, &conv, &mu, &outer));
+        else
+            FEGB_TRY(demean_cg<double>(P, cfg.fe_tol, cfg.fe_max_iter, &it, &conv, &mu, &outer));
+    } else if (cfg.precision == FEGB_PREC_MIXED) {
         FEGB_TRY(demean_mixed(P, cfg.fe_tol, cfg.fe_max_iter, &it, &conv, &mu, &outer));
-    else
+    } else {
         FEGB_TRY(demean_plain(P, cfg.fe_tol, cfg.fe_max_iter, &it, &conv, &mu));
+    }
     if (n > 0) {
         int TR = std::max(1, std::min(64, 24576 / (8 * P.C)));
         size_t smem = sizeof(double) * (size_t)TR * P.C;

@@ -2,12 +2,14 @@
 // clustering and demeaning entry points with the reference's signatures and
 // status convention, implemented on this library's deterministic kernels.
 #include "fe_gpu_runtime.h"
+#include "fegb.h"
 #include "common.cuh"
 #include "linalg.cuh"
 #include "prep.cuh"
 #include "sweep.cuh"
 
 #include <algorithm>
+#include <atomic>
 #include <cstdarg>
 #include <cstring>
 #include <mutex>
@@ -42,6 +44,13 @@ int set_cuda_error(cudaError_t err, const char* context) {
 }
 
 const char* last_error() { return g_last_error; }
+
+namespace {
+std::atomic<long long> g_launches{0};
+}
+
+void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+long long launches() { return g_launches.load(std::memory_order_relaxed); }
 
 int num_sms() {
     static int cached_dev = -1;
@@ -207,6 +216,11 @@ int grouped_sums(const double* X, long long rs, long long cs, int C, const Sorte
     sp.head = head;
     sp.tail = tail;
     FEGB_TRY(launch_seg_sweep<double>(sp, kLegacy));
+    int32_t* long_list = nullptr;
+    int n_long = 0;
+    FEGB_TRY(scr.alloc(&long_list, (size_t)G, "long groups"));
+    FEGB_TRY(find_long_groups(si.off, G, R, long_list, &n_long, kLegacy));
+    FEGB_TRY(launch_long_sums(si.off, head, tail, R, C, long_list, n_long, sums, kLegacy));
     FinalizeParams f{};
     f.G = G;
     f.C = C;
@@ -322,6 +336,8 @@ int d2h(void* dst, const void* src, size_t bytes, const char* what) {
 using namespace fegb;
 
 extern "C" {
+
+long long fegb_kernel_launches(void) { return fegb::launches(); }
 
 int fe_gpu_runtime_is_available(void) {
     int count = 0;

@@ -72,8 +72,13 @@ __global__ void __launch_bounds__(SW_THREADS)
             g[u] = ok ? gseq[jj] : cur;
             row[u] = ok ? (perm ? (long long)perm[jj] : jj) : -1;
         }
+        if (p.no_data) {
 #pragma unroll
-        for (int u = 0; u < U; ++u) v[u] = row[u] >= 0 ? X[row[u] * p.rs + colc * p.cs] : T(0);
+            for (int u = 0; u < U; ++u) v[u] = T(0);
+        } else {
+#pragma unroll
+            for (int u = 0; u < U; ++u) v[u] = row[u] >= 0 ? X[row[u] * p.rs + colc * p.cs] : T(0);
+        }
         for (int e = 0; e < np; ++e) {
             const int32_t* __restrict__ pg = p.pend.gid[e];
             const T* __restrict__ tb = p.pend.tab[e];
@@ -81,7 +86,7 @@ __global__ void __launch_bounds__(SW_THREADS)
             for (int u = 0; u < U; ++u)
                 if (row[u] >= 0) v[u] -= tb[(long long)pg[j + u] * C + colc];
         }
-        if (p.writeback && col_ok) {
+        if (p.writeback && col_ok && !p.no_data) {
 #pragma unroll
             for (int u = 0; u < U; ++u)
                 if (row[u] >= 0) X[row[u] * p.rs + col * p.cs] = v[u];
@@ -158,7 +163,7 @@ __global__ void smallg_sweep_kernel(SmallGParams<T> p, int P) {
             for (int u = 0; u < U; ++u) {
                 ok[u] = (j + u) < r1;
                 g[u] = ok[u] ? gid[j + u] : 0;
-                v[u] = ok[u] ? X[(j + u) * C + col] : T(0);
+                v[u] = (ok[u] && !p.no_data) ? X[(j + u) * C + col] : T(0);
             }
             for (int e = 0; e < np; ++e) {
                 const int32_t* __restrict__ pg = p.pend.gid[e];
@@ -167,7 +172,7 @@ __global__ void smallg_sweep_kernel(SmallGParams<T> p, int P) {
                 for (int u = 0; u < U; ++u)
                     if (ok[u]) v[u] -= tb[(long long)pg[j + u] * C + col];
             }
-            if (p.writeback) {
+            if (p.writeback && !p.no_data) {
 #pragma unroll
                 for (int u = 0; u < U; ++u)
                     if (ok[u]) X[(j + u) * C + col] = v[u];
@@ -187,6 +192,29 @@ __global__ void smallg_sweep_kernel(SmallGParams<T> p, int P) {
 
 constexpr int FIN_THREADS = 256;
 
+// Group sum (g, c) from a finalize source: small-G block partials in block
+// order, or a segment run / chunk-edge partials in chunk order.
+__device__ __forceinline__ double source_sum(const FinalizeParams& p, int g, int c, long long idx, long long total) {
+    double sum = 0.0;
+    if (p.partials) {
+        for (int b = 0; b < p.nblocks; ++b) sum += p.partials[(long long)b * total + idx];
+    } else if (!p.off) {
+        sum = p.sums[idx];
+    } else {
+        const int s = p.off[g], e = p.off[g + 1];
+        if (e > s) {
+            const long long qs = s / p.R, qe = (e - 1) / p.R;
+            if (qs == qe || qe - qs > SEG_LONG_SPAN) {
+                sum = p.sums[idx];  // complete run, or folded by launch_long_sums
+            } else {
+                sum = p.tail[qs * p.C + c];
+                for (long long q = qs + 1; q <= qe; ++q) sum += p.head[q * p.C + c];
+            }
+        }
+    }
+    return sum;
+}
+
 __global__ void __launch_bounds__(FIN_THREADS) finalize_kernel(FinalizeParams p) {
     __shared__ double red[FIN_THREADS / 32];
     __shared__ bool am_last;
@@ -196,21 +224,7 @@ __global__ void __launch_bounds__(FIN_THREADS) finalize_kernel(FinalizeParams p)
     if (idx < total) {
         const int g = (int)(idx / p.C);
         const int c = (int)(idx - (long long)g * p.C);
-        double sum = 0.0;
-        if (p.partials) {
-            for (int b = 0; b < p.nblocks; ++b) sum += p.partials[(long long)b * total + idx];
-        } else {
-            const int s = p.off[g], e = p.off[g + 1];
-            if (e > s) {
-                const long long qs = s / p.R, qe = (e - 1) / p.R;
-                if (qs == qe) {
-                    sum = p.sums[idx];
-                } else {
-                    sum = p.tail[qs * p.C + c];
-                    for (long long q = qs + 1; q <= qe; ++q) sum += p.head[q * p.C + c];
-                }
-            }
-        }
+        const double sum = source_sum(p, g, c, idx, total);
         const int cnt = p.counts ? p.counts[g] : 0;
         if (p.sum_out) p.sum_out[idx] = sum;
         // reciprocal multiply, as in src/gpu/fe_gpu_runtime.cu:195-200
@@ -287,6 +301,194 @@ __global__ void convert_kernel(const double* __restrict__ src, float* __restrict
     long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const long long stride = (long long)gridDim.x * blockDim.x;
     for (; i < n; i += stride) dst[i] = (float)src[i];
+}
+
+
+// Per-block, per-column partial sums of prod over a block's elements
+// (element idx has column idx % C); fixed order, deterministic.
+__device__ __forceinline__ void column_partials(double prod, long long base, int C, double* smem, double* out) {
+    smem[threadIdx.x] = prod;
+    __syncthreads();
+    if (threadIdx.x < C) {
+        const int c = threadIdx.x;
+        const int first = (int)((c - base % C + C) % C);
+        double acc = 0.0;
+        for (int j = first; j < FIN_THREADS; j += C) acc += smem[j];
+        out[(long long)blockIdx.x * C + c] = acc;
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(FIN_THREADS) cg_q_kernel(FinalizeParams src, const T* __restrict__ p,
+                                                            T* __restrict__ q, double* __restrict__ pq_partials) {
+    __shared__ double smem[FIN_THREADS];
+    const long long total = (long long)src.G * src.C;
+    const long long base = (long long)blockIdx.x * FIN_THREADS;
+    const long long idx = base + threadIdx.x;
+    double prod = 0.0;
+    if (idx < total) {
+        const int g = (int)(idx / src.C);
+        const int c = (int)(idx - (long long)g * src.C);
+        const double ssum = source_sum(src, g, c, idx, total);
+        const double pv = (double)p[idx];
+        // ssum = -(sum over the group's rows of the other dimensions' p)
+        const double qv = (double)src.counts[g] * pv - ssum;
+        q[idx] = (T)qv;
+        prod = pv * qv;
+    }
+    column_partials(prod, base, src.C, smem, pq_partials);
+}
+
+// Fixed-shape block tree: thread t folds elements t, t + 256, ... in order,
+// then a fixed pairwise tree over the 256 thread sums.
+__device__ __forceinline__ double block_tree_sum(double v, double* smem) {
+    smem[threadIdx.x] = v;
+    __syncthreads();
+    for (int w = FIN_THREADS / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) smem[threadIdx.x] += smem[threadIdx.x + w];
+        __syncthreads();
+    }
+    double r = smem[0];
+    __syncthreads();
+    return r;
+}
+
+// out[c] = fold over b of partials[b * C + c]; one block per column.
+__global__ void __launch_bounds__(FIN_THREADS)
+    fold_partials_kernel(const double* __restrict__ partials, int nb, int C, double* __restrict__ out) {
+    __shared__ double smem[FIN_THREADS];
+    const int c = blockIdx.x;
+    double acc = 0.0;
+    for (int b = threadIdx.x; b < nb; b += FIN_THREADS) acc += partials[(long long)b * C + c];
+    double t = block_tree_sum(acc, smem);
+    if (threadIdx.x == 0) out[c] = t;
+}
+
+// One block per long group: tail of its first chunk plus the heads of the
+// following chunks, for every column.
+__global__ void __launch_bounds__(FIN_THREADS)
+    long_sums_kernel(const int32_t* __restrict__ off, const double* __restrict__ head,
+                     const double* __restrict__ tail, int R, int C, const int32_t* __restrict__ list,
+                     double* __restrict__ sums) {
+    __shared__ double smem[FIN_THREADS];
+    const int g = list[blockIdx.x];
+    const long long qs = off[g] / R, qe = (off[g + 1] - 1) / R;
+    for (int c = 0; c < C; ++c) {
+        double acc = 0.0;
+        for (long long q = qs + 1 + threadIdx.x; q <= qe; q += FIN_THREADS) acc += head[q * C + c];
+        double t = block_tree_sum(acc, smem);
+        if (threadIdx.x == 0) sums[(long long)g * C + c] = tail[qs * C + c] + t;
+    }
+}
+
+// One warp per (g, c): strided fold over the block partials, then a fixed
+// shuffle tree.
+__global__ void fold_smallg_kernel(const double* __restrict__ partials, int nblocks, long long GC,
+                                   double* __restrict__ sums) {
+    const long long w = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (w >= GC) return;
+    double acc = 0.0;
+    for (int b = lane; b < nblocks; b += 32) acc += partials[(long long)b * GC + w];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+    if (lane == 0) sums[w] = acc;
+}
+
+__global__ void find_long_kernel(const int32_t* __restrict__ off, int G, int R, int32_t* __restrict__ list,
+                                 int* __restrict__ count) {
+    int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= G) return;
+    const int s = off[g], e = off[g + 1];
+    if (e > s && (long long)((e - 1) / R) - (long long)(s / R) > SEG_LONG_SPAN) list[atomicAdd(count, 1)] = g;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(FIN_THREADS)
+    cg_update_kernel(long long Gt, int C, const int32_t* __restrict__ counts, const double* __restrict__ rz,
+                     const double* __restrict__ pq, const T* __restrict__ p, const T* __restrict__ q,
+                     double* __restrict__ alpha, T* __restrict__ r, T* __restrict__ z,
+                     double* __restrict__ rz_partials, unsigned long long* __restrict__ zmax) {
+    __shared__ double smem[FIN_THREADS];
+    __shared__ double red[FIN_THREADS / 32];
+    const long long total = Gt * C;
+    const long long base = (long long)blockIdx.x * FIN_THREADS;
+    const long long idx = base + threadIdx.x;
+    double prod = 0.0, az = 0.0;
+    if (idx < total) {
+        const long long g = idx / C;
+        const int c = (int)(idx - g * C);
+        const double den = pq[c];
+        const double a = den != 0.0 ? rz[c] / den : 0.0;
+        alpha[idx] += a * (double)p[idx];
+        const double rv = (double)r[idx] - a * (double)q[idx];
+        const int cnt = counts[g];
+        const double zv = cnt > 0 ? rv / (double)cnt : 0.0;
+        r[idx] = (T)rv;
+        z[idx] = (T)zv;
+        prod = rv * zv;
+        az = fabs(zv);
+    }
+    column_partials(prod, base, C, smem, rz_partials);
+    az = warp_max(az);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = az;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double m = red[0];
+        for (int w = 1; w < FIN_THREADS / 32; ++w) m = fmax(m, red[w]);
+        atomic_max_nonneg(zmax, m);
+    }
+}
+
+template <typename T>
+__global__ void cg_direction_kernel(long long Gt, int C, const double* __restrict__ rz_old,
+                                    const double* __restrict__ rz_new, const T* __restrict__ z, T* __restrict__ p) {
+    const long long total = Gt * C;
+    long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long st = (long long)gridDim.x * blockDim.x;
+    for (; idx < total; idx += st) {
+        const int c = (int)(idx % C);
+        const double b = rz_old[c] != 0.0 ? rz_new[c] / rz_old[c] : 0.0;
+        p[idx] = (T)((double)z[idx] + b * (double)p[idx]);
+    }
+}
+
+__global__ void copy_scalars_kernel(const double* __restrict__ src, double* __restrict__ dst, int C) {
+    const int c = threadIdx.x;
+    if (c < C) dst[c] = src[c];
+}
+
+template <typename T>
+__global__ void __launch_bounds__(FIN_THREADS)
+    cg_init_kernel(long long Gt, int C, const int32_t* __restrict__ counts, const double* __restrict__ mu,
+                   T* __restrict__ r, T* __restrict__ z, T* __restrict__ p, double* __restrict__ rz_partials,
+                   unsigned long long* __restrict__ zmax) {
+    __shared__ double smem[FIN_THREADS];
+    __shared__ double red[FIN_THREADS / 32];
+    const long long total = Gt * C;
+    const long long base = (long long)blockIdx.x * FIN_THREADS;
+    const long long idx = base + threadIdx.x;
+    double prod = 0.0, az = 0.0;
+    if (idx < total) {
+        const long long g = idx / C;
+        const int cnt = counts[g];
+        const double m = cnt > 0 ? mu[idx] : 0.0;
+        const double rv = (double)cnt * m;
+        r[idx] = (T)rv;
+        z[idx] = (T)m;
+        p[idx] = (T)m;
+        prod = rv * m;
+        az = fabs(m);
+    }
+    column_partials(prod, base, C, smem, rz_partials);
+    az = warp_max(az);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = az;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double mm = red[0];
+        for (int w = 1; w < FIN_THREADS / 32; ++w) mm = fmax(mm, red[w]);
+        atomic_max_nonneg(zmax, mm);
+    }
 }
 
 constexpr int SMALLG_SMEM_BUDGET = 96 * 1024;
@@ -366,6 +568,104 @@ int launch_convert_f64_f32(const double* src, float* dst, long long n, cudaStrea
     FEGB_LAUNCH_CHECK("convert");
     return 0;
 }
+
+
+int cg_partial_blocks(long long gc) { return (int)((gc + FIN_THREADS - 1) / FIN_THREADS); }
+
+template <typename T>
+int launch_cg_q(const FinalizeParams& src, const T* p, T* q, double* pq_partials, cudaStream_t s) {
+    long long total = (long long)src.G * src.C;
+    if (total <= 0) return 0;
+    cg_q_kernel<T><<<cg_partial_blocks(total), FIN_THREADS, 0, s>>>(src, p, q, pq_partials);
+    FEGB_LAUNCH_CHECK("cg q");
+    return 0;
+}
+
+int launch_fold_partials(const double* partials, int nb, int C, double* out, cudaStream_t s) {
+    fold_partials_kernel<<<C, FIN_THREADS, 0, s>>>(partials, nb, C, out);
+    FEGB_LAUNCH_CHECK("fold partials");
+    return 0;
+}
+
+int find_long_groups(const int32_t* off, int G, int R, int32_t* list, int* n_long, cudaStream_t s) {
+    *n_long = 0;
+    if (G <= 0) return 0;
+    int* cnt = nullptr;
+    FEGB_CUDA(cudaMallocAsync(&cnt, sizeof(int), s), "long groups counter");
+    FEGB_CUDA(cudaMemsetAsync(cnt, 0, sizeof(int), s), "long groups reset");
+    find_long_kernel<<<(G + 255) / 256, 256, 0, s>>>(off, G, R, list, cnt);
+    FEGB_LAUNCH_CHECK("find long groups");
+    FEGB_CUDA(cudaMemcpyAsync(n_long, cnt, sizeof(int), cudaMemcpyDeviceToHost, s), "long groups count");
+    FEGB_CUDA(cudaFreeAsync(cnt, s), "long groups free");
+    FEGB_CUDA(cudaStreamSynchronize(s), "long groups sync");
+    return 0;
+}
+
+int launch_long_sums(const int32_t* off, const double* head, const double* tail, int R, int C, const int32_t* list,
+                     int n_long, double* sums, cudaStream_t s) {
+    if (n_long <= 0) return 0;
+    long_sums_kernel<<<n_long, FIN_THREADS, 0, s>>>(off, head, tail, R, C, list, sums);
+    FEGB_LAUNCH_CHECK("long group sums");
+    return 0;
+}
+
+int launch_fold_smallg(const double* partials, int nblocks, int G, int C, double* sums, cudaStream_t s) {
+    long long GC = (long long)G * C;
+    if (GC <= 0) return 0;
+    fold_smallg_kernel<<<(unsigned)((GC * 32 + 255) / 256), 256, 0, s>>>(partials, nblocks, GC, sums);
+    FEGB_LAUNCH_CHECK("fold small-G partials");
+    return 0;
+}
+
+template <typename T>
+int launch_cg_update(long long Gt, int C, const int32_t* counts, const double* rz, const double* pq, const T* p,
+                     const T* q, double* alpha, T* r, T* z, double* rz_partials, unsigned long long* zmax,
+                     cudaStream_t s) {
+    long long total = Gt * C;
+    if (total <= 0) return 0;
+    cg_update_kernel<T><<<cg_partial_blocks(total), FIN_THREADS, 0, s>>>(Gt, C, counts, rz, pq, p, q, alpha, r, z,
+                                                                         rz_partials, zmax);
+    FEGB_LAUNCH_CHECK("cg update");
+    return 0;
+}
+
+template <typename T>
+int launch_cg_direction(long long Gt, int C, double* rz_old, const double* rz_new, const T* z, T* p, cudaStream_t s) {
+    long long total = Gt * C;
+    if (total > 0) {
+        cg_direction_kernel<T><<<grid_stride_blocks(total, 256), 256, 0, s>>>(Gt, C, rz_old, rz_new, z, p);
+        FEGB_LAUNCH_CHECK("cg direction");
+    }
+    copy_scalars_kernel<<<1, ((C + 31) / 32) * 32, 0, s>>>(rz_new, rz_old, C);
+    FEGB_LAUNCH_CHECK("cg scalars");
+    return 0;
+}
+
+template <typename T>
+int launch_cg_init(long long Gt, int C, const int32_t* counts, const double* mu, T* r, T* z, T* p,
+                   double* rz_partials, unsigned long long* zmax, cudaStream_t s) {
+    long long total = Gt * C;
+    if (total <= 0) return 0;
+    cg_init_kernel<T><<<cg_partial_blocks(total), FIN_THREADS, 0, s>>>(Gt, C, counts, mu, r, z, p, rz_partials, zmax);
+    FEGB_LAUNCH_CHECK("cg init");
+    return 0;
+}
+
+template int launch_cg_q<double>(const FinalizeParams&, const double*, double*, double*, cudaStream_t);
+template int launch_cg_q<float>(const FinalizeParams&, const float*, float*, double*, cudaStream_t);
+template int launch_cg_update<double>(long long, int, const int32_t*, const double*, const double*, const double*,
+                                      const double*, double*, double*, double*, double*, unsigned long long*,
+                                      cudaStream_t);
+template int launch_cg_update<float>(long long, int, const int32_t*, const double*, const double*, const float*,
+                                     const float*, double*, float*, float*, double*, unsigned long long*,
+                                     cudaStream_t);
+template int launch_cg_direction<double>(long long, int, double*, const double*, const double*, double*,
+                                         cudaStream_t);
+template int launch_cg_direction<float>(long long, int, double*, const double*, const float*, float*, cudaStream_t);
+template int launch_cg_init<double>(long long, int, const int32_t*, const double*, double*, double*, double*,
+                                    double*, unsigned long long*, cudaStream_t);
+template int launch_cg_init<float>(long long, int, const int32_t*, const double*, float*, float*, float*, double*,
+                                   unsigned long long*, cudaStream_t);
 
 template int launch_seg_sweep<double>(const SegSweepParams<double>&, cudaStream_t);
 template int launch_seg_sweep<float>(const SegSweepParams<float>&, cudaStream_t);

@@ -50,6 +50,7 @@ struct SegSweepParams {
     const int32_t* gseq;   // 0-based group id at each traversal position (non-decreasing)
     PendingSet<T> pend;    // gid arrays indexed by traversal position
     int writeback;         // write the pending-adjusted rows back (storage order only)
+    int no_data;           // 1: rows are not read (value = 0 - pending), used by the CG operator
     int R;                 // positions per chunk
     double* sums;          // G x C, runs complete inside one chunk
     double* head;          // nchunks x C
@@ -65,6 +66,7 @@ struct SmallGParams {
     int G;
     PendingSet<T> pend;    // gid arrays indexed by storage row
     int writeback;
+    int no_data;
     long long rows_per_block;
     double* partials;      // nblocks x G x C
 };
@@ -74,6 +76,8 @@ struct FinalizeParams {
     int C;
     // source of the group sums: segments (off/sums/head/tail, chunk size R) or
     // small-G block partials (partials, nblocks)
+    // source of the group sums: off == null && partials == null means sums[]
+    // already holds complete group sums
     const int32_t* off;
     const double* sums;
     const double* head;
@@ -100,6 +104,19 @@ struct FinalizeParams {
     unsigned long long* max_update_bits;
 };
 
+// Groups whose segment run spans more than SEG_LONG_SPAN chunks have their
+// chunk-edge partials folded by a block-wide tree (launch_long_sums) into
+// sums[g]; finalize-type kernels then read sums[g] for them.
+constexpr int SEG_LONG_SPAN = 32;
+
+// Lists the long groups of a segment traversal (device list, count on host).
+int find_long_groups(const int32_t* off, int G, int R, int32_t* list, int* n_long, cudaStream_t s);
+// sums[g][c] = tail[qs][c] + sum_{qs<q<=qe} head[q][c] for the listed groups.
+int launch_long_sums(const int32_t* off, const double* head, const double* tail, int R, int C, const int32_t* list,
+                     int n_long, double* sums, cudaStream_t s);
+// sums[g][c] = sum_b partials[b][g][c] (small-G block partials, fixed tree order).
+int launch_fold_smallg(const double* partials, int nblocks, int G, int C, double* sums, cudaStream_t s);
+
 // Launch helpers. Return 0 or a status.
 template <typename T>
 int launch_seg_sweep(const SegSweepParams<T>& p, cudaStream_t s);
@@ -120,5 +137,38 @@ int launch_apply_pending(T* X, int C, long long n, const PendingSet<T>& pend, cu
 
 // dst (float) = (float) src (double), n elements
 int launch_convert_f64_f32(const double* src, float* dst, long long n, cudaStream_t s);
+
+// ---- conjugate gradients on the FE normal equations (D'D a = D'e) ----
+// G-space vectors of all dimensions are concatenated: element (g, c) of
+// dimension d sits at ((goff_d + g) * C + c). Per-column scalars (C values)
+// live on the device; dot products use per-block partials folded in block
+// order, so every reduction is deterministic.
+
+// q_d = counts_d * p_d - S_d, where S_d are the group sums of a no-data sweep
+// with pending tables {p_e, e != d} (sums of -p_e over the rows of each
+// group). Also writes per-block partials of p.q per column.
+template <typename T>
+int launch_cg_q(const FinalizeParams& src, const T* p, T* q, double* pq_partials, cudaStream_t s);
+int cg_partial_blocks(long long gc);
+
+// out[c] = sum_b partials[b * C + c] for b < nb (fixed order)
+int launch_fold_partials(const double* partials, int nb, int C, double* out, cudaStream_t s);
+
+// a = rz / pq per column (0 where pq == 0), then for every element:
+// alpha += a p, r -= a q, z = r / count (0 for empty groups); partials of
+// r.z per column and max |z| (bits, device scalar).
+template <typename T>
+int launch_cg_update(long long Gt, int C, const int32_t* counts, const double* rz, const double* pq, const T* p,
+                     const T* q, double* alpha, T* r, T* z, double* rz_partials, unsigned long long* zmax,
+                     cudaStream_t s);
+
+// b = rz_new / rz_old per column; p = z + b p; rz_old = rz_new
+template <typename T>
+int launch_cg_direction(long long Gt, int C, double* rz_old, const double* rz_new, const T* z, T* p, cudaStream_t s);
+
+// r = counts * mu, z = p = mu (cast to T); partials of r.z and max |z|
+template <typename T>
+int launch_cg_init(long long Gt, int C, const int32_t* counts, const double* mu, T* r, T* z, T* p,
+                   double* rz_partials, unsigned long long* zmax, cudaStream_t s);
 
 }  // namespace fegb

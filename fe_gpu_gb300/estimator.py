@@ -78,7 +78,7 @@ class fe_estimation_result:  # src/core/fe_pipeline.f90:37-64
     stats: dict = field(default_factory=dict)
 
 
-def _make_config(cfg: fe_runtime_config, stream: Optional[int] = None):
+def _make_config(cfg: fe_runtime_config, stream: Optional[int] = None, profile: bool = False):
     c = N.FegbConfig()
     N.lib().fegb_config_init(C.byref(c))
     c.fe_tol = float(cfg.fe_tolerance)
@@ -102,6 +102,7 @@ def _make_config(cfg: fe_runtime_config, stream: Optional[int] = None):
         setattr(c, field_p, C.cast(arr, C.POINTER(C.c_int)))
     c.verbose = 1 if cfg.verbose else 0
     c.stream = C.c_void_p(stream) if stream else None
+    c.profile = 1 if profile else 0
     return c, keep
 
 
@@ -142,7 +143,8 @@ def _ptr(a: np.ndarray) -> int:
 
 
 def fe_gpu_estimate(cfg: fe_runtime_config, header: Optional[fe_dataset_header], host: fe_host_arrays,
-                    group_sizes: Optional[Sequence[int]] = None) -> fe_estimation_result:
+                    group_sizes: Optional[Sequence[int]] = None, stream: Optional[int] = None,
+                    profile: bool = False) -> fe_estimation_result:
     """fe_gpu_estimate (src/core/fe_pipeline.f90:516) over host arrays: the
     upload, within-transform, normal equations and SEs all run in libfegb.so."""
     y = np.ascontiguousarray(host.y, dtype=np.float64)
@@ -154,7 +156,7 @@ def fe_gpu_estimate(cfg: fe_runtime_config, header: Optional[fe_dataset_header],
     if fe.ndim != 2 or fe.shape[1] != n:
         raise ValueError("fe_ids must have shape (n_fe, n)")
     k, l, n_fe = W.shape[1], Z.shape[1], fe.shape[0]
-    c, keep = _make_config(cfg)
+    c, keep = _make_config(cfg, stream, profile)
     beta = np.zeros(max(k, 1))
     se = np.zeros(max(k, 1))
     res = N.FegbResult()
@@ -170,11 +172,11 @@ def fe_gpu_estimate(cfg: fe_runtime_config, header: Optional[fe_dataset_header],
 
 def fe_gpu_estimate_device(cfg: fe_runtime_config, n: int, k: int, l: int, d_y: int, d_W: Optional[int],
                            d_Z: Optional[int], d_fe_ids: Sequence[int], group_sizes: Optional[Sequence[int]] = None,
-                           stream: Optional[int] = None, header: Optional[fe_dataset_header] = None
-                           ) -> fe_estimation_result:
+                           stream: Optional[int] = None, header: Optional[fe_dataset_header] = None,
+                           profile: bool = False) -> fe_estimation_result:
     """Same fit over device arrays (raw device pointers), e.g. from the
     fe_gpu_dataset upload (src/gpu/fe_gpu_data.f90:41-120)."""
-    c, keep = _make_config(cfg, stream)
+    c, keep = _make_config(cfg, stream, profile)
     n_fe = len(d_fe_ids)
     ptrs = (C.c_void_p * max(1, n_fe))(*[C.c_void_p(int(p)) for p in d_fe_ids])
     beta = np.zeros(max(k, 1))

@@ -54,6 +54,7 @@ typedef struct fegb_config {
     const int* iv_instruments;/* 1-based instrument columns */
     int verbose;
     void* stream;             /* cudaStream_t to run on; NULL = the library's own stream */
+    int profile;              /* 1: time every sweep launch with CUDA events (fills prof_* in the result) */
 } fegb_config;
 
 typedef struct fegb_result {
@@ -89,6 +90,11 @@ typedef struct fegb_result {
     double time_regression;
     double time_se;
     double time_total;
+    /* sweep-kernel timing when cfg.profile = 1, by kernel family:
+     * [0] segment sweep FP64, [1] segment sweep FP32, [2] small-G sweep FP64, [3] small-G sweep FP32 */
+    int prof_launches[4];
+    double prof_seconds[4];   /* summed CUDA-event durations of those launches */
+    double prof_bytes[4];     /* summed algorithmic bytes of those launches */
 } fegb_result;
 
 /* Default configuration (tolerance 1e-6, 500 iterations, FP64, AP, GPU conventions). */
@@ -128,6 +134,9 @@ int fegb_compact_ids(const int* d_raw, long long n, int* d_out, int* n_levels);
 
 /* G_d = max id per dimension over device id arrays; status 1 if an id < 1. */
 int fegb_group_sizes(const int* const* d_fe_ids, int n_fe, long long n, int* sizes);
+
+/* Number of kernel launches issued by this library since it was loaded. */
+long long fegb_kernel_launches(void);
 
 /* Iterated singleton removal: d_keep (device, n bytes) gets 1 for kept rows. */
 int fegb_drop_singletons(const int* const* d_fe_ids, const int* sizes, int n_fe, long long n, unsigned char* d_keep,

@@ -8,7 +8,7 @@ import pytest
 
 ROOT = Path(__file__).resolve().parents[1]
 HEADERS = sorted((ROOT / "include").glob("*.h"))
-DECL = re.compile(r"^\s*(?:int|void)\s+([A-Za-z_][A-Za-z0-9_]*)\s*\(", re.M)
+DECL = re.compile(r"^\s*(?:int|void|long long)\s+([A-Za-z_][A-Za-z0-9_]*)\s*\(", re.M)
 
 
 def declared_symbols():

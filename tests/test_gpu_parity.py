@@ -31,26 +31,30 @@ def six_row_case():
     return fe_host_arrays(y=y, W=np.asfortranarray(W), Z=np.zeros((6, 0), order="F"), fe_ids=fe)
 
 
+@pytest.mark.parametrize("method", ["ap", "cg"])
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
-def test_reference_regression_known_answer(built, precision):
+def test_reference_regression_known_answer(built, method, precision):
     # tests/test_gpu_regression.f90: beta = (1.5, -0.75) to 1e-8 at fe_tol 1e-10
     host = six_row_case()
-    cfg = fe_runtime_config(fe_tolerance=1e-10, fe_max_iterations=500, precision=precision)
+    cfg = fe_runtime_config(fe_tolerance=1e-10, fe_max_iterations=500, precision=precision,
+                            demean_cg=(method == "cg"))
     res = fe_gpu_estimate(cfg, None, host)
     assert res.converged
     assert res.solver_info == 0
     np.testing.assert_allclose(res.beta, [1.5, -0.75], atol=1e-8, rtol=0)
 
 
+@pytest.mark.parametrize("method", ["ap", "cg"])
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
-def test_reference_demean_known_answer(built, precision):
+def test_reference_demean_known_answer(built, method, precision):
     # tests/test_gpu_demean.f90:43-125: group means < 1e-6 after tol 1e-8, 200 iterations
     y = np.array([1.0, 2.0, 3.0, -2.0, -1.0, 0.5])
     W = np.asfortranarray(np.array([[1.0, 0.0], [1.5, -2.0], [-0.5, 1.0], [-1.0, 0.5], [2.0, 1.5], [-0.5, -1.0]]))
     fe = np.array([[1, 1, 2, 2, 3, 3], [1, 2, 1, 2, 1, 2]], dtype=np.int32)
     host = fe_host_arrays(y=y, W=W, Z=np.zeros((6, 0), order="F"), fe_ids=fe)
     conv, iters, mu = fe_gpu_within_transform(fe_runtime_config(fe_tolerance=1e-8, fe_max_iterations=200,
-                                                                precision=precision), host)
+                                                                precision=precision, demean_cg=(method == "cg")),
+                                              host)
     assert conv
     for d in range(2):
         for g in range(1, fe[d].max() + 1):
@@ -73,12 +77,13 @@ def test_demean_matches_oracle_symmetric_scheme(built):
     np.testing.assert_allclose(host.W, oW, atol=1e-9)
 
 
+@pytest.mark.parametrize("method", ["ap", "cg"])
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 @pytest.mark.parametrize("clusters", [[], [1], [1, 3], [1, 2, 3]])
-def test_nls_panel_gpu_conventions(built, precision, clusters):
+def test_nls_panel_gpu_conventions(built, method, precision, clusters):
     hdr, host = nls_panel(n_ids=1500, seed=11)
     cfg = fe_runtime_config(fe_tolerance=1e-8, fe_max_iterations=20000, cluster_fe_dims=clusters,
-                            precision=precision)
+                            precision=precision, demean_cg=(method == "cg"))
     res = fe_gpu_estimate(cfg, hdr, host)
     ref = O.gpu_estimate(host.y, host.W, host.fe_ids, tol=1e-12, max_iter=200000, cluster_dims=clusters)
     assert res.converged
@@ -103,11 +108,12 @@ def test_nls_panel_cpu_conventions(built, clusters):
     assert res.dof_resid == ref.stats["dof_resid"]
 
 
+@pytest.mark.parametrize("method", ["ap", "cg"])
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
-def test_worker_firm_small(built, precision):
+def test_worker_firm_small(built, method, precision):
     hdr, host = worker_firm_panel(n_workers=20000, n_firms=2000, n_periods=10, switch_prob=0.1, seed=5)
     cfg = fe_runtime_config(fe_tolerance=1e-8, fe_max_iterations=20000, cluster_fe_dims=[1, 2, 3],
-                            precision=precision)
+                            precision=precision, demean_cg=(method == "cg"))
     res = fe_gpu_estimate(cfg, hdr, host)
     ref = O.gpu_estimate(host.y, host.W, host.fe_ids, tol=1e-11, max_iter=200000, cluster_dims=[1, 2, 3])
     assert res.converged
@@ -129,12 +135,13 @@ def iv_case(n=6000, seed=3):
     return fe_host_arrays(y=y, W=W, Z=np.asfortranarray(z), fe_ids=fe)
 
 
+@pytest.mark.parametrize("method", ["ap", "cg"])
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 @pytest.mark.parametrize("clusters", [[], [1, 2]])
-def test_iv_gpu_conventions(built, precision, clusters):
+def test_iv_gpu_conventions(built, method, precision, clusters):
     host = iv_case()
     cfg = fe_runtime_config(fe_tolerance=1e-8, fe_max_iterations=20000, cluster_fe_dims=clusters,
-                            iv_regressors=[1], precision=precision)
+                            iv_regressors=[1], precision=precision, demean_cg=(method == "cg"))
     res = fe_gpu_estimate(cfg, None, host)
     ref = O.gpu_estimate(host.y, host.W, host.fe_ids, Z=host.Z, tol=1e-12, max_iter=200000, cluster_dims=clusters,
                          iv_regressors=[1])
@@ -144,9 +151,11 @@ def test_iv_gpu_conventions(built, precision, clusters):
     assert rel(res.se, ref.se) < SE_RTOL
 
 
-def test_deterministic_bitwise(built):
+@pytest.mark.parametrize("method", ["ap", "cg"])
+def test_deterministic_bitwise(built, method):
     hdr, host = worker_firm_panel(n_workers=5000, n_firms=700, n_periods=8, switch_prob=0.2, seed=9)
-    cfg = fe_runtime_config(fe_tolerance=1e-8, fe_max_iterations=20000, cluster_fe_dims=[1, 2])
+    cfg = fe_runtime_config(fe_tolerance=1e-8, fe_max_iterations=20000, cluster_fe_dims=[1, 2], precision="mixed",
+                            demean_cg=(method == "cg"))
     a = fe_gpu_estimate(cfg, hdr, host)
     b = fe_gpu_estimate(cfg, hdr, host)
     assert a.fe_iterations == b.fe_iterations

@@ -309,10 +309,12 @@ def main():
     d2h = 2 * k * 8
 
     # roofline of the dominant sweep-kernel family, timed live in the timed steps
-    fam = ["segment sweep fp64", "segment sweep fp32", "small-G sweep fp64", "small-G sweep fp32"]
-    secs = [sum(r.stats["prof_seconds"][i] for r in results) for i in range(4)]
-    nlaunch = [sum(r.stats["prof_launches"][i] for r in results) for i in range(4)]
-    nbytes = [sum(r.stats["prof_bytes"][i] for r in results) for i in range(4)]
+    fam = ["segment sweep fp64", "segment sweep fp32", "small-G sweep fp64", "small-G sweep fp32",
+           "CG operator segment sweep fp64", "CG operator segment sweep fp32", "CG operator small-G sweep fp64",
+           "CG operator small-G sweep fp32"]
+    secs = [sum(r.stats["prof_seconds"][i] for r in results) for i in range(8)]
+    nlaunch = [sum(r.stats["prof_launches"][i] for r in results) for i in range(8)]
+    nbytes = [sum(r.stats["prof_bytes"][i] for r in results) for i in range(8)]
     top = int(np.argmax(secs))
     peak, peak_kind = measured_hbm_peak()
     achieved = nbytes[top] / secs[top] / 1e9 if secs[top] > 0 else 0.0
@@ -353,7 +355,7 @@ def main():
                      "alg_bytes_per_launch": nbytes[top] / max(1, nlaunch[top]),
                      "all_families": {fam[i]: {"launches": nlaunch[i], "seconds": secs[i],
                                                "gbs": (nbytes[i] / secs[i] / 1e9) if secs[i] else None}
-                                      for i in range(4)}},
+                                      for i in range(8) if nlaunch[i]}},
         "clocks": clocks,
     }
     if rank == 0 and not args.no_cpu_baseline:

@@ -78,9 +78,9 @@ class FegbResult(C.Structure):
         ("time_regression", C.c_double),
         ("time_se", C.c_double),
         ("time_total", C.c_double),
-        ("prof_launches", C.c_int * 4),
-        ("prof_seconds", C.c_double * 4),
-        ("prof_bytes", C.c_double * 4),
+        ("prof_launches", C.c_int * 8),
+        ("prof_seconds", C.c_double * 8),
+        ("prof_bytes", C.c_double * 8),
     ]
 
     def as_dict(self) -> dict:

@@ -67,7 +67,7 @@ struct Problem {
     double* prev_change = nullptr;
     unsigned long long* change_bits = nullptr;  // n_fe
     unsigned long long* max_bits = nullptr;     // [0] iteration max, [1] mu max
-    unsigned* done = nullptr;
+    double* max_partials = nullptr;              // per-block maxima of a finalize launch
     double* sums = nullptr;
     double* head = nullptr;
     double* tail = nullptr;
@@ -76,6 +76,7 @@ struct Problem {
     long long Gt = 0;
     std::vector<long long> goff;
     int32_t* counts_all = nullptr;
+    double* inv_counts_all = nullptr;
     double* alpha_all = nullptr;
     double* mu_all = nullptr;
     int smallg_nb = 0;
@@ -104,6 +105,7 @@ int collect_profile(Problem& P, fegb_result* res) {
     for (auto& t : P.timed) {
         float ms = 0.f;
         FEGB_CUDA(cudaEventElapsedTime(&ms, t.a, t.b), "profile elapsed");
+        if (t.kind < 0 || t.kind >= 8) continue;
         res->prof_launches[t.kind] += 1;
         res->prof_seconds[t.kind] += ms * 1e-3;
         res->prof_bytes[t.kind] += t.bytes;
@@ -195,14 +197,11 @@ __global__ void count_ids_kernel(const int32_t* __restrict__ gid, long long n, i
     for (; i < n; i += st) atomicAdd(&counts[gid[i]], 1);
 }
 
-__global__ void reset_relax_kernel(double* relax, double* prev_change, unsigned long long* change_bits, unsigned* done,
-                                   int n) {
+__global__ void reset_relax_kernel(double* relax, double* prev_change, int n) {
     int d = threadIdx.x;
     if (d < n) {
         relax[d] = 1.5;
         prev_change[d] = DBL_MAX;
-        change_bits[d] = 0ull;
-        done[d] = 0u;
     }
 }
 
@@ -408,6 +407,8 @@ int build_problem(Problem& P, long long n_in, int k, int l, int n_fe, const doub
         FEGB_TRY(dalloc(scr, &D.pend64, gc, "pending means"));
         if (mixed) FEGB_TRY(dalloc(scr, &D.pend32, gc, "pending means fp32"));
     }
+    FEGB_TRY(dalloc(scr, &P.inv_counts_all, (size_t)std::max(1LL, P.Gt), "inverse counts"));
+    FEGB_TRY(launch_inv_counts(P.counts_all, P.Gt, P.inv_counts_all, s));
     for (int d = 0; d < n_fe; ++d) {
         Dim& D = P.dims[d];
         D.gid_at_perm.assign(n_fe, nullptr);
@@ -429,7 +430,7 @@ int build_problem(Problem& P, long long n_in, int k, int l, int n_fe, const doub
     FEGB_TRY(dalloc(scr, &P.prev_change, (size_t)std::max(1, n_fe), "prev change"));
     FEGB_TRY(dalloc(scr, &P.change_bits, (size_t)std::max(1, n_fe), "change"));
     FEGB_TRY(dalloc(scr, &P.max_bits, 2, "max update"));
-    FEGB_TRY(dalloc(scr, &P.done, (size_t)std::max(1, n_fe), "done counters"));
+    FEGB_TRY(dalloc(scr, &P.max_partials, (size_t)finalize_blocks((long long)gmax * C) + 1, "max partials"));
     // sweep order: ascending group count, exchange sort of fe_gpu_demean.f90:104-114
     P.order.resize(n_fe);
     for (int d = 0; d < n_fe; ++d) P.order[d] = d;
@@ -553,6 +554,7 @@ FinalizeParams finalize_base(const Problem& P, int d) {
         f.R = CHUNK_R;
     }
     f.counts = D.counts;
+    f.inv_counts = P.inv_counts_all + P.goff[d];
     return f;
 }
 
@@ -582,9 +584,8 @@ int project(Problem& P, int d, T* data, PendingList& pl, const ProjectionOpts& o
     f.pend32 = D.pend32;
     f.pend_accumulate = accumulate ? 1 : 0;
     f.alpha = o.alpha ? D.alpha : nullptr;
-    f.change_bits = P.change_bits + d;
+    f.max_partials = P.max_partials;
     f.do_relax_update = 1;
-    f.done_counter = P.done + d;
     f.relax_rw = P.relax + d;
     f.prev_change = P.prev_change + d;
     f.max_update_bits = P.max_bits;
@@ -617,8 +618,7 @@ int reset_ap_state(Problem& P, bool alpha) {
             FEGB_CUDA(cudaMemsetAsync(P.dims[d].alpha, 0, gc * sizeof(double), P.s), "reset alpha");
     }
     if (P.n_fe > 0) {
-        reset_relax_kernel<<<1, 32 * ((P.n_fe + 31) / 32), 0, P.s>>>(P.relax, P.prev_change, P.change_bits, P.done,
-                                                                    P.n_fe);
+        reset_relax_kernel<<<1, 32 * ((P.n_fe + 31) / 32), 0, P.s>>>(P.relax, P.prev_change, P.n_fe);
         FEGB_LAUNCH_CHECK("reset relaxation");
     }
     return 0;
@@ -689,6 +689,7 @@ int fp64_mean_pass(Problem& P, bool apply_alpha, double* mu_max) {
             FEGB_TRY(sweep_sums<double>(P, d, P.X, ps, first && apply_alpha));
             FinalizeParams f = finalize_base(P, d);
             f.mean_out = D.mu;
+            f.max_partials = P.max_partials;
             f.change_bits = P.max_bits + 1;
             FEGB_TRY(launch_finalize(f, P.s));
             bool rw = first && apply_alpha;
@@ -770,7 +771,7 @@ template <typename T>
 struct CGBuffers {
     T *r = nullptr, *z = nullptr, *p = nullptr, *q = nullptr;
     double *rz = nullptr, *rz_new = nullptr, *pq = nullptr;
-    double *rz_part = nullptr, *pq_part = nullptr;
+    double *rz_part = nullptr, *pq_part = nullptr, *zmax_part = nullptr;
     unsigned long long* zmax = nullptr;
     int rz_blocks = 0, pq_blocks = 0;
     std::vector<int> pq_block_off;
@@ -794,6 +795,7 @@ int cg_alloc(Problem& P, CGBuffers<T>& B) {
         B.pq_block_off[d + 1] = B.pq_block_off[d] + cg_partial_blocks((long long)std::max(1, P.dims[d].G) * P.C);
     B.pq_blocks = B.pq_block_off[P.n_fe];
     FEGB_TRY(dalloc(scr, &B.rz_part, (size_t)B.rz_blocks * P.C, "cg rz partials"));
+    FEGB_TRY(dalloc(scr, &B.zmax_part, (size_t)B.rz_blocks, "cg zmax partials"));
     FEGB_TRY(dalloc(scr, &B.pq_part, (size_t)std::max(1, B.pq_blocks) * P.C, "cg pq partials"));
     FEGB_CUDA(cudaMemsetAsync(B.pq_part, 0, sizeof(double) * (size_t)std::max(1, B.pq_blocks) * P.C, P.s),
               "cg pq partials zero");
@@ -808,6 +810,14 @@ int cg_apply(Problem& P, CGBuffers<T>& B) {
     for (int d = 0; d < P.n_fe; ++d) {
         Dim& D = P.dims[d];
         if (D.G <= 0) continue;
+        Problem::Timed tm{};
+        if (P.profile) {
+            tm.kind = 4 + (D.mode == MODE_SMALLG ? 2 : 0) + (sizeof(T) == 4 ? 1 : 0);
+            tm.bytes = (double)P.n * 4.0 * (P.n_fe - (D.mode == MODE_SMALLG ? 0 : 0));
+            FEGB_CUDA(cudaEventCreate(&tm.a), "profile event");
+            FEGB_CUDA(cudaEventCreate(&tm.b), "profile event");
+            FEGB_CUDA(cudaEventRecord(tm.a, P.s), "profile record");
+        }
         PendingSet<T> ps{};
         ps.n = 0;
         for (int e = 0; e < P.n_fe; ++e) {
@@ -849,6 +859,10 @@ int cg_apply(Problem& P, CGBuffers<T>& B) {
             FEGB_TRY(launch_seg_sweep<T>(sp, P.s));
             FEGB_TRY(launch_long_sums(D.off, P.head, P.tail, CHUNK_R, C, D.long_list, D.n_long, P.sums, P.s));
         }
+        if (P.profile) {
+            FEGB_CUDA(cudaEventRecord(tm.b, P.s), "profile record");
+            P.timed.push_back(tm);
+        }
         FinalizeParams src = finalize_base(P, d);
         FEGB_TRY(launch_cg_q<T>(src, B.p + P.goff[d] * C, B.q + P.goff[d] * C, B.pq_part + (size_t)B.pq_block_off[d] * C,
                                 P.s));
@@ -863,8 +877,7 @@ int cg_apply(Problem& P, CGBuffers<T>& B) {
 template <typename T>
 int cg_solve(Problem& P, CGBuffers<T>& B, double inner_tol, int max_it, int* iters, double* zmax_out) {
     const int C = P.C;
-    FEGB_CUDA(cudaMemsetAsync(B.zmax, 0, sizeof(unsigned long long), P.s), "cg zmax reset");
-    FEGB_TRY(launch_cg_init<T>(P.Gt, C, P.counts_all, P.mu_all, B.r, B.z, B.p, B.rz_part, B.zmax, P.s));
+    FEGB_TRY(launch_cg_init<T>(P.Gt, C, P.counts_all, P.mu_all, B.r, B.z, B.p, B.rz_part, B.zmax_part, B.zmax, P.s));
     FEGB_TRY(launch_fold_partials(B.rz_part, B.rz_blocks, C, B.rz, P.s));
     double best = DBL_MAX;
     int since_best = 0;
@@ -872,9 +885,8 @@ int cg_solve(Problem& P, CGBuffers<T>& B, double inner_tol, int max_it, int* ite
     double zm = 0.0;
     for (; it < max_it; ++it) {
         FEGB_TRY(cg_apply<T>(P, B));
-        FEGB_CUDA(cudaMemsetAsync(B.zmax, 0, sizeof(unsigned long long), P.s), "cg zmax reset");
-        FEGB_TRY(launch_cg_update<T>(P.Gt, C, P.counts_all, B.rz, B.pq, B.p, B.q, P.alpha_all, B.r, B.z, B.rz_part,
-                                     B.zmax, P.s));
+        FEGB_TRY(launch_cg_update<T>(P.Gt, C, P.inv_counts_all, B.rz, B.pq, B.p, B.q, P.alpha_all, B.r, B.z,
+                                     B.rz_part, B.zmax_part, B.zmax, P.s));
         FEGB_TRY(launch_fold_partials(B.rz_part, B.rz_blocks, C, B.rz_new, P.s));
         unsigned long long bits = 0;
         FEGB_TRY(d2h_sync(&bits, B.zmax, sizeof(bits), P.s, "cg zmax copy"));

@@ -29,7 +29,7 @@ struct SweepUnroll {
 };
 
 template <typename T>
-__global__ void __launch_bounds__(SW_THREADS)
+__global__ void __launch_bounds__(SW_THREADS, 4)
     seg_sweep_kernel(SegSweepParams<T> p, int L, int P, int CT, long long n_items) {
     constexpr int U = SweepUnroll<T>::U;
     constexpr bool kF32 = sizeof(T) == 4;
@@ -63,21 +63,21 @@ __global__ void __launch_bounds__(SW_THREADS)
 
     for (long long j = j0; j < j1; j += U) {
         int g[U];
-        long long row[U];
+        int row[U];  // row indices fit in int32 (n < 2^31)
         T v[U];
 #pragma unroll
         for (int u = 0; u < U; ++u) {
             const long long jj = j + u;
             const bool ok = jj < j1;
             g[u] = ok ? gseq[jj] : cur;
-            row[u] = ok ? (perm ? (long long)perm[jj] : jj) : -1;
+            row[u] = ok ? ((perm && !p.no_data) ? perm[jj] : (int)jj) : -1;
         }
         if (p.no_data) {
 #pragma unroll
             for (int u = 0; u < U; ++u) v[u] = T(0);
         } else {
 #pragma unroll
-            for (int u = 0; u < U; ++u) v[u] = row[u] >= 0 ? X[row[u] * p.rs + colc * p.cs] : T(0);
+            for (int u = 0; u < U; ++u) v[u] = row[u] >= 0 ? X[(long long)row[u] * p.rs + colc * p.cs] : T(0);
         }
         for (int e = 0; e < np; ++e) {
             const int32_t* __restrict__ pg = p.pend.gid[e];
@@ -89,7 +89,7 @@ __global__ void __launch_bounds__(SW_THREADS)
         if (p.writeback && col_ok && !p.no_data) {
 #pragma unroll
             for (int u = 0; u < U; ++u)
-                if (row[u] >= 0) X[row[u] * p.rs + col * p.cs] = v[u];
+                if (row[u] >= 0) X[(long long)row[u] * p.rs + col * p.cs] = v[u];
         }
 #pragma unroll
         for (int u = 0; u < U; ++u) {
@@ -132,20 +132,23 @@ __global__ void __launch_bounds__(SW_THREADS)
 }
 
 template <typename T>
-__global__ void smallg_sweep_kernel(SmallGParams<T> p, int P) {
+__global__ void __launch_bounds__(256, 4) smallg_sweep_kernel(SmallGParams<T> p, int P) {
     constexpr int U = SweepUnroll<T>::U;
-    extern __shared__ double tabs[];
+    // per-slot tables in the storage type (FP32 sums over a slot's short
+    // row range in the FP32 form), folded across slots in FP64
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T* tabs = reinterpret_cast<T*>(smem_raw);
     const int C = p.C;  // C <= 32, one column per lane
     const int nwarps = blockDim.x >> 5;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int nslots = nwarps * P;
     const int GC = p.G * C;
-    for (int i = threadIdx.x; i < nslots * GC; i += blockDim.x) tabs[i] = 0.0;
+    for (int i = threadIdx.x; i < nslots * GC; i += blockDim.x) tabs[i] = T(0);
     __syncthreads();
     const int slot = lane / C;
     if (slot < P) {
         const int s = warp * P + slot;
-        double* tab = tabs + (long long)s * GC;
+        T* tab = tabs + (long long)s * GC;
         const int col = lane - slot * C;
         const long long rb0 = (long long)blockIdx.x * p.rows_per_block;
         const long long rb1 = min(p.n, rb0 + p.rows_per_block);
@@ -179,13 +182,13 @@ __global__ void smallg_sweep_kernel(SmallGParams<T> p, int P) {
             }
 #pragma unroll
             for (int u = 0; u < U; ++u)
-                if (ok[u]) tab[g[u] * C + col] += (double)v[u];
+                if (ok[u]) tab[g[u] * C + col] += v[u];
         }
     }
     __syncthreads();
     for (int e = threadIdx.x; e < GC; e += blockDim.x) {
         double t = 0.0;
-        for (int s = 0; s < nslots; ++s) t += tabs[(long long)s * GC + e];
+        for (int s = 0; s < nslots; ++s) t += (double)tabs[(long long)s * GC + e];
         p.partials[(long long)blockIdx.x * GC + e] = t;
     }
 }
@@ -217,7 +220,6 @@ __device__ __forceinline__ double source_sum(const FinalizeParams& p, int g, int
 
 __global__ void __launch_bounds__(FIN_THREADS) finalize_kernel(FinalizeParams p) {
     __shared__ double red[FIN_THREADS / 32];
-    __shared__ bool am_last;
     const long long idx = (long long)blockIdx.x * FIN_THREADS + threadIdx.x;
     const long long total = (long long)p.G * p.C;
     double amax = 0.0;
@@ -228,7 +230,8 @@ __global__ void __launch_bounds__(FIN_THREADS) finalize_kernel(FinalizeParams p)
         const int cnt = p.counts ? p.counts[g] : 0;
         if (p.sum_out) p.sum_out[idx] = sum;
         // reciprocal multiply, as in src/gpu/fe_gpu_runtime.cu:195-200
-        double mean = cnt > 0 ? sum * (1.0 / (double)cnt) : 0.0;
+        const double inv = p.inv_counts ? p.inv_counts[g] : (cnt > 0 ? 1.0 / (double)cnt : 0.0);
+        double mean = sum * inv;
         if (p.bias) mean += p.bias[idx];
         if (p.mean_out) p.mean_out[idx] = mean;
         double mixed = mean;
@@ -247,39 +250,43 @@ __global__ void __launch_bounds__(FIN_THREADS) finalize_kernel(FinalizeParams p)
         if (p.alpha) p.alpha[idx] += mixed;
         amax = fabs(mixed);
     }
-    if (p.change_bits) {
+    if (p.max_partials) {
         amax = warp_max(amax);
         if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = amax;
         __syncthreads();
         if (threadIdx.x == 0) {
             double m = red[0];
             for (int w = 1; w < FIN_THREADS / 32; ++w) m = fmax(m, red[w]);
-            atomic_max_nonneg(p.change_bits, m);
+            p.max_partials[blockIdx.x] = m;
         }
     }
-    if (p.do_relax_update) {
-        if (threadIdx.x == 0) {
-            __threadfence();
-            unsigned ticket = atomicAdd(p.done_counter, 1u);
-            am_last = (ticket == gridDim.x - 1);
-        }
+}
+
+// Folds the per-block maxima of one finalize launch; updates the dimension's
+// relaxation from the change of this projection relative to the previous one.
+__global__ void __launch_bounds__(FIN_THREADS) finalize_epilogue_kernel(FinalizeParams p, int nb) {
+    __shared__ double smem[FIN_THREADS];
+    double m = 0.0;
+    for (int b = threadIdx.x; b < nb; b += FIN_THREADS) m = fmax(m, p.max_partials[b]);
+    smem[threadIdx.x] = m;
+    __syncthreads();
+    for (int w = FIN_THREADS / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) smem[threadIdx.x] = fmax(smem[threadIdx.x], smem[threadIdx.x + w]);
         __syncthreads();
-        if (am_last && threadIdx.x == 0) {
-            __threadfence();
-            volatile unsigned long long* cb = p.change_bits;
-            const double cd = bits_dbl(*cb);
-            const double pc = *p.prev_change;
-            double r = *p.relax_rw;
-            if (cd > pc * 1.05)
-                r = fmax(0.4, r * 0.5);
-            else if (cd < pc * 0.8)
-                r = fmin(2.0, r * 1.10);
-            *p.relax_rw = r;
-            *p.prev_change = cd;
-            atomic_max_nonneg(p.max_update_bits, cd);
-            *cb = 0ull;
-            *p.done_counter = 0u;
-        }
+    }
+    if (threadIdx.x != 0) return;
+    const double cd = smem[0];
+    if (p.change_bits) atomic_max_nonneg(p.change_bits, cd);
+    if (p.do_relax_update) {
+        const double pc = *p.prev_change;
+        double r = *p.relax_rw;
+        if (cd > pc * 1.05)
+            r = fmax(0.4, r * 0.5);
+        else if (cd < pc * 0.8)
+            r = fmin(2.0, r * 1.10);
+        *p.relax_rw = r;
+        *p.prev_change = cd;
+        atomic_max_nonneg(p.max_update_bits, cd);
     }
 }
 
@@ -405,25 +412,29 @@ __global__ void find_long_kernel(const int32_t* __restrict__ off, int G, int R, 
 
 template <typename T>
 __global__ void __launch_bounds__(FIN_THREADS)
-    cg_update_kernel(long long Gt, int C, const int32_t* __restrict__ counts, const double* __restrict__ rz,
+    cg_update_kernel(long long Gt, int C, const double* __restrict__ inv_counts, const double* __restrict__ rz,
                      const double* __restrict__ pq, const T* __restrict__ p, const T* __restrict__ q,
                      double* __restrict__ alpha, T* __restrict__ r, T* __restrict__ z,
-                     double* __restrict__ rz_partials, unsigned long long* __restrict__ zmax) {
+                     double* __restrict__ rz_partials, double* __restrict__ zmax_partials) {
     __shared__ double smem[FIN_THREADS];
     __shared__ double red[FIN_THREADS / 32];
+    __shared__ double step[64];
     const long long total = Gt * C;
     const long long base = (long long)blockIdx.x * FIN_THREADS;
     const long long idx = base + threadIdx.x;
+    if (threadIdx.x < C && threadIdx.x < 64) {
+        const double den = pq[threadIdx.x];
+        step[threadIdx.x] = den != 0.0 ? rz[threadIdx.x] / den : 0.0;
+    }
+    __syncthreads();
     double prod = 0.0, az = 0.0;
     if (idx < total) {
         const long long g = idx / C;
         const int c = (int)(idx - g * C);
-        const double den = pq[c];
-        const double a = den != 0.0 ? rz[c] / den : 0.0;
+        const double a = C <= 64 ? step[c] : (pq[c] != 0.0 ? rz[c] / pq[c] : 0.0);
         alpha[idx] += a * (double)p[idx];
         const double rv = (double)r[idx] - a * (double)q[idx];
-        const int cnt = counts[g];
-        const double zv = cnt > 0 ? rv / (double)cnt : 0.0;
+        const double zv = rv * inv_counts[g];
         r[idx] = (T)rv;
         z[idx] = (T)zv;
         prod = rv * zv;
@@ -436,21 +447,34 @@ __global__ void __launch_bounds__(FIN_THREADS)
     if (threadIdx.x == 0) {
         double m = red[0];
         for (int w = 1; w < FIN_THREADS / 32; ++w) m = fmax(m, red[w]);
-        atomic_max_nonneg(zmax, m);
+        zmax_partials[blockIdx.x] = m;
     }
 }
 
 template <typename T>
 __global__ void cg_direction_kernel(long long Gt, int C, const double* __restrict__ rz_old,
                                     const double* __restrict__ rz_new, const T* __restrict__ z, T* __restrict__ p) {
+    __shared__ double beta[64];
+    if (threadIdx.x < C && threadIdx.x < 64)
+        beta[threadIdx.x] = rz_old[threadIdx.x] != 0.0 ? rz_new[threadIdx.x] / rz_old[threadIdx.x] : 0.0;
+    __syncthreads();
     const long long total = Gt * C;
     long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const long long st = (long long)gridDim.x * blockDim.x;
+    // column of idx, advanced incrementally (no 64-bit division per element)
+    int c = (int)(idx % C);
+    const int cstep = (int)(st % C);
     for (; idx < total; idx += st) {
-        const int c = (int)(idx % C);
-        const double b = rz_old[c] != 0.0 ? rz_new[c] / rz_old[c] : 0.0;
+        const double b = C <= 64 ? beta[c] : (rz_old[c] != 0.0 ? rz_new[c] / rz_old[c] : 0.0);
         p[idx] = (T)((double)z[idx] + b * (double)p[idx]);
+        c += cstep;
+        if (c >= C) c -= C;
     }
+}
+
+__global__ void inv_counts_kernel(const int32_t* __restrict__ counts, long long G, double* __restrict__ inv) {
+    long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (g < G) inv[g] = counts[g] > 0 ? 1.0 / (double)counts[g] : 0.0;
 }
 
 __global__ void copy_scalars_kernel(const double* __restrict__ src, double* __restrict__ dst, int C) {
@@ -462,7 +486,7 @@ template <typename T>
 __global__ void __launch_bounds__(FIN_THREADS)
     cg_init_kernel(long long Gt, int C, const int32_t* __restrict__ counts, const double* __restrict__ mu,
                    T* __restrict__ r, T* __restrict__ z, T* __restrict__ p, double* __restrict__ rz_partials,
-                   unsigned long long* __restrict__ zmax) {
+                   double* __restrict__ zmax_partials) {
     __shared__ double smem[FIN_THREADS];
     __shared__ double red[FIN_THREADS / 32];
     const long long total = Gt * C;
@@ -487,8 +511,23 @@ __global__ void __launch_bounds__(FIN_THREADS)
     if (threadIdx.x == 0) {
         double mm = red[0];
         for (int w = 1; w < FIN_THREADS / 32; ++w) mm = fmax(mm, red[w]);
-        atomic_max_nonneg(zmax, mm);
+        zmax_partials[blockIdx.x] = mm;
     }
+}
+
+// out (bits) = max over partials (one block, fixed tree); max is exact.
+__global__ void __launch_bounds__(FIN_THREADS) fold_max_kernel(const double* __restrict__ partials, int nb,
+                                                              unsigned long long* __restrict__ out) {
+    __shared__ double smem[FIN_THREADS];
+    double m = 0.0;
+    for (int b = threadIdx.x; b < nb; b += FIN_THREADS) m = fmax(m, partials[b]);
+    smem[threadIdx.x] = m;
+    __syncthreads();
+    for (int w = FIN_THREADS / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) smem[threadIdx.x] = fmax(smem[threadIdx.x], smem[threadIdx.x + w]);
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *out = dbl_bits(smem[0]);
 }
 
 constexpr int SMALLG_SMEM_BUDGET = 96 * 1024;
@@ -527,7 +566,7 @@ int launch_smallg_sweep(const SmallGParams<T>& p, int nblocks, cudaStream_t s) {
     if (p.n <= 0) return 0;
     if (!smallg_eligible(p.G, p.C)) return set_error("small-G sweep: G=%d C=%d not eligible", p.G, p.C);
     const int P = 32 / p.C;
-    const long long per_warp = (long long)P * p.G * p.C * sizeof(double);
+    const long long per_warp = (long long)P * p.G * p.C * sizeof(T);
     int nwarps = (int)(SMALLG_SMEM_BUDGET / per_warp);
     if (nwarps > 8) nwarps = 8;
     if (nwarps < 1) nwarps = 1;
@@ -551,6 +590,10 @@ int launch_finalize(const FinalizeParams& p, cudaStream_t s) {
     unsigned blocks = (unsigned)((total + FIN_THREADS - 1) / FIN_THREADS);
     finalize_kernel<<<blocks, FIN_THREADS, 0, s>>>(p);
     FEGB_LAUNCH_CHECK("finalize");
+    if (p.max_partials && (p.change_bits || p.do_relax_update)) {
+        finalize_epilogue_kernel<<<1, FIN_THREADS, 0, s>>>(p, (int)blocks);
+        FEGB_LAUNCH_CHECK("finalize epilogue");
+    }
     return 0;
 }
 
@@ -617,15 +660,25 @@ int launch_fold_smallg(const double* partials, int nblocks, int G, int C, double
     return 0;
 }
 
+int launch_inv_counts(const int32_t* counts, long long G, double* inv_counts, cudaStream_t s) {
+    if (G <= 0) return 0;
+    inv_counts_kernel<<<(unsigned)((G + 255) / 256), 256, 0, s>>>(counts, G, inv_counts);
+    FEGB_LAUNCH_CHECK("inverse counts");
+    return 0;
+}
+
 template <typename T>
-int launch_cg_update(long long Gt, int C, const int32_t* counts, const double* rz, const double* pq, const T* p,
-                     const T* q, double* alpha, T* r, T* z, double* rz_partials, unsigned long long* zmax,
-                     cudaStream_t s) {
+int launch_cg_update(long long Gt, int C, const double* inv_counts, const double* rz, const double* pq, const T* p,
+                     const T* q, double* alpha, T* r, T* z, double* rz_partials, double* zmax_partials,
+                     unsigned long long* zmax, cudaStream_t s) {
     long long total = Gt * C;
     if (total <= 0) return 0;
-    cg_update_kernel<T><<<cg_partial_blocks(total), FIN_THREADS, 0, s>>>(Gt, C, counts, rz, pq, p, q, alpha, r, z,
-                                                                         rz_partials, zmax);
+    const int nb = cg_partial_blocks(total);
+    cg_update_kernel<T><<<nb, FIN_THREADS, 0, s>>>(Gt, C, inv_counts, rz, pq, p, q, alpha, r, z, rz_partials,
+                                                   zmax_partials);
     FEGB_LAUNCH_CHECK("cg update");
+    fold_max_kernel<<<1, FIN_THREADS, 0, s>>>(zmax_partials, nb, zmax);
+    FEGB_LAUNCH_CHECK("cg max fold");
     return 0;
 }
 
@@ -643,29 +696,32 @@ int launch_cg_direction(long long Gt, int C, double* rz_old, const double* rz_ne
 
 template <typename T>
 int launch_cg_init(long long Gt, int C, const int32_t* counts, const double* mu, T* r, T* z, T* p,
-                   double* rz_partials, unsigned long long* zmax, cudaStream_t s) {
+                   double* rz_partials, double* zmax_partials, unsigned long long* zmax, cudaStream_t s) {
     long long total = Gt * C;
     if (total <= 0) return 0;
-    cg_init_kernel<T><<<cg_partial_blocks(total), FIN_THREADS, 0, s>>>(Gt, C, counts, mu, r, z, p, rz_partials, zmax);
+    const int nb = cg_partial_blocks(total);
+    cg_init_kernel<T><<<nb, FIN_THREADS, 0, s>>>(Gt, C, counts, mu, r, z, p, rz_partials, zmax_partials);
     FEGB_LAUNCH_CHECK("cg init");
+    fold_max_kernel<<<1, FIN_THREADS, 0, s>>>(zmax_partials, nb, zmax);
+    FEGB_LAUNCH_CHECK("cg max fold");
     return 0;
 }
 
 template int launch_cg_q<double>(const FinalizeParams&, const double*, double*, double*, cudaStream_t);
 template int launch_cg_q<float>(const FinalizeParams&, const float*, float*, double*, cudaStream_t);
-template int launch_cg_update<double>(long long, int, const int32_t*, const double*, const double*, const double*,
-                                      const double*, double*, double*, double*, double*, unsigned long long*,
-                                      cudaStream_t);
-template int launch_cg_update<float>(long long, int, const int32_t*, const double*, const double*, const float*,
-                                     const float*, double*, float*, float*, double*, unsigned long long*,
+template int launch_cg_update<double>(long long, int, const double*, const double*, const double*, const double*,
+                                      const double*, double*, double*, double*, double*, double*,
+                                      unsigned long long*, cudaStream_t);
+template int launch_cg_update<float>(long long, int, const double*, const double*, const double*, const float*,
+                                     const float*, double*, float*, float*, double*, double*, unsigned long long*,
                                      cudaStream_t);
 template int launch_cg_direction<double>(long long, int, double*, const double*, const double*, double*,
                                          cudaStream_t);
 template int launch_cg_direction<float>(long long, int, double*, const double*, const float*, float*, cudaStream_t);
 template int launch_cg_init<double>(long long, int, const int32_t*, const double*, double*, double*, double*,
-                                    double*, unsigned long long*, cudaStream_t);
+                                    double*, double*, unsigned long long*, cudaStream_t);
 template int launch_cg_init<float>(long long, int, const int32_t*, const double*, float*, float*, float*, double*,
-                                   unsigned long long*, cudaStream_t);
+                                   double*, unsigned long long*, cudaStream_t);
 
 template int launch_seg_sweep<double>(const SegSweepParams<double>&, cudaStream_t);
 template int launch_seg_sweep<float>(const SegSweepParams<float>&, cudaStream_t);

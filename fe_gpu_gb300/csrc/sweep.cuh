@@ -86,6 +86,7 @@ struct FinalizeParams {
     const double* partials;
     int nblocks;
     const int32_t* counts;  // G group sizes
+    const double* inv_counts;  // optional G reciprocals (0 for empty groups); used instead of dividing
     const double* bias;     // optional G x C added to the mean
     double* prev;           // optional over-relaxation memory; null = no mixing
     const double* relax;    // device scalar (relaxation of this dimension), used when prev != null
@@ -95,14 +96,19 @@ struct FinalizeParams {
     double* alpha;          // optional accumulated FE coefficients (+= mixed)
     double* mean_out;       // optional plain means
     double* sum_out;        // optional plain sums
-    unsigned long long* change_bits;  // optional absmax(mixed) of this launch (bits)
-    // last-block relaxation update (fe_gpu_demean.f90:213-218)
+    // max |mixed| of this launch: per-block maxima in max_partials, folded by
+    // a one-block kernel into change_bits (atomic max, one per launch) and,
+    // with do_relax_update, into the adaptive relaxation state
+    // (fe_gpu_demean.f90:213-218)
+    double* max_partials;
+    unsigned long long* change_bits;
     int do_relax_update;
-    unsigned int* done_counter;
     double* relax_rw;
     double* prev_change;
     unsigned long long* max_update_bits;
 };
+
+inline int finalize_blocks(long long gc) { return (int)((gc + 255) / 256); }
 
 // Groups whose segment run spans more than SEG_LONG_SPAN chunks have their
 // chunk-edge partials folded by a block-wide tree (launch_long_sums) into
@@ -158,17 +164,20 @@ int launch_fold_partials(const double* partials, int nb, int C, double* out, cud
 // alpha += a p, r -= a q, z = r / count (0 for empty groups); partials of
 // r.z per column and max |z| (bits, device scalar).
 template <typename T>
-int launch_cg_update(long long Gt, int C, const int32_t* counts, const double* rz, const double* pq, const T* p,
-                     const T* q, double* alpha, T* r, T* z, double* rz_partials, unsigned long long* zmax,
-                     cudaStream_t s);
+int launch_cg_update(long long Gt, int C, const double* inv_counts, const double* rz, const double* pq, const T* p,
+                     const T* q, double* alpha, T* r, T* z, double* rz_partials, double* zmax_partials,
+                     unsigned long long* zmax, cudaStream_t s);
 
 // b = rz_new / rz_old per column; p = z + b p; rz_old = rz_new
 template <typename T>
 int launch_cg_direction(long long Gt, int C, double* rz_old, const double* rz_new, const T* z, T* p, cudaStream_t s);
 
 // r = counts * mu, z = p = mu (cast to T); partials of r.z and max |z|
+// inv_counts[g] = 1 / counts[g] (0 for empty groups)
+int launch_inv_counts(const int32_t* counts, long long G, double* inv_counts, cudaStream_t s);
+
 template <typename T>
 int launch_cg_init(long long Gt, int C, const int32_t* counts, const double* mu, T* r, T* z, T* p,
-                   double* rz_partials, unsigned long long* zmax, cudaStream_t s);
+                   double* rz_partials, double* zmax_partials, unsigned long long* zmax, cudaStream_t s);
 
 }  // namespace fegb

@@ -91,10 +91,15 @@ typedef struct fegb_result {
     double time_se;
     double time_total;
     /* sweep-kernel timing when cfg.profile = 1, by kernel family:
-     * [0] segment sweep FP64, [1] segment sweep FP32, [2] small-G sweep FP64, [3] small-G sweep FP32 */
-    int prof_launches[4];
-    double prof_seconds[4];   /* summed CUDA-event durations of those launches */
-    double prof_bytes[4];     /* summed algorithmic bytes of those launches */
+     * data sweeps (rows read, and written back in storage order):
+     *   [0] segment FP64, [1] segment FP32, [2] small-G FP64, [3] small-G FP32
+     *   algorithmic bytes n (4 + 2 C s) per launch;
+     * CG operator sweeps (no row data; ids and L2-resident FE tables):
+     *   [4] segment FP64, [5] segment FP32, [6] small-G FP64, [7] small-G FP32
+     *   algorithmic bytes n * 4 * (number of id arrays read) per launch */
+    int prof_launches[8];
+    double prof_seconds[8];   /* summed CUDA-event durations of those launches */
+    double prof_bytes[8];     /* summed algorithmic bytes of those launches */
 } fegb_result;
 
 /* Default configuration (tolerance 1e-6, 500 iterations, FP64, AP, GPU conventions). */

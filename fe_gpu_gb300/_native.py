@@ -126,6 +126,7 @@ SIGNATURES = {
     "fe_gpu_linalg_init": (_I, []),
     "fe_gpu_linalg_shutdown": (_I, []),
     "fe_gpu_syrk": (_I, [_I, _I, _D, _P, _I, _D, _P]),
+    "fe_gpu_syrk_noalloc": (_I, [_I, _I, _D, _P, _I, _D, _P]),
     "fe_gpu_gemv": (_I, [_I, _I, _D, _P, _I, _P, _D, _P]),
     "fe_gpu_residual": (_I, [_I, _I, _P, _I, _P, _P, _P]),
     "fe_gpu_dot": (_I, [_I, _P, _P, _DP]),

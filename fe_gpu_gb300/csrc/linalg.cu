@@ -1,7 +1,9 @@
 // Tall-skinny reductions and small dense kernels (see linalg.cuh).
 #include "linalg.cuh"
 
+#include <algorithm>
 #include <cmath>
+#include <mutex>
 
 namespace fegb {
 
@@ -562,3 +564,106 @@ int dense_finalize_cov(int k, double* acc, double scalar, int do_psd, double* se
 }
 
 }  // namespace fegb
+
+// ---------------------------------------------------------------------------
+// Allocation-free cross product (fe_gpu_syrk_noalloc, include/fe_gpu_runtime.h).
+//
+// fe_gpu_syrk takes the per-block partial sums of its reduction from the
+// stream-ordered memory pool. Some callers cannot let a library allocate
+// device memory while they run: a host that owns every device buffer through
+// its own allocator and budget, or code that must not touch the allocator
+// at all in a latency-critical section. For them this variant keeps the
+// partials in a fixed file-scope device array of
+// NOALLOC_BLOCKS x NOALLOC_MAX_PAIRS doubles (152 x 528 x 8 B = 642 KB, held
+// by every GPU that loads the library until the process exits), which bounds
+// the input to at most NOALLOC_MAX_COLS = 32 columns.
+//
+// The device address of the array is looked up once per device with
+// cudaGetSymbolAddress, by the first call made while that device is current;
+// make that first call before capturing any stream. Every call shares the
+// one array: calls whose kernels overlap on the GPU (other host threads, or
+// other streams) race on it. Each launch overwrites every partial it later
+// reads, so nothing has to be cleared between calls.
+// ---------------------------------------------------------------------------
+namespace fegb {
+
+namespace {
+
+constexpr int NOALLOC_BLOCKS = 152;
+constexpr int NOALLOC_MAX_COLS = 32;
+constexpr int NOALLOC_MAX_PAIRS = NOALLOC_MAX_COLS * (NOALLOC_MAX_COLS + 1) / 2;
+
+__device__ __align__(256) double g_syrk_noalloc_partials[NOALLOC_BLOCKS * NOALLOC_MAX_PAIRS];
+
+constexpr int NOALLOC_MAX_DEVICES = 64;
+std::mutex g_noalloc_mu;
+double* g_noalloc_partials[NOALLOC_MAX_DEVICES] = {};
+
+// Device address of the partials array for the current device (set-up on the
+// first call per device).
+int noalloc_partials(double** out) {
+    int dev = 0;
+    FEGB_CUDA(cudaGetDevice(&dev), "cudaGetDevice");
+    if (dev < 0 || dev >= NOALLOC_MAX_DEVICES) return set_error("fe_gpu_syrk_noalloc: device %d out of range", dev);
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (!g_noalloc_partials[dev]) {
+        void* p = nullptr;
+        FEGB_CUDA(cudaGetSymbolAddress(&p, g_syrk_noalloc_partials), "cudaGetSymbolAddress (syrk scratch)");
+        g_noalloc_partials[dev] = static_cast<double*>(p);
+    }
+    *out = g_noalloc_partials[dev];
+    return 0;
+}
+
+}  // namespace
+
+}  // namespace fegb
+
+extern "C" int fe_gpu_syrk_noalloc(int n_rows, int n_cols, double alpha, const double* W, int ldW, double beta,
+                                   double* Q) {
+    using namespace fegb;
+    if (n_cols == 0) return set_ok();
+    if (n_cols < 0 || n_rows < 0) return set_error("fe_gpu_syrk_noalloc: negative dimension");
+    if (n_cols > NOALLOC_MAX_COLS)
+        return set_error("fe_gpu_syrk_noalloc: n_cols=%d exceeds the %d-column limit of its fixed scratch", n_cols,
+                         NOALLOC_MAX_COLS);
+    double* partials = nullptr;
+    FEGB_TRY(noalloc_partials(&partials));
+    const cudaStream_t s = 0;  // legacy default stream, as the rest of the kernel-level ABI
+    const int npairs = n_cols * (n_cols + 1) / 2;
+    int nb = 0;
+    if (n_rows > 0) {
+        long long blocks = std::min<long long>(((long long)n_rows + CP_TR - 1) / CP_TR, NOALLOC_BLOCKS);
+        long long rpb = ((long long)n_rows + blocks - 1) / blocks;
+        rpb = ((rpb + CP_TR - 1) / CP_TR) * CP_TR;
+        nb = (int)(((long long)n_rows + rpb - 1) / rpb);
+        CPParams p;
+        p.A = W;
+        p.ars = 1;
+        p.acs = ldW;
+        p.a = n_cols;
+        p.B = W;
+        p.brs = 1;
+        p.bcs = ldW;
+        p.b = n_cols;
+        p.n = n_rows;
+        p.gram = 1;
+        p.p0 = 0;
+        p.npairs = npairs;
+        p.phases = npairs <= 128 ? CP_THREADS / npairs : 1;
+        p.rows_per_block = rpb;
+        p.partials = partials;
+        const size_t smem = sizeof(double) * CP_TR * n_cols;
+        if (npairs <= 128)
+            crossprod_kernel<1><<<nb, CP_THREADS, smem, s>>>(p);
+        else
+            crossprod_kernel<4><<<nb, CP_THREADS, smem, s>>>(p);
+        FEGB_LAUNCH_CHECK("syrk noalloc");
+    }
+    // nb = 0 (no rows) leaves Q = beta Q on the upper triangle
+    crossprod_reduce_kernel<<<(npairs + 255) / 256, 256, 0, s>>>(partials, nb, npairs, 0, 1, 1, n_cols, alpha, beta, Q,
+                                                                  n_cols);
+    FEGB_LAUNCH_CHECK("syrk noalloc reduce");
+    FEGB_CUDA(cudaStreamSynchronize(s), "syrk noalloc sync");
+    return set_ok();
+}

@@ -60,6 +60,16 @@ int fe_gpu_linalg_init(void);
 int fe_gpu_linalg_shutdown(void);
 /* Q (upper triangle, n_cols x n_cols, ld n_cols) = alpha W^T W + beta Q */
 int fe_gpu_syrk(int n_rows, int n_cols, double alpha, const double* W, int ldW, double beta, double* Q);
+/* Same result as fe_gpu_syrk without allocating device memory (no
+ * counterpart in the reference). For callers that cannot let a library
+ * allocate while they run -- a host that owns every device buffer through its
+ * own allocator and budget, or a section that must not touch the allocator.
+ * Its partial sums live in a fixed 642 KB device array held by every GPU that
+ * loads the library; n_cols is limited to 32 (larger requests return a
+ * nonzero status). The first call on each device (with that device current)
+ * looks up the array's address; make it before any stream capture. All calls
+ * share the array: calls that overlap on the GPU race. */
+int fe_gpu_syrk_noalloc(int n_rows, int n_cols, double alpha, const double* W, int ldW, double beta, double* Q);
 /* b = alpha W^T y + beta b */
 int fe_gpu_gemv(int n_rows, int n_cols, double alpha, const double* W, int ldW, const double* y, double beta,
                 double* b);

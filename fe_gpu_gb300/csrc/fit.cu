@@ -45,6 +45,8 @@ struct Dim {
     std::vector<int32_t*> gid_at_perm;  // [e] gid of dim e at traversal positions (gather)
     int32_t* long_list = nullptr;       // groups spanning more than SEG_LONG_SPAN chunks
     int n_long = 0;
+    int32_t* long_list_cg = nullptr;    // the same for the CG operator's chunk size
+    int n_long_cg = 0;
     double* prev = nullptr;
     double* pend64 = nullptr;
     float* pend32 = nullptr;
@@ -258,7 +260,8 @@ double bits_to_double(unsigned long long b) {
 
 // Builds the storage-order problem from device inputs in the reference layout.
 int build_problem(Problem& P, long long n_in, int k, int l, int n_fe, const double* y, const double* W, const double* Z,
-                  const int32_t* const* ids, const int* G_in, bool drop_singletons, bool mixed, long long* n_single) {
+                  const int32_t* const* ids, const int* G_in, bool drop_singletons, bool mixed, long long* n_single,
+                  bool sorted_all = false) {
     cudaStream_t s = P.s;
     Scratch& scr = *P.scr;
     P.k = k;
@@ -372,7 +375,8 @@ int build_problem(Problem& P, long long n_in, int k, int l, int n_fe, const doub
         } else {
             D.mode = MODE_GATHER;
         }
-        if (D.mode == MODE_GATHER && n > 0) {
+        const bool need_sorted = D.mode == MODE_GATHER || (sorted_all && d != P.primary);
+        if (need_sorted && n > 0) {
             uint32_t* sorted = nullptr;
             FEGB_TRY(dalloc(scr, &sorted, (size_t)n, "gather gseq"));
             FEGB_TRY(dalloc(scr, &D.perm, (size_t)n, "gather perm"));
@@ -380,7 +384,7 @@ int build_problem(Problem& P, long long n_in, int k, int l, int n_fe, const doub
                                     bits_for((unsigned long long)D.G), s, scr));
             D.gseq = reinterpret_cast<int32_t*>(sorted);
         }
-        if (D.mode != MODE_SMALLG) {
+        if (D.mode != MODE_SMALLG || need_sorted) {
             FEGB_TRY(dalloc(scr, &D.off, (size_t)D.G + 1, "offsets"));
             if (n > 0) {
                 FEGB_TRY(segment_offsets(reinterpret_cast<const uint32_t*>(D.gseq), n, D.G, D.off, s));
@@ -392,8 +396,13 @@ int build_problem(Problem& P, long long n_in, int k, int l, int n_fe, const doub
                 FEGB_LAUNCH_CHECK("counts");
                 FEGB_TRY(dalloc(scr, &D.long_list, (size_t)D.G, "long groups"));
                 FEGB_TRY(find_long_groups(D.off, D.G, CHUNK_R, D.long_list, &D.n_long, s));
+                if (sorted_all) {
+                    FEGB_TRY(dalloc(scr, &D.long_list_cg, (size_t)D.G, "long groups (cg)"));
+                    FEGB_TRY(find_long_groups(D.off, D.G, CG_CHUNK, D.long_list_cg, &D.n_long_cg, s));
+                }
             }
-        } else {
+        }
+        if (D.mode == MODE_SMALLG) {
             FEGB_CUDA(cudaMemsetAsync(D.counts, 0, sizeof(int32_t) * (size_t)D.G, s), "counts zero");
             if (n > 0) {
                 count_ids_kernel<<<grid_stride_blocks(n, 256), 256, 0, s>>>(D.gid, n, D.counts);
@@ -412,7 +421,7 @@ int build_problem(Problem& P, long long n_in, int k, int l, int n_fe, const doub
     for (int d = 0; d < n_fe; ++d) {
         Dim& D = P.dims[d];
         D.gid_at_perm.assign(n_fe, nullptr);
-        if (D.mode != MODE_GATHER || n == 0) continue;
+        if (!(D.mode == MODE_GATHER || (sorted_all && d != P.primary)) || n == 0) continue;
         for (int e = 0; e < n_fe; ++e) {
             if (e == d) continue;
             FEGB_TRY(dalloc(scr, &D.gid_at_perm[e], (size_t)n, "gid at perm"));
@@ -769,9 +778,11 @@ int demean_mixed(Problem& P, double tol, int max_iter, int* iterations, int* con
 // Scratch of the CG solve in storage type T.
 template <typename T>
 struct CGBuffers {
-    T *r = nullptr, *z = nullptr, *p = nullptr, *q = nullptr;
+    T *r = nullptr, *z = nullptr, *p = nullptr, *q = nullptr, *x = nullptr, *inv = nullptr;
+    int ld = 0;  // padded row stride of the G-space vectors
     double *rz = nullptr, *rz_new = nullptr, *pq = nullptr;
     double *rz_part = nullptr, *pq_part = nullptr, *zmax_part = nullptr;
+    double *sums = nullptr, *head = nullptr, *tail = nullptr;
     unsigned long long* zmax = nullptr;
     int rz_blocks = 0, pq_blocks = 0;
     std::vector<int> pq_block_off;
@@ -780,25 +791,43 @@ struct CGBuffers {
 template <typename T>
 int cg_alloc(Problem& P, CGBuffers<T>& B) {
     Scratch& scr = *P.scr;
-    const size_t n = (size_t)std::max(1LL, P.Gt) * P.C;
+    B.ld = cg_row_stride(P.C, (int)sizeof(T));
+    const size_t n = (size_t)std::max(1LL, P.Gt) * B.ld;
     FEGB_TRY(dalloc(scr, &B.r, n, "cg r"));
     FEGB_TRY(dalloc(scr, &B.z, n, "cg z"));
     FEGB_TRY(dalloc(scr, &B.p, n, "cg p"));
     FEGB_TRY(dalloc(scr, &B.q, n, "cg q"));
-    FEGB_TRY(dalloc(scr, &B.rz, (size_t)P.C, "cg rz"));
-    FEGB_TRY(dalloc(scr, &B.rz_new, (size_t)P.C, "cg rz new"));
-    FEGB_TRY(dalloc(scr, &B.pq, (size_t)P.C, "cg pq"));
+    FEGB_TRY(dalloc(scr, &B.x, n, "cg solution"));
+    FEGB_TRY(dalloc(scr, &B.inv, (size_t)std::max(1LL, P.Gt), "cg inverse counts"));
+    FEGB_TRY(launch_inv_counts_t<T>(P.counts_all, P.Gt, B.inv, P.s));
+    const int L = B.ld;
+    FEGB_TRY(dalloc(scr, &B.rz, (size_t)L, "cg rz"));
+    FEGB_TRY(dalloc(scr, &B.rz_new, (size_t)L, "cg rz new"));
+    FEGB_TRY(dalloc(scr, &B.pq, (size_t)L, "cg pq"));
     FEGB_TRY(dalloc(scr, &B.zmax, 1, "cg zmax"));
-    B.rz_blocks = cg_partial_blocks(P.Gt * P.C);
+    B.rz_blocks = cg_partial_blocks(P.Gt * L);
     B.pq_block_off.assign(P.n_fe + 1, 0);
     for (int d = 0; d < P.n_fe; ++d)
-        B.pq_block_off[d + 1] = B.pq_block_off[d] + cg_partial_blocks((long long)std::max(1, P.dims[d].G) * P.C);
+        B.pq_block_off[d + 1] = B.pq_block_off[d] + cg_partial_blocks((long long)std::max(1, P.dims[d].G) * L);
     B.pq_blocks = B.pq_block_off[P.n_fe];
-    FEGB_TRY(dalloc(scr, &B.rz_part, (size_t)B.rz_blocks * P.C, "cg rz partials"));
+    FEGB_TRY(dalloc(scr, &B.rz_part, (size_t)B.rz_blocks * L, "cg rz partials"));
     FEGB_TRY(dalloc(scr, &B.zmax_part, (size_t)B.rz_blocks, "cg zmax partials"));
-    FEGB_TRY(dalloc(scr, &B.pq_part, (size_t)std::max(1, B.pq_blocks) * P.C, "cg pq partials"));
-    FEGB_CUDA(cudaMemsetAsync(B.pq_part, 0, sizeof(double) * (size_t)std::max(1, B.pq_blocks) * P.C, P.s),
+    FEGB_TRY(dalloc(scr, &B.pq_part, (size_t)std::max(1, B.pq_blocks) * L, "cg pq partials"));
+    FEGB_CUDA(cudaMemsetAsync(B.pq_part, 0, sizeof(double) * (size_t)std::max(1, B.pq_blocks) * L, P.s),
               "cg pq partials zero");
+    // the operator sweep writes sums/head/tail at the padded stride
+    if (L > P.C) {
+        long long nchunks = std::max(1LL, seg_nchunks(P.n, CG_CHUNK));
+        int gmax = 1;
+        for (int d = 0; d < P.n_fe; ++d) gmax = std::max(gmax, P.dims[d].G);
+        FEGB_TRY(dalloc(scr, &B.sums, (size_t)gmax * L, "cg sums"));
+        FEGB_TRY(dalloc(scr, &B.head, (size_t)nchunks * L, "cg heads"));
+        FEGB_TRY(dalloc(scr, &B.tail, (size_t)nchunks * L, "cg tails"));
+    } else {
+        B.sums = P.sums;
+        B.head = P.head;
+        B.tail = P.tail;
+    }
     return 0;
 }
 
@@ -807,13 +836,14 @@ int cg_alloc(Problem& P, CGBuffers<T>& B) {
 template <typename T>
 int cg_apply(Problem& P, CGBuffers<T>& B) {
     const int C = P.C;
+    const int L = B.ld;
     for (int d = 0; d < P.n_fe; ++d) {
         Dim& D = P.dims[d];
         if (D.G <= 0) continue;
         Problem::Timed tm{};
         if (P.profile) {
             tm.kind = 4 + (D.mode == MODE_SMALLG ? 2 : 0) + (sizeof(T) == 4 ? 1 : 0);
-            tm.bytes = (double)P.n * 4.0 * (P.n_fe - (D.mode == MODE_SMALLG ? 0 : 0));
+            tm.bytes = (double)P.n * 4.0 * P.n_fe;  // destination + source ids per position
             FEGB_CUDA(cudaEventCreate(&tm.a), "profile event");
             FEGB_CUDA(cudaEventCreate(&tm.b), "profile event");
             FEGB_CUDA(cudaEventRecord(tm.a, P.s), "profile record");
@@ -826,58 +856,52 @@ int cg_apply(Problem& P, CGBuffers<T>& B) {
             ps.tab[ps.n] = B.p + P.goff[e] * C;
             ++ps.n;
         }
-        if (D.mode == MODE_SMALLG) {
-            SmallGParams<T> sp{};
-            sp.X = nullptr;
-            sp.C = C;
-            sp.n = P.n;
-            sp.gid = D.gid;
-            sp.G = D.G;
-            sp.pend = ps;
-            sp.writeback = 0;
-            sp.no_data = 1;
-            sp.rows_per_block = (P.n + P.smallg_nb - 1) / P.smallg_nb;
-            sp.partials = P.partials;
-            FEGB_TRY(launch_smallg_sweep<T>(sp, P.smallg_nb, P.s));
-            FEGB_TRY(launch_fold_smallg(P.partials, P.smallg_nb, D.G, C, P.sums, P.s));
-        } else {
-            SegSweepParams<T> sp{};
-            sp.X = nullptr;
-            sp.rs = C;
-            sp.cs = 1;
-            sp.C = C;
-            sp.n = P.n;
-            sp.perm = D.mode == MODE_GATHER ? D.perm : nullptr;
-            sp.gseq = D.gseq;
-            sp.pend = ps;
-            sp.writeback = 0;
-            sp.no_data = 1;
-            sp.R = CHUNK_R;
-            sp.sums = P.sums;
-            sp.head = P.head;
-            sp.tail = P.tail;
-            FEGB_TRY(launch_seg_sweep<T>(sp, P.s));
-            FEGB_TRY(launch_long_sums(D.off, P.head, P.tail, CHUNK_R, C, D.long_list, D.n_long, P.sums, P.s));
+        // every dimension is traversed in its group-sorted order (identity for the primary)
+        CGRowsParams<T> rp{};
+        rp.n = P.n;
+        rp.C = C;
+        rp.ld = L;
+        rp.gseq = D.gseq;
+        rp.n_src = 0;
+        for (int e = 0; e < P.n_fe; ++e) {
+            if (e == d) continue;
+            rp.src_gid[rp.n_src] = d == P.primary ? P.dims[e].gid : D.gid_at_perm[e];
+            rp.src_tab[rp.n_src] = B.p + P.goff[e] * L;
+            ++rp.n_src;
         }
+        rp.sums = B.sums;
+        rp.head = B.head;
+        rp.tail = B.tail;
+        FEGB_TRY(launch_cg_rows<T>(rp, P.s));
+        FEGB_TRY(launch_long_sums(D.off, B.head, B.tail, CG_CHUNK, L, D.long_list_cg, D.n_long_cg, B.sums, P.s));
         if (P.profile) {
             FEGB_CUDA(cudaEventRecord(tm.b, P.s), "profile record");
             P.timed.push_back(tm);
         }
-        FinalizeParams src = finalize_base(P, d);
-        FEGB_TRY(launch_cg_q<T>(src, B.p + P.goff[d] * C, B.q + P.goff[d] * C, B.pq_part + (size_t)B.pq_block_off[d] * C,
-                                P.s));
+        FinalizeParams src{};
+        src.G = D.G;
+        src.C = L;
+        src.off = D.off;
+        src.sums = B.sums;
+        src.head = B.head;
+        src.tail = B.tail;
+        src.R = CG_CHUNK;
+        src.counts = D.counts;
+        FEGB_TRY(launch_cg_q<T>(src, C, B.p + P.goff[d] * L, B.q + P.goff[d] * L,
+                                B.pq_part + (size_t)B.pq_block_off[d] * L, P.s));
         P.projections += 1;
-        P.demean_bytes += (double)P.n * 4.0 * (P.n_fe + (D.mode == MODE_GATHER ? 1 : 0));
+        P.demean_bytes += (double)P.n * 4.0 * P.n_fe;
     }
-    return launch_fold_partials(B.pq_part, B.pq_blocks, C, B.pq, P.s);
+    return launch_fold_partials(B.pq_part, B.pq_blocks, L, B.pq, P.s);
 }
 
 // Preconditioned (group-count) CG on D'D delta = D'r, r = current FP64
 // residual whose group means are in mu_all; delta accumulates into alpha_all.
 template <typename T>
 int cg_solve(Problem& P, CGBuffers<T>& B, double inner_tol, int max_it, int* iters, double* zmax_out) {
-    const int C = P.C;
-    FEGB_TRY(launch_cg_init<T>(P.Gt, C, P.counts_all, P.mu_all, B.r, B.z, B.p, B.rz_part, B.zmax_part, B.zmax, P.s));
+    const int C = B.ld;  // vector ops run over the padded rows (padding stays zero)
+    FEGB_TRY(launch_cg_init<T>(P.Gt, C, P.C, P.counts_all, P.mu_all, B.r, B.z, B.p, B.x, B.rz_part, B.zmax_part,
+                               B.zmax, P.s));
     FEGB_TRY(launch_fold_partials(B.rz_part, B.rz_blocks, C, B.rz, P.s));
     double best = DBL_MAX;
     int since_best = 0;
@@ -885,8 +909,8 @@ int cg_solve(Problem& P, CGBuffers<T>& B, double inner_tol, int max_it, int* ite
     double zm = 0.0;
     for (; it < max_it; ++it) {
         FEGB_TRY(cg_apply<T>(P, B));
-        FEGB_TRY(launch_cg_update<T>(P.Gt, C, P.inv_counts_all, B.rz, B.pq, B.p, B.q, P.alpha_all, B.r, B.z,
-                                     B.rz_part, B.zmax_part, B.zmax, P.s));
+        FEGB_TRY(launch_cg_update<T>(P.Gt, C, B.inv, B.rz, B.pq, B.p, B.q, B.x, B.r, B.z, B.rz_part, B.zmax_part,
+                                     B.zmax, P.s));
         FEGB_TRY(launch_fold_partials(B.rz_part, B.rz_blocks, C, B.rz_new, P.s));
         unsigned long long bits = 0;
         FEGB_TRY(d2h_sync(&bits, B.zmax, sizeof(bits), P.s, "cg zmax copy"));
@@ -906,7 +930,8 @@ int cg_solve(Problem& P, CGBuffers<T>& B, double inner_tol, int max_it, int* ite
     }
     *iters = it;
     *zmax_out = zm;
-    return 0;
+    // the increment of this solve becomes the FP64 table applied by the next FP64 pass
+    return launch_to_f64<T>(B.x, B.ld, P.alpha_all, P.C, P.Gt, P.s);
 }
 
 // FP64 refinement loop around a CG inner solve in storage type T.
@@ -933,7 +958,6 @@ int demean_cg(Problem& P, double tol, int max_iter, int* iterations, int* conver
         if (total >= max_iter) break;
         if (round > 2 && mu > 0.5 * mu_prev) break;
         mu_prev = mu;
-        FEGB_CUDA(cudaMemsetAsync(P.alpha_all, 0, sizeof(double) * (size_t)P.Gt * P.C, P.s), "alpha zero");
         const double inner_tol =
             sizeof(T) == 4 ? std::max(0.5 * tol, 2e-6 * mu) : std::max(0.5 * tol, 1e-12 * mu);
         int it = 0;
@@ -1472,7 +1496,8 @@ int estimate_device_impl(const fegb_config* cfg_in, long long n, int k, int l, i
     auto t0 = Clock::now();
     long long n_single = 0;
     FEGB_TRY(build_problem(P, n, k, l, n_fe, y, W, Z, ids, group_sizes, cfg.drop_singletons != 0,
-                           cfg.precision == FEGB_PREC_MIXED && cfg.demean_method == FEGB_DEMEAN_AP, &n_single));
+                           cfg.precision == FEGB_PREC_MIXED && cfg.demean_method == FEGB_DEMEAN_AP, &n_single,
+                           cfg.demean_method == FEGB_DEMEAN_CG));
     std::vector<int> G(n_fe);
     for (int d = 0; d < n_fe; ++d) G[d] = P.dims[d].G;
     // TSS of the raw y over the rows used
@@ -1585,7 +1610,8 @@ int fegb_within_transform(const fegb_config* cfg_in, long long n, int k, int l, 
     for (int d = 0; d < n_fe; ++d) ids[d] = d_fe_ids[d];
     long long n_single = 0;
     FEGB_TRY(build_problem(P, n, k, l, n_fe, d_y, d_W, d_Z, ids.data(), group_sizes, false,
-                           cfg.precision == FEGB_PREC_MIXED && cfg.demean_method == FEGB_DEMEAN_AP, &n_single));
+                           cfg.precision == FEGB_PREC_MIXED && cfg.demean_method == FEGB_DEMEAN_AP, &n_single,
+                           cfg.demean_method == FEGB_DEMEAN_CG));
     int it = 0, conv = 1, outer = 0;
     double mu = 0.0;
     if (cfg.demean_method == FEGB_DEMEAN_CG) {

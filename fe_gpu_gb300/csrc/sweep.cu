@@ -312,38 +312,44 @@ __global__ void convert_kernel(const double* __restrict__ src, float* __restrict
 
 
 // Per-block, per-column partial sums of prod over a block's elements
-// (element idx has column idx % C); fixed order, deterministic.
-__device__ __forceinline__ void column_partials(double prod, long long base, int C, double* smem, double* out) {
+// (element idx has column idx % C); fixed order, deterministic. Accumulates in
+// A (FP32 for the FP32 form, FP64 otherwise); stored as FP64.
+template <typename A>
+__device__ __forceinline__ void column_partials(A prod, long long base, int C, A* smem, double* out) {
     smem[threadIdx.x] = prod;
     __syncthreads();
     if (threadIdx.x < C) {
         const int c = threadIdx.x;
         const int first = (int)((c - base % C + C) % C);
-        double acc = 0.0;
+        A acc = A(0);
         for (int j = first; j < FIN_THREADS; j += C) acc += smem[j];
-        out[(long long)blockIdx.x * C + c] = acc;
+        out[(long long)blockIdx.x * C + c] = (double)acc;
     }
 }
 
 template <typename T>
-__global__ void __launch_bounds__(FIN_THREADS) cg_q_kernel(FinalizeParams src, const T* __restrict__ p,
+__global__ void __launch_bounds__(FIN_THREADS) cg_q_kernel(FinalizeParams src, int creal, const T* __restrict__ p,
                                                             T* __restrict__ q, double* __restrict__ pq_partials) {
-    __shared__ double smem[FIN_THREADS];
+    __shared__ T smem[FIN_THREADS];
     const long long total = (long long)src.G * src.C;
     const long long base = (long long)blockIdx.x * FIN_THREADS;
     const long long idx = base + threadIdx.x;
-    double prod = 0.0;
+    T prod = T(0);
     if (idx < total) {
         const int g = (int)(idx / src.C);
         const int c = (int)(idx - (long long)g * src.C);
-        const double ssum = source_sum(src, g, c, idx, total);
-        const double pv = (double)p[idx];
-        // ssum = -(sum over the group's rows of the other dimensions' p)
-        const double qv = (double)src.counts[g] * pv - ssum;
-        q[idx] = (T)qv;
-        prod = pv * qv;
+        if (c < creal) {
+            const double ssum = source_sum(src, g, c, idx, total);
+            const T pv = p[idx];
+            // ssum = -(sum over the group's rows of the other dimensions' p)
+            const T qv = (T)src.counts[g] * pv - (T)ssum;
+            q[idx] = qv;
+            prod = pv * qv;
+        } else {
+            q[idx] = T(0);
+        }
     }
-    column_partials(prod, base, src.C, smem, pq_partials);
+    column_partials<T>(prod, base, src.C, smem, pq_partials);
 }
 
 // Fixed-shape block tree: thread t folds elements t, t + 256, ... in order,
@@ -412,42 +418,46 @@ __global__ void find_long_kernel(const int32_t* __restrict__ off, int G, int R, 
 
 template <typename T>
 __global__ void __launch_bounds__(FIN_THREADS)
-    cg_update_kernel(long long Gt, int C, const double* __restrict__ inv_counts, const double* __restrict__ rz,
+    cg_update_kernel(long long Gt, int C, const T* __restrict__ inv_counts, const double* __restrict__ rz,
                      const double* __restrict__ pq, const T* __restrict__ p, const T* __restrict__ q,
-                     double* __restrict__ alpha, T* __restrict__ r, T* __restrict__ z,
-                     double* __restrict__ rz_partials, double* __restrict__ zmax_partials) {
-    __shared__ double smem[FIN_THREADS];
-    __shared__ double red[FIN_THREADS / 32];
-    __shared__ double step[64];
+                     T* __restrict__ x, T* __restrict__ r, T* __restrict__ z, double* __restrict__ rz_partials,
+                     double* __restrict__ zmax_partials) {
+    __shared__ T smem[FIN_THREADS];
+    __shared__ T red[FIN_THREADS / 32];
+    __shared__ T step[64];
     const long long total = Gt * C;
     const long long base = (long long)blockIdx.x * FIN_THREADS;
     const long long idx = base + threadIdx.x;
     if (threadIdx.x < C && threadIdx.x < 64) {
         const double den = pq[threadIdx.x];
-        step[threadIdx.x] = den != 0.0 ? rz[threadIdx.x] / den : 0.0;
+        step[threadIdx.x] = (T)(den != 0.0 ? rz[threadIdx.x] / den : 0.0);
     }
     __syncthreads();
-    double prod = 0.0, az = 0.0;
+    T prod = T(0), az = T(0);
     if (idx < total) {
         const long long g = idx / C;
         const int c = (int)(idx - g * C);
-        const double a = C <= 64 ? step[c] : (pq[c] != 0.0 ? rz[c] / pq[c] : 0.0);
-        alpha[idx] += a * (double)p[idx];
-        const double rv = (double)r[idx] - a * (double)q[idx];
-        const double zv = rv * inv_counts[g];
-        r[idx] = (T)rv;
-        z[idx] = (T)zv;
+        const T a = C <= 64 ? step[c] : (T)(pq[c] != 0.0 ? rz[c] / pq[c] : 0.0);
+        x[idx] += a * p[idx];
+        const T rv = r[idx] - a * q[idx];
+        const T zv = rv * inv_counts[g];
+        r[idx] = rv;
+        z[idx] = zv;
         prod = rv * zv;
-        az = fabs(zv);
+        az = zv < T(0) ? -zv : zv;
     }
-    column_partials(prod, base, C, smem, rz_partials);
-    az = warp_max(az);
+    column_partials<T>(prod, base, C, smem, rz_partials);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const T y = __shfl_xor_sync(0xffffffffu, az, o);
+        az = y > az ? y : az;
+    }
     if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = az;
     __syncthreads();
     if (threadIdx.x == 0) {
-        double m = red[0];
-        for (int w = 1; w < FIN_THREADS / 32; ++w) m = fmax(m, red[w]);
-        zmax_partials[blockIdx.x] = m;
+        T m = red[0];
+        for (int w = 1; w < FIN_THREADS / 32; ++w) m = red[w] > m ? red[w] : m;
+        zmax_partials[blockIdx.x] = (double)m;
     }
 }
 
@@ -465,8 +475,8 @@ __global__ void cg_direction_kernel(long long Gt, int C, const double* __restric
     int c = (int)(idx % C);
     const int cstep = (int)(st % C);
     for (; idx < total; idx += st) {
-        const double b = C <= 64 ? beta[c] : (rz_old[c] != 0.0 ? rz_new[c] / rz_old[c] : 0.0);
-        p[idx] = (T)((double)z[idx] + b * (double)p[idx]);
+        const T b = C <= 64 ? (T)beta[c] : (T)(rz_old[c] != 0.0 ? rz_new[c] / rz_old[c] : 0.0);
+        p[idx] = z[idx] + b * p[idx];
         c += cstep;
         if (c >= C) c -= C;
     }
@@ -484,35 +494,57 @@ __global__ void copy_scalars_kernel(const double* __restrict__ src, double* __re
 
 template <typename T>
 __global__ void __launch_bounds__(FIN_THREADS)
-    cg_init_kernel(long long Gt, int C, const int32_t* __restrict__ counts, const double* __restrict__ mu,
-                   T* __restrict__ r, T* __restrict__ z, T* __restrict__ p, double* __restrict__ rz_partials,
-                   double* __restrict__ zmax_partials) {
-    __shared__ double smem[FIN_THREADS];
-    __shared__ double red[FIN_THREADS / 32];
+    cg_init_kernel(long long Gt, int C, int creal, const int32_t* __restrict__ counts, const double* __restrict__ mu,
+                   T* __restrict__ r, T* __restrict__ z, T* __restrict__ p, T* __restrict__ x,
+                   double* __restrict__ rz_partials, double* __restrict__ zmax_partials) {
+    __shared__ T smem[FIN_THREADS];
+    __shared__ T red[FIN_THREADS / 32];
     const long long total = Gt * C;
     const long long base = (long long)blockIdx.x * FIN_THREADS;
     const long long idx = base + threadIdx.x;
-    double prod = 0.0, az = 0.0;
+    T prod = T(0), az = T(0);
     if (idx < total) {
         const long long g = idx / C;
+        const int c = (int)(idx - g * C);
         const int cnt = counts[g];
-        const double m = cnt > 0 ? mu[idx] : 0.0;
-        const double rv = (double)cnt * m;
-        r[idx] = (T)rv;
-        z[idx] = (T)m;
-        p[idx] = (T)m;
+        const T m = (cnt > 0 && c < creal) ? (T)mu[g * creal + c] : T(0);
+        const T rv = (T)cnt * m;
+        r[idx] = rv;
+        z[idx] = m;
+        p[idx] = m;
+        x[idx] = T(0);
         prod = rv * m;
-        az = fabs(m);
+        az = m < T(0) ? -m : m;
     }
-    column_partials(prod, base, C, smem, rz_partials);
-    az = warp_max(az);
+    column_partials<T>(prod, base, C, smem, rz_partials);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const T y = __shfl_xor_sync(0xffffffffu, az, o);
+        az = y > az ? y : az;
+    }
     if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = az;
     __syncthreads();
     if (threadIdx.x == 0) {
-        double mm = red[0];
-        for (int w = 1; w < FIN_THREADS / 32; ++w) mm = fmax(mm, red[w]);
-        zmax_partials[blockIdx.x] = mm;
+        T mm = red[0];
+        for (int w = 1; w < FIN_THREADS / 32; ++w) mm = red[w] > mm ? red[w] : mm;
+        zmax_partials[blockIdx.x] = (double)mm;
     }
+}
+
+template <typename T>
+__global__ void to_f64_kernel(const T* __restrict__ src, int ld, double* __restrict__ dst, int C, long long n) {
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long st = (long long)gridDim.x * blockDim.x;
+    for (; i < n; i += st) {
+        const long long g = i / C;
+        dst[i] = (double)src[g * ld + (i - g * C)];
+    }
+}
+
+template <typename T>
+__global__ void inv_counts_t_kernel(const int32_t* __restrict__ counts, long long G, T* __restrict__ inv) {
+    long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (g < G) inv[g] = counts[g] > 0 ? T(1) / (T)counts[g] : T(0);
 }
 
 // out (bits) = max over partials (one block, fixed tree); max is exact.
@@ -616,10 +648,10 @@ int launch_convert_f64_f32(const double* src, float* dst, long long n, cudaStrea
 int cg_partial_blocks(long long gc) { return (int)((gc + FIN_THREADS - 1) / FIN_THREADS); }
 
 template <typename T>
-int launch_cg_q(const FinalizeParams& src, const T* p, T* q, double* pq_partials, cudaStream_t s) {
+int launch_cg_q(const FinalizeParams& src, int creal, const T* p, T* q, double* pq_partials, cudaStream_t s) {
     long long total = (long long)src.G * src.C;
     if (total <= 0) return 0;
-    cg_q_kernel<T><<<cg_partial_blocks(total), FIN_THREADS, 0, s>>>(src, p, q, pq_partials);
+    cg_q_kernel<T><<<cg_partial_blocks(total), FIN_THREADS, 0, s>>>(src, creal, p, q, pq_partials);
     FEGB_LAUNCH_CHECK("cg q");
     return 0;
 }
@@ -668,13 +700,13 @@ int launch_inv_counts(const int32_t* counts, long long G, double* inv_counts, cu
 }
 
 template <typename T>
-int launch_cg_update(long long Gt, int C, const double* inv_counts, const double* rz, const double* pq, const T* p,
-                     const T* q, double* alpha, T* r, T* z, double* rz_partials, double* zmax_partials,
+int launch_cg_update(long long Gt, int C, const T* inv_counts, const double* rz, const double* pq, const T* p,
+                     const T* q, T* x, T* r, T* z, double* rz_partials, double* zmax_partials,
                      unsigned long long* zmax, cudaStream_t s) {
     long long total = Gt * C;
     if (total <= 0) return 0;
     const int nb = cg_partial_blocks(total);
-    cg_update_kernel<T><<<nb, FIN_THREADS, 0, s>>>(Gt, C, inv_counts, rz, pq, p, q, alpha, r, z, rz_partials,
+    cg_update_kernel<T><<<nb, FIN_THREADS, 0, s>>>(Gt, C, inv_counts, rz, pq, p, q, x, r, z, rz_partials,
                                                    zmax_partials);
     FEGB_LAUNCH_CHECK("cg update");
     fold_max_kernel<<<1, FIN_THREADS, 0, s>>>(zmax_partials, nb, zmax);
@@ -695,33 +727,232 @@ int launch_cg_direction(long long Gt, int C, double* rz_old, const double* rz_ne
 }
 
 template <typename T>
-int launch_cg_init(long long Gt, int C, const int32_t* counts, const double* mu, T* r, T* z, T* p,
+int launch_cg_init(long long Gt, int C, int creal, const int32_t* counts, const double* mu, T* r, T* z, T* p, T* x,
                    double* rz_partials, double* zmax_partials, unsigned long long* zmax, cudaStream_t s) {
     long long total = Gt * C;
     if (total <= 0) return 0;
     const int nb = cg_partial_blocks(total);
-    cg_init_kernel<T><<<nb, FIN_THREADS, 0, s>>>(Gt, C, counts, mu, r, z, p, rz_partials, zmax_partials);
+    cg_init_kernel<T><<<nb, FIN_THREADS, 0, s>>>(Gt, C, creal, counts, mu, r, z, p, x, rz_partials, zmax_partials);
     FEGB_LAUNCH_CHECK("cg init");
     fold_max_kernel<<<1, FIN_THREADS, 0, s>>>(zmax_partials, nb, zmax);
     FEGB_LAUNCH_CHECK("cg max fold");
     return 0;
 }
 
-template int launch_cg_q<double>(const FinalizeParams&, const double*, double*, double*, cudaStream_t);
-template int launch_cg_q<float>(const FinalizeParams&, const float*, float*, double*, cudaStream_t);
+template int launch_cg_q<double>(const FinalizeParams&, int, const double*, double*, double*, cudaStream_t);
+template int launch_cg_q<float>(const FinalizeParams&, int, const float*, float*, double*, cudaStream_t);
 template int launch_cg_update<double>(long long, int, const double*, const double*, const double*, const double*,
                                       const double*, double*, double*, double*, double*, double*,
                                       unsigned long long*, cudaStream_t);
-template int launch_cg_update<float>(long long, int, const double*, const double*, const double*, const float*,
-                                     const float*, double*, float*, float*, double*, double*, unsigned long long*,
+template int launch_cg_update<float>(long long, int, const float*, const double*, const double*, const float*,
+                                     const float*, float*, float*, float*, double*, double*, unsigned long long*,
                                      cudaStream_t);
+
+template <typename T>
+int launch_to_f64(const T* src, int ld, double* dst, int C, long long G, cudaStream_t s) {
+    const long long n = G * C;
+    if (n <= 0) return 0;
+    to_f64_kernel<T><<<grid_stride_blocks(n, 256), 256, 0, s>>>(src, ld, dst, C, n);
+    FEGB_LAUNCH_CHECK("to fp64");
+    return 0;
+}
+template int launch_to_f64<float>(const float*, int, double*, int, long long, cudaStream_t);
+template int launch_to_f64<double>(const double*, int, double*, int, long long, cudaStream_t);
+
+template <typename T>
+int launch_inv_counts_t(const int32_t* counts, long long G, T* inv, cudaStream_t s) {
+    if (G <= 0) return 0;
+    inv_counts_t_kernel<T><<<(unsigned)((G + 255) / 256), 256, 0, s>>>(counts, G, inv);
+    FEGB_LAUNCH_CHECK("inverse counts");
+    return 0;
+}
+template int launch_inv_counts_t<float>(const int32_t*, long long, float*, cudaStream_t);
+template int launch_inv_counts_t<double>(const int32_t*, long long, double*, cudaStream_t);
 template int launch_cg_direction<double>(long long, int, double*, const double*, const double*, double*,
                                          cudaStream_t);
 template int launch_cg_direction<float>(long long, int, double*, const double*, const float*, float*, cudaStream_t);
-template int launch_cg_init<double>(long long, int, const int32_t*, const double*, double*, double*, double*,
-                                    double*, double*, unsigned long long*, cudaStream_t);
-template int launch_cg_init<float>(long long, int, const int32_t*, const double*, float*, float*, float*, double*,
-                                   double*, unsigned long long*, cudaStream_t);
+template int launch_cg_init<double>(long long, int, int, const int32_t*, const double*, double*, double*, double*,
+                                    double*, double*, double*, unsigned long long*, cudaStream_t);
+template int launch_cg_init<float>(long long, int, int, const int32_t*, const double*, float*, float*, float*, float*,
+                                   double*, double*, unsigned long long*, cudaStream_t);
+
+
+// ----------------------- row-per-lane CG operator sweep -----------------------
+
+
+// TILE = columns per pass (compile-time register tile; all per-column arrays
+// stay in registers because every loop over TILE is fully unrolled).
+template <typename T, int CGR_TILE>
+__global__ void __launch_bounds__(256, (sizeof(T) == 4 && CGR_TILE <= 12) ? 4 : 2) cg_rows_kernel(CGRowsParams<T> p, int ntiles) {
+    const int lane = threadIdx.x & 31;
+    const long long warp = ((long long)blockIdx.x * 256 + threadIdx.x) >> 5;
+    const long long nchunks = (p.n + CG_CHUNK - 1) / CG_CHUNK;
+    if (warp >= nchunks * ntiles) return;  // whole warp exits together
+    const long long q = warp / ntiles;
+    const int c0 = (int)(warp - q * ntiles) * CGR_TILE;
+    const int C = p.C;
+    const int LD = p.ld;
+    const int cw = min(CGR_TILE, C - c0);
+    const long long j0 = q * CG_CHUNK;
+    const long long j1 = min(j0 + (long long)CG_CHUNK, p.n);
+    const long long ls = j0 + (long long)lane * CG_LANE_POS;
+    const long long le = min(ls + CG_LANE_POS, j1);
+    const bool empty = ls >= le;
+    const int32_t* __restrict__ gseq = p.gseq;
+
+    int firstg = -1, cur = -1;
+    bool single = true;
+    T head[CGR_TILE], run[CGR_TILE];
+#pragma unroll
+    for (int i = 0; i < CGR_TILE; ++i) {
+        head[i] = T(0);
+        run[i] = T(0);
+    }
+    for (long long j = ls; j < le; ++j) {
+        const int g = __ldcs(gseq + j);
+        T v[CGR_TILE];
+#pragma unroll
+        for (int i = 0; i < CGR_TILE; ++i) v[i] = T(0);
+        for (int e = 0; e < p.n_src; ++e) {
+            const T* __restrict__ tab = p.src_tab[e] + (long long)__ldcs(p.src_gid[e] + j) * LD + c0;
+            // 16-byte vector loads of the padded row (LD and c0 are multiples of the vector width)
+            constexpr int VEC = 16 / (int)sizeof(T);
+            constexpr int NV = (CGR_TILE + VEC - 1) / VEC;
+#pragma unroll
+            for (int k = 0; k < NV; ++k) {
+                if (k * VEC >= cw) break;
+                if constexpr (sizeof(T) == 4) {
+                    const float4 w = *reinterpret_cast<const float4*>(tab + 4 * k);
+                    const T wv[4] = {w.x, w.y, w.z, w.w};
+#pragma unroll
+                    for (int m = 0; m < 4; ++m)
+                        if (4 * k + m < CGR_TILE) v[4 * k + m] -= wv[m];
+                } else {
+                    const double2 w = *reinterpret_cast<const double2*>(tab + 2 * k);
+                    const T wv[2] = {w.x, w.y};
+#pragma unroll
+                    for (int m = 0; m < 2; ++m)
+                        if (2 * k + m < CGR_TILE) v[2 * k + m] -= wv[m];
+                }
+            }
+        }
+        if (j == ls) {
+            firstg = cur = g;
+#pragma unroll
+            for (int i = 0; i < CGR_TILE; ++i) run[i] = v[i];
+            continue;
+        }
+        if (g != cur) {
+            if (single) {
+#pragma unroll
+                for (int i = 0; i < CGR_TILE; ++i) head[i] = run[i];
+                single = false;
+            } else {
+                // a run that starts and ends inside this lane is complete
+                double* dst = p.sums + (long long)cur * LD + c0;
+#pragma unroll
+                for (int i = 0; i < CGR_TILE; ++i)
+                    if (i < cw) dst[i] = (double)run[i];
+            }
+            cur = g;
+#pragma unroll
+            for (int i = 0; i < CGR_TILE; ++i) run[i] = v[i];
+        } else {
+#pragma unroll
+            for (int i = 0; i < CGR_TILE; ++i) run[i] += v[i];
+        }
+    }
+    const int lastg = cur;
+    if (single) {
+#pragma unroll
+        for (int i = 0; i < CGR_TILE; ++i) head[i] = run[i];
+    }
+    // empty lanes (only in the last chunk) are transparent: they continue the
+    // previous lane's run with a zero contribution
+    const unsigned full = 0xffffffffu;
+    const int lane_end = 31 - __clz(__ballot_sync(full, !empty));
+    const int fill_g = __shfl_sync(full, lastg, lane_end);
+    const int fg = empty ? fill_g : firstg;
+    const int lg = empty ? fill_g : lastg;
+    const int prev_lg = __shfl_up_sync(full, lg, 1);
+    const bool cont = lane > 0 && (empty || fg == prev_lg);
+    const bool sgl = empty || single;
+    const unsigned next_cont_mask = __ballot_sync(full, cont);
+    // lanes whose last run starts inside them (every lane except a single-run
+    // lane that continues its left neighbour's run); lane 0 always qualifies
+    const unsigned tail_start_mask = __ballot_sync(full, !(sgl && cont));
+    const unsigned below = lane == 0 ? 0u : (tail_start_mask & ((1u << lane) - 1u));
+    const int head_start_lane = cont ? (31 - __clz(below)) : lane;
+    // a run reaching this lane from the left began at the chunk's first
+    // position only if it began in lane 0 and lane 0 holds a single run
+    const bool lane0_single = __shfl_sync(full, sgl ? 1 : 0, 0) != 0;
+    const bool head_from_start = cont ? (head_start_lane == 0 && lane0_single) : (lane == 0);
+    const bool before = j0 > 0 && gseq[j0 - 1] == gseq[j0];
+    const bool after = j1 < p.n && gseq[j1] == gseq[j1 - 1];
+    const bool tail_ends_here = !empty && (lane == lane_end || !((next_cont_mask >> (lane + 1)) & 1u));
+
+#pragma unroll
+    for (int i = 0; i < CGR_TILE; ++i) {
+        if (i >= cw) continue;  // uniform across the warp
+        // out_l = a_l out_{l-1} + b_l, a_l = 1 when this lane is one run continuing from the left
+        double a = (sgl && cont) ? 1.0 : 0.0;
+        double b = empty ? 0.0 : (double)(single ? head[i] : run[i]);
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const double a_up = __shfl_up_sync(full, a, o);
+            const double b_up = __shfl_up_sync(full, b, o);
+            if (lane >= o) {
+                b = b + a * b_up;
+                a = a * a_up;
+            }
+        }
+        const double out = b;
+        double in = __shfl_up_sync(full, out, 1);
+        if (lane == 0) in = 0.0;
+        const long long col = c0 + i;
+        if (!empty && !single) {
+            // head run of a multi-run lane ends inside this lane
+            const double val = (cont ? in : 0.0) + (double)head[i];
+            if (head_from_start && before)
+                p.head[q * LD + col] = val;
+            else
+                p.sums[(long long)fg * LD + col] = val;
+        }
+        if (tail_ends_here) {
+            const bool from_start = sgl && head_from_start;
+            const bool at_end = lane == lane_end;
+            if (from_start && before)
+                p.head[q * LD + col] = out;
+            else if (at_end && after)
+                p.tail[q * LD + col] = out;
+            else
+                p.sums[(long long)lg * LD + col] = out;
+        }
+    }
+}
+
+template <typename T, int TILE>
+int launch_cg_rows_tile(const CGRowsParams<T>& p, cudaStream_t s) {
+    const int ntiles = (p.C + TILE - 1) / TILE;
+    const long long warps = ((p.n + CG_CHUNK - 1) / CG_CHUNK) * ntiles;
+    const long long blocks = (warps * 32 + 255) / 256;
+    cg_rows_kernel<T, TILE><<<(unsigned)blocks, 256, 0, s>>>(p, ntiles);
+    FEGB_LAUNCH_CHECK("cg operator sweep");
+    return 0;
+}
+
+template <typename T>
+int launch_cg_rows(const CGRowsParams<T>& p, cudaStream_t s) {
+    if (p.n <= 0) return 0;
+    if (p.C <= 4) return launch_cg_rows_tile<T, 4>(p, s);
+    if (p.C <= 8) return launch_cg_rows_tile<T, 8>(p, s);
+    if (p.C == 9) return launch_cg_rows_tile<T, 9>(p, s);
+    if (p.C <= 12) return launch_cg_rows_tile<T, 12>(p, s);
+    return launch_cg_rows_tile<T, 16>(p, s);
+}
+
+template int launch_cg_rows<double>(const CGRowsParams<double>&, cudaStream_t);
+template int launch_cg_rows<float>(const CGRowsParams<float>&, cudaStream_t);
 
 template int launch_seg_sweep<double>(const SegSweepParams<double>&, cudaStream_t);
 template int launch_seg_sweep<float>(const SegSweepParams<float>&, cudaStream_t);

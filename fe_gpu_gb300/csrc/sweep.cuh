@@ -144,6 +144,43 @@ int launch_apply_pending(T* X, int C, long long n, const PendingSet<T>& pend, cu
 // dst (float) = (float) src (double), n elements
 int launch_convert_f64_f32(const double* src, float* dst, long long n, cudaStream_t s);
 
+// ---- row-per-lane operator sweep for the CG normal-equation operator ----
+// Position j of a dimension's group-sorted order has destination group
+// gseq[j] and source ids src_gid[e][j] for the other dimensions; the sweep
+// forms, per destination group, sum over its positions of
+// -(sum_e src_tab[e][src_gid[e][j]]) (no row data). Each warp owns a chunk of
+// CG_CHUNK = 32 x 16 positions; each lane accumulates its 16 positions (runs
+// of equal destination in registers, storage type T); runs that cross lanes
+// are combined by a warp scan in FP64. Output layout as the segment sweep
+// (sums / head / tail with chunk size CG_CHUNK).
+constexpr int CG_LANE_POS = 16;
+constexpr int CG_CHUNK = 32 * CG_LANE_POS;
+
+template <typename T>
+struct CGRowsParams {
+    long long n;
+    int C;                 // real columns
+    int ld;                // row stride of the tables and of sums/head/tail (see cg_row_stride)
+    const int32_t* gseq;
+    int n_src;
+    const int32_t* src_gid[SWEEP_MAXP];
+    const T* src_tab[SWEEP_MAXP];
+    double* sums;
+    double* head;
+    double* tail;
+};
+
+template <typename T>
+int launch_cg_rows(const CGRowsParams<T>& p, cudaStream_t s);
+
+// Row stride of the CG G-space vectors: rows padded to 16-byte vectors (a
+// multiple of 16 columns above 16) so that table rows load as float4/double2.
+inline int cg_row_stride(int C, int elem_bytes) {
+    const int vec = 16 / elem_bytes;
+    if (C <= 16) return ((C + vec - 1) / vec) * vec;
+    return ((C + 15) / 16) * 16;
+}
+
 // ---- conjugate gradients on the FE normal equations (D'D a = D'e) ----
 // G-space vectors of all dimensions are concatenated: element (g, c) of
 // dimension d sits at ((goff_d + g) * C + c). Per-column scalars (C values)
@@ -153,20 +190,27 @@ int launch_convert_f64_f32(const double* src, float* dst, long long n, cudaStrea
 // q_d = counts_d * p_d - S_d, where S_d are the group sums of a no-data sweep
 // with pending tables {p_e, e != d} (sums of -p_e over the rows of each
 // group). Also writes per-block partials of p.q per column.
+// src.C is the padded row stride; columns at or beyond creal are padding (q = 0).
 template <typename T>
-int launch_cg_q(const FinalizeParams& src, const T* p, T* q, double* pq_partials, cudaStream_t s);
+int launch_cg_q(const FinalizeParams& src, int creal, const T* p, T* q, double* pq_partials, cudaStream_t s);
 int cg_partial_blocks(long long gc);
 
 // out[c] = sum_b partials[b * C + c] for b < nb (fixed order)
 int launch_fold_partials(const double* partials, int nb, int C, double* out, cudaStream_t s);
 
-// a = rz / pq per column (0 where pq == 0), then for every element:
-// alpha += a p, r -= a q, z = r / count (0 for empty groups); partials of
-// r.z per column and max |z| (bits, device scalar).
+// a = rz / pq per column (0 where pq == 0), then for every element, in T:
+// x += a p, r -= a q, z = r / count (0 for empty groups); partials of r.z
+// per column and max |z| (bits, device scalar).
 template <typename T>
-int launch_cg_update(long long Gt, int C, const double* inv_counts, const double* rz, const double* pq, const T* p,
-                     const T* q, double* alpha, T* r, T* z, double* rz_partials, double* zmax_partials,
+int launch_cg_update(long long Gt, int C, const T* inv_counts, const double* rz, const double* pq, const T* p,
+                     const T* q, T* x, T* r, T* z, double* rz_partials, double* zmax_partials,
                      unsigned long long* zmax, cudaStream_t s);
+// dst[g * C + c] = (double) src[g * ld + c] for c < C
+template <typename T>
+int launch_to_f64(const T* src, int ld, double* dst, int C, long long G, cudaStream_t s);
+// inv[g] = 1 / counts[g] in T (0 for empty groups)
+template <typename T>
+int launch_inv_counts_t(const int32_t* counts, long long G, T* inv, cudaStream_t s);
 
 // b = rz_new / rz_old per column; p = z + b p; rz_old = rz_new
 template <typename T>
@@ -176,8 +220,9 @@ int launch_cg_direction(long long Gt, int C, double* rz_old, const double* rz_ne
 // inv_counts[g] = 1 / counts[g] (0 for empty groups)
 int launch_inv_counts(const int32_t* counts, long long G, double* inv_counts, cudaStream_t s);
 
+// C is the padded row stride, creal the columns of mu (G x creal).
 template <typename T>
-int launch_cg_init(long long Gt, int C, const int32_t* counts, const double* mu, T* r, T* z, T* p,
+int launch_cg_init(long long Gt, int C, int creal, const int32_t* counts, const double* mu, T* r, T* z, T* p, T* x,
                    double* rz_partials, double* zmax_partials, unsigned long long* zmax, cudaStream_t s);
 
 }  // namespace fegb

@@ -350,7 +350,12 @@ def main():
         "gpu_launches": int(launches / args.steps) * args.steps,
         "roofline": {"bound": "hbm", "kernel": fam[top], "achieved": achieved, "peak": peak,
                      "peak_source": peak_kind, "unit": "GB/s", "frac": achieved / peak if peak else None,
-                     "traffic": traffic_per_launch, "launches": nlaunch[top],
+                     "traffic": traffic_per_launch,
+                     "traffic_source": ("ncu dram__bytes_read.sum + dram__bytes_write.sum per launch, "
+                                        "profiles/cg_rows_worker_firm_20M.md") if traffic_per_launch else None,
+                     "alg_bytes_definition": ("N (4 D + (D-1) C s): ids and gathered FE-table rows per operator launch"
+                                              if top >= 4 else "N (4 + 2 C s): rows read and written once, one id"),
+                     "launches": nlaunch[top],
                      "avg_launch_ms": secs[top] / max(1, nlaunch[top]) * 1e3,
                      "alg_bytes_per_launch": nbytes[top] / max(1, nlaunch[top]),
                      "all_families": {fam[i]: {"launches": nlaunch[i], "seconds": secs[i],
@@ -370,9 +375,16 @@ def main():
     return 0
 
 
-# DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) from
-# the ncu captures summarised under profiles/, scaled to the workload.
-TRAFFIC_PER_LAUNCH: dict = {}
+# DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of the
+# dominant kernel families, from the ncu capture summarised in
+# profiles/cg_rows_worker_firm_20M.md (first operator launches of one fit:
+# worker and firm dimensions for the segment family, time for the small-G
+# family). Other workloads were not captured: the gathered tables change size
+# with the FE group counts, so the traffic does not scale with the rows.
+TRAFFIC_PER_LAUNCH: dict = {
+    ("worker_firm_20M", "CG operator segment sweep fp32"): 6.592e+08,
+    ("worker_firm_20M", "CG operator small-G sweep fp32"): 1.144e+09,
+}
 
 
 if __name__ == "__main__":

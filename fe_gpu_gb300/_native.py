@@ -102,6 +102,17 @@ class FeGpuDeviceInfo(C.Structure):
     ]
 
 
+DESIGN_MAX_FACTORS = 8  # FEGB_DESIGN_MAX_FACTORS
+
+
+class FegbDesignFactor(C.Structure):
+    _fields_ = [("src", C.c_int), ("level", C.c_int), ("is_dummy", C.c_int)]
+
+
+class FegbDesignColumn(C.Structure):
+    _fields_ = [("n_factors", C.c_int), ("factors", FegbDesignFactor * DESIGN_MAX_FACTORS)]
+
+
 _P = C.c_void_p
 _I = C.c_int
 _LL = C.c_longlong
@@ -154,6 +165,8 @@ SIGNATURES = {
     "fegb_group_sizes": (_I, [C.POINTER(C.c_void_p), _I, _LL, _IP]),
     "fegb_drop_singletons": (_I, [C.POINTER(C.c_void_p), _IP, _I, _LL, _P, C.POINTER(C.c_longlong)]),
     "fegb_kernel_launches": (_LL, []),
+    "fegb_design_levels": (_I, [_P, _LL, _I, _IP, _IP, _P]),
+    "fegb_build_design": (_I, [C.POINTER(C.c_void_p), _I, _LL, C.POINTER(FegbDesignColumn), _I, _P, _LL, _P]),
 }
 
 

@@ -193,10 +193,19 @@ __global__ void counts_from_offsets_kernel(const int32_t* __restrict__ off, int 
     if (g < G) counts[g] = off[g + 1] - off[g];
 }
 
-__global__ void count_ids_kernel(const int32_t* __restrict__ gid, long long n, int32_t* __restrict__ counts) {
+// Group sizes of a small-G dimension: a shared-memory histogram per block,
+// then one global add per (block, group). Integer sums, so the result does not
+// depend on the order of the adds.
+__global__ void count_ids_kernel(const int32_t* __restrict__ gid, long long n, int G, int32_t* __restrict__ counts) {
+    extern __shared__ int32_t hist[];
+    for (int g = threadIdx.x; g < G; g += blockDim.x) hist[g] = 0;
+    __syncthreads();
     long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const long long st = (long long)gridDim.x * blockDim.x;
-    for (; i < n; i += st) atomicAdd(&counts[gid[i]], 1);
+    for (; i < n; i += st) atomicAdd(&hist[gid[i]], 1);
+    __syncthreads();
+    for (int g = threadIdx.x; g < G; g += blockDim.x)
+        if (hist[g]) atomicAdd(&counts[g], hist[g]);
 }
 
 __global__ void reset_relax_kernel(double* relax, double* prev_change, int n) {
@@ -403,10 +412,13 @@ int build_problem(Problem& P, long long n_in, int k, int l, int n_fe, const doub
             }
         }
         if (D.mode == MODE_SMALLG) {
-            FEGB_CUDA(cudaMemsetAsync(D.counts, 0, sizeof(int32_t) * (size_t)D.G, s), "counts zero");
-            if (n > 0) {
-                count_ids_kernel<<<grid_stride_blocks(n, 256), 256, 0, s>>>(D.gid, n, D.counts);
-                FEGB_LAUNCH_CHECK("count ids");
+            if (!need_sorted) {  // sorted dimensions already have counts from their offsets
+                FEGB_CUDA(cudaMemsetAsync(D.counts, 0, sizeof(int32_t) * (size_t)D.G, s), "counts zero");
+                if (n > 0 && D.G > 0) {
+                    count_ids_kernel<<<std::min<unsigned>(grid_stride_blocks(n, 256), 4u * (unsigned)num_sms()), 256,
+                                       sizeof(int32_t) * (size_t)D.G, s>>>(D.gid, n, D.G, D.counts);
+                    FEGB_LAUNCH_CHECK("count ids");
+                }
             }
             gmax_small = std::max(gmax_small, D.G);
         }
@@ -831,6 +843,12 @@ int cg_alloc(Problem& P, CGBuffers<T>& B) {
     return 0;
 }
 
+// Algorithmic bytes of one operator sweep: per position the destination id,
+// D-1 source ids and D-1 gathered source rows of C values of size s.
+inline double cg_operator_bytes(const Problem& P, size_t s) {
+    return (double)P.n * (4.0 * P.n_fe + (double)(P.n_fe - 1) * P.C * (double)s);
+}
+
 // q = D'D p, dimension by dimension: a no-data sweep over d's traversal with
 // the other dimensions' p as pending tables, then q_d = counts_d p_d - sums.
 template <typename T>
@@ -843,7 +861,7 @@ int cg_apply(Problem& P, CGBuffers<T>& B) {
         Problem::Timed tm{};
         if (P.profile) {
             tm.kind = 4 + (D.mode == MODE_SMALLG ? 2 : 0) + (sizeof(T) == 4 ? 1 : 0);
-            tm.bytes = (double)P.n * 4.0 * P.n_fe;  // destination + source ids per position
+            tm.bytes = cg_operator_bytes(P, sizeof(T));
             FEGB_CUDA(cudaEventCreate(&tm.a), "profile event");
             FEGB_CUDA(cudaEventCreate(&tm.b), "profile event");
             FEGB_CUDA(cudaEventRecord(tm.a, P.s), "profile record");
@@ -890,7 +908,7 @@ int cg_apply(Problem& P, CGBuffers<T>& B) {
         FEGB_TRY(launch_cg_q<T>(src, C, B.p + P.goff[d] * L, B.q + P.goff[d] * L,
                                 B.pq_part + (size_t)B.pq_block_off[d] * L, P.s));
         P.projections += 1;
-        P.demean_bytes += (double)P.n * 4.0 * P.n_fe;
+        P.demean_bytes += cg_operator_bytes(P, sizeof(T));
     }
     return launch_fold_partials(B.pq_part, B.pq_blocks, L, B.pq, P.s);
 }

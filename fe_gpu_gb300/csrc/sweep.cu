@@ -778,12 +778,142 @@ template int launch_cg_init<float>(long long, int, int, const int32_t*, const do
 
 
 // ----------------------- row-per-lane CG operator sweep -----------------------
+//
+// The kernel is bound by L1 sector lookups: gathers of scattered table rows
+// cost one lookup per 32-byte sector per lane, about one lookup per SM cycle.
+// So ids are read 4 positions per 128-bit load (not kept in L1,
+// marked evict-first in L2), and table rows, padded to 32-byte multiples, are
+// read with 256-bit loads marked evict-last in L2 so the G-space tables stay
+// cached across the positions that revisit them.
 
+__device__ __forceinline__ unsigned long long l2_policy_evict_last() {
+    unsigned long long pol;
+    asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(pol));
+    return pol;
+}
+__device__ __forceinline__ unsigned long long l2_policy_evict_first() {
+    unsigned long long pol;
+    asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));
+    return pol;
+}
+
+// CG_IDV consecutive int32 ids from a 16-byte aligned address
+constexpr int CG_IDV = 4;
+__device__ __forceinline__ void ld_ids(const int32_t* ptr, int (&o)[CG_IDV], unsigned long long pol) {
+    asm("ld.global.nc.L1::no_allocate.L2::cache_hint.v4.b32 {%0,%1,%2,%3}, [%4], %5;"
+                 : "=r"(o[0]), "=r"(o[1]), "=r"(o[2]), "=r"(o[3])
+                 : "l"(ptr), "l"(pol));
+}
+
+// Pieces of a table row: NE consecutive elements at an address aligned to
+// the piece's vector size (pieces start at 32-byte boundaries of the row).
+template <int NE>
+__device__ __forceinline__ void ld_piece(const float* ptr, float (&o)[NE], unsigned long long pol) {
+    if constexpr (NE == 8) {
+        asm("ld.global.nc.L2::cache_hint.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8], %9;"
+                     : "=f"(o[0]), "=f"(o[1]), "=f"(o[2]), "=f"(o[3]), "=f"(o[4]), "=f"(o[5]), "=f"(o[6]), "=f"(o[7])
+                     : "l"(ptr), "l"(pol));
+    } else if constexpr (NE == 4) {
+        asm("ld.global.nc.L2::cache_hint.v4.f32 {%0,%1,%2,%3}, [%4], %5;"
+                     : "=f"(o[0]), "=f"(o[1]), "=f"(o[2]), "=f"(o[3])
+                     : "l"(ptr), "l"(pol));
+    } else if constexpr (NE == 2) {
+        asm("ld.global.nc.L2::cache_hint.v2.f32 {%0,%1}, [%2], %3;" : "=f"(o[0]), "=f"(o[1]) : "l"(ptr), "l"(pol));
+    } else {
+        static_assert(NE == 1, "piece width");
+        asm("ld.global.nc.L2::cache_hint.f32 %0, [%1], %2;" : "=f"(o[0]) : "l"(ptr), "l"(pol));
+    }
+}
+template <int NE>
+__device__ __forceinline__ void ld_piece(const double* ptr, double (&o)[NE], unsigned long long pol) {
+    if constexpr (NE == 4) {
+        asm("ld.global.nc.L2::cache_hint.v4.f64 {%0,%1,%2,%3}, [%4], %5;"
+                     : "=d"(o[0]), "=d"(o[1]), "=d"(o[2]), "=d"(o[3])
+                     : "l"(ptr), "l"(pol));
+    } else if constexpr (NE == 2) {
+        asm("ld.global.nc.L2::cache_hint.v2.f64 {%0,%1}, [%2], %3;" : "=d"(o[0]), "=d"(o[1]) : "l"(ptr), "l"(pol));
+    } else {
+        static_assert(NE == 1, "piece width");
+        asm("ld.global.nc.L2::cache_hint.f64 %0, [%1], %2;" : "=d"(o[0]) : "l"(ptr), "l"(pol));
+    }
+}
+
+// smallest supported piece width holding w elements of a row (W = 256-bit width)
+template <int W>
+__host__ __device__ constexpr int piece_width(int w) {
+    return w >= W ? W : (w > W / 2 ? W : (w > 2 ? (W >= 4 ? 4 : W) : (w == 2 ? 2 : 1)));
+}
+
+// v[0..TILE) -= row[0..cw) of one source table (row already offset to column c0)
+template <typename T, int TILE, int K = 0>
+__device__ __forceinline__ void cg_sub_row(const T* __restrict__ row, int cw, T (&v)[TILE], unsigned long long pol) {
+    constexpr int W = 32 / (int)sizeof(T);  // elements per 256-bit load
+    if constexpr (K * W < TILE) {
+        if (K * W >= cw) return;
+        constexpr int left = TILE - K * W;
+        constexpr int NE = piece_width<W>(left < W ? left : W);
+        T w[NE];
+        ld_piece<NE>(row + W * K, w, pol);
+#pragma unroll
+        for (int m = 0; m < NE; ++m)
+            if (W * K + m < TILE) v[W * K + m] -= w[m];
+        cg_sub_row<T, TILE, K + 1>(row, cw, v, pol);
+    }
+}
+
+#ifndef CG_ROWS_MINB
+#define CG_ROWS_MINB 3
+#endif
+
+template <typename T, int TILE>
+struct CGRun {
+    T head[TILE];
+    T run[TILE];
+    int firstg;
+    int cur;
+    bool single;
+    bool started;
+};
+
+// Adds one position (group g, contribution v) to the lane's run state.
+template <typename T, int TILE>
+__device__ __forceinline__ void cg_run_push(CGRun<T, TILE>& st, int g, const T (&v)[TILE], double* __restrict__ sums,
+                                            int LD, int c0, int cw) {
+    if (!st.started) {
+        st.started = true;
+        st.firstg = st.cur = g;
+#pragma unroll
+        for (int i = 0; i < TILE; ++i) st.run[i] = v[i];
+        return;
+    }
+    if (g != st.cur) {
+        if (st.single) {
+#pragma unroll
+            for (int i = 0; i < TILE; ++i) st.head[i] = st.run[i];
+            st.single = false;
+        } else {
+            // a run that starts and ends inside this lane is complete
+            double* dst = sums + (long long)st.cur * LD + c0;
+#pragma unroll
+            for (int i = 0; i < TILE; ++i)
+                if (i < cw) dst[i] = (double)st.run[i];
+        }
+        st.cur = g;
+#pragma unroll
+        for (int i = 0; i < TILE; ++i) st.run[i] = v[i];
+    } else {
+#pragma unroll
+        for (int i = 0; i < TILE; ++i) st.run[i] += v[i];
+    }
+}
 
 // TILE = columns per pass (compile-time register tile; all per-column arrays
 // stay in registers because every loop over TILE is fully unrolled).
-template <typename T, int CGR_TILE>
-__global__ void __launch_bounds__(256, (sizeof(T) == 4 && CGR_TILE <= 12) ? 4 : 2) cg_rows_kernel(CGRowsParams<T> p, int ntiles) {
+// NSRC = number of source dimensions when the vector id path is used
+// (1..3); NSRC = 0 reads ids one position at a time for any n_src.
+template <typename T, int CGR_TILE, int NSRC>
+__global__ void __launch_bounds__(256, (sizeof(T) == 4 && CGR_TILE <= 12) ? CG_ROWS_MINB : 2)
+    cg_rows_kernel(CGRowsParams<T> p, int ntiles) {
     const int lane = threadIdx.x & 31;
     const long long warp = ((long long)blockIdx.x * 256 + threadIdx.x) >> 5;
     const long long nchunks = (p.n + CG_CHUNK - 1) / CG_CHUNK;
@@ -799,73 +929,76 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 && CGR_TILE <= 12) ? 4 : 
     const long long le = min(ls + CG_LANE_POS, j1);
     const bool empty = ls >= le;
     const int32_t* __restrict__ gseq = p.gseq;
+    const unsigned long long keep = l2_policy_evict_last();
 
-    int firstg = -1, cur = -1;
-    bool single = true;
-    T head[CGR_TILE], run[CGR_TILE];
+    CGRun<T, CGR_TILE> st;
 #pragma unroll
     for (int i = 0; i < CGR_TILE; ++i) {
-        head[i] = T(0);
-        run[i] = T(0);
+        st.head[i] = T(0);
+        st.run[i] = T(0);
     }
-    for (long long j = ls; j < le; ++j) {
-        const int g = __ldcs(gseq + j);
-        T v[CGR_TILE];
+    st.firstg = -1;
+    st.cur = -1;
+    st.single = true;
+    st.started = false;
+
+    if constexpr (NSRC > 0) {
+        const unsigned long long stream = l2_policy_evict_first();
+        const T* tabs[NSRC];
+        const int32_t* sgid[NSRC];
 #pragma unroll
-        for (int i = 0; i < CGR_TILE; ++i) v[i] = T(0);
-        for (int e = 0; e < p.n_src; ++e) {
-            const T* __restrict__ tab = p.src_tab[e] + (long long)__ldcs(p.src_gid[e] + j) * LD + c0;
-            // 16-byte vector loads of the padded row (LD and c0 are multiples of the vector width)
-            constexpr int VEC = 16 / (int)sizeof(T);
-            constexpr int NV = (CGR_TILE + VEC - 1) / VEC;
+        for (int e = 0; e < NSRC; ++e) {
+            tabs[e] = p.src_tab[e] + c0;
+            sgid[e] = p.src_gid[e];
+        }
+#pragma unroll 1
+        for (int h = 0; h < CG_LANE_POS / CG_IDV; ++h) {
+            const long long jb = ls + CG_IDV * h;
+            if (jb + CG_IDV <= le) {
+                int gq[CG_IDV];
+                int sid[NSRC][CG_IDV];
+                ld_ids(gseq + jb, gq, stream);
 #pragma unroll
-            for (int k = 0; k < NV; ++k) {
-                if (k * VEC >= cw) break;
-                if constexpr (sizeof(T) == 4) {
-                    const float4 w = *reinterpret_cast<const float4*>(tab + 4 * k);
-                    const T wv[4] = {w.x, w.y, w.z, w.w};
+                for (int e = 0; e < NSRC; ++e) ld_ids(sgid[e] + jb, sid[e], stream);
 #pragma unroll
-                    for (int m = 0; m < 4; ++m)
-                        if (4 * k + m < CGR_TILE) v[4 * k + m] -= wv[m];
-                } else {
-                    const double2 w = *reinterpret_cast<const double2*>(tab + 2 * k);
-                    const T wv[2] = {w.x, w.y};
+                for (int m = 0; m < CG_IDV; ++m) {
+                    T v[CGR_TILE];
 #pragma unroll
-                    for (int m = 0; m < 2; ++m)
-                        if (2 * k + m < CGR_TILE) v[2 * k + m] -= wv[m];
+                    for (int i = 0; i < CGR_TILE; ++i) v[i] = T(0);
+#pragma unroll
+                    for (int e = 0; e < NSRC; ++e)
+                        cg_sub_row<T, CGR_TILE>(tabs[e] + (long long)sid[e][m] * LD, cw, v, keep);
+                    cg_run_push(st, gq[m], v, p.sums, LD, c0, cw);
+                }
+            } else {
+                // ragged end of the last chunk
+                for (long long j = jb; j < le; ++j) {
+                    T v[CGR_TILE];
+#pragma unroll
+                    for (int i = 0; i < CGR_TILE; ++i) v[i] = T(0);
+#pragma unroll
+                    for (int e = 0; e < NSRC; ++e)
+                        cg_sub_row<T, CGR_TILE>(tabs[e] + (long long)__ldg(sgid[e] + j) * LD, cw, v, keep);
+                    cg_run_push(st, __ldg(gseq + j), v, p.sums, LD, c0, cw);
                 }
             }
         }
-        if (j == ls) {
-            firstg = cur = g;
+    } else {
+        for (long long j = ls; j < le; ++j) {
+            T v[CGR_TILE];
 #pragma unroll
-            for (int i = 0; i < CGR_TILE; ++i) run[i] = v[i];
-            continue;
-        }
-        if (g != cur) {
-            if (single) {
-#pragma unroll
-                for (int i = 0; i < CGR_TILE; ++i) head[i] = run[i];
-                single = false;
-            } else {
-                // a run that starts and ends inside this lane is complete
-                double* dst = p.sums + (long long)cur * LD + c0;
-#pragma unroll
-                for (int i = 0; i < CGR_TILE; ++i)
-                    if (i < cw) dst[i] = (double)run[i];
-            }
-            cur = g;
-#pragma unroll
-            for (int i = 0; i < CGR_TILE; ++i) run[i] = v[i];
-        } else {
-#pragma unroll
-            for (int i = 0; i < CGR_TILE; ++i) run[i] += v[i];
+            for (int i = 0; i < CGR_TILE; ++i) v[i] = T(0);
+            for (int e = 0; e < p.n_src; ++e)
+                cg_sub_row<T, CGR_TILE>(p.src_tab[e] + (long long)__ldcs(p.src_gid[e] + j) * LD + c0, cw, v, keep);
+            cg_run_push(st, __ldcs(gseq + j), v, p.sums, LD, c0, cw);
         }
     }
-    const int lastg = cur;
+    const int firstg = st.firstg;
+    const bool single = st.single;
+    const int lastg = st.cur;
     if (single) {
 #pragma unroll
-        for (int i = 0; i < CGR_TILE; ++i) head[i] = run[i];
+        for (int i = 0; i < CGR_TILE; ++i) st.head[i] = st.run[i];
     }
     // empty lanes (only in the last chunk) are transparent: they continue the
     // previous lane's run with a zero contribution
@@ -891,28 +1024,38 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 && CGR_TILE <= 12) ? 4 : 
     const bool after = j1 < p.n && gseq[j1] == gseq[j1 - 1];
     const bool tail_ends_here = !empty && (lane == lane_end || !((next_cont_mask >> (lane + 1)) & 1u));
 
+    // Lane carries: out_l = b_l + (a_l ? out_{l-1} : 0), a_l = 1 when this lane is
+    // one run continuing from the left. The flags are the same for every
+    // column: the inclusive scan's per-level flags are computed once, and each
+    // column then costs one shuffle and one conditional add per level, in the
+    // storage type.
+    bool ak[5];
+    {
+        bool acur = sgl && cont;
+#pragma unroll
+        for (int k = 0; k < 5; ++k) {
+            const int o = 1 << k;
+            ak[k] = acur && lane >= o;
+            const bool a_up = __shfl_up_sync(full, acur ? 1 : 0, o) != 0;
+            if (lane >= o) acur = acur && a_up;
+        }
+    }
 #pragma unroll
     for (int i = 0; i < CGR_TILE; ++i) {
         if (i >= cw) continue;  // uniform across the warp
-        // out_l = a_l out_{l-1} + b_l, a_l = 1 when this lane is one run continuing from the left
-        double a = (sgl && cont) ? 1.0 : 0.0;
-        double b = empty ? 0.0 : (double)(single ? head[i] : run[i]);
+        T b = empty ? T(0) : (single ? st.head[i] : st.run[i]);
 #pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const double a_up = __shfl_up_sync(full, a, o);
-            const double b_up = __shfl_up_sync(full, b, o);
-            if (lane >= o) {
-                b = b + a * b_up;
-                a = a * a_up;
-            }
+        for (int k = 0; k < 5; ++k) {
+            const T b_up = __shfl_up_sync(full, b, 1 << k);
+            if (ak[k]) b += b_up;
         }
-        const double out = b;
-        double in = __shfl_up_sync(full, out, 1);
-        if (lane == 0) in = 0.0;
+        const T out = b;
+        T in = __shfl_up_sync(full, out, 1);
+        if (lane == 0) in = T(0);
         const long long col = c0 + i;
         if (!empty && !single) {
             // head run of a multi-run lane ends inside this lane
-            const double val = (cont ? in : 0.0) + (double)head[i];
+            const double val = (double)((cont ? in : T(0)) + st.head[i]);
             if (head_from_start && before)
                 p.head[q * LD + col] = val;
             else
@@ -922,33 +1065,50 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 && CGR_TILE <= 12) ? 4 : 
             const bool from_start = sgl && head_from_start;
             const bool at_end = lane == lane_end;
             if (from_start && before)
-                p.head[q * LD + col] = out;
+                p.head[q * LD + col] = (double)out;
             else if (at_end && after)
-                p.tail[q * LD + col] = out;
+                p.tail[q * LD + col] = (double)out;
             else
-                p.sums[(long long)lg * LD + col] = out;
+                p.sums[(long long)lg * LD + col] = (double)out;
         }
     }
 }
 
-template <typename T, int TILE>
+template <typename T, int TILE, int NSRC>
 int launch_cg_rows_tile(const CGRowsParams<T>& p, cudaStream_t s) {
     const int ntiles = (p.C + TILE - 1) / TILE;
     const long long warps = ((p.n + CG_CHUNK - 1) / CG_CHUNK) * ntiles;
     const long long blocks = (warps * 32 + 255) / 256;
-    cg_rows_kernel<T, TILE><<<(unsigned)blocks, 256, 0, s>>>(p, ntiles);
+    cg_rows_kernel<T, TILE, NSRC><<<(unsigned)blocks, 256, 0, s>>>(p, ntiles);
     FEGB_LAUNCH_CHECK("cg operator sweep");
     return 0;
+}
+
+template <typename T, int TILE>
+int launch_cg_rows_nsrc(const CGRowsParams<T>& p, cudaStream_t s) {
+    // the vector id path needs 16-byte aligned id arrays
+    bool aligned = (reinterpret_cast<uintptr_t>(p.gseq) & 15u) == 0;
+    for (int e = 0; e < p.n_src; ++e) aligned = aligned && (reinterpret_cast<uintptr_t>(p.src_gid[e]) & 15u) == 0;
+    if (aligned) {
+        if (p.n_src == 1) return launch_cg_rows_tile<T, TILE, 1>(p, s);
+        if (p.n_src == 2) return launch_cg_rows_tile<T, TILE, 2>(p, s);
+        if (p.n_src == 3) return launch_cg_rows_tile<T, TILE, 3>(p, s);
+    }
+    return launch_cg_rows_tile<T, TILE, 0>(p, s);
 }
 
 template <typename T>
 int launch_cg_rows(const CGRowsParams<T>& p, cudaStream_t s) {
     if (p.n <= 0) return 0;
-    if (p.C <= 4) return launch_cg_rows_tile<T, 4>(p, s);
-    if (p.C <= 8) return launch_cg_rows_tile<T, 8>(p, s);
-    if (p.C == 9) return launch_cg_rows_tile<T, 9>(p, s);
-    if (p.C <= 12) return launch_cg_rows_tile<T, 12>(p, s);
-    return launch_cg_rows_tile<T, 16>(p, s);
+    // table rows are read in 32-byte pieces: the stride and the tables must allow it
+    if (p.ld % (32 / (int)sizeof(T)) != 0) return set_error("cg operator: row stride %d is not a 32-byte multiple", p.ld);
+    for (int e = 0; e < p.n_src; ++e)
+        if ((reinterpret_cast<uintptr_t>(p.src_tab[e]) & 31u) != 0) return set_error("cg operator: unaligned table");
+    if (p.C <= 4) return launch_cg_rows_nsrc<T, 4>(p, s);
+    if (p.C <= 8) return launch_cg_rows_nsrc<T, 8>(p, s);
+    if (p.C == 9) return launch_cg_rows_nsrc<T, 9>(p, s);
+    if (p.C <= 12) return launch_cg_rows_nsrc<T, 12>(p, s);
+    return launch_cg_rows_nsrc<T, 16>(p, s);
 }
 
 template int launch_cg_rows<double>(const CGRowsParams<double>&, cudaStream_t);

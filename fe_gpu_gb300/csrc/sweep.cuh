@@ -173,10 +173,10 @@ struct CGRowsParams {
 template <typename T>
 int launch_cg_rows(const CGRowsParams<T>& p, cudaStream_t s);
 
-// Row stride of the CG G-space vectors: rows padded to 16-byte vectors (a
-// multiple of 16 columns above 16) so that table rows load as float4/double2.
+// Row stride of the CG G-space vectors: rows padded to 32-byte multiples (a
+// multiple of 16 columns above 16) so that table rows load as 256-bit vectors.
 inline int cg_row_stride(int C, int elem_bytes) {
-    const int vec = 16 / elem_bytes;
+    const int vec = 32 / elem_bytes;
     if (C <= 16) return ((C + vec - 1) / vec) * vec;
     return ((C + 15) / 16) * 16;
 }

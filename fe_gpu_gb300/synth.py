@@ -195,3 +195,21 @@ def iv_panel(n: int = 10_000_000, g=(500_000, 50_000, 30), seed: int = BASE_SEED
     raw = dict(y=y, x_end=x_end, cat_end=cat_end, z1=z1, zc=zc, cat_a=cat_a, cat_b=cat_b,
                **{f"x{j + 1}": x_exog[:, j] for j in range(6)})
     return raw, fe
+
+
+IV_FORMULA = ("y ~ x_end i.2.cat_end x1 x2 x3 x4 x5 x6 x1&x2 i.cat_a&&i.cat_b (x_end i.2.cat_end ~ z1 i.zc), "
+              "fe(f1 f2 f3) cluster(f1 f2)")
+
+
+def iv_formula_panel(n: int = 10_000_000, g=(500_000, 50_000, 30), seed: int = BASE_SEED + 2):
+    """iv_panel as a raw dataset plus the formula that expands it: regressors
+    [x_end, cat_end, x1..x6, cat_a, cat_b], instruments [z1, zc], FEs f1..f3.
+    IV_FORMULA expands to 90 regressors (x_end, 3 cat_end dummies with base 2,
+    x1..x6, x1&x2, 19 + 3 + 57 columns of i.cat_a&&i.cat_b) and 20 instruments
+    (z1 and 19 zc dummies)."""
+    raw, fe = iv_panel(n=n, g=g, seed=seed)
+    names_x = ["x_end", "cat_end"] + [f"x{j}" for j in range(1, 7)] + ["cat_a", "cat_b"]
+    W = np.column_stack([raw[k].astype(np.float64) for k in names_x])
+    Z = np.column_stack([raw["z1"], raw["zc"].astype(np.float64)])
+    hdr, host = _pack(raw["y"], W, Z, fe, names_x, ["f1", "f2", "f3"], names_z=["z1", "zc"])
+    return hdr, host, IV_FORMULA

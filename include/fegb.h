@@ -83,7 +83,7 @@ typedef struct fegb_result {
     /* instrumentation */
     int projections;          /* FE projections executed (all precisions) */
     int outer_iterations;     /* FP64 refinement passes (mixed form) */
-    double demean_bytes;      /* algorithmic bytes of the sweeps: sum over projections of n*(4 + 2*C*s) */
+    double demean_bytes;      /* algorithmic bytes of all sweep launches (per-family formulas below) */
     double time_h2d;          /* seconds */
     double time_prep;
     double time_demean;
@@ -94,9 +94,9 @@ typedef struct fegb_result {
      * data sweeps (rows read, and written back in storage order):
      *   [0] segment FP64, [1] segment FP32, [2] small-G FP64, [3] small-G FP32
      *   algorithmic bytes n (4 + 2 C s) per launch;
-     * CG operator sweeps (no row data; ids and L2-resident FE tables):
+     * CG operator sweeps (no row data; ids and gathered FE table rows):
      *   [4] segment FP64, [5] segment FP32, [6] small-G FP64, [7] small-G FP32
-     *   algorithmic bytes n * 4 * (number of id arrays read) per launch */
+     *   algorithmic bytes n (4 D + (D-1) C s) per launch, D = FE dimensions */
     int prof_launches[8];
     double prof_seconds[8];   /* summed CUDA-event durations of those launches */
     double prof_bytes[8];     /* summed algorithmic bytes of those launches */
@@ -142,6 +142,34 @@ int fegb_group_sizes(const int* const* d_fe_ids, int n_fe, long long n, int* siz
 
 /* Number of kernel launches issued by this library since it was loaded. */
 long long fegb_kernel_launches(void);
+
+/* ---- formula design-matrix expansion (src/src_main.f90:595-1440) ----
+ * Every expanded regressor or instrument is a product of factors taken left
+ * to right; a factor is a raw source column or the dummy of one of its levels
+ * (1.0 where nint(x) == level, else 0.0). */
+#define FEGB_DESIGN_MAX_FACTORS 8
+typedef struct fegb_design_factor {
+    int src;       /* index into the list of source columns */
+    int level;     /* level of the dummy (used when is_dummy = 1) */
+    int is_dummy;  /* 1: factor = (nint(x) == level); 0: factor = x */
+} fegb_design_factor;
+
+typedef struct fegb_design_column {
+    int n_factors; /* 1..FEGB_DESIGN_MAX_FACTORS */
+    fegb_design_factor factors[FEGB_DESIGN_MAX_FACTORS];
+} fegb_design_column;
+
+/* Levels of a categorical device column (collect_levels_for_column,
+ * src/src_main.f90:1390-1435): the first max_levels distinct values lying
+ * within 1e-6 of an integer, in order of first appearance, written sorted
+ * ascending to the host array levels[max_levels]; *n_levels on the host. */
+int fegb_design_levels(const double* d_col, long long n, int max_levels, int* levels, int* n_levels, void* stream);
+
+/* Expanded columns on the device: column j of d_out (at d_out + j*ld_out,
+ * n values) = product of cols[j].factors over the device source columns
+ * d_src[0..n_src) (host array of device pointers, n values each). */
+int fegb_build_design(const double* const* d_src, int n_src, long long n, const fegb_design_column* cols, int n_cols,
+                      double* d_out, long long ld_out, void* stream);
 
 /* Iterated singleton removal: d_keep (device, n bytes) gets 1 for kept rows. */
 int fegb_drop_singletons(const int* const* d_fe_ids, const int* sizes, int n_fe, long long n, unsigned char* d_keep,

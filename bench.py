@@ -46,6 +46,27 @@ WORKLOADS = {
 }
 
 
+# 2SLS with categorical expansion: the formula is expanded on the device
+# (90 regressors, 20 instruments) and fitted with 2-way clustered SEs.
+FORMULA_WORKLOADS = {
+    "iv_10M": dict(n=10_000_000, g=(500_000, 50_000, 30), seed=20261205,
+                   desc="10M rows, FEs 500k/50k/30 uniform; 2SLS: continuous + 4-level categorical (base 2) "
+                        "endogenous, continuous + 20-level instrument, i.a&&i.b (20x4), x1&x2, 6 exogenous; "
+                        "2-way clustered; formula expanded on the device to 90 regressors and 20 instruments"),
+    "iv_1M": dict(n=1_000_000, g=(50_000, 5_000, 30), seed=20261205, desc="small case of iv_10M for profiling"),
+}
+
+
+# Batched specifications: many independent regressions fitted together.
+BATCH_WORKLOADS = {
+    "batch_512": dict(n_specs=512, total_rows=100e6, seed=20261207,
+                      desc="512 independent specifications, rows log-uniform in [5k, 2M] (about 100M in total), "
+                           "1-3 FEs with levels ~ rows^0.7, 2-24 regressors, 75% OLS / 25% 2SLS (1-2 endogenous), "
+                           "1-3-way clustering; one within-transform per column-count class"),
+    "batch_64": dict(n_specs=64, total_rows=4e6, seed=20261207, desc="small case of batch_512 for profiling"),
+}
+
+
 def dist_env():
     return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(
         os.environ.get("LOCAL_RANK", "0"))
@@ -180,7 +201,8 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="worker_firm_20M")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS) + sorted(FORMULA_WORKLOADS) + sorted(BATCH_WORKLOADS),
+                    default="worker_firm_20M")
     ap.add_argument("--precision", choices=["mixed", "fp64"], default="mixed")
     ap.add_argument("--method", choices=["cg", "ap"], default="cg",
                     help="within-transform of the headline form (the FP64 comparison always uses AP)")
@@ -193,6 +215,10 @@ def main():
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload in FORMULA_WORKLOADS:
+        return run_formula(args)
+    if args.workload in BATCH_WORKLOADS:
+        return run_batch(args)
 
     import torch
 
@@ -373,6 +399,362 @@ def main():
 
         dist.destroy_process_group()
     return 0
+
+
+FAMILIES = ["segment sweep fp64", "segment sweep fp32", "small-G sweep fp64", "small-G sweep fp32",
+            "CG operator segment sweep fp64", "CG operator segment sweep fp32", "CG operator small-G sweep fp64",
+            "CG operator small-G sweep fp32"]
+
+
+def roofline_of(results, workload):
+    secs = [sum(r.stats["prof_seconds"][i] for r in results) for i in range(8)]
+    nlaunch = [sum(r.stats["prof_launches"][i] for r in results) for i in range(8)]
+    nbytes = [sum(r.stats["prof_bytes"][i] for r in results) for i in range(8)]
+    top = int(np.argmax(secs))
+    peak, peak_kind = measured_hbm_peak()
+    achieved = nbytes[top] / secs[top] / 1e9 if secs[top] > 0 else 0.0
+    traffic = TRAFFIC_PER_LAUNCH.get((workload, FAMILIES[top]))
+    return {"bound": "hbm", "kernel": FAMILIES[top], "achieved": achieved, "peak": peak, "peak_source": peak_kind,
+            "unit": "GB/s", "frac": achieved / peak if peak else None, "traffic": traffic,
+            "alg_bytes_definition": ("N (4 D + (D-1) C s): ids and gathered FE-table rows per operator launch"
+                                     if top >= 4 else "N (4 + 2 C s): rows read and written once, one id"),
+            "launches": nlaunch[top], "avg_launch_ms": secs[top] / max(1, nlaunch[top]) * 1e3,
+            "alg_bytes_per_launch": nbytes[top] / max(1, nlaunch[top]),
+            "all_families": {FAMILIES[i]: {"launches": nlaunch[i], "seconds": secs[i],
+                                           "gbs": (nbytes[i] / secs[i] / 1e9) if secs[i] else None}
+                             for i in range(8) if nlaunch[i]}}
+
+
+def run_formula(args):
+    """Formula workloads: each step expands the formula on the device from the
+    resident raw columns and fits it (the plain FP64 AP form beside it); e2e
+    runs the whole formula fit from pinned host arrays."""
+    import torch
+
+    from fe_gpu_gb300 import _native
+    from fe_gpu_gb300.estimator import fe_runtime_config
+    from fe_gpu_gb300.formula import RawDevice, expand_formula, fe_gpu_estimate_formula, fit_formula
+    from fe_gpu_gb300.synth import iv_formula_panel
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    w = FORMULA_WORKLOADS[args.workload]
+    hdr, host, formula = iv_formula_panel(n=w["n"], g=w["g"], seed=w["seed"])
+    n = host.y.shape[0]
+    stream = torch.cuda.Stream()
+    raw = RawDevice(hdr, host)
+
+    def cfg_for(precision, method):
+        return fe_runtime_config(fe_tolerance=1e-8, fe_max_iterations=100000, precision=precision,
+                                 demean_cg=(method == "cg"))
+
+    def step(precision, method, profile=False):
+        ff, cfg2 = expand_formula(formula, raw, cfg_for(precision, method), stream.cuda_stream)
+        res = fit_formula(ff, cfg2, hdr, stream.cuda_stream, profile)
+        ff.buffers["W"].free()
+        if ff.plan.instruments is not None:
+            ff.buffers["Z"].free()
+        return res
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+
+            dist.barrier()
+
+    def timed(precision, method, steps, profile):
+        barrier()
+        torch.cuda.synchronize()
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        l0 = _native.lib().fegb_kernel_launches()
+        ev0.record(stream)
+        results = [step(precision, method, profile) for _ in range(steps)]
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        barrier()
+        ms = ev0.elapsed_time(ev1) / steps
+        if world > 1:
+            import torch.distributed as dist
+
+            t = torch.tensor([ms], device=torch.device("cuda", local))
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms = float(t.item())
+        return ms, results, _native.lib().fegb_kernel_launches() - l0
+
+    if args.profile_case:
+        for p, m in (("mixed", "cg"), ("fp64", "cg"), ("mixed", "ap"), ("fp64", "ap")):
+            if args.case != "all" and args.case != f"{p}-{m}":
+                continue
+            r = step(p, m)
+            print(p, m, r.fe_iterations, r.stats["outer_iterations"], r.stats["time_total"], flush=True)
+        return 0
+
+    for _ in range(args.warmup):
+        step(args.precision, args.method)
+    sampler = ClockSampler(local)
+    sampler.start()
+    ms, results, launches = timed(args.precision, args.method, args.steps, True)
+    clocks = sampler.stop()
+    last = results[-1]
+    fp64_ms, fp64_res = None, None
+    if args.fp64_steps > 0:
+        step("fp64", "ap")
+        fp64_ms, fr, _ = timed("fp64", "ap", args.fp64_steps, False)
+        fp64_res = fr[-1]
+
+    # end to end from pinned host arrays through the formula front end
+    def pinned(a, dtype):
+        t = torch.empty(a.size, dtype=dtype, pin_memory=True).numpy()
+        return t
+
+    from fe_gpu_gb300.bin_io import fe_host_arrays
+
+    py = pinned(host.y, torch.float64)
+    py[:] = host.y
+    pW = pinned(host.W, torch.float64).reshape(host.W.shape[1], n).T
+    pW[:] = host.W
+    pZ = pinned(host.Z, torch.float64).reshape(host.Z.shape[1], n).T
+    pZ[:] = host.Z
+    pf = pinned(host.fe_ids, torch.int32).reshape(n, host.fe_ids.shape[0]).T
+    pf[:] = host.fe_ids
+    hp = fe_host_arrays(y=py, W=pW, Z=pZ, fe_ids=pf)
+    fe_gpu_estimate_formula(formula, hdr, hp, cfg_for(args.precision, args.method), stream.cuda_stream)
+    barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.e2e_steps):
+        er = fe_gpu_estimate_formula(formula, hdr, hp, cfg_for(args.precision, args.method), stream.cuda_stream)
+    torch.cuda.synchronize()
+    e2e_s = (time.perf_counter() - t0) / args.e2e_steps
+    k = len(last.beta)
+    line = {
+        "metric": METRIC, "value": world * n / (ms / 1e3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32-sweeps+f64" if args.precision == "mixed" else "f64", "data": "synthetic (seeded)",
+        "config": {"workload": args.workload, "description": w["desc"], "rows": n, "formula": formula,
+                   "regressors": k, "instruments": last.formula.l, "columns": 1 + k + last.formula.l,
+                   "fe_tol": 1e-8, "precision": args.precision, "within_transform": args.method,
+                   "l2": "inputs larger than L2", "parallelism": f"replicas x{world}"},
+        "fit_time_s": ms / 1e3,
+        "fit_breakdown_s": {key: last.stats[key] for key in ("time_prep", "time_demean", "time_regression",
+                                                              "time_se")},
+        "fe_iterations": last.fe_iterations, "outer_iterations": last.stats["outer_iterations"],
+        "is_iv": last.is_iv, "n_instruments": last.n_instruments,
+        "fp64_ap_fit_time_s": fp64_ms / 1e3 if fp64_ms else None,
+        "speedup_vs_plain_fp64_ap": (fp64_ms / ms) if fp64_ms else None,
+        "beta_max_rel_diff_mixed_vs_fp64": (float(np.max(np.abs(last.beta - fp64_res.beta) /
+                                                         np.abs(fp64_res.beta))) if fp64_res else None),
+        "se_max_rel_diff_mixed_vs_fp64": (float(np.max(np.abs(last.se - fp64_res.se) / np.abs(fp64_res.se)))
+                                          if fp64_res else None),
+        "e2e": {"value": world * n / e2e_s, "unit": UNIT, "h2d_bytes_per_step": raw.h2d_bytes,
+                "d2h_bytes_per_step": 2 * k * 8, "seconds_per_step": e2e_s},
+        "gpu_launches": int(launches / args.steps) * args.steps,
+        "roofline": roofline_of(results, args.workload),
+        "clocks": clocks,
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = formula_cpu_baseline(os.cpu_count() or 1)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+    return 0
+
+
+def run_batch(args):
+    """Batched specifications: one step fits every specification with
+    fegb_estimate_batch (inputs resident in HBM); beside it the same
+    specifications as sequential plain FP64 fits; e2e adds the host-to-device
+    copies of every specification from pinned memory."""
+    import torch
+
+    from fe_gpu_gb300 import _native
+    from fe_gpu_gb300.estimator import (DeviceBuffer, fe_batch_spec, fe_gpu_estimate_batch, fe_gpu_estimate_device,
+                                        fe_runtime_config)
+    from fe_gpu_gb300.synth import batch_specs
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    w = BATCH_WORKLOADS[args.workload]
+    specs = batch_specs(n_specs=w["n_specs"], total_rows=w["total_rows"], seed=w["seed"])
+    stream = torch.cuda.Stream()
+    rows = sum(h.y.shape[0] for h, _ in specs)
+
+    def upload():
+        bufs, out = [], []
+        for host, extra in specs:
+            by = DeviceBuffer.from_array(host.y)
+            bW = DeviceBuffer.from_array(np.asfortranarray(host.W))
+            bZ = DeviceBuffer.from_array(np.asfortranarray(host.Z)) if host.Z.shape[1] else None
+            bf = [DeviceBuffer.from_array(np.ascontiguousarray(host.fe_ids[d])) for d in range(host.fe_ids.shape[0])]
+            bufs.append((by, bW, bZ, bf))
+            out.append(fe_batch_spec(n=host.y.shape[0], k=host.W.shape[1], l=host.Z.shape[1], d_y=by.ptr,
+                                     d_W=bW.ptr, d_Z=bZ.ptr if bZ else None, d_fe_ids=[b.ptr for b in bf],
+                                     cluster_fe_dims=extra["cluster_fe_dims"], iv_regressors=extra["iv_regressors"]))
+        return bufs, out
+
+    bufs, dspecs = upload()
+    h2d = sum(h.y.nbytes + h.W.nbytes + h.Z.nbytes + h.fe_ids.nbytes for h, _ in specs)
+    cfg = fe_runtime_config(fe_tolerance=1e-8, fe_max_iterations=100000, precision=args.precision,
+                            demean_cg=(args.method == "cg"))
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+
+            dist.barrier()
+
+    def timed(fn, steps):
+        barrier()
+        torch.cuda.synchronize()
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        l0 = _native.lib().fegb_kernel_launches()
+        ev0.record(stream)
+        out = [fn() for _ in range(steps)]
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        barrier()
+        ms = ev0.elapsed_time(ev1) / steps
+        if world > 1:
+            import torch.distributed as dist
+
+            t = torch.tensor([ms], device=torch.device("cuda", local))
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms = float(t.item())
+        return ms, out, _native.lib().fegb_kernel_launches() - l0
+
+    def batch_fit(profile=False):
+        return fe_gpu_estimate_batch(cfg, dspecs, stream=stream.cuda_stream, profile=profile)
+
+    def sequential_fp64():
+        out = []
+        for (host, extra), sp in zip(specs, dspecs):
+            c1 = fe_runtime_config(fe_tolerance=1e-8, fe_max_iterations=100000, precision="fp64", demean_cg=False,
+                                   cluster_fe_dims=extra["cluster_fe_dims"], iv_regressors=extra["iv_regressors"])
+            out.append(fe_gpu_estimate_device(c1, sp.n, sp.k, sp.l, sp.d_y, sp.d_W, sp.d_Z, sp.d_fe_ids,
+                                              stream=stream.cuda_stream))
+        return out
+
+    if args.profile_case:
+        r = batch_fit()
+        print("batch", len(r), r[0].fe_iterations, flush=True)
+        return 0
+
+    for _ in range(args.warmup):
+        batch_fit()
+    sampler = ClockSampler(local)
+    sampler.start()
+    ms, outs, launches = timed(lambda: batch_fit(True), args.steps)
+    clocks = sampler.stop()
+    last = outs[-1]
+    seq_ms, seq = None, None
+    if args.fp64_steps > 0:
+        seq_ms, so, _ = timed(sequential_fp64, 1)
+        seq = so[-1]
+    # e2e: fresh uploads from pinned host memory, then the batched fit
+    pinned = []
+    for host, _ in specs:
+        arrs = []
+        for a, dt in ((host.y, torch.float64), (np.asfortranarray(host.W), torch.float64),
+                      (np.asfortranarray(host.Z), torch.float64), (np.asfortranarray(host.fe_ids), torch.int32)):
+            t = torch.empty(a.size, dtype=dt, pin_memory=True).numpy()
+            t[:] = a.reshape(-1, order="F")
+            arrs.append(t)
+        pinned.append(arrs)
+
+    def e2e_step():
+        from fe_gpu_gb300.estimator import DeviceBuffer as DB
+
+        bl, sl = [], []
+        for (host, extra), (py, pW, pZ, pf) in zip(specs, pinned):
+            n, k, l, nfe = host.y.shape[0], host.W.shape[1], host.Z.shape[1], host.fe_ids.shape[0]
+            by, bW = DB.from_array(py), DB.from_array(pW)
+            bZ = DB.from_array(pZ) if l else None
+            fe2 = pf.reshape(nfe, n, order="F")
+            bf = [DB.from_array(np.ascontiguousarray(fe2[d])) for d in range(nfe)]
+            bl.append((by, bW, bZ, bf))
+            sl.append(fe_batch_spec(n=n, k=k, l=l, d_y=by.ptr, d_W=bW.ptr, d_Z=bZ.ptr if bZ else None,
+                                    d_fe_ids=[b.ptr for b in bf], cluster_fe_dims=extra["cluster_fe_dims"],
+                                    iv_regressors=extra["iv_regressors"]))
+        return fe_gpu_estimate_batch(cfg, sl, stream=stream.cuda_stream)
+
+    e2e_step()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.e2e_steps):
+        e2e_step()
+    torch.cuda.synchronize()
+    e2e_s = (time.perf_counter() - t0) / args.e2e_steps
+    ktot = sum(h.W.shape[1] for h, _ in specs)
+    diffs_b = [float(np.max(np.abs(a.beta - b.beta) / np.maximum(np.abs(b.beta), 1e-300))) for a, b in zip(last, seq)] \
+        if seq else []
+    diffs_s = [float(np.max(np.abs(a.se - b.se) / np.maximum(np.abs(b.se), 1e-300))) for a, b in zip(last, seq)] \
+        if seq else []
+    line = {
+        "metric": METRIC, "value": world * rows / (ms / 1e3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32-sweeps+f64" if args.precision == "mixed" else "f64", "data": "synthetic (seeded)",
+        "config": {"workload": args.workload, "description": w["desc"], "specs": len(specs), "rows": rows,
+                   "fe_tol": 1e-8, "precision": args.precision, "within_transform": args.method,
+                   "l2": "inputs larger than L2", "parallelism": f"replicas x{world}"},
+        "fit_time_s": ms / 1e3,
+        "specs_per_s": len(specs) / (ms / 1e3),
+        "iv_specs": sum(1 for r in last if r.is_iv),
+        "fe_iterations_max": max(r.fe_iterations for r in last),
+        "sequential_fp64_time_s": seq_ms / 1e3 if seq_ms else None,
+        "speedup_vs_sequential_fp64": (seq_ms / ms) if seq_ms else None,
+        "beta_max_rel_diff_vs_sequential_fp64": max(diffs_b) if diffs_b else None,
+        "se_max_rel_diff_vs_sequential_fp64": max(diffs_s) if diffs_s else None,
+        "e2e": {"value": world * rows / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": 2 * ktot * 8, "seconds_per_step": e2e_s},
+        "gpu_launches": int(launches / args.steps) * args.steps,
+        "roofline": roofline_of([r for step_results in outs for r in step_results], args.workload),
+        "clocks": clocks,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+    return 0
+
+
+def formula_cpu_baseline(threads):
+    """The oracle's GPU-convention estimator (2SLS; the reference CPU path has
+    no 2SLS) on a bounded sample: the same design at 500k rows, expanded with
+    the oracle's numpy restatement."""
+    from fe_gpu_gb300.formula import parse_formula_string, plan_design
+    from fe_gpu_gb300.synth import iv_formula_panel
+    from oracle import design_ref as D
+    from oracle import oracle as O
+
+    hdr, host, formula = iv_formula_panel(n=500_000, g=(25_000, 2_500, 30), seed=20261205)
+    spec = parse_formula_string(formula)
+    src = {("W", j): host.W[:, j] for j in range(host.W.shape[1])}
+    src.update({("Z", j): host.Z[:, j] for j in range(host.Z.shape[1])})
+    os.environ["OMP_NUM_THREADS"] = str(threads)
+    t0 = time.perf_counter()
+    plan = plan_design(spec, hdr.regressor_names, hdr.instrument_names, lambda m, c: D.collect_levels(src[(m, c)]))
+    W = D.expand(src, [c.factors for c in plan.regressors])
+    Z = D.expand(src, [c.factors for c in plan.instruments])
+    r = O.gpu_estimate(host.y, W, host.fe_ids, Z=Z, tol=1e-8, max_iter=100000, cluster_dims=[1, 2],
+                       iv_regressors=plan.iv_regressors, iv_instruments=plan.iv_instrument_cols)
+    dt = time.perf_counter() - t0
+    n = host.y.shape[0]
+    return {"value": n / dt, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{n} rows (FEs 25k/2.5k/30), same formula: numpy expansion + oracle 2SLS fit with the "
+                      f"reference GPU conventions, {r.stats['fe_iterations']} AP iterations, {dt:.2f} s"}
 
 
 # DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of the

@@ -113,6 +113,25 @@ class FegbDesignColumn(C.Structure):
     _fields_ = [("n_factors", C.c_int), ("factors", FegbDesignFactor * DESIGN_MAX_FACTORS)]
 
 
+class FegbSpec(C.Structure):
+    _fields_ = [
+        ("n", C.c_longlong),
+        ("k", C.c_int),
+        ("l", C.c_int),
+        ("n_fe", C.c_int),
+        ("y", C.c_void_p),
+        ("W", C.c_void_p),
+        ("Z", C.c_void_p),
+        ("fe_ids", C.POINTER(C.c_void_p)),
+        ("n_cluster_dims", C.c_int),
+        ("cluster_dims", C.POINTER(C.c_int)),
+        ("n_iv_regressors", C.c_int),
+        ("iv_regressors", C.POINTER(C.c_int)),
+        ("n_iv_instruments", C.c_int),
+        ("iv_instruments", C.POINTER(C.c_int)),
+    ]
+
+
 _P = C.c_void_p
 _I = C.c_int
 _LL = C.c_longlong
@@ -165,6 +184,7 @@ SIGNATURES = {
     "fegb_group_sizes": (_I, [C.POINTER(C.c_void_p), _I, _LL, _IP]),
     "fegb_drop_singletons": (_I, [C.POINTER(C.c_void_p), _IP, _I, _LL, _P, C.POINTER(C.c_longlong)]),
     "fegb_kernel_launches": (_LL, []),
+    "fegb_estimate_batch": (_I, [C.POINTER(FegbConfig), _I, C.POINTER(FegbSpec), _DP, _DP, C.POINTER(FegbResult)]),
     "fegb_design_levels": (_I, [_P, _LL, _I, _IP, _IP, _P]),
     "fegb_build_design": (_I, [C.POINTER(C.c_void_p), _I, _LL, C.POINTER(FegbDesignColumn), _I, _P, _LL, _P]),
 }

@@ -70,7 +70,7 @@ def build_cuda(force: bool = False, verbose: bool = False) -> Path:
     lib = BUILD / LIB_NAME
     if force or jobs or _stale(lib, objs):
         tmp = BUILD / (LIB_NAME + ".tmp")
-        _run([nvcc, *ARCH, "-shared", "-o", str(tmp), *map(str, objs)])
+        _run([nvcc, *ARCH, "-shared", "-o", str(tmp), *map(str, objs), "-lpthread"])
         os.replace(tmp, lib)
     if verbose:
         print("built", lib)

@@ -16,7 +16,7 @@
 #include <climits>
 #include <cmath>
 
-#include "../../include/fegb.h"
+#include "fegb.h"
 
 namespace fegb {
 namespace {

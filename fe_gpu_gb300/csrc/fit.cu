@@ -12,6 +12,10 @@
 #include "sweep.cuh"
 
 #include <algorithm>
+#include <thread>
+#include <string>
+#include <mutex>
+#include <atomic>
 #include <cfloat>
 #include <chrono>
 #include <climits>
@@ -1118,8 +1122,23 @@ struct FitTimes {
     double prep = 0, demean = 0, regression = 0, se = 0;
 };
 
+// Within-transform done outside the fit (the batched path demeans many
+// specifications together and estimates each on its own rows).
+struct PreDemeaned {
+    int iterations = 0;
+    int converged = 1;
+    int outer = 0;
+    double max_update = 0.0;
+    double seconds = 0.0;
+    int projections = 0;
+    double demean_bytes = 0.0;
+    fegb_result prof{};  // sweep-family timings of the shared within-transform (when profiling)
+    bool carry_profile = false;  // copy them into the result of the fit that uses this state
+};
+
 int estimate_on_problem(Problem& P, const fegb_config& cfg, const int* G_all, long long n_raw, double tss_total,
-                        double* beta_out, double* se_out, fegb_result* res, FitTimes& tm) {
+                        double* beta_out, double* se_out, fegb_result* res, FitTimes& tm,
+                        const PreDemeaned* pre = nullptr) {
     cudaStream_t s = P.s;
     Scratch& scr = *P.scr;
     const int k = P.k, l = P.l, C = P.C, n_fe = P.n_fe;
@@ -1149,7 +1168,12 @@ int estimate_on_problem(Problem& P, const fegb_config& cfg, const int* G_all, lo
     auto t0 = Clock::now();
     int iters = 0, conv = 1, outer = 0;
     double mu = 0.0;
-    if (cfg.demean_method == FEGB_DEMEAN_CG) {
+    if (pre) {
+        iters = pre->iterations;
+        conv = pre->converged;
+        outer = pre->outer;
+        mu = pre->max_update;
+    } else if (cfg.demean_method == FEGB_DEMEAN_CG) {
         if (cfg.precision == FEGB_PREC_MIXED)
             FEGB_TRY(demean_cg<float>(P, cfg.fe_tol, cfg.fe_max_iter, &iters, &conv, &mu, &outer));
         else
@@ -1160,7 +1184,7 @@ int estimate_on_problem(Problem& P, const fegb_config& cfg, const int* G_all, lo
         FEGB_TRY(demean_plain(P, cfg.fe_tol, cfg.fe_max_iter, &iters, &conv, &mu));
     }
     FEGB_CUDA(cudaStreamSynchronize(s), "demean sync");
-    tm.demean = seconds_since(t0);
+    tm.demean = pre ? pre->seconds : seconds_since(t0);
     FEGB_TRY(collect_profile(P, res));
     res->converged = conv;
     res->fe_iterations = iters;
@@ -1168,6 +1192,17 @@ int estimate_on_problem(Problem& P, const fegb_config& cfg, const int* G_all, lo
     res->outer_iterations = outer;
     res->projections = P.projections;
     res->demean_bytes = P.demean_bytes;
+    if (pre) {
+        res->projections = pre->projections;
+        res->demean_bytes = pre->demean_bytes;
+        if (pre->carry_profile) {
+            for (int f = 0; f < 8; ++f) {
+                res->prof_launches[f] = pre->prof.prof_launches[f];
+                res->prof_seconds[f] = pre->prof.prof_seconds[f];
+                res->prof_bytes[f] = pre->prof.prof_bytes[f];
+            }
+        }
+    }
     if (k <= 0) return 0;
 
     // ---------------- normal equations ----------------
@@ -1489,7 +1524,8 @@ class StreamHolder {
 
 int estimate_device_impl(const fegb_config* cfg_in, long long n, int k, int l, int n_fe, const double* y,
                          const double* W, const double* Z, const int32_t* const* ids, const int* group_sizes,
-                         double* beta, double* se, fegb_result* result, double t_h2d, cudaStream_t s) {
+                         double* beta, double* se, fegb_result* result, double t_h2d, cudaStream_t s,
+                         const PreDemeaned* pre = nullptr, const double* y_raw = nullptr) {
     auto t_start = Clock::now();
     fegb_config cfg;
     if (cfg_in)
@@ -1514,8 +1550,8 @@ int estimate_device_impl(const fegb_config* cfg_in, long long n, int k, int l, i
     auto t0 = Clock::now();
     long long n_single = 0;
     FEGB_TRY(build_problem(P, n, k, l, n_fe, y, W, Z, ids, group_sizes, cfg.drop_singletons != 0,
-                           cfg.precision == FEGB_PREC_MIXED && cfg.demean_method == FEGB_DEMEAN_AP, &n_single,
-                           cfg.demean_method == FEGB_DEMEAN_CG));
+                           !pre && cfg.precision == FEGB_PREC_MIXED && cfg.demean_method == FEGB_DEMEAN_AP, &n_single,
+                           !pre && cfg.demean_method == FEGB_DEMEAN_CG));
     std::vector<int> G(n_fe);
     for (int d = 0; d < n_fe; ++d) G[d] = P.dims[d].G;
     // TSS of the raw y over the rows used
@@ -1524,7 +1560,10 @@ int estimate_device_impl(const fegb_config* cfg_in, long long n, int k, int l, i
         double* ycol = nullptr;
         FEGB_TRY(scr.alloc(&ycol, (size_t)std::max(1LL, P.n), "y column"));
         // copy the strided column 0 of the data block into a contiguous vector
-        if (P.n > 0) {
+        // (or the raw y when the block was demeaned beforehand)
+        if (y_raw && P.n > 0) {
+            FEGB_CUDA(cudaMemcpyAsync(ycol, y_raw, sizeof(double) * P.n, cudaMemcpyDeviceToDevice, s), "raw y copy");
+        } else if (P.n > 0) {
             FEGB_CUDA(cudaMemcpy2DAsync(ycol, sizeof(double), P.X, sizeof(double) * P.C, sizeof(double), (size_t)P.n,
                                         cudaMemcpyDeviceToDevice, s),
                       "y column copy");
@@ -1535,7 +1574,7 @@ int estimate_device_impl(const fegb_config* cfg_in, long long n, int k, int l, i
     tm.prep = seconds_since(t0);
     res->n_obs_used = P.n;
     res->n_singletons = n_single;
-    int st = estimate_on_problem(P, cfg, G.data(), n, tss, beta, se, res, tm);
+    int st = estimate_on_problem(P, cfg, G.data(), n, tss, beta, se, res, tm, pre);
     FEGB_CUDA(cudaStreamSynchronize(s), "fit sync");
     res->time_h2d = t_h2d;
     res->time_prep = tm.prep;
@@ -1544,6 +1583,331 @@ int estimate_device_impl(const fegb_config* cfg_in, long long n, int k, int l, i
     res->time_se = tm.se;
     res->time_total = seconds_since(t_start) + t_h2d;
     if (st != 0) return st;
+    return set_ok();
+}
+
+// In-place within-transform of device columns (column-major, ld n).
+int within_impl(const fegb_config& cfg, long long n, int k, int l, int n_fe, double* d_y, double* d_W, double* d_Z,
+                const int32_t* const* ids, const int* group_sizes, cudaStream_t s, PreDemeaned* out) {
+    configure_mem_pool();
+    auto t0 = Clock::now();
+    Scratch scr(s);
+    Problem P;
+    P.s = s;
+    P.scr = &scr;
+    P.profile = cfg.profile != 0;
+    long long n_single = 0;
+    FEGB_TRY(build_problem(P, n, k, l, n_fe, d_y, d_W, d_Z, ids, group_sizes, false,
+                           cfg.precision == FEGB_PREC_MIXED && cfg.demean_method == FEGB_DEMEAN_AP, &n_single,
+                           cfg.demean_method == FEGB_DEMEAN_CG));
+    int it = 0, conv = 1, outer = 0;
+    double mu = 0.0;
+    if (cfg.demean_method == FEGB_DEMEAN_CG) {
+        if (cfg.precision == FEGB_PREC_MIXED)
+            FEGB_TRY(demean_cg<float>(P, cfg.fe_tol, cfg.fe_max_iter, &it, &conv, &mu, &outer));
+        else
+            FEGB_TRY(demean_cg<double>(P, cfg.fe_tol, cfg.fe_max_iter, &it, &conv, &mu, &outer));
+    } else if (cfg.precision == FEGB_PREC_MIXED) {
+        FEGB_TRY(demean_mixed(P, cfg.fe_tol, cfg.fe_max_iter, &it, &conv, &mu, &outer));
+    } else {
+        FEGB_TRY(demean_plain(P, cfg.fe_tol, cfg.fe_max_iter, &it, &conv, &mu));
+    }
+    if (n > 0) {
+        int TR = std::max(1, std::min(64, 24576 / (8 * P.C)));
+        size_t smem = sizeof(double) * (size_t)TR * P.C;
+        scatter_x_kernel<<<(unsigned)((n + TR - 1) / TR), 256, smem, s>>>(P.X, P.row_of, n, P.C, k, l, n, TR, d_y, d_W,
+                                                                         d_Z);
+        FEGB_LAUNCH_CHECK("scatter data block");
+    }
+    FEGB_CUDA(cudaStreamSynchronize(s), "within sync");
+    out->iterations = it;
+    out->converged = conv;
+    out->outer = outer;
+    out->max_update = mu;
+    out->seconds = seconds_since(t0);
+    out->projections = P.projections;
+    out->demean_bytes = P.demean_bytes;
+    std::memset(&out->prof, 0, sizeof(out->prof));
+    FEGB_TRY(collect_profile(P, &out->prof));
+    return 0;
+}
+
+// ------------------------- batched specifications -------------------------
+//
+// Specifications are stacked into one problem per column-count class: rows
+// one after the other, FE ids shifted so that every specification owns its
+// own groups, missing FE dimensions filled with one group per specification
+// (a group that every FE dimension already spans, so it changes no
+// projection). The stacked system is block diagonal, so one within-transform
+// gives every specification its own demeaned columns; each is then estimated
+// on its own rows with the single-fit code, the within-transform skipped.
+
+constexpr int BATCH_MAX_FE = SWEEP_MAXP;
+constexpr int BATCH_FIT_THREADS = 8;  // host threads (one stream each) fitting specifications after the demean
+
+struct BatchSpecDev {
+    long long row0;
+    long long n;
+    int k, l, n_fe;
+    const double* y;
+    const double* W;
+    const double* Z;
+    const int32_t* ids[BATCH_MAX_FE];
+    int goff[BATCH_MAX_FE];  // first stacked group (0-based) of each dimension
+};
+
+// Max over a block of 256 threads (result valid in thread 0).
+__device__ int block_reduce_max_int(int v) {
+    __shared__ int red[8];
+    for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
+    __syncthreads();  // red[] may still be read by a previous call
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        v = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : INT_MIN;
+        for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
+    }
+    return v;
+}
+
+// Max and min id of every specification and dimension: one block per spec.
+__global__ void batch_id_range_kernel(const BatchSpecDev* __restrict__ sp, int d, int* __restrict__ gmax,
+                                      int* __restrict__ gmin) {
+    const BatchSpecDev& S = sp[blockIdx.x];
+    int mx = 0, mn = INT_MAX;
+    if (d < S.n_fe)
+        for (long long i = threadIdx.x; i < S.n; i += blockDim.x) {
+            const int v = S.ids[d][i];
+            mx = max(mx, v);
+            mn = min(mn, v);
+        }
+    mx = block_reduce_max_int(mx);
+    mn = -block_reduce_max_int(-mn);
+    if (threadIdx.x == 0) {
+        gmax[blockIdx.x] = mx;
+        gmin[blockIdx.x] = mn;
+    }
+}
+
+__device__ __forceinline__ int batch_spec_of(const BatchSpecDev* sp, int ns, long long i) {
+    int lo = 0, hi = ns - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (sp[mid].row0 <= i)
+            lo = mid;
+        else
+            hi = mid - 1;
+    }
+    return lo;
+}
+
+// Stacked columns (column-major, ld N): y, then W, then Z, then zeros up to kb
+// columns; stacked 1-based ids with the per-spec group offsets.
+__global__ void batch_stack_kernel(const BatchSpecDev* __restrict__ sp, int ns, long long N, int kb, int fe_b,
+                                   double* __restrict__ yb, double* __restrict__ Wb, int32_t* __restrict__ idsb) {
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long st = (long long)gridDim.x * blockDim.x;
+    for (; i < N; i += st) {
+        const int si = batch_spec_of(sp, ns, i);
+        const BatchSpecDev& S = sp[si];
+        const long long r = i - S.row0;
+        yb[i] = S.y[r];
+        for (int c = 0; c < kb; ++c) {
+            double v = 0.0;
+            if (c < S.k)
+                v = S.W[(long long)c * S.n + r];
+            else if (c < S.k + S.l)
+                v = S.Z[(long long)(c - S.k) * S.n + r];
+            Wb[(long long)c * N + i] = v;
+        }
+        for (int d = 0; d < fe_b; ++d)
+            idsb[(long long)d * N + i] = S.goff[d] + (d < S.n_fe ? S.ids[d][r] : 1);
+    }
+}
+
+// padded column count of a specification's class
+int batch_class(int C) {
+    if (C <= 4) return 4;
+    if (C <= 8) return 8;
+    if (C <= 12) return 12;
+    if (C <= 16) return 16;
+    if (C <= 24) return 24;
+    if (C <= 32) return 32;
+    return ((C + 15) / 16) * 16;
+}
+
+int estimate_batch_impl(const fegb_config& cfg, int n_specs, const fegb_spec* specs, double* beta, double* se,
+                        fegb_result* results, cudaStream_t s) {
+    if (n_specs < 0) return set_error("n_specs < 0");
+    if (n_specs == 0) return set_ok();
+    if (!specs || !results) return set_error("batch: null specs or results");
+    if (cfg.drop_singletons) return set_error("batch: singleton dropping is not supported for batched specifications");
+    configure_mem_pool();
+    std::vector<long long> boff(n_specs + 1, 0);
+    for (int i = 0; i < n_specs; ++i) {
+        const fegb_spec& S = specs[i];
+        if (S.n <= 0 || S.k < 0 || S.l < 0) return set_error("batch spec %d: invalid sizes", i);
+        if (S.n > 0x7fffffffLL) return set_error("batch spec %d: n exceeds the int32 row range", i);
+        if (S.n_fe < 1 || S.n_fe > BATCH_MAX_FE) return set_error("batch spec %d: n_fe must be 1..%d", i, BATCH_MAX_FE);
+        if (!S.y || (S.k > 0 && !S.W) || (S.l > 0 && !S.Z) || !S.fe_ids)
+            return set_error("batch spec %d: null array", i);
+        boff[i + 1] = boff[i] + S.k;
+    }
+    if (boff[n_specs] > 0 && (!beta || !se)) return set_error("batch: beta/se output arrays are required");
+    // specifications by column-count class, in spec order
+    std::vector<std::pair<int, int>> order;
+    for (int i = 0; i < n_specs; ++i) order.push_back({batch_class(1 + specs[i].k + specs[i].l), i});
+    std::stable_sort(order.begin(), order.end(),
+                     [](const std::pair<int, int>& a, const std::pair<int, int>& b) { return a.first < b.first; });
+    size_t pos = 0;
+    while (pos < order.size()) {
+        size_t end = pos;
+        while (end < order.size() && order[end].first == order[pos].first) ++end;
+        const int cb = order[pos].first;
+        const int kb = cb - 1;
+        std::vector<int> idx;
+        for (size_t t = pos; t < end; ++t) idx.push_back(order[t].second);
+        pos = end;
+        const int ns = (int)idx.size();
+        Scratch scr(s);
+        std::vector<BatchSpecDev> hs(ns);
+        long long N = 0;
+        int fe_b = 1;
+        for (int t = 0; t < ns; ++t) {
+            const fegb_spec& S = specs[idx[t]];
+            BatchSpecDev& D = hs[t];
+            std::memset(&D, 0, sizeof(D));
+            D.row0 = N;
+            D.n = S.n;
+            D.k = S.k;
+            D.l = S.l;
+            D.n_fe = S.n_fe;
+            D.y = S.y;
+            D.W = S.W;
+            D.Z = S.Z;
+            for (int d = 0; d < S.n_fe; ++d) D.ids[d] = S.fe_ids[d];
+            N += S.n;
+            fe_b = std::max(fe_b, S.n_fe);
+        }
+        if (N > 0x7fffffffLL) return set_error("batch: %lld stacked rows exceed the int32 row range", N);
+        BatchSpecDev* dsp = nullptr;
+        FEGB_TRY(scr.alloc(&dsp, (size_t)ns, "batch specs"));
+        FEGB_CUDA(cudaMemcpyAsync(dsp, hs.data(), sizeof(BatchSpecDev) * ns, cudaMemcpyHostToDevice, s),
+                  "batch specs copy");
+        // group sizes of every spec and dimension
+        int *gmax = nullptr, *gmin = nullptr;
+        FEGB_TRY(scr.alloc(&gmax, (size_t)ns * fe_b, "batch group max"));
+        FEGB_TRY(scr.alloc(&gmin, (size_t)ns * fe_b, "batch group min"));
+        for (int d = 0; d < fe_b; ++d) {
+            batch_id_range_kernel<<<ns, 256, 0, s>>>(dsp, d, gmax + (size_t)d * ns, gmin + (size_t)d * ns);
+            FEGB_LAUNCH_CHECK("batch id range");
+        }
+        std::vector<int> hmax((size_t)ns * fe_b), hmin((size_t)ns * fe_b);
+        FEGB_CUDA(cudaMemcpyAsync(hmax.data(), gmax, sizeof(int) * hmax.size(), cudaMemcpyDeviceToHost, s), "gmax");
+        FEGB_CUDA(cudaMemcpyAsync(hmin.data(), gmin, sizeof(int) * hmin.size(), cudaMemcpyDeviceToHost, s), "gmin");
+        FEGB_CUDA(cudaStreamSynchronize(s), "batch sizes sync");
+        std::vector<int> Gb(fe_b, 0);
+        std::vector<std::vector<int>> Gs(ns, std::vector<int>(fe_b, 1));
+        for (int d = 0; d < fe_b; ++d) {
+            long long acc = 0;
+            for (int t = 0; t < ns; ++t) {
+                if (d < hs[t].n_fe) {
+                    if (hmin[(size_t)d * ns + t] < 1)
+                        return set_error("batch spec %d: FE dimension %d has an id < 1", idx[t], d + 1);
+                    Gs[t][d] = hmax[(size_t)d * ns + t];
+                }
+                hs[t].goff[d] = (int)acc;
+                acc += Gs[t][d];
+            }
+            if (acc > 0x7fffffffLL) return set_error("batch: stacked groups exceed the int32 range");
+            Gb[d] = (int)acc;
+        }
+        FEGB_CUDA(cudaMemcpyAsync(dsp, hs.data(), sizeof(BatchSpecDev) * ns, cudaMemcpyHostToDevice, s),
+                  "batch offsets copy");
+        double *yb = nullptr, *Wb = nullptr;
+        int32_t* idsb = nullptr;
+        FEGB_TRY(scr.alloc(&yb, (size_t)N, "stacked y"));
+        FEGB_TRY(scr.alloc(&Wb, (size_t)N * kb, "stacked columns"));
+        FEGB_TRY(scr.alloc(&idsb, (size_t)N * fe_b, "stacked ids"));
+        batch_stack_kernel<<<grid_stride_blocks(N, 256), 256, 0, s>>>(dsp, ns, N, kb, fe_b, yb, Wb, idsb);
+        FEGB_LAUNCH_CHECK("batch stack");
+        std::vector<const int32_t*> ids_b(fe_b);
+        for (int d = 0; d < fe_b; ++d) ids_b[d] = idsb + (size_t)d * N;
+        PreDemeaned pre;
+        FEGB_TRY(within_impl(cfg, N, kb, 0, fe_b, yb, Wb, nullptr, ids_b.data(), Gb.data(), s, &pre));
+        // every specification on its own demeaned rows; the fits are
+        // independent, so a few host threads run them on their own streams
+        auto fit_one = [&](int t, cudaStream_t ws) -> int {
+            const int si = idx[t];
+            const fegb_spec& S = specs[si];
+            Scratch sub(ws);
+            double *dy = nullptr, *dW = nullptr, *dZ = nullptr;
+            FEGB_TRY(sub.alloc(&dy, (size_t)S.n, "spec y"));
+            FEGB_TRY(sub.alloc(&dW, (size_t)S.n * std::max(1, S.k), "spec W"));
+            FEGB_TRY(sub.alloc(&dZ, (size_t)S.n * std::max(1, S.l), "spec Z"));
+            const long long r0 = hs[t].row0;
+            FEGB_CUDA(cudaMemcpyAsync(dy, yb + r0, sizeof(double) * S.n, cudaMemcpyDeviceToDevice, ws), "spec y");
+            if (S.k > 0)
+                FEGB_CUDA(cudaMemcpy2DAsync(dW, sizeof(double) * S.n, Wb + r0, sizeof(double) * N,
+                                            sizeof(double) * S.n, S.k, cudaMemcpyDeviceToDevice, ws),
+                          "spec W");
+            if (S.l > 0)
+                FEGB_CUDA(cudaMemcpy2DAsync(dZ, sizeof(double) * S.n, Wb + (size_t)S.k * N + r0, sizeof(double) * N,
+                                            sizeof(double) * S.n, S.l, cudaMemcpyDeviceToDevice, ws),
+                          "spec Z");
+            fegb_config cs = cfg;
+            cs.stream = ws;
+            cs.n_cluster_dims = S.n_cluster_dims;
+            cs.cluster_dims = S.cluster_dims;
+            cs.n_iv_regressors = S.n_iv_regressors;
+            cs.iv_regressors = S.iv_regressors;
+            cs.n_iv_instruments = S.n_iv_instruments;
+            cs.iv_instruments = S.iv_instruments;
+            std::vector<const int32_t*> sid(S.n_fe);
+            for (int d = 0; d < S.n_fe; ++d) sid[d] = S.fe_ids[d];
+            std::vector<int> gsz(Gs[t].begin(), Gs[t].begin() + S.n_fe);
+            PreDemeaned mine = pre;
+            mine.carry_profile = t == 0;  // the class's sweep timings are reported once, on its first spec
+            return estimate_device_impl(&cs, S.n, S.k, S.l, S.n_fe, dy, dW, dZ, sid.data(), gsz.data(),
+                                        beta + boff[si], se + boff[si], &results[si], 0.0, ws, &mine, S.y);
+        };
+        const int nthreads = std::min(ns, BATCH_FIT_THREADS);
+        std::atomic<int> next{0};
+        std::atomic<int> failed{0};
+        std::mutex err_mu;
+        std::string err_msg;
+        int err_status = 0;
+        auto worker = [&]() {
+            cudaStream_t ws = nullptr;
+            if (cudaStreamCreateWithFlags(&ws, cudaStreamNonBlocking) != cudaSuccess) {
+                failed = 1;
+                std::lock_guard<std::mutex> g(err_mu);
+                if (!err_status) {
+                    err_status = 1;
+                    err_msg = "batch: cannot create a worker stream";
+                }
+                return;
+            }
+            for (int t = next++; t < ns && !failed; t = next++) {
+                int st = fit_one(t, ws);
+                if (st != 0) {
+                    failed = 1;
+                    std::lock_guard<std::mutex> g(err_mu);
+                    if (!err_status) {
+                        err_status = st;
+                        err_msg = std::string("batch spec ") + std::to_string(idx[t]) + ": " + last_error();
+                    }
+                }
+            }
+            cudaStreamSynchronize(ws);
+            cudaStreamDestroy(ws);
+        };
+        std::vector<std::thread> pool;
+        for (int w = 1; w < nthreads; ++w) pool.emplace_back(worker);
+        worker();
+        for (auto& th : pool) th.join();
+        if (err_status) return set_error("%s", err_msg.c_str());
+    }
     return set_ok();
 }
 
@@ -1618,42 +1982,25 @@ int fegb_within_transform(const fegb_config* cfg_in, long long n, int k, int l, 
     else
         fegb_config_init(&cfg);
     StreamHolder sh(cfg.stream);
-    cudaStream_t s = sh.get();
-    configure_mem_pool();
-    Scratch scr(s);
-    Problem P;
-    P.s = s;
-    P.scr = &scr;
     std::vector<const int32_t*> ids(n_fe);
     for (int d = 0; d < n_fe; ++d) ids[d] = d_fe_ids[d];
-    long long n_single = 0;
-    FEGB_TRY(build_problem(P, n, k, l, n_fe, d_y, d_W, d_Z, ids.data(), group_sizes, false,
-                           cfg.precision == FEGB_PREC_MIXED && cfg.demean_method == FEGB_DEMEAN_AP, &n_single,
-                           cfg.demean_method == FEGB_DEMEAN_CG));
-    int it = 0, conv = 1, outer = 0;
-    double mu = 0.0;
-    if (cfg.demean_method == FEGB_DEMEAN_CG) {
-        if (cfg.precision == FEGB_PREC_MIXED)
-            FEGB_TRY(demean_cg<float>(P, cfg.fe_tol, cfg.fe_max_iter, &it, &conv, &mu, &outer));
-        else
-            FEGB_TRY(demean_cg<double>(P, cfg.fe_tol, cfg.fe_max_iter, &it, &conv, &mu, &outer));
-    } else if (cfg.precision == FEGB_PREC_MIXED) {
-        FEGB_TRY(demean_mixed(P, cfg.fe_tol, cfg.fe_max_iter, &it, &conv, &mu, &outer));
-    } else {
-        FEGB_TRY(demean_plain(P, cfg.fe_tol, cfg.fe_max_iter, &it, &conv, &mu));
-    }
-    if (n > 0) {
-        int TR = std::max(1, std::min(64, 24576 / (8 * P.C)));
-        size_t smem = sizeof(double) * (size_t)TR * P.C;
-        scatter_x_kernel<<<(unsigned)((n + TR - 1) / TR), 256, smem, s>>>(P.X, P.row_of, n, P.C, k, l, n, TR, d_y, d_W,
-                                                                         d_Z);
-        FEGB_LAUNCH_CHECK("scatter data block");
-    }
-    FEGB_CUDA(cudaStreamSynchronize(s), "within sync");
-    if (converged) *converged = conv;
-    if (iterations) *iterations = it;
-    if (max_update) *max_update = mu;
+    PreDemeaned st;
+    FEGB_TRY(within_impl(cfg, n, k, l, n_fe, d_y, d_W, d_Z, ids.data(), group_sizes, sh.get(), &st));
+    if (converged) *converged = st.converged;
+    if (iterations) *iterations = st.iterations;
+    if (max_update) *max_update = st.max_update;
     return set_ok();
+}
+
+int fegb_estimate_batch(const fegb_config* cfg_in, int n_specs, const fegb_spec* specs, double* beta, double* se,
+                        fegb_result* results) {
+    fegb_config cfg;
+    if (cfg_in)
+        cfg = *cfg_in;
+    else
+        fegb_config_init(&cfg);
+    StreamHolder sh(cfg.stream);
+    return estimate_batch_impl(cfg, n_specs, specs, beta, se, results, sh.get());
 }
 
 int fegb_cluster_ids(const int* const* d_fe_ids, const int* sizes, int n_dims, long long n, int* d_out_ids,

@@ -461,20 +461,20 @@ int crossprod(const MatView& A, const MatView& B, long long n, bool gram, bool u
     nb = (n + rpb - 1) / rpb;
     size_t smem = sizeof(double) * CP_TR * (gram ? a : a + b);
     if (smem > 200 * 1024) return set_error("crossprod: %d x %d columns exceed the shared-memory tile", a, b);
-    static bool attr_done = false;
-    if (!attr_done) {
-        FEGB_CUDA(cudaFuncSetAttribute(crossprod_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024),
-                  "crossprod attr");
-        FEGB_CUDA(cudaFuncSetAttribute(crossprod_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024),
-                  "crossprod attr");
-        FEGB_CUDA(cudaFuncSetAttribute(crossprod_kernel<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024),
-                  "crossprod attr");
-        FEGB_CUDA(cudaFuncSetAttribute(crossprod_kernel<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024),
-                  "crossprod attr");
-        FEGB_CUDA(cudaFuncSetAttribute(crossprod_kernel<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024),
-                  "crossprod attr");
-        attr_done = true;
-    }
+    // set once (thread-safe static initialisation) before any launch with a large tile
+    static const cudaError_t attr_status = []() {
+        cudaError_t e = cudaSuccess;
+        const int lim = 200 * 1024;
+        if (e == cudaSuccess) e = cudaFuncSetAttribute(crossprod_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+        if (e == cudaSuccess) e = cudaFuncSetAttribute(crossprod_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+        if (e == cudaSuccess) e = cudaFuncSetAttribute(crossprod_kernel<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(crossprod_kernel<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(crossprod_kernel<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+        return e;
+    }();
+    if (attr_status != cudaSuccess) return set_cuda_error(attr_status, "crossprod attr");
     for (long long p0 = 0; p0 < total_pairs; p0 += CP_MAXPAIRS_LAUNCH) {
         const int np = (int)std::min<long long>(CP_MAXPAIRS_LAUNCH, total_pairs - p0);
         double* partials = nullptr;

@@ -53,17 +53,18 @@ void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 long long launches() { return g_launches.load(std::memory_order_relaxed); }
 
 int num_sms() {
-    static int cached_dev = -1;
-    static int cached = 0;
+    // per device, computed once; safe to call from several host threads
+    static std::mutex mu;
+    static std::vector<std::pair<int, int>> cache;
     int dev = 0;
     cudaGetDevice(&dev);
-    if (dev != cached_dev) {
-        int v = 0;
-        if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || v <= 0) v = 132;
-        cached = v;
-        cached_dev = dev;
-    }
-    return cached;
+    std::lock_guard<std::mutex> lk(mu);
+    for (auto& e : cache)
+        if (e.first == dev) return e.second;
+    int v = 0;
+    if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || v <= 0) v = 132;
+    cache.push_back({dev, v});
+    return v;
 }
 
 void configure_mem_pool() {

@@ -603,14 +603,10 @@ int launch_smallg_sweep(const SmallGParams<T>& p, int nblocks, cudaStream_t s) {
     if (nwarps > 8) nwarps = 8;
     if (nwarps < 1) nwarps = 1;
     size_t smem = (size_t)nwarps * per_warp;
-    static bool attr_set[2] = {false, false};
-    const int which = sizeof(T) == 4 ? 1 : 0;
-    if (!attr_set[which]) {
-        FEGB_CUDA(cudaFuncSetAttribute(smallg_sweep_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       SMALLG_SMEM_BUDGET),
-                  "small-G smem attribute");
-        attr_set[which] = true;
-    }
+    // set once per instantiation (thread-safe static initialisation)
+    static const cudaError_t attr_status =
+        cudaFuncSetAttribute(smallg_sweep_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMALLG_SMEM_BUDGET);
+    if (attr_status != cudaSuccess) return set_cuda_error(attr_status, "small-G smem attribute");
     smallg_sweep_kernel<T><<<nblocks, nwarps * 32, smem, s>>>(p, P);
     FEGB_LAUNCH_CHECK("small-G sweep");
     return 0;

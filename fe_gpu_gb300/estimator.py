@@ -8,6 +8,7 @@ fe_gpu_runtime_malloc (no torch dependency).
 """
 from __future__ import annotations
 
+import copy
 import ctypes as C
 from dataclasses import dataclass, field
 from typing import Optional, Sequence
@@ -191,6 +192,63 @@ def fe_gpu_estimate_device(cfg: fe_runtime_config, n: int, k: int, l: int, d_y: 
     N.check(st, "fegb_estimate_device")
     del keep
     return _result_from(res, beta[:k].copy(), se[:k].copy(), cfg, header)
+
+
+@dataclass
+class fe_batch_spec:
+    """One specification of a batch: device pointers in the fegb_estimate_device
+    layout plus its own cluster dimensions and IV columns."""
+    n: int
+    k: int
+    l: int
+    d_y: int
+    d_W: Optional[int]
+    d_Z: Optional[int]
+    d_fe_ids: Sequence[int]
+    cluster_fe_dims: Sequence[int] = ()
+    iv_regressors: Sequence[int] = ()
+    iv_instrument_cols: Sequence[int] = ()
+
+
+def fe_gpu_estimate_batch(cfg: fe_runtime_config, specs: Sequence[fe_batch_spec], stream: Optional[int] = None,
+                          profile: bool = False) -> list:
+    """fegb_estimate_batch: many independent fits sharing one within-transform
+    per column-count class. cfg supplies tolerance, precision, method and SE
+    convention; every spec its own clusters and IV columns."""
+    c, keep = _make_config(cfg, stream, profile)
+    m = len(specs)
+    arr = (N.FegbSpec * max(1, m))()
+    for i, sp in enumerate(specs):
+        ids = (C.c_void_p * max(1, len(sp.d_fe_ids)))(*[C.c_void_p(int(p)) for p in sp.d_fe_ids])
+        keep.append(ids)
+        a = arr[i]
+        a.n, a.k, a.l, a.n_fe = int(sp.n), int(sp.k), int(sp.l), len(sp.d_fe_ids)
+        a.y = C.c_void_p(int(sp.d_y))
+        a.W = C.c_void_p(int(sp.d_W)) if sp.d_W else None
+        a.Z = C.c_void_p(int(sp.d_Z)) if sp.d_Z else None
+        a.fe_ids = C.cast(ids, C.POINTER(C.c_void_p))
+        for name, fn, fp in (("cluster_fe_dims", "n_cluster_dims", "cluster_dims"),
+                             ("iv_regressors", "n_iv_regressors", "iv_regressors"),
+                             ("iv_instrument_cols", "n_iv_instruments", "iv_instruments")):
+            vals = N.int_array(list(getattr(sp, name)))
+            keep.append(vals)
+            setattr(a, fn, len(getattr(sp, name)))
+            setattr(a, fp, C.cast(vals, C.POINTER(C.c_int)))
+    ktot = sum(int(sp.k) for sp in specs)
+    beta = np.zeros(max(ktot, 1))
+    se = np.zeros(max(ktot, 1))
+    res = (N.FegbResult * max(1, m))()
+    st = N.lib().fegb_estimate_batch(C.byref(c), m, arr, beta.ctypes.data_as(C.POINTER(C.c_double)),
+                                     se.ctypes.data_as(C.POINTER(C.c_double)), res)
+    N.check(st, "fegb_estimate_batch")
+    del keep
+    out, off = [], 0
+    for i, sp in enumerate(specs):
+        cfg_i = copy.copy(cfg)
+        cfg_i.cluster_fe_dims = list(sp.cluster_fe_dims)
+        out.append(_result_from(res[i], beta[off:off + sp.k].copy(), se[off:off + sp.k].copy(), cfg_i, None))
+        off += sp.k
+    return out
 
 
 def fe_gpu_within_transform_device(cfg: fe_runtime_config, n: int, k: int, l: int, d_y: int, d_W: Optional[int],

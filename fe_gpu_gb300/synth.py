@@ -18,6 +18,8 @@ shape (n_fe, n)) plus a header carrying names. Seeds default to
 """
 from __future__ import annotations
 
+from typing import Optional
+
 import numpy as np
 
 from .bin_io import fe_dataset_header, fe_host_arrays
@@ -213,3 +215,42 @@ def iv_formula_panel(n: int = 10_000_000, g=(500_000, 50_000, 30), seed: int = B
     Z = np.column_stack([raw["z1"], raw["zc"].astype(np.float64)])
     hdr, host = _pack(raw["y"], W, Z, fe, names_x, ["f1", "f2", "f3"], names_z=["z1", "zc"])
     return hdr, host, IV_FORMULA
+
+
+def batch_specs(n_specs: int = 512, total_rows: float = 100e6, row_range=(5_000, 2_000_000), seed: int = BASE_SEED + 4,
+                max_rows: Optional[int] = None):
+    """Independent specifications of uneven size for the batched path: rows
+    log-uniform in row_range (rescaled so they add up to about total_rows),
+    1-3 FEs with level counts proportional to rows^0.7, 2-24 N(0, 1)
+    regressors, 75% OLS and 25% 2SLS (1-2 endogenous regressors, 1-3 extra
+    instruments), 1-3-way clustering. Per-spec seeds are seed * 1000 + spec.
+    Returns [(host arrays, dict(cluster_fe_dims, iv_regressors))]."""
+    rng = np.random.default_rng(seed)
+    lo, hi = np.log(row_range[0]), np.log(row_range[1])
+    rows = np.exp(rng.uniform(lo, hi, n_specs))
+    rows *= total_rows / rows.sum()
+    rows = np.clip(np.round(rows), 500, max_rows or np.inf).astype(np.int64)
+    out = []
+    for s in range(n_specs):
+        r = np.random.default_rng(seed * 1000 + s)
+        n = int(rows[s])
+        n_fe = int(r.integers(1, 4))
+        G = [max(2, int(round(c * n ** 0.7))) for c in r.uniform(0.2, 1.0, n_fe)]
+        fe = [r.integers(1, g + 1, size=n, dtype=np.int32) for g in G]
+        k = int(r.integers(2, 25))
+        iv = r.random() < 0.25
+        n_endog = int(r.integers(1, 3)) if iv else 0
+        n_endog = min(n_endog, k - 1)
+        l = n_endog + int(r.integers(0, 3)) if iv else 0
+        X = r.standard_normal((n, k))
+        Zm = r.standard_normal((n, l)) if l else np.zeros((n, 0))
+        u = r.standard_normal(n)
+        for j in range(n_endog):  # endogenous columns driven by the instruments and the error
+            X[:, j] += Zm @ r.uniform(0.4, 0.8, l) + 0.4 * u
+        y = X @ r.uniform(-1, 1, k) + sum(r.normal(0, 0.3, g)[f - 1] for g, f in zip(G, fe)) + u
+        ncl = int(r.integers(1, n_fe + 1))
+        cl = sorted(r.choice(np.arange(1, n_fe + 1), size=ncl, replace=False).tolist())
+        host = fe_host_arrays(y=y, W=np.asfortranarray(X), Z=np.asfortranarray(Zm),
+                              fe_ids=np.asfortranarray(np.vstack(fe)))
+        out.append((host, dict(cluster_fe_dims=cl, iv_regressors=list(range(1, n_endog + 1)))))
+    return out

@@ -143,6 +143,40 @@ int fegb_group_sizes(const int* const* d_fe_ids, int n_fe, long long n, int* siz
 /* Number of kernel launches issued by this library since it was loaded. */
 long long fegb_kernel_launches(void);
 
+/* ---- batched specifications ----
+ * One independent regression of a batch: its own rows, columns, FE ids,
+ * cluster dimensions and IV columns (device arrays in the layout of
+ * fegb_estimate_device). */
+typedef struct fegb_spec {
+    long long n;               /* rows (> 0) */
+    int k, l, n_fe;            /* regressors, instruments, FE dimensions (1..8) */
+    const double* y;           /* device, n */
+    const double* W;           /* device, n x k column-major (ld n) */
+    const double* Z;           /* device, n x l column-major (ld n); may be NULL when l = 0 */
+    const int* const* fe_ids;  /* host array of n_fe device pointers to n 1-based ids */
+    int n_cluster_dims;
+    const int* cluster_dims;   /* 1-based FE dimensions of this spec */
+    int n_iv_regressors;
+    const int* iv_regressors;  /* 1-based endogenous columns of W */
+    int n_iv_instruments;
+    const int* iv_instruments; /* 1-based columns of Z (0 entries = all) */
+} fegb_spec;
+
+/* Fits n_specs independent specifications with one within-transform per
+ * column-count class: the specifications of a class are stacked into one
+ * problem whose FE groups are disjoint by specification and demeaned
+ * together (the stacked system is block diagonal, so each specification gets
+ * exactly its own projection); each is then estimated on its own rows.
+ * Tolerance, precision, method and SE convention come from cfg (singleton
+ * dropping is not supported here); cluster dimensions and IV columns from
+ * each spec. beta and se are host arrays of sum(k) values in spec order;
+ * results[i] describes spec i (fe_iterations, converged, max_update and
+ * time_demean are those of its class's shared within-transform; with
+ * cfg.profile the class's sweep timings appear once, in the prof_* fields of
+ * the class's first spec). */
+int fegb_estimate_batch(const fegb_config* cfg, int n_specs, const fegb_spec* specs, double* beta, double* se,
+                        fegb_result* results);
+
 /* ---- formula design-matrix expansion (src/src_main.f90:595-1440) ----
  * Every expanded regressor or instrument is a product of factors taken left
  * to right; a factor is a raw source column or the dummy of one of its levels

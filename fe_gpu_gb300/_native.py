@@ -132,6 +132,26 @@ class FegbSpec(C.Structure):
     ]
 
 
+class FegbDataset(C.Structure):
+    _fields_ = [
+        ("n", C.c_longlong),
+        ("k", C.c_int),
+        ("l", C.c_int),
+        ("n_fe", C.c_int),
+        ("has_cluster", C.c_int),
+        ("has_weights", C.c_int),
+        ("precision_flag", C.c_int),
+        ("metadata_offset", C.c_longlong),
+        ("y", C.c_void_p),
+        ("W", C.c_void_p),
+        ("Z", C.c_void_p),
+        ("fe_ids", C.c_void_p),
+        ("cluster", C.c_void_p),
+        ("weights", C.c_void_p),
+        ("seconds", C.c_double),
+    ]
+
+
 _P = C.c_void_p
 _I = C.c_int
 _LL = C.c_longlong
@@ -184,6 +204,10 @@ SIGNATURES = {
     "fegb_group_sizes": (_I, [C.POINTER(C.c_void_p), _I, _LL, _IP]),
     "fegb_drop_singletons": (_I, [C.POINTER(C.c_void_p), _IP, _I, _LL, _P, C.POINTER(C.c_longlong)]),
     "fegb_kernel_launches": (_LL, []),
+    "fegb_reconstruct_fe": (_I, [C.POINTER(FegbConfig), _LL, _I, _I, _P, _P, _DP, C.POINTER(C.c_void_p), _IP, _DP,
+                                 C.POINTER(C.c_longlong), _IP, _DP]),
+    "fegb_load_bin": (_I, [C.c_char_p, C.POINTER(FegbDataset)]),
+    "fegb_free_dataset": (_I, [C.POINTER(FegbDataset)]),
     "fegb_estimate_batch": (_I, [C.POINTER(FegbConfig), _I, C.POINTER(FegbSpec), _DP, _DP, C.POINTER(FegbResult)]),
     "fegb_design_levels": (_I, [_P, _LL, _I, _IP, _IP, _P]),
     "fegb_build_design": (_I, [C.POINTER(C.c_void_p), _I, _LL, C.POINTER(FegbDesignColumn), _I, _P, _LL, _P]),

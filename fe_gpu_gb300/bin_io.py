@@ -250,3 +250,68 @@ def write_dataset(path: str, y, W, fe_ids, Z=None, cluster=None, weights=None, p
                     _write_text(f, s)
             _write_text(f, metadata.get("cluster", ""))
             _write_text(f, metadata.get("weights", ""))
+
+
+def read_metadata(path: str, offset: int, hdr: fe_dataset_header) -> fe_dataset_header:
+    """Reads the META names block at byte offset into hdr (the tail parsed by
+    load_dataset_from_file, src/io/fe_data_io.f90:360-389)."""
+    if offset <= 0:
+        return hdr
+    with open(path, "rb") as f:
+        f.seek(offset)
+        raw = f.read()
+    mv = memoryview(raw)
+    if bytes(mv[0:4]) != b"META":
+        raise FeDataError("Unexpected metadata marker in dataset file")
+    (version,) = struct.unpack_from("<i", mv, 4)
+    if version != 1:
+        raise FeDataError("Unsupported metadata version in dataset file")
+    p = 8
+    hdr.depvar_name, p = _read_text(mv, p)
+    hdr.regressor_names, p = _read_text_list(mv, p)
+    hdr.instrument_names, p = _read_text_list(mv, p)
+    hdr.fe_names, p = _read_text_list(mv, p)
+    hdr.cluster_name, p = _read_text(mv, p)
+    hdr.weight_name, p = _read_text(mv, p)
+    return hdr
+
+
+class DeviceDataset:
+    """A .bin dataset loaded straight into device memory (fegb_load_bin).
+    Device pointers: y, W, Z (column-major, ld n), fe_ids[d]; freed on close()."""
+
+    def __init__(self, path: str):
+        import ctypes as C
+
+        from . import _native as N
+
+        self._ds = N.FegbDataset()
+        N.check(N.lib().fegb_load_bin(str(path).encode(), C.byref(self._ds)), "fegb_load_bin")
+        d = self._ds
+        self.n, self.k, self.l, self.n_fe = d.n, d.k, d.l, d.n_fe
+        self.seconds = d.seconds
+        self.header = fe_dataset_header(n_obs=d.n, n_regressors=d.k, n_instruments=d.l, n_fe=d.n_fe,
+                                        has_cluster=bool(d.has_cluster), has_weights=bool(d.has_weights),
+                                        precision_flag=d.precision_flag)
+        read_metadata(path, d.metadata_offset, self.header)
+        self.y = d.y or 0
+        self.W = d.W or 0
+        self.Z = d.Z or 0
+        self.fe_ids = [(d.fe_ids or 0) + 4 * self.n * j for j in range(self.n_fe)]
+        self.cluster = d.cluster or 0
+        self.weights = d.weights or 0
+
+    def close(self) -> None:
+        import ctypes as C
+
+        from . import _native as N
+
+        if self._ds is not None:
+            N.check(N.lib().fegb_free_dataset(C.byref(self._ds)), "fegb_free_dataset")
+            self._ds = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -807,29 +807,33 @@ struct CGBuffers {
 template <typename T>
 int cg_alloc(Problem& P, CGBuffers<T>& B) {
     Scratch& scr = *P.scr;
+    // r, z, q, x: compact rows of C; p (gathered by the operator sweep): rows padded to B.ld
     B.ld = cg_row_stride(P.C, (int)sizeof(T));
-    const size_t n = (size_t)std::max(1LL, P.Gt) * B.ld;
-    FEGB_TRY(dalloc(scr, &B.r, n, "cg r"));
-    FEGB_TRY(dalloc(scr, &B.z, n, "cg z"));
-    FEGB_TRY(dalloc(scr, &B.p, n, "cg p"));
-    FEGB_TRY(dalloc(scr, &B.q, n, "cg q"));
-    FEGB_TRY(dalloc(scr, &B.x, n, "cg solution"));
+    const int C = P.C;
+    const size_t nc = (size_t)std::max(1LL, P.Gt) * C;
+    const size_t np = (size_t)std::max(1LL, P.Gt) * B.ld;
+    FEGB_TRY(dalloc(scr, &B.r, nc, "cg r"));
+    FEGB_TRY(dalloc(scr, &B.z, nc, "cg z"));
+    FEGB_TRY(dalloc(scr, &B.p, np, "cg p"));
+    FEGB_CUDA(cudaMemsetAsync(B.p, 0, sizeof(T) * np, P.s), "cg p padding zero");
+    FEGB_TRY(dalloc(scr, &B.q, nc, "cg q"));
+    FEGB_TRY(dalloc(scr, &B.x, nc, "cg solution"));
     FEGB_TRY(dalloc(scr, &B.inv, (size_t)std::max(1LL, P.Gt), "cg inverse counts"));
     FEGB_TRY(launch_inv_counts_t<T>(P.counts_all, P.Gt, B.inv, P.s));
     const int L = B.ld;
-    FEGB_TRY(dalloc(scr, &B.rz, (size_t)L, "cg rz"));
-    FEGB_TRY(dalloc(scr, &B.rz_new, (size_t)L, "cg rz new"));
-    FEGB_TRY(dalloc(scr, &B.pq, (size_t)L, "cg pq"));
+    FEGB_TRY(dalloc(scr, &B.rz, (size_t)C, "cg rz"));
+    FEGB_TRY(dalloc(scr, &B.rz_new, (size_t)C, "cg rz new"));
+    FEGB_TRY(dalloc(scr, &B.pq, (size_t)C, "cg pq"));
     FEGB_TRY(dalloc(scr, &B.zmax, 1, "cg zmax"));
-    B.rz_blocks = cg_partial_blocks(P.Gt * L);
+    B.rz_blocks = cg_partial_blocks(P.Gt * C);
     B.pq_block_off.assign(P.n_fe + 1, 0);
     for (int d = 0; d < P.n_fe; ++d)
-        B.pq_block_off[d + 1] = B.pq_block_off[d] + cg_partial_blocks((long long)std::max(1, P.dims[d].G) * L);
+        B.pq_block_off[d + 1] = B.pq_block_off[d] + cg_partial_blocks((long long)std::max(1, P.dims[d].G) * C);
     B.pq_blocks = B.pq_block_off[P.n_fe];
-    FEGB_TRY(dalloc(scr, &B.rz_part, (size_t)B.rz_blocks * L, "cg rz partials"));
+    FEGB_TRY(dalloc(scr, &B.rz_part, (size_t)B.rz_blocks * C, "cg rz partials"));
     FEGB_TRY(dalloc(scr, &B.zmax_part, (size_t)B.rz_blocks, "cg zmax partials"));
-    FEGB_TRY(dalloc(scr, &B.pq_part, (size_t)std::max(1, B.pq_blocks) * L, "cg pq partials"));
-    FEGB_CUDA(cudaMemsetAsync(B.pq_part, 0, sizeof(double) * (size_t)std::max(1, B.pq_blocks) * L, P.s),
+    FEGB_TRY(dalloc(scr, &B.pq_part, (size_t)std::max(1, B.pq_blocks) * C, "cg pq partials"));
+    FEGB_CUDA(cudaMemsetAsync(B.pq_part, 0, sizeof(double) * (size_t)std::max(1, B.pq_blocks) * C, P.s),
               "cg pq partials zero");
     // the operator sweep writes sums/head/tail at the padded stride
     if (L > P.C) {
@@ -878,7 +882,46 @@ int cg_apply(Problem& P, CGBuffers<T>& B) {
             ps.tab[ps.n] = B.p + P.goff[e] * C;
             ++ps.n;
         }
-        // every dimension is traversed in its group-sorted order (identity for the primary)
+        if (D.mode == MODE_SMALLG) {
+            // few groups: storage order with private per-slot tables, so the
+            // other dimensions' rows are read in storage order (the primary's
+            // once per run) instead of once per group of this dimension
+            SmallGParams<T> sp{};
+            sp.X = nullptr;
+            sp.C = C;
+            sp.n = P.n;
+            sp.gid = D.gid;
+            sp.G = D.G;
+            sp.pend.n = 0;
+            for (int e = 0; e < P.n_fe; ++e) {
+                if (e == d) continue;
+                sp.pend.gid[sp.pend.n] = P.dims[e].gid;
+                sp.pend.tab[sp.pend.n] = B.p + P.goff[e] * L;
+                ++sp.pend.n;
+            }
+            sp.tld = L;
+            sp.no_data = 1;
+            sp.writeback = 0;
+            sp.rows_per_block = (P.n + P.smallg_nb - 1) / P.smallg_nb;
+            sp.partials = P.partials;
+            FEGB_TRY(launch_smallg_sweep<T>(sp, P.smallg_nb, P.s));
+            FEGB_TRY(launch_fold_smallg(P.partials, P.smallg_nb, D.G, C, P.sums, P.s));
+            if (P.profile) {
+                FEGB_CUDA(cudaEventRecord(tm.b, P.s), "profile record");
+                P.timed.push_back(tm);
+            }
+            FinalizeParams src{};
+            src.G = D.G;
+            src.C = C;
+            src.sums = P.sums;  // complete group sums, compact rows
+            src.counts = D.counts;
+            FEGB_TRY(launch_cg_q<T>(src, C, B.p + P.goff[d] * L, L, B.q + P.goff[d] * C,
+                                    B.pq_part + (size_t)B.pq_block_off[d] * C, P.s));
+            P.projections += 1;
+            P.demean_bytes += cg_operator_bytes(P, sizeof(T));
+            continue;
+        }
+        // every other dimension is traversed in its group-sorted order (identity for the primary)
         CGRowsParams<T> rp{};
         rp.n = P.n;
         rp.C = C;
@@ -909,20 +952,20 @@ int cg_apply(Problem& P, CGBuffers<T>& B) {
         src.tail = B.tail;
         src.R = CG_CHUNK;
         src.counts = D.counts;
-        FEGB_TRY(launch_cg_q<T>(src, C, B.p + P.goff[d] * L, B.q + P.goff[d] * L,
-                                B.pq_part + (size_t)B.pq_block_off[d] * L, P.s));
+        FEGB_TRY(launch_cg_q<T>(src, C, B.p + P.goff[d] * L, L, B.q + P.goff[d] * C,
+                                B.pq_part + (size_t)B.pq_block_off[d] * C, P.s));
         P.projections += 1;
         P.demean_bytes += cg_operator_bytes(P, sizeof(T));
     }
-    return launch_fold_partials(B.pq_part, B.pq_blocks, L, B.pq, P.s);
+    return launch_fold_partials(B.pq_part, B.pq_blocks, C, B.pq, P.s);
 }
 
 // Preconditioned (group-count) CG on D'D delta = D'r, r = current FP64
 // residual whose group means are in mu_all; delta accumulates into alpha_all.
 template <typename T>
 int cg_solve(Problem& P, CGBuffers<T>& B, double inner_tol, int max_it, int* iters, double* zmax_out) {
-    const int C = B.ld;  // vector ops run over the padded rows (padding stays zero)
-    FEGB_TRY(launch_cg_init<T>(P.Gt, C, P.C, P.counts_all, P.mu_all, B.r, B.z, B.p, B.x, B.rz_part, B.zmax_part,
+    const int C = P.C;  // vector ops run over compact rows; p keeps the padded stride B.ld
+    FEGB_TRY(launch_cg_init<T>(P.Gt, C, P.counts_all, P.mu_all, B.r, B.z, B.p, B.ld, B.x, B.rz_part, B.zmax_part,
                                B.zmax, P.s));
     FEGB_TRY(launch_fold_partials(B.rz_part, B.rz_blocks, C, B.rz, P.s));
     double best = DBL_MAX;
@@ -931,8 +974,8 @@ int cg_solve(Problem& P, CGBuffers<T>& B, double inner_tol, int max_it, int* ite
     double zm = 0.0;
     for (; it < max_it; ++it) {
         FEGB_TRY(cg_apply<T>(P, B));
-        FEGB_TRY(launch_cg_update<T>(P.Gt, C, B.inv, B.rz, B.pq, B.p, B.q, B.x, B.r, B.z, B.rz_part, B.zmax_part,
-                                     B.zmax, P.s));
+        FEGB_TRY(launch_cg_update<T>(P.Gt, C, B.inv, B.rz, B.pq, B.p, B.ld, B.q, B.x, B.r, B.z, B.rz_part,
+                                     B.zmax_part, B.zmax, P.s));
         FEGB_TRY(launch_fold_partials(B.rz_part, B.rz_blocks, C, B.rz_new, P.s));
         unsigned long long bits = 0;
         FEGB_TRY(d2h_sync(&bits, B.zmax, sizeof(bits), P.s, "cg zmax copy"));
@@ -948,12 +991,12 @@ int cg_solve(Problem& P, CGBuffers<T>& B, double inner_tol, int max_it, int* ite
             ++it;
             break;  // the recursive residual stopped improving at this precision
         }
-        FEGB_TRY(launch_cg_direction<T>(P.Gt, C, B.rz, B.rz_new, B.z, B.p, P.s));
+        FEGB_TRY(launch_cg_direction<T>(P.Gt, C, B.rz, B.rz_new, B.z, B.p, B.ld, P.s));
     }
     *iters = it;
     *zmax_out = zm;
     // the increment of this solve becomes the FP64 table applied by the next FP64 pass
-    return launch_to_f64<T>(B.x, B.ld, P.alpha_all, P.C, P.Gt, P.s);
+    return launch_to_f64<T>(B.x, P.C, P.alpha_all, P.C, P.Gt, P.s);
 }
 
 // FP64 refinement loop around a CG inner solve in storage type T.
@@ -1210,7 +1253,7 @@ int estimate_on_problem(Problem& P, const fegb_config& cfg, const int* G_all, lo
     double* gram = nullptr;
     FEGB_TRY(scr.alloc(&gram, (size_t)C * C, "gram"));
     MatView xv{P.X, C, 1, C};
-    FEGB_TRY(crossprod(xv, xv, n, true, false, 1.0, 0.0, gram, C, s, scr));
+    FEGB_TRY(crossprod_auto(xv, xv, n, true, false, 1.0, 0.0, gram, C, s, scr));
     std::vector<double> hg((size_t)C * C);
     FEGB_TRY(d2h_sync(hg.data(), gram, sizeof(double) * C * C, s, "gram copy"));
     auto Gm = [&](int i, int j) { return hg[(size_t)i + (size_t)j * C]; };
@@ -1448,7 +1491,7 @@ int estimate_on_problem(Problem& P, const fegb_config& cfg, const int* G_all, lo
             FEGB_TRY(sub.alloc(&Sc, (size_t)n_cl * ns, "cluster scores"));
             FEGB_TRY(cluster_score_sums(P, S, ns, perm, gseq, off, n_cl, Sc, sub));
             MatView sv{Sc, ns, 1, ns};
-            FEGB_TRY(crossprod(sv, sv, n_cl, true, false, 1.0, 0.0, meat, ns, s, sub));
+            FEGB_TRY(crossprod_auto(sv, sv, n_cl, true, false, 1.0, 0.0, meat, ns, s, sub));
             const double* Mk = meat;
             int ldm = ns;
             if (use_iv) {
@@ -1584,6 +1627,101 @@ int estimate_device_impl(const fegb_config* cfg_in, long long n, int k, int l, i
     res->time_total = seconds_since(t_start) + t_h2d;
     if (st != 0) return st;
     return set_ok();
+}
+
+// ------------------------- FE reconstruction (--save-fe) -------------------------
+//
+// reconstruct_and_save_fixed_effects (src/core/fe_pipeline.f90:1619-1733):
+// the residual r = y - W beta is swept dimension by dimension in index order
+// (forward Gauss-Seidel, no relaxation); each dimension's group means, centred
+// on their count-weighted mean, are added to its FE values and subtracted from
+// r, until the largest update is below the tolerance. The weighted mean of
+// the group means is the mean of r, which those subtractions keep constant, so
+// the loop equals plain forward AP on r - mean(r) with the FE values as the
+// accumulated updates: that is what runs here, on the sweep kernels.
+
+__global__ void fe_resid_kernel(const double* __restrict__ y, const double* __restrict__ W, long long n, int k,
+                                const double* __restrict__ beta, double* __restrict__ r) {
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long st = (long long)gridDim.x * blockDim.x;
+    for (; i < n; i += st) {
+        double v = y[i];
+        for (int j = 0; j < k; ++j) v -= W[(long long)j * n + i] * beta[j];  // column by column, as the reference
+        r[i] = v;
+    }
+}
+
+__global__ void shift_kernel(double* __restrict__ r, long long n, double m) {
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long st = (long long)gridDim.x * blockDim.x;
+    for (; i < n; i += st) r[i] -= m;
+}
+
+int reconstruct_fe_impl(const fegb_config& cfg, long long n, int k, int n_fe, const double* y, const double* W,
+                        const double* beta_host, const int32_t* const* ids, const int* group_sizes, double* values,
+                        long long* counts, int* iterations, double* max_update, cudaStream_t s) {
+    *iterations = 0;
+    *max_update = 0.0;
+    if (n <= 0 || n_fe <= 0) return 0;
+    configure_mem_pool();
+    Scratch scr(s);
+    double *r = nullptr, *b = nullptr;
+    FEGB_TRY(scr.alloc(&r, (size_t)n, "fe residual"));
+    FEGB_TRY(scr.alloc(&b, (size_t)std::max(1, k), "fe beta"));
+    if (k > 0) FEGB_TRY(h2d_sync(b, beta_host, sizeof(double) * k, s, "beta upload"));
+    fe_resid_kernel<<<grid_stride_blocks(n, 256), 256, 0, s>>>(y, W, n, k, b, r);
+    FEGB_LAUNCH_CHECK("fe residual");
+    // mean of r (fixed-order partial sums)
+    {
+        int nb = (int)std::min<long long>((long long)num_sms() * 4, (n + 255) / 256);
+        double* part = nullptr;
+        FEGB_TRY(scr.alloc(&part, (size_t)nb, "fe mean partials"));
+        tss_partials_kernel<<<nb, 256, 0, s>>>(r, n, 0.0, nullptr, part);
+        FEGB_LAUNCH_CHECK("fe mean");
+        std::vector<double> h(nb);
+        FEGB_TRY(d2h_sync(h.data(), part, sizeof(double) * nb, s, "fe mean copy"));
+        double sum = 0.0;
+        for (double v : h) sum += v;
+        shift_kernel<<<grid_stride_blocks(n, 256), 256, 0, s>>>(r, n, sum / (double)n);
+        FEGB_LAUNCH_CHECK("fe centre");
+    }
+    Problem P;
+    P.s = s;
+    P.scr = &scr;
+    long long n_single = 0;
+    FEGB_TRY(build_problem(P, n, 0, 0, n_fe, r, nullptr, nullptr, ids, group_sizes, false, false, &n_single, false));
+    FEGB_TRY(reset_ap_state(P, true));
+    PendingList pl;
+    ProjectionOpts o;
+    o.alpha = true;
+    o.mixing = false;
+    double mu = 0.0;
+    const int max_iter = std::max(1, cfg.fe_max_iter);
+    int it = max_iter + 1;  // a DO loop that runs to completion leaves its index one past the end
+    for (int iter = 1; iter <= max_iter; ++iter) {
+        FEGB_CUDA(cudaMemsetAsync(P.max_bits, 0, sizeof(unsigned long long), s), "reset max");
+        for (int d = 0; d < n_fe; ++d) FEGB_TRY(project<double>(P, d, P.X, pl, o));
+        unsigned long long bits = 0;
+        FEGB_TRY(d2h_sync(&bits, P.max_bits, sizeof(bits), s, "fe max copy"));
+        mu = bits_to_double(bits);
+        if (mu < cfg.fe_tol) {
+            it = iter;
+            break;
+        }
+    }
+    *iterations = it;
+    *max_update = mu;
+    long long off = 0;
+    for (int d = 0; d < n_fe; ++d) {
+        const Dim& D = P.dims[d];
+        if (D.G <= 0) continue;
+        FEGB_TRY(d2h_sync(values + off, D.alpha, sizeof(double) * D.G, s, "fe values copy"));
+        std::vector<int32_t> c(D.G);
+        FEGB_TRY(d2h_sync(c.data(), D.counts, sizeof(int32_t) * D.G, s, "fe counts copy"));
+        for (int g = 0; g < D.G; ++g) counts[off + g] = c[g];
+        off += D.G;
+    }
+    return 0;
 }
 
 // In-place within-transform of device columns (column-major, ld n).
@@ -1989,6 +2127,27 @@ int fegb_within_transform(const fegb_config* cfg_in, long long n, int k, int l, 
     if (converged) *converged = st.converged;
     if (iterations) *iterations = st.iterations;
     if (max_update) *max_update = st.max_update;
+    return set_ok();
+}
+
+int fegb_reconstruct_fe(const fegb_config* cfg_in, long long n, int k, int n_fe, const double* d_y, const double* d_W,
+                        const double* beta, const int* const* d_fe_ids, const int* group_sizes, double* fe_values,
+                        long long* fe_counts, int* iterations, double* max_update) {
+    fegb_config cfg;
+    if (cfg_in)
+        cfg = *cfg_in;
+    else
+        fegb_config_init(&cfg);
+    if (n < 0 || k < 0 || n_fe < 0) return set_error("invalid sizes");
+    if (n > 0x7fffffffLL) return set_error("n=%lld exceeds the int32 row range", n);
+    if (n > 0 && (!d_y || (k > 0 && (!d_W || !beta)) || (n_fe > 0 && !d_fe_ids)))
+        return set_error("fegb_reconstruct_fe: null argument");
+    if (!fe_values || !fe_counts || !iterations || !max_update) return set_error("fegb_reconstruct_fe: null output");
+    StreamHolder sh(cfg.stream);
+    std::vector<const int32_t*> ids(n_fe);
+    for (int d = 0; d < n_fe; ++d) ids[d] = d_fe_ids[d];
+    FEGB_TRY(reconstruct_fe_impl(cfg, n, k, n_fe, d_y, d_W, beta, ids.data(), group_sizes, fe_values, fe_counts,
+                                 iterations, max_update, sh.get()));
     return set_ok();
 }
 

@@ -513,6 +513,177 @@ int crossprod(const MatView& A, const MatView& B, long long n, bool gram, bool u
     return 0;
 }
 
+// ------------------------- split-FP32 cross products -------------------------
+
+namespace {
+
+constexpr int DS_TR = 64;   // rows per shared-memory tile (and per FP64 fold)
+constexpr int DS_PPT = 4;   // output entries per thread
+constexpr int DS_PAIRS_PER_BLOCK = CP_THREADS * DS_PPT;
+
+// Largest magnitude the split path accepts: products and 64-row partial sums
+// stay far inside the FP32 range (2^127).
+constexpr double DS_MAX_ABS = 1152921504606846976.0;  // 2^60
+
+// dst[r * w + c] = (hi, lo) of src element (r, c): hi = fl32(x), lo = fl32(x - hi)
+// (x - hi is exact in FP64). *bad is set when a value is not finite or exceeds
+// DS_MAX_ABS; the caller then uses the FP64 path.
+__global__ void split_fp32_kernel(const double* __restrict__ src, long long rs, long long cs, int w, long long n,
+                                  float2* __restrict__ dst, int* __restrict__ bad) {
+    const long long total = n * w;
+    long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long st = (long long)gridDim.x * blockDim.x;
+    bool out_of_range = false;
+    for (; e < total; e += st) {
+        const long long r = e / w;
+        const int c = (int)(e - r * w);
+        const double x = src[r * rs + (long long)c * cs];
+        out_of_range |= !(fabs(x) <= DS_MAX_ABS);
+        const float hi = __double2float_rn(x);
+        const float lo = __double2float_rn(x - (double)hi);
+        dst[e] = make_float2(hi, lo);
+    }
+    if (__any_sync(0xffffffffu, out_of_range) && (threadIdx.x & 31) == 0) atomicOr(bad, 1);
+}
+
+struct DSParams {
+    const float2* A;  // n x a, row-major
+    int a;
+    const float2* B;  // n x b, row-major (== A for a Gram)
+    int b;
+    long long n;
+    int gram;
+    long long p0;     // first pair of this launch
+    int npairs;
+    long long rows_per_block;
+    double* partials;  // row blocks x npairs
+};
+
+__global__ void __launch_bounds__(CP_THREADS) crossprod_split_kernel(DSParams p) {
+    extern __shared__ float2 dsm[];
+    float2* sA = dsm;
+    float2* sB = p.gram ? dsm : dsm + DS_TR * p.a;
+    const int t = threadIdx.x;
+    const int chunk0 = blockIdx.y * DS_PAIRS_PER_BLOCK;
+    int pi[DS_PPT], pj[DS_PPT];
+    bool pv[DS_PPT];
+    float sh[DS_PPT], sl[DS_PPT];
+    double acc[DS_PPT];
+#pragma unroll
+    for (int s = 0; s < DS_PPT; ++s) {
+        const int local = chunk0 + t + s * CP_THREADS;
+        pv[s] = local < p.npairs;
+        pair_ij(p.p0 + (pv[s] ? local : 0), p.gram, p.a, pi[s], pj[s]);
+        sh[s] = 0.f;
+        sl[s] = 0.f;
+        acc[s] = 0.0;
+    }
+    const long long r0 = (long long)blockIdx.x * p.rows_per_block;
+    const long long r1 = min(p.n, r0 + p.rows_per_block);
+    for (long long tile = r0; tile < r1; tile += DS_TR) {
+        const int rows = (int)min((long long)DS_TR, r1 - tile);
+        for (int e = t; e < rows * p.a; e += CP_THREADS) sA[e] = p.A[tile * p.a + e];
+        if (!p.gram)
+            for (int e = t; e < rows * p.b; e += CP_THREADS) sB[e] = p.B[tile * p.b + e];
+        __syncthreads();
+        for (int r = 0; r < rows; ++r) {
+#pragma unroll
+            for (int s = 0; s < DS_PPT; ++s) {
+                if (!pv[s]) continue;
+                const float2 x = sA[r * p.a + pi[s]];
+                const float2 y = sB[r * p.b + pj[s]];
+                // (xh + xl)(yh + yl) = ph + pe + cross, ph + pe exact (TwoProd by FMA)
+                // (the _rn intrinsics are never contracted into FMAs, which TwoSum relies on)
+                const float ph = __fmul_rn(x.x, y.x);
+                const float pe = fmaf(x.x, y.x, -ph);
+                const float cr = fmaf(x.x, y.y, x.y * y.x);
+                // TwoSum of the running high part and ph; the rounding error goes to sl
+                const float s1 = __fadd_rn(sh[s], ph);
+                const float bb = __fsub_rn(s1, sh[s]);
+                const float err = __fadd_rn(__fsub_rn(sh[s], __fsub_rn(s1, bb)), __fsub_rn(ph, bb));
+                sh[s] = s1;
+                sl[s] += err + (pe + cr);
+            }
+        }
+#pragma unroll
+        for (int s = 0; s < DS_PPT; ++s) {
+            acc[s] += (double)sh[s] + (double)sl[s];
+            sh[s] = 0.f;
+            sl[s] = 0.f;
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int s = 0; s < DS_PPT; ++s)
+        if (pv[s]) p.partials[(long long)blockIdx.x * p.npairs + chunk0 + t + s * CP_THREADS] = acc[s];
+}
+
+}  // namespace
+
+int crossprod_split(const MatView& A, const MatView& B, long long n, bool gram, bool upper_only, double alpha,
+                    double beta, double* out, int ldo, cudaStream_t s, Scratch& scr) {
+    const int a = A.cols, b = gram ? A.cols : B.cols;
+    if (a <= 0 || b <= 0) return 0;
+    if (n <= 0) return crossprod(A, B, n, gram, upper_only, alpha, beta, out, ldo, s, scr);
+    const size_t smem = sizeof(float2) * DS_TR * (gram ? a : a + b);
+    if (smem > 200 * 1024) return crossprod(A, B, n, gram, upper_only, alpha, beta, out, ldo, s, scr);
+    static const cudaError_t attr_status =
+        cudaFuncSetAttribute(crossprod_split_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    if (attr_status != cudaSuccess) return set_cuda_error(attr_status, "split crossprod attr");
+    float2 *sa = nullptr, *sb = nullptr;
+    int* bad = nullptr;
+    FEGB_TRY(scr.alloc(&bad, 1, "split range flag"));
+    FEGB_CUDA(cudaMemsetAsync(bad, 0, sizeof(int), s), "split flag reset");
+    FEGB_TRY(scr.alloc(&sa, (size_t)n * a, "split A"));
+    split_fp32_kernel<<<grid_stride_blocks(n * a, 256), 256, 0, s>>>(A.ptr, A.rs, A.cs, a, n, sa, bad);
+    FEGB_LAUNCH_CHECK("split A");
+    if (!gram) {
+        FEGB_TRY(scr.alloc(&sb, (size_t)n * b, "split B"));
+        split_fp32_kernel<<<grid_stride_blocks(n * b, 256), 256, 0, s>>>(B.ptr, B.rs, B.cs, b, n, sb, bad);
+        FEGB_LAUNCH_CHECK("split B");
+    }
+    int hbad = 0;
+    FEGB_CUDA(cudaMemcpyAsync(&hbad, bad, sizeof(int), cudaMemcpyDeviceToHost, s), "split flag copy");
+    FEGB_CUDA(cudaStreamSynchronize(s), "split flag sync");
+    if (hbad) return crossprod(A, B, n, gram, upper_only, alpha, beta, out, ldo, s, scr);
+    const long long total_pairs = gram ? (long long)a * (a + 1) / 2 : (long long)a * b;
+    long long nb = std::min<long long>((n + DS_TR - 1) / DS_TR, (long long)num_sms() * 4);
+    long long rpb = (n + nb - 1) / nb;
+    rpb = ((rpb + DS_TR - 1) / DS_TR) * DS_TR;
+    nb = (n + rpb - 1) / rpb;
+    for (long long p0 = 0; p0 < total_pairs; p0 += CP_MAXPAIRS_LAUNCH) {
+        const int np = (int)std::min<long long>(CP_MAXPAIRS_LAUNCH, total_pairs - p0);
+        double* partials = nullptr;
+        FEGB_TRY(scr.alloc(&partials, (size_t)nb * np, "split crossprod partials"));
+        DSParams p;
+        p.A = sa;
+        p.a = a;
+        p.B = gram ? sa : sb;
+        p.b = b;
+        p.n = n;
+        p.gram = gram ? 1 : 0;
+        p.p0 = p0;
+        p.npairs = np;
+        p.rows_per_block = rpb;
+        p.partials = partials;
+        dim3 grid((unsigned)nb, (unsigned)((np + DS_PAIRS_PER_BLOCK - 1) / DS_PAIRS_PER_BLOCK));
+        crossprod_split_kernel<<<grid, CP_THREADS, smem, s>>>(p);
+        FEGB_LAUNCH_CHECK("split crossprod");
+        crossprod_reduce_kernel<<<(np + 255) / 256, 256, 0, s>>>(partials, (int)nb, np, p0, gram, upper_only, a, alpha,
+                                                                  beta, out, ldo);
+        FEGB_LAUNCH_CHECK("split crossprod reduce");
+    }
+    return 0;
+}
+
+int crossprod_auto(const MatView& A, const MatView& B, long long n, bool gram, bool upper_only, double alpha,
+                   double beta, double* out, int ldo, cudaStream_t s, Scratch& scr) {
+    const long long pairs = gram ? (long long)A.cols * (A.cols + 1) / 2 : (long long)A.cols * B.cols;
+    if (pairs >= CROSSPROD_SPLIT_MIN_PAIRS && n >= 4096)
+        return crossprod_split(A, B, n, gram, upper_only, alpha, beta, out, ldo, s, scr);
+    return crossprod(A, B, n, gram, upper_only, alpha, beta, out, ldo, s, scr);
+}
+
 int residual_scores(const double* X, int C, long long n, const double* beta, int k, const int* score_cols_dev,
                     int n_score, double* S, double* resid, double* rss_dev, cudaStream_t s, Scratch& scr) {
     int nb = (int)std::min<long long>((long long)num_sms() * 8, std::max(1LL, (n + RS_THREADS - 1) / RS_THREADS));

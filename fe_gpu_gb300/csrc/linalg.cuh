@@ -23,6 +23,20 @@ struct MatView {
 int crossprod(const MatView& A, const MatView& B, long long n, bool gram, bool upper_only, double alpha, double beta,
               double* out, int ldo, cudaStream_t s, Scratch& scr);
 
+// Same result through the FP32 pipe: every FP64 value is split into an FP32
+// pair (hi + lo, 48 significant bits), products are formed error-free
+// (TwoProd by FMA plus the cross terms), summed with TwoSum into an FP32 pair
+// per output and folded into FP64 every tile of rows. Relative error per term
+// about 2^-47, against 2^-53 for FP64 products; GB300 issues FP32 at about 60x
+// its FP64 rate, so wide cross products run several times faster. Used by the
+// estimator when an output has at least CROSSPROD_SPLIT_MIN_PAIRS entries.
+constexpr long long CROSSPROD_SPLIT_MIN_PAIRS = 300;
+int crossprod_split(const MatView& A, const MatView& B, long long n, bool gram, bool upper_only, double alpha,
+                    double beta, double* out, int ldo, cudaStream_t s, Scratch& scr);
+// crossprod_split when the output is large enough, else crossprod.
+int crossprod_auto(const MatView& A, const MatView& B, long long n, bool gram, bool upper_only, double alpha,
+                   double beta, double* out, int ldo, cudaStream_t s, Scratch& scr);
+
 // Residual and score rows from the AoS block X (n x C, col 0 = y, 1..k = W):
 // r_i = y_i - sum_j W_ij beta_j; if S != null, S[i][t] = r_i * X[i][score_cols[t]]
 // (t < n_score); if resid != null, resid[i] = r_i. rss (device scalar) = sum r_i^2.

@@ -158,6 +158,7 @@ __global__ void __launch_bounds__(256, 4) smallg_sweep_kernel(SmallGParams<T> p,
         const int32_t* __restrict__ gid = p.gid;
         T* __restrict__ X = p.X;
         const int np = p.pend.n;
+        const long long tld = p.tld > 0 ? p.tld : C;
         for (long long j = r0; j < r1; j += U) {
             int g[U];
             T v[U];
@@ -173,7 +174,7 @@ __global__ void __launch_bounds__(256, 4) smallg_sweep_kernel(SmallGParams<T> p,
                 const T* __restrict__ tb = p.pend.tab[e];
 #pragma unroll
                 for (int u = 0; u < U; ++u)
-                    if (ok[u]) v[u] -= tb[(long long)pg[j + u] * C + col];
+                    if (ok[u]) v[u] -= tb[(long long)pg[j + u] * tld + col];
             }
             if (p.writeback && !p.no_data) {
 #pragma unroll
@@ -328,28 +329,25 @@ __device__ __forceinline__ void column_partials(A prod, long long base, int C, A
 }
 
 template <typename T>
-__global__ void __launch_bounds__(FIN_THREADS) cg_q_kernel(FinalizeParams src, int creal, const T* __restrict__ p,
-                                                            T* __restrict__ q, double* __restrict__ pq_partials) {
+__global__ void __launch_bounds__(FIN_THREADS) cg_q_kernel(FinalizeParams src, int C, const T* __restrict__ p,
+                                                            int pld, T* __restrict__ q, double* __restrict__ pq_partials) {
+    // compact elements (g, c < C); the sweep sums use the padded stride src.C, p uses pld
     __shared__ T smem[FIN_THREADS];
-    const long long total = (long long)src.G * src.C;
+    const long long total = (long long)src.G * C;
     const long long base = (long long)blockIdx.x * FIN_THREADS;
     const long long idx = base + threadIdx.x;
     T prod = T(0);
     if (idx < total) {
-        const int g = (int)(idx / src.C);
-        const int c = (int)(idx - (long long)g * src.C);
-        if (c < creal) {
-            const double ssum = source_sum(src, g, c, idx, total);
-            const T pv = p[idx];
-            // ssum = -(sum over the group's rows of the other dimensions' p)
-            const T qv = (T)src.counts[g] * pv - (T)ssum;
-            q[idx] = qv;
-            prod = pv * qv;
-        } else {
-            q[idx] = T(0);
-        }
+        const int g = (int)(idx / C);
+        const int c = (int)(idx - (long long)g * C);
+        const double ssum = source_sum(src, g, c, (long long)g * src.C + c, (long long)src.G * src.C);
+        const T pv = p[(long long)g * pld + c];
+        // ssum = -(sum over the group's rows of the other dimensions' p)
+        const T qv = (T)src.counts[g] * pv - (T)ssum;
+        q[idx] = qv;
+        prod = pv * qv;
     }
-    column_partials<T>(prod, base, src.C, smem, pq_partials);
+    column_partials<T>(prod, base, C, smem, pq_partials);
 }
 
 // Fixed-shape block tree: thread t folds elements t, t + 256, ... in order,
@@ -419,7 +417,7 @@ __global__ void find_long_kernel(const int32_t* __restrict__ off, int G, int R, 
 template <typename T>
 __global__ void __launch_bounds__(FIN_THREADS)
     cg_update_kernel(long long Gt, int C, const T* __restrict__ inv_counts, const double* __restrict__ rz,
-                     const double* __restrict__ pq, const T* __restrict__ p, const T* __restrict__ q,
+                     const double* __restrict__ pq, const T* __restrict__ p, int pld, const T* __restrict__ q,
                      T* __restrict__ x, T* __restrict__ r, T* __restrict__ z, double* __restrict__ rz_partials,
                      double* __restrict__ zmax_partials) {
     __shared__ T smem[FIN_THREADS];
@@ -438,7 +436,7 @@ __global__ void __launch_bounds__(FIN_THREADS)
         const long long g = idx / C;
         const int c = (int)(idx - g * C);
         const T a = C <= 64 ? step[c] : (T)(pq[c] != 0.0 ? rz[c] / pq[c] : 0.0);
-        x[idx] += a * p[idx];
+        x[idx] += a * p[g * pld + c];
         const T rv = r[idx] - a * q[idx];
         const T zv = rv * inv_counts[g];
         r[idx] = rv;
@@ -463,7 +461,8 @@ __global__ void __launch_bounds__(FIN_THREADS)
 
 template <typename T>
 __global__ void cg_direction_kernel(long long Gt, int C, const double* __restrict__ rz_old,
-                                    const double* __restrict__ rz_new, const T* __restrict__ z, T* __restrict__ p) {
+                                    const double* __restrict__ rz_new, const T* __restrict__ z, T* __restrict__ p,
+                                    int pld) {
     __shared__ double beta[64];
     if (threadIdx.x < C && threadIdx.x < 64)
         beta[threadIdx.x] = rz_old[threadIdx.x] != 0.0 ? rz_new[threadIdx.x] / rz_old[threadIdx.x] : 0.0;
@@ -471,14 +470,21 @@ __global__ void cg_direction_kernel(long long Gt, int C, const double* __restric
     const long long total = Gt * C;
     long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const long long st = (long long)gridDim.x * blockDim.x;
-    // column of idx, advanced incrementally (no 64-bit division per element)
-    int c = (int)(idx % C);
-    const int cstep = (int)(st % C);
+    // (g, c) of idx, advanced incrementally (no 64-bit division per element)
+    long long g = idx / C;
+    int c = (int)(idx - g * C);
+    const long long gstep = st / C;
+    const int cstep = (int)(st - gstep * C);
     for (; idx < total; idx += st) {
         const T b = C <= 64 ? (T)beta[c] : (T)(rz_old[c] != 0.0 ? rz_new[c] / rz_old[c] : 0.0);
-        p[idx] = z[idx] + b * p[idx];
+        T* pe = p + g * pld + c;
+        *pe = z[idx] + b * *pe;
+        g += gstep;
         c += cstep;
-        if (c >= C) c -= C;
+        if (c >= C) {
+            c -= C;
+            ++g;
+        }
     }
 }
 
@@ -494,8 +500,8 @@ __global__ void copy_scalars_kernel(const double* __restrict__ src, double* __re
 
 template <typename T>
 __global__ void __launch_bounds__(FIN_THREADS)
-    cg_init_kernel(long long Gt, int C, int creal, const int32_t* __restrict__ counts, const double* __restrict__ mu,
-                   T* __restrict__ r, T* __restrict__ z, T* __restrict__ p, T* __restrict__ x,
+    cg_init_kernel(long long Gt, int C, const int32_t* __restrict__ counts, const double* __restrict__ mu,
+                   T* __restrict__ r, T* __restrict__ z, T* __restrict__ p, int pld, T* __restrict__ x,
                    double* __restrict__ rz_partials, double* __restrict__ zmax_partials) {
     __shared__ T smem[FIN_THREADS];
     __shared__ T red[FIN_THREADS / 32];
@@ -507,11 +513,11 @@ __global__ void __launch_bounds__(FIN_THREADS)
         const long long g = idx / C;
         const int c = (int)(idx - g * C);
         const int cnt = counts[g];
-        const T m = (cnt > 0 && c < creal) ? (T)mu[g * creal + c] : T(0);
+        const T m = cnt > 0 ? (T)mu[g * C + c] : T(0);
         const T rv = (T)cnt * m;
         r[idx] = rv;
         z[idx] = m;
-        p[idx] = m;
+        p[g * pld + c] = m;
         x[idx] = T(0);
         prod = rv * m;
         az = m < T(0) ? -m : m;
@@ -644,10 +650,10 @@ int launch_convert_f64_f32(const double* src, float* dst, long long n, cudaStrea
 int cg_partial_blocks(long long gc) { return (int)((gc + FIN_THREADS - 1) / FIN_THREADS); }
 
 template <typename T>
-int launch_cg_q(const FinalizeParams& src, int creal, const T* p, T* q, double* pq_partials, cudaStream_t s) {
-    long long total = (long long)src.G * src.C;
+int launch_cg_q(const FinalizeParams& src, int C, const T* p, int pld, T* q, double* pq_partials, cudaStream_t s) {
+    long long total = (long long)src.G * C;
     if (total <= 0) return 0;
-    cg_q_kernel<T><<<cg_partial_blocks(total), FIN_THREADS, 0, s>>>(src, creal, p, q, pq_partials);
+    cg_q_kernel<T><<<cg_partial_blocks(total), FIN_THREADS, 0, s>>>(src, C, p, pld, q, pq_partials);
     FEGB_LAUNCH_CHECK("cg q");
     return 0;
 }
@@ -697,12 +703,12 @@ int launch_inv_counts(const int32_t* counts, long long G, double* inv_counts, cu
 
 template <typename T>
 int launch_cg_update(long long Gt, int C, const T* inv_counts, const double* rz, const double* pq, const T* p,
-                     const T* q, T* x, T* r, T* z, double* rz_partials, double* zmax_partials,
+                     int pld, const T* q, T* x, T* r, T* z, double* rz_partials, double* zmax_partials,
                      unsigned long long* zmax, cudaStream_t s) {
     long long total = Gt * C;
     if (total <= 0) return 0;
     const int nb = cg_partial_blocks(total);
-    cg_update_kernel<T><<<nb, FIN_THREADS, 0, s>>>(Gt, C, inv_counts, rz, pq, p, q, x, r, z, rz_partials,
+    cg_update_kernel<T><<<nb, FIN_THREADS, 0, s>>>(Gt, C, inv_counts, rz, pq, p, pld, q, x, r, z, rz_partials,
                                                    zmax_partials);
     FEGB_LAUNCH_CHECK("cg update");
     fold_max_kernel<<<1, FIN_THREADS, 0, s>>>(zmax_partials, nb, zmax);
@@ -711,10 +717,11 @@ int launch_cg_update(long long Gt, int C, const T* inv_counts, const double* rz,
 }
 
 template <typename T>
-int launch_cg_direction(long long Gt, int C, double* rz_old, const double* rz_new, const T* z, T* p, cudaStream_t s) {
+int launch_cg_direction(long long Gt, int C, double* rz_old, const double* rz_new, const T* z, T* p, int pld,
+                        cudaStream_t s) {
     long long total = Gt * C;
     if (total > 0) {
-        cg_direction_kernel<T><<<grid_stride_blocks(total, 256), 256, 0, s>>>(Gt, C, rz_old, rz_new, z, p);
+        cg_direction_kernel<T><<<grid_stride_blocks(total, 256), 256, 0, s>>>(Gt, C, rz_old, rz_new, z, p, pld);
         FEGB_LAUNCH_CHECK("cg direction");
     }
     copy_scalars_kernel<<<1, ((C + 31) / 32) * 32, 0, s>>>(rz_new, rz_old, C);
@@ -723,24 +730,24 @@ int launch_cg_direction(long long Gt, int C, double* rz_old, const double* rz_ne
 }
 
 template <typename T>
-int launch_cg_init(long long Gt, int C, int creal, const int32_t* counts, const double* mu, T* r, T* z, T* p, T* x,
+int launch_cg_init(long long Gt, int C, const int32_t* counts, const double* mu, T* r, T* z, T* p, int pld, T* x,
                    double* rz_partials, double* zmax_partials, unsigned long long* zmax, cudaStream_t s) {
     long long total = Gt * C;
     if (total <= 0) return 0;
     const int nb = cg_partial_blocks(total);
-    cg_init_kernel<T><<<nb, FIN_THREADS, 0, s>>>(Gt, C, creal, counts, mu, r, z, p, x, rz_partials, zmax_partials);
+    cg_init_kernel<T><<<nb, FIN_THREADS, 0, s>>>(Gt, C, counts, mu, r, z, p, pld, x, rz_partials, zmax_partials);
     FEGB_LAUNCH_CHECK("cg init");
     fold_max_kernel<<<1, FIN_THREADS, 0, s>>>(zmax_partials, nb, zmax);
     FEGB_LAUNCH_CHECK("cg max fold");
     return 0;
 }
 
-template int launch_cg_q<double>(const FinalizeParams&, int, const double*, double*, double*, cudaStream_t);
-template int launch_cg_q<float>(const FinalizeParams&, int, const float*, float*, double*, cudaStream_t);
-template int launch_cg_update<double>(long long, int, const double*, const double*, const double*, const double*,
+template int launch_cg_q<double>(const FinalizeParams&, int, const double*, int, double*, double*, cudaStream_t);
+template int launch_cg_q<float>(const FinalizeParams&, int, const float*, int, float*, double*, cudaStream_t);
+template int launch_cg_update<double>(long long, int, const double*, const double*, const double*, const double*, int,
                                       const double*, double*, double*, double*, double*, double*,
                                       unsigned long long*, cudaStream_t);
-template int launch_cg_update<float>(long long, int, const float*, const double*, const double*, const float*,
+template int launch_cg_update<float>(long long, int, const float*, const double*, const double*, const float*, int,
                                      const float*, float*, float*, float*, double*, double*, unsigned long long*,
                                      cudaStream_t);
 
@@ -764,12 +771,13 @@ int launch_inv_counts_t(const int32_t* counts, long long G, T* inv, cudaStream_t
 }
 template int launch_inv_counts_t<float>(const int32_t*, long long, float*, cudaStream_t);
 template int launch_inv_counts_t<double>(const int32_t*, long long, double*, cudaStream_t);
-template int launch_cg_direction<double>(long long, int, double*, const double*, const double*, double*,
+template int launch_cg_direction<double>(long long, int, double*, const double*, const double*, double*, int,
                                          cudaStream_t);
-template int launch_cg_direction<float>(long long, int, double*, const double*, const float*, float*, cudaStream_t);
-template int launch_cg_init<double>(long long, int, int, const int32_t*, const double*, double*, double*, double*,
+template int launch_cg_direction<float>(long long, int, double*, const double*, const float*, float*, int,
+                                        cudaStream_t);
+template int launch_cg_init<double>(long long, int, const int32_t*, const double*, double*, double*, double*, int,
                                     double*, double*, double*, unsigned long long*, cudaStream_t);
-template int launch_cg_init<float>(long long, int, int, const int32_t*, const double*, float*, float*, float*, float*,
+template int launch_cg_init<float>(long long, int, const int32_t*, const double*, float*, float*, float*, int, float*,
                                    double*, double*, unsigned long long*, cudaStream_t);
 
 

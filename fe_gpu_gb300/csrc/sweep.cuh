@@ -69,6 +69,7 @@ struct SmallGParams {
     int no_data;
     long long rows_per_block;
     double* partials;      // nblocks x G x C
+    int tld;               // row stride of the pending tables (0 = C)
 };
 
 struct FinalizeParams {
@@ -183,16 +184,18 @@ inline int cg_row_stride(int C, int elem_bytes) {
 
 // ---- conjugate gradients on the FE normal equations (D'D a = D'e) ----
 // G-space vectors of all dimensions are concatenated: element (g, c) of
-// dimension d sits at ((goff_d + g) * C + c). Per-column scalars (C values)
-// live on the device; dot products use per-block partials folded in block
-// order, so every reduction is deterministic.
+// dimension d sits at ((goff_d + g) * C + c) for r, z, q and x (compact rows).
+// The direction p, which the operator sweep gathers, has rows padded to the
+// stride pld (cg_row_stride), its padding kept at zero. Per-column scalars
+// (C values) live on the device; dot products use per-block partials folded
+// in block order, so every reduction is deterministic.
 
 // q_d = counts_d * p_d - S_d, where S_d are the group sums of a no-data sweep
 // with pending tables {p_e, e != d} (sums of -p_e over the rows of each
 // group). Also writes per-block partials of p.q per column.
-// src.C is the padded row stride; columns at or beyond creal are padding (q = 0).
+// src.C is the padded row stride of the sweep sums; q is compact (C columns).
 template <typename T>
-int launch_cg_q(const FinalizeParams& src, int creal, const T* p, T* q, double* pq_partials, cudaStream_t s);
+int launch_cg_q(const FinalizeParams& src, int C, const T* p, int pld, T* q, double* pq_partials, cudaStream_t s);
 int cg_partial_blocks(long long gc);
 
 // out[c] = sum_b partials[b * C + c] for b < nb (fixed order)
@@ -203,7 +206,7 @@ int launch_fold_partials(const double* partials, int nb, int C, double* out, cud
 // per column and max |z| (bits, device scalar).
 template <typename T>
 int launch_cg_update(long long Gt, int C, const T* inv_counts, const double* rz, const double* pq, const T* p,
-                     const T* q, T* x, T* r, T* z, double* rz_partials, double* zmax_partials,
+                     int pld, const T* q, T* x, T* r, T* z, double* rz_partials, double* zmax_partials,
                      unsigned long long* zmax, cudaStream_t s);
 // dst[g * C + c] = (double) src[g * ld + c] for c < C
 template <typename T>
@@ -214,15 +217,16 @@ int launch_inv_counts_t(const int32_t* counts, long long G, T* inv, cudaStream_t
 
 // b = rz_new / rz_old per column; p = z + b p; rz_old = rz_new
 template <typename T>
-int launch_cg_direction(long long Gt, int C, double* rz_old, const double* rz_new, const T* z, T* p, cudaStream_t s);
+int launch_cg_direction(long long Gt, int C, double* rz_old, const double* rz_new, const T* z, T* p, int pld,
+                        cudaStream_t s);
 
 // r = counts * mu, z = p = mu (cast to T); partials of r.z and max |z|
 // inv_counts[g] = 1 / counts[g] (0 for empty groups)
 int launch_inv_counts(const int32_t* counts, long long G, double* inv_counts, cudaStream_t s);
 
-// C is the padded row stride, creal the columns of mu (G x creal).
+// mu is G x C; p is written at the padded stride pld (its padding is left untouched).
 template <typename T>
-int launch_cg_init(long long Gt, int C, int creal, const int32_t* counts, const double* mu, T* r, T* z, T* p, T* x,
+int launch_cg_init(long long Gt, int C, const int32_t* counts, const double* mu, T* r, T* z, T* p, int pld, T* x,
                    double* rz_partials, double* zmax_partials, unsigned long long* zmax, cudaStream_t s);
 
 }  // namespace fegb

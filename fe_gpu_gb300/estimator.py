@@ -356,3 +356,66 @@ def build_cluster_ids(fe_ids: np.ndarray, group_sizes: Sequence[int], subset_dim
                                       sizes.ctypes.data_as(C.POINTER(C.c_int)), len(dims), out.ctypes.data,
                                       C.byref(nc))
     return out, (nc.value if st == 0 else 0), st
+
+
+def fe_gpu_reconstruct_fe(cfg: fe_runtime_config, host: fe_host_arrays, beta: np.ndarray,
+                          group_sizes: Optional[Sequence[int]] = None) -> tuple:
+    """FE values of --save-fe (reconstruct_and_save_fixed_effects,
+    src/core/fe_pipeline.f90:1619-1733) on the device, from host arrays and the
+    fitted beta. Returns ([values per dimension], [counts per dimension],
+    iterations, max_update); values[d][g - 1] belongs to level g."""
+    y = np.ascontiguousarray(host.y, dtype=np.float64)
+    n = y.shape[0]
+    W = np.asfortranarray(host.W, dtype=np.float64) if host.W is not None else np.zeros((n, 0), order="F")
+    fe = np.asarray(host.fe_ids, dtype=np.int32)
+    k, n_fe = W.shape[1], fe.shape[0]
+    gs = [int(v) for v in (group_sizes if group_sizes is not None else fe.max(axis=1))]
+    by, bW = DeviceBuffer.from_array(y), DeviceBuffer.from_array(W)
+    bids = [DeviceBuffer.from_array(np.ascontiguousarray(fe[d])) for d in range(n_fe)]
+    ptrs = (C.c_void_p * max(1, n_fe))(*[C.c_void_p(b.ptr) for b in bids])
+    b = np.ascontiguousarray(beta[:k], dtype=np.float64)
+    total = sum(gs)
+    vals = np.zeros(max(1, total))
+    cnts = np.zeros(max(1, total), dtype=np.int64)
+    it = C.c_int(0)
+    mu = C.c_double(0)
+    c, keep = _make_config(cfg)
+    gsa = N.int_array(gs)
+    st = N.lib().fegb_reconstruct_fe(C.byref(c), n, k, n_fe, C.c_void_p(by.ptr), C.c_void_p(bW.ptr) if k else None,
+                                     b.ctypes.data_as(C.POINTER(C.c_double)), ptrs, C.cast(gsa, C.POINTER(C.c_int)),
+                                     vals.ctypes.data_as(C.POINTER(C.c_double)),
+                                     cnts.ctypes.data_as(C.POINTER(C.c_longlong)), C.byref(it), C.byref(mu))
+    N.check(st, "fegb_reconstruct_fe")
+    del keep
+    out_v, out_c, off = [], [], 0
+    for g in gs:
+        out_v.append(vals[off:off + g].copy())
+        out_c.append(cnts[off:off + g].copy())
+        off += g
+    return out_v, out_c, it.value, mu.value
+
+
+def format_es24_16(v: float) -> str:
+    """Fortran ES24.16: one digit before the point, 16 after, exponent
+    'E+dd' when it fits two digits and '+ddd' (no letter) otherwise,
+    right-aligned in 24 characters."""
+    m, e = f"{v:.16E}".split("E")
+    ex = int(e)
+    tail = f"E{ex:+03d}" if abs(ex) <= 99 else f"{ex:+04d}"
+    return f"{m}{tail}".rjust(24)
+
+
+def write_fe_outputs(prefix: str, values: Sequence[np.ndarray], counts: Sequence[np.ndarray]) -> list:
+    """write_fe_outputs (src/core/fe_pipeline.f90:1735-1771): one
+    <prefix>_fe<d>.csv per dimension, header 'level_id,fe_value', one line
+    'g,value' (I0, ES24.16) per level with a nonzero count."""
+    paths = []
+    for d, (v, c) in enumerate(zip(values, counts), start=1):
+        path = f"{prefix}_fe{d}.csv"
+        with open(path, "w") as f:
+            f.write("level_id,fe_value\n")
+            for g in range(len(v)):
+                if c[g] > 0:
+                    f.write(f"{g + 1},{format_es24_16(float(v[g]))}\n")
+        paths.append(path)
+    return paths

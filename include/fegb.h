@@ -143,6 +143,43 @@ int fegb_group_sizes(const int* const* d_fe_ids, int n_fe, long long n, int* siz
 /* Number of kernel launches issued by this library since it was loaded. */
 long long fegb_kernel_launches(void);
 
+/* FE reconstruction of --save-fe (reconstruct_and_save_fixed_effects,
+ * src/core/fe_pipeline.f90:1619-1733): forward Gauss-Seidel sweeps of the
+ * residual y - W beta (beta: host, k values), dimension by dimension, each
+ * dimension's group means centred and accumulated, until the largest update
+ * is below cfg.fe_tol (at most cfg.fe_max_iter sweeps). fe_values and
+ * fe_counts (host) receive sum(G_d) entries, dimension by dimension (group g of
+ * dimension d at offset sum_{e<d} G_e + g - 1); groups with count 0 have value 0. */
+int fegb_reconstruct_fe(const fegb_config* cfg, long long n, int k, int n_fe, const double* d_y, const double* d_W,
+                        const double* beta, const int* const* d_fe_ids, const int* group_sizes, double* fe_values,
+                        long long* fe_counts, int* iterations, double* max_update);
+
+/* ---- the .bin dataset straight to device memory ----
+ * Replaces the host loader load_dataset_from_file (src/io/fe_data_io.f90:23-389)
+ * plus the upload: the header is detected as the reference does (new/old
+ * header, FP64/FP32 values, optional precision flag and META block), every
+ * column is read in chunks into pinned buffers by a pool of host threads and
+ * copied to its place on the device; FP32 values are widened to FP64 there.
+ * Device buffers are owned by the caller: release them with fegb_free_dataset.
+ * The META names block, when present, starts at metadata_offset. */
+typedef struct fegb_dataset {
+    long long n;
+    int k, l, n_fe;
+    int has_cluster, has_weights;
+    int precision_flag;         /* values on disk: 0 FP64, 1 FP32 */
+    long long metadata_offset;  /* byte offset of the META block, 0 when absent */
+    double* y;                  /* device, n */
+    double* W;                  /* device, n x k column-major (ld n); NULL when k = 0 */
+    double* Z;                  /* device, n x l column-major (ld n); NULL when l = 0 */
+    int* fe_ids;                /* device, dimension d at fe_ids + d * n (1-based ids) */
+    int* cluster;               /* device, n; NULL unless has_cluster */
+    double* weights;            /* device, n; NULL unless has_weights */
+    double seconds;             /* wall time of the load */
+} fegb_dataset;
+
+int fegb_load_bin(const char* path, fegb_dataset* out);
+int fegb_free_dataset(fegb_dataset* ds);
+
 /* ---- batched specifications ----
  * One independent regression of a batch: its own rows, columns, FE ids,
  * cluster dimensions and IV columns (device arrays in the layout of

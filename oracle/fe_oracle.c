@@ -1187,3 +1187,82 @@ done:
     free(Z);
     return 0;
 }
+
+
+/* src/core/fe_pipeline.f90:1619-1733 (reconstruct_and_save_fixed_effects). */
+int orc_reconstruct_fe(long long n, int k, int n_fe, const double* y, const double* W, const double* beta,
+                       const int32_t* fe_ids, const int32_t* sizes, double tol, int max_iter, double* values,
+                       long long* counts, int* iterations, double* max_update) {
+    *iterations = 0;
+    *max_update = 0.0;
+    if (n_fe <= 0 || n <= 0) return 0;
+    long long* off = (long long*)calloc((size_t)n_fe + 1, sizeof(long long));
+    int gmax = 0;
+    for (int d = 0; d < n_fe; ++d) {
+        off[d + 1] = off[d] + sizes[d];
+        if (sizes[d] > gmax) gmax = sizes[d];
+    }
+    double* r = (double*)malloc(sizeof(double) * (size_t)n);
+    double* gsum = (double*)malloc(sizeof(double) * (size_t)(gmax > 0 ? gmax : 1));
+    double* gmean = (double*)malloc(sizeof(double) * (size_t)(gmax > 0 ? gmax : 1));
+    if (!off || !r || !gsum || !gmean) {
+        free(off); free(r); free(gsum); free(gmean);
+        return 1;
+    }
+    for (long long j = 0; j < n; ++j) r[j] = y[j];
+    for (int c = 0; c < k; ++c)  /* residual = residual - W(:, j) * beta(j), column by column */
+        for (long long j = 0; j < n; ++j) r[j] -= W[(size_t)c * n + j] * beta[c];
+    for (long long t = 0; t < off[n_fe]; ++t) {
+        values[t] = 0.0;
+        counts[t] = 0;
+    }
+    for (long long j = 0; j < n; ++j)
+        for (int d = 0; d < n_fe; ++d) {
+            const int g = fe_ids[(size_t)j * n_fe + d];
+            if (g >= 1 && g <= sizes[d]) counts[off[d] + g - 1] += 1;
+        }
+    double mu = 0.0;
+    int iter;
+    for (iter = 1; iter <= max_iter; ++iter) {
+        mu = 0.0;
+        for (int d = 0; d < n_fe; ++d) {
+            const int G = sizes[d];
+            for (int g = 0; g < G; ++g) gsum[g] = 0.0;
+            for (long long j = 0; j < n; ++j) {
+                const int g = fe_ids[(size_t)j * n_fe + d];
+                if (g >= 1 && g <= G) gsum[g - 1] += r[j];
+            }
+            double wsum = 0.0;
+            long long tot = 0;
+            for (int g = 0; g < G; ++g) {
+                const long long c = counts[off[d] + g];
+                if (c > 0) {
+                    gmean[g] = gsum[g] / (double)c;
+                    wsum += gmean[g] * (double)c;
+                    tot += c;
+                } else {
+                    gmean[g] = 0.0;
+                }
+            }
+            const double center = tot > 0 ? wsum / (double)tot : 0.0;
+            for (int g = 0; g < G; ++g) {
+                if (counts[off[d] + g] > 0) {
+                    gmean[g] -= center;
+                    values[off[d] + g] += gmean[g];
+                    if (fabs(gmean[g]) > mu) mu = fabs(gmean[g]);
+                } else {
+                    gmean[g] = 0.0;
+                }
+            }
+            for (long long j = 0; j < n; ++j) {
+                const int g = fe_ids[(size_t)j * n_fe + d];
+                if (g >= 1 && g <= G) r[j] -= gmean[g - 1];
+            }
+        }
+        if (mu < tol) break;
+    }
+    *iterations = iter;
+    *max_update = mu;
+    free(off); free(r); free(gsum); free(gmean);
+    return 0;
+}

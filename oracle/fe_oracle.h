@@ -99,6 +99,17 @@ int orc_demean_symmetric(double* y, double* W, int k, double* Z, int l, long lon
                          int* converged, double* max_update);
 
 /* fe_pipeline.f90:71-513 */
+/* FE reconstruction of --save-fe (src/core/fe_pipeline.f90:1619-1733),
+ * restated loop for loop: residual = y - sum_j W_j beta_j; per iteration and
+ * FE dimension d = 1..n_fe: group sums, means, centring on the count-weighted
+ * mean, fe_values += means, residual -= means; stop when max |mean| < tol.
+ * fe_ids: n_fe x n, dimension fastest. values/counts: sum(G_d) entries,
+ * dimension by dimension. *iterations follows the reference's DO loop
+ * (max_iter + 1 when the tolerance was not reached). */
+int orc_reconstruct_fe(long long n, int k, int n_fe, const double* y, const double* W, const double* beta,
+                       const int32_t* fe_ids, const int32_t* sizes, double tol, int max_iter, double* values,
+                       long long* counts, int* iterations, double* max_update);
+
 int orc_cpu_estimate(const orc_config* cfg, long long n, int k, int n_fe, const double* y, const double* W,
                      const int32_t* fe_ids, const int32_t* group_sizes, double* beta, double* se,
                      orc_result* res);

@@ -97,6 +97,8 @@ def lib():
         _lib.orc_demean_symmetric.argtypes = [P, P, C.c_int, P, C.c_int, C.c_longlong, C.c_int, P, P, C.c_double,
                                               C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_double)]
         _lib.orc_chol_solve_invert.argtypes = [C.c_int, P, P, P, P]
+        _lib.orc_reconstruct_fe.argtypes = [C.c_longlong, C.c_int, C.c_int, P, P, P, P, P, C.c_double, C.c_int, P, P,
+                                            C.POINTER(C.c_int), C.POINTER(C.c_double)]
         _lib.orc_psd_fix.argtypes = [C.c_int, P]
     return _lib
 
@@ -253,3 +255,30 @@ def psd_fix(A):
     A = np.asfortranarray(A, dtype=np.float64).copy(order="F")
     applied = lib().orc_psd_fix(A.shape[0], A.ctypes.data)
     return A, bool(applied)
+
+
+def reconstruct_fe(y, W, fe_ids, beta, tol=1e-8, max_iter=100000, sizes=None):
+    """FE values of --save-fe, restated loop for loop
+    (src/core/fe_pipeline.f90:1619-1733). Returns ([values per dimension],
+    [counts per dimension], iterations, max_update)."""
+    y, W, _, fe = _prep(y, W, None, fe_ids)
+    n_fe, n = fe.shape
+    k = W.shape[1]
+    sizes = np.asarray(group_sizes(fe) if sizes is None else sizes, dtype=np.int32)
+    b = np.ascontiguousarray(np.asarray(beta, dtype=np.float64)[:k])
+    total = int(sizes.sum())
+    vals = np.zeros(max(1, total))
+    cnts = np.zeros(max(1, total), dtype=np.int64)
+    it = C.c_int(0)
+    mu = C.c_double(0)
+    st = lib().orc_reconstruct_fe(C.c_longlong(n), k, n_fe, y.ctypes.data, W.ctypes.data, b.ctypes.data,
+                                  fe.ctypes.data, sizes.ctypes.data, C.c_double(tol), max_iter, vals.ctypes.data,
+                                  cnts.ctypes.data, C.byref(it), C.byref(mu))
+    if st != 0:
+        raise RuntimeError("orc_reconstruct_fe failed")
+    out_v, out_c, off = [], [], 0
+    for g in sizes:
+        out_v.append(vals[off:off + g].copy())
+        out_c.append(cnts[off:off + g].copy())
+        off += g
+    return out_v, out_c, it.value, mu.value

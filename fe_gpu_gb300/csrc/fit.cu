@@ -802,6 +802,12 @@ struct CGBuffers {
     unsigned long long* zmax = nullptr;
     int rz_blocks = 0, pq_blocks = 0;
     std::vector<int> pq_block_off;
+    // small-G dimension folded into the primary's storage-order operator pass (-1 = none)
+    int sg_dim = -1;
+    long long* sg_part = nullptr;       // per block of that pass: G_s x C int64 sums
+    long long sg_blocks = 0;
+    unsigned long long* pmax = nullptr;  // max |p| (bits)
+    double* pmax_part = nullptr;         // per direction block
 };
 
 template <typename T>
@@ -835,6 +841,23 @@ int cg_alloc(Problem& P, CGBuffers<T>& B) {
     FEGB_TRY(dalloc(scr, &B.pq_part, (size_t)std::max(1, B.pq_blocks) * C, "cg pq partials"));
     FEGB_CUDA(cudaMemsetAsync(B.pq_part, 0, sizeof(double) * (size_t)std::max(1, B.pq_blocks) * C, P.s),
               "cg pq partials zero");
+    // one small-G dimension can ride on the primary's storage-order pass
+    // (FP32 form; see CGRowsParams::sg_src)
+    if (sizeof(T) == 4 && P.n_fe >= 2 && P.n_fe - 1 <= 3) {
+        int cand = -1, nsmall = 0;
+        for (int d = 0; d < P.n_fe; ++d)
+            if (d != P.primary && P.dims[d].mode == MODE_SMALLG && P.dims[d].G > 0) {
+                cand = d;
+                ++nsmall;
+            }
+        if (nsmall == 1 && (size_t)P.dims[cand].G * C * sizeof(long long) <= CG_SG_SMEM_MAX) {
+            B.sg_dim = cand;
+            B.sg_blocks = cg_rows_blocks(P.n, C, cg_rows_tile(C));
+            FEGB_TRY(dalloc(scr, &B.sg_part, (size_t)B.sg_blocks * P.dims[cand].G * C, "cg small-G side sums"));
+            FEGB_TRY(dalloc(scr, &B.pmax, 1, "cg pmax"));
+            FEGB_TRY(dalloc(scr, &B.pmax_part, (size_t)grid_stride_blocks(P.Gt * C, 256), "cg pmax partials"));
+        }
+    }
     // the operator sweep writes sums/head/tail at the padded stride
     if (L > P.C) {
         long long nchunks = std::max(1LL, seg_nchunks(P.n, CG_CHUNK));
@@ -863,9 +886,28 @@ template <typename T>
 int cg_apply(Problem& P, CGBuffers<T>& B) {
     const int C = P.C;
     const int L = B.ld;
-    for (int d = 0; d < P.n_fe; ++d) {
+    // the primary first: its pass also produces the folded small-G dimension's sums
+    std::vector<int> order;
+    order.push_back(P.primary);
+    for (int d = 0; d < P.n_fe; ++d)
+        if (d != P.primary) order.push_back(d);
+    for (int d : order) {
         Dim& D = P.dims[d];
         if (D.G <= 0) continue;
+        if (d == B.sg_dim) {
+            // sums accumulated by the primary's pass: fold the block tables, add counts * p_s
+            FEGB_TRY(launch_cg_sg_fold<T>(B.sg_part, (int)B.sg_blocks, D.G, C, B.pmax, P.n_fe, P.n, D.counts,
+                                          B.p + P.goff[d] * L, L, P.sums, P.s));
+            FinalizeParams src{};
+            src.G = D.G;
+            src.C = C;
+            src.sums = P.sums;
+            src.counts = D.counts;
+            FEGB_TRY(launch_cg_q<T>(src, C, B.p + P.goff[d] * L, L, B.q + P.goff[d] * C,
+                                    B.pq_part + (size_t)B.pq_block_off[d] * C, P.s));
+            P.projections += 1;
+            continue;
+        }
         Problem::Timed tm{};
         if (P.profile) {
             tm.kind = 4 + (D.mode == MODE_SMALLG ? 2 : 0) + (sizeof(T) == 4 ? 1 : 0);
@@ -937,6 +979,20 @@ int cg_apply(Problem& P, CGBuffers<T>& B) {
         rp.sums = B.sums;
         rp.head = B.head;
         rp.tail = B.tail;
+        if (d == P.primary && B.sg_dim >= 0) {
+            int idx = 0;
+            for (int e = 0; e < P.n_fe; ++e) {
+                if (e == d) continue;
+                if (e == B.sg_dim) rp.sg_src = idx;
+                ++idx;
+            }
+            rp.sg_G = P.dims[B.sg_dim].G;
+            rp.n_dims = P.n_fe;
+            rp.prim_tab = B.p + P.goff[d] * L;
+            rp.pmax_bits = B.pmax;
+            rp.sg_part = B.sg_part;
+            if (!cg_rows_vector_path(rp)) return set_error("cg operator: small-G side output without the vector path");
+        }
         FEGB_TRY(launch_cg_rows<T>(rp, P.s));
         FEGB_TRY(launch_long_sums(D.off, B.head, B.tail, CG_CHUNK, L, D.long_list_cg, D.n_long_cg, B.sums, P.s));
         if (P.profile) {
@@ -960,13 +1016,148 @@ int cg_apply(Problem& P, CGBuffers<T>& B) {
     return launch_fold_partials(B.pq_part, B.pq_blocks, C, B.pq, P.s);
 }
 
+// ---- graph-driven CG loop ----
+// One CG iteration (operator, update, fold, convergence test, direction) is
+// captured once per fit as the body of a conditional while-node; a one-thread
+// kernel applies the host loop's stopping rules on the device and clears the
+// node's condition, so the solve runs without a host round trip per
+// iteration. Used whenever kernel timing (profile) is off.
+struct CGLoopCtl {
+    double tol;
+    double best;
+    double zm;
+    int max_it;
+    int it;
+    int since_best;
+    int stop;
+};
+
+__global__ void cg_loop_reset_kernel(CGLoopCtl* c, double tol, int max_it) {
+    c->tol = tol;
+    c->best = DBL_MAX;
+    c->zm = 0.0;
+    c->max_it = max_it;
+    c->it = 0;
+    c->since_best = 0;
+    c->stop = 0;
+}
+
+// the stopping rules of the host loop in cg_solve_host
+__global__ void cg_loop_check_kernel(const unsigned long long* __restrict__ zmax_bits, CGLoopCtl* c,
+                                     cudaGraphConditionalHandle h) {
+    const double zm = __longlong_as_double((long long)*zmax_bits);
+    c->zm = zm;
+    const int it = c->it + 1;
+    c->it = it;
+    bool stop = false;
+    if (zm < c->tol) {
+        stop = true;
+    } else if (zm < 0.9 * c->best) {
+        c->best = zm;
+        c->since_best = 0;
+    } else if (++c->since_best > 60) {
+        stop = true;  // the recursive residual stopped improving at this precision
+    }
+    if (it >= c->max_it) stop = true;
+    c->stop = stop ? 1 : 0;
+    cudaGraphSetConditional(h, stop ? 0u : 1u);
+}
+
+template <typename T>
+struct CGGraph {
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    CGLoopCtl* ctl = nullptr;  // device
+    ~CGGraph() {
+        if (exec) cudaGraphExecDestroy(exec);
+        if (graph) cudaGraphDestroy(graph);
+    }
+};
+
+// Builds the loop graph; returns nonzero (and leaves G empty) when the driver
+// refuses any step, in which case the caller keeps the host loop.
+template <typename T>
+int cg_build_graph(Problem& P, CGBuffers<T>& B, CGGraph<T>& G) {
+    if (cudaGraphCreate(&G.graph, 0) != cudaSuccess) return 1;
+    cudaGraphConditionalHandle h;
+    if (cudaGraphConditionalHandleCreate(&h, G.graph, 1, cudaGraphCondAssignDefault) != cudaSuccess) return 1;
+    // the parameter struct has no default constructor: zeroed storage, as the API requires
+    alignas(cudaGraphNodeParams) unsigned char npbuf[sizeof(cudaGraphNodeParams)];
+    std::memset(npbuf, 0, sizeof(npbuf));
+    cudaGraphNodeParams& np = *reinterpret_cast<cudaGraphNodeParams*>(npbuf);
+    np.type = cudaGraphNodeTypeConditional;
+    np.conditional.handle = h;
+    np.conditional.type = cudaGraphCondTypeWhile;
+    np.conditional.size = 1;
+    cudaGraphNode_t node;
+    if (cudaGraphAddNode(&node, G.graph, nullptr, nullptr, 0, &np) != cudaSuccess) return 1;
+    cudaGraph_t body = np.conditional.phGraph_out[0];
+    cudaStream_t cs = nullptr;
+    if (cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking) != cudaSuccess) return 1;
+    if (cudaStreamBeginCaptureToGraph(cs, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed) != cudaSuccess) {
+        cudaStreamDestroy(cs);
+        return 1;
+    }
+    cudaStream_t saved = P.s;
+    P.s = cs;
+    const int C = P.C;
+    int st = cg_apply<T>(P, B);
+    if (!st)
+        st = launch_cg_update<T>(P.Gt, C, B.inv, B.rz, B.pq, B.p, B.ld, B.q, B.x, B.r, B.z, B.rz_part, B.zmax_part,
+                                 B.zmax, cs);
+    if (!st) st = launch_fold_partials(B.rz_part, B.rz_blocks, C, B.rz_new, cs);
+    if (!st) {
+        cg_loop_check_kernel<<<1, 1, 0, cs>>>(B.zmax, G.ctl, h);
+        count_launch();
+        if (cudaPeekAtLastError() != cudaSuccess) st = 1;
+    }
+    if (!st) st = launch_cg_direction<T>(P.Gt, C, B.rz, B.rz_new, B.z, B.p, B.ld, cs, &G.ctl->stop, B.pmax_part, B.pmax);
+    P.s = saved;
+    cudaGraph_t captured = nullptr;
+    const cudaError_t ec = cudaStreamEndCapture(cs, &captured);
+    cudaStreamDestroy(cs);
+    if (st || ec != cudaSuccess) return 1;
+    if (cudaGraphInstantiate(&G.exec, G.graph, 0) != cudaSuccess) return 1;
+    return 0;
+}
+
+template <typename T>
+int cg_solve_host(Problem& P, CGBuffers<T>& B, double inner_tol, int max_it, int* iters, double* zmax_out);
+
 // Preconditioned (group-count) CG on D'D delta = D'r, r = current FP64
 // residual whose group means are in mu_all; delta accumulates into alpha_all.
+// With a loop graph the iterations run on the device (same stopping rules).
 template <typename T>
-int cg_solve(Problem& P, CGBuffers<T>& B, double inner_tol, int max_it, int* iters, double* zmax_out) {
+int cg_solve(Problem& P, CGBuffers<T>& B, double inner_tol, int max_it, int* iters, double* zmax_out,
+             CGGraph<T>* G = nullptr) {
+    if (G && G->exec && max_it > 0) {
+        const int C = P.C;
+        FEGB_TRY(launch_cg_init<T>(P.Gt, C, P.counts_all, P.mu_all, B.r, B.z, B.p, B.ld, B.x, B.rz_part, B.zmax_part,
+                                   B.zmax, P.s));
+        if (B.pmax)  // p = z at the start: max |p| = max |z|
+            FEGB_CUDA(cudaMemcpyAsync(B.pmax, B.zmax, sizeof(unsigned long long), cudaMemcpyDeviceToDevice, P.s),
+                      "cg pmax init");
+        FEGB_TRY(launch_fold_partials(B.rz_part, B.rz_blocks, C, B.rz, P.s));
+        cg_loop_reset_kernel<<<1, 1, 0, P.s>>>(G->ctl, inner_tol, max_it);
+        FEGB_LAUNCH_CHECK("cg loop reset");
+        FEGB_CUDA(cudaGraphLaunch(G->exec, P.s), "cg loop graph launch");
+        CGLoopCtl h;
+        FEGB_TRY(d2h_sync(&h, G->ctl, sizeof(h), P.s, "cg loop state copy"));
+        *iters = h.it;
+        *zmax_out = h.zm;
+        return launch_to_f64<T>(B.x, P.C, P.alpha_all, P.C, P.Gt, P.s);
+    }
+    return cg_solve_host<T>(P, B, inner_tol, max_it, iters, zmax_out);
+}
+
+template <typename T>
+int cg_solve_host(Problem& P, CGBuffers<T>& B, double inner_tol, int max_it, int* iters, double* zmax_out) {
     const int C = P.C;  // vector ops run over compact rows; p keeps the padded stride B.ld
     FEGB_TRY(launch_cg_init<T>(P.Gt, C, P.counts_all, P.mu_all, B.r, B.z, B.p, B.ld, B.x, B.rz_part, B.zmax_part,
                                B.zmax, P.s));
+    if (B.pmax)  // p = z at the start: max |p| = max |z|
+        FEGB_CUDA(cudaMemcpyAsync(B.pmax, B.zmax, sizeof(unsigned long long), cudaMemcpyDeviceToDevice, P.s),
+                  "cg pmax init");
     FEGB_TRY(launch_fold_partials(B.rz_part, B.rz_blocks, C, B.rz, P.s));
     double best = DBL_MAX;
     int since_best = 0;
@@ -991,7 +1182,7 @@ int cg_solve(Problem& P, CGBuffers<T>& B, double inner_tol, int max_it, int* ite
             ++it;
             break;  // the recursive residual stopped improving at this precision
         }
-        FEGB_TRY(launch_cg_direction<T>(P.Gt, C, B.rz, B.rz_new, B.z, B.p, B.ld, P.s));
+        FEGB_TRY(launch_cg_direction<T>(P.Gt, C, B.rz, B.rz_new, B.z, B.p, B.ld, P.s, nullptr, B.pmax_part, B.pmax));
     }
     *iters = it;
     *zmax_out = zm;
@@ -1009,6 +1200,16 @@ int demean_cg(Problem& P, double tol, int max_iter, int* iterations, int* conver
     if (P.n_fe == 0 || P.n == 0) return 0;
     CGBuffers<T> B;
     FEGB_TRY(cg_alloc<T>(P, B));
+    CGGraph<T> G;
+    bool use_graph = false;
+    if (!P.profile) {
+        FEGB_TRY(dalloc(*P.scr, &G.ctl, 1, "cg loop state"));
+        use_graph = cg_build_graph<T>(P, B, G) == 0;
+        if (!use_graph) {
+            cudaGetLastError();  // the host loop takes over
+            set_ok();
+        }
+    }
     const int max_outer = 12;
     double mu = 0.0, mu_prev = DBL_MAX;
     int total = 0, hit = 0;
@@ -1027,7 +1228,7 @@ int demean_cg(Problem& P, double tol, int max_iter, int* iterations, int* conver
             sizeof(T) == 4 ? std::max(0.5 * tol, 2e-6 * mu) : std::max(0.5 * tol, 1e-12 * mu);
         int it = 0;
         double zm = 0.0;
-        FEGB_TRY(cg_solve<T>(P, B, inner_tol, max_iter - total, &it, &zm));
+        FEGB_TRY(cg_solve<T>(P, B, inner_tol, max_iter - total, &it, &zm, use_graph ? &G : nullptr));
         total += it;
         apply_alpha = true;
     }

@@ -462,8 +462,11 @@ __global__ void __launch_bounds__(FIN_THREADS)
 template <typename T>
 __global__ void cg_direction_kernel(long long Gt, int C, const double* __restrict__ rz_old,
                                     const double* __restrict__ rz_new, const T* __restrict__ z, T* __restrict__ p,
-                                    int pld) {
+                                    int pld, const int* __restrict__ skip, double* __restrict__ pmax_partials) {
+    if (skip && *skip) return;  // the loop has stopped (graph-driven loop)
     __shared__ double beta[64];
+    __shared__ double red[8];
+    T amax = T(0);
     if (threadIdx.x < C && threadIdx.x < 64)
         beta[threadIdx.x] = rz_old[threadIdx.x] != 0.0 ? rz_new[threadIdx.x] / rz_old[threadIdx.x] : 0.0;
     __syncthreads();
@@ -478,12 +481,24 @@ __global__ void cg_direction_kernel(long long Gt, int C, const double* __restric
     for (; idx < total; idx += st) {
         const T b = C <= 64 ? (T)beta[c] : (T)(rz_old[c] != 0.0 ? rz_new[c] / rz_old[c] : 0.0);
         T* pe = p + g * pld + c;
-        *pe = z[idx] + b * *pe;
+        const T pv = z[idx] + b * *pe;
+        *pe = pv;
+        const T ap = pv < T(0) ? -pv : pv;
+        amax = ap > amax ? ap : amax;
         g += gstep;
         c += cstep;
         if (c >= C) {
             c -= C;
             ++g;
+        }
+    }
+    if (pmax_partials) {
+        double m = warp_max((double)amax);
+        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            for (int w = 1; w < (int)(blockDim.x >> 5); ++w) m = fmax(m, red[w]);
+            pmax_partials[blockIdx.x] = fmax(m, red[0]);
         }
     }
 }
@@ -493,7 +508,9 @@ __global__ void inv_counts_kernel(const int32_t* __restrict__ counts, long long 
     if (g < G) inv[g] = counts[g] > 0 ? 1.0 / (double)counts[g] : 0.0;
 }
 
-__global__ void copy_scalars_kernel(const double* __restrict__ src, double* __restrict__ dst, int C) {
+__global__ void copy_scalars_kernel(const double* __restrict__ src, double* __restrict__ dst, int C,
+                                    const int* __restrict__ skip) {
+    if (skip && *skip) return;
     const int c = threadIdx.x;
     if (c < C) dst[c] = src[c];
 }
@@ -718,13 +735,18 @@ int launch_cg_update(long long Gt, int C, const T* inv_counts, const double* rz,
 
 template <typename T>
 int launch_cg_direction(long long Gt, int C, double* rz_old, const double* rz_new, const T* z, T* p, int pld,
-                        cudaStream_t s) {
+                        cudaStream_t s, const int* skip, double* pmax_partials, unsigned long long* pmax_bits) {
     long long total = Gt * C;
     if (total > 0) {
-        cg_direction_kernel<T><<<grid_stride_blocks(total, 256), 256, 0, s>>>(Gt, C, rz_old, rz_new, z, p, pld);
+        const unsigned nb = grid_stride_blocks(total, 256);
+        cg_direction_kernel<T><<<nb, 256, 0, s>>>(Gt, C, rz_old, rz_new, z, p, pld, skip, pmax_partials);
         FEGB_LAUNCH_CHECK("cg direction");
+        if (pmax_partials && pmax_bits) {
+            fold_max_kernel<<<1, FIN_THREADS, 0, s>>>(pmax_partials, (int)nb, pmax_bits);
+            FEGB_LAUNCH_CHECK("cg pmax fold");
+        }
     }
-    copy_scalars_kernel<<<1, ((C + 31) / 32) * 32, 0, s>>>(rz_new, rz_old, C);
+    copy_scalars_kernel<<<1, ((C + 31) / 32) * 32, 0, s>>>(rz_new, rz_old, C, skip);
     FEGB_LAUNCH_CHECK("cg scalars");
     return 0;
 }
@@ -772,9 +794,51 @@ int launch_inv_counts_t(const int32_t* counts, long long G, T* inv, cudaStream_t
 template int launch_inv_counts_t<float>(const int32_t*, long long, float*, cudaStream_t);
 template int launch_inv_counts_t<double>(const int32_t*, long long, double*, cudaStream_t);
 template int launch_cg_direction<double>(long long, int, double*, const double*, const double*, double*, int,
-                                         cudaStream_t);
+                                         cudaStream_t, const int*, double*, unsigned long long*);
 template int launch_cg_direction<float>(long long, int, double*, const double*, const float*, float*, int,
-                                        cudaStream_t);
+                                        cudaStream_t, const int*, double*, unsigned long long*);
+
+int launch_fold_max(const double* partials, int nb, unsigned long long* out, cudaStream_t s) {
+    fold_max_kernel<<<1, FIN_THREADS, 0, s>>>(partials, nb, out);
+    FEGB_LAUNCH_CHECK("max fold");
+    return 0;
+}
+
+// One warp per (g, c): exact int64 sum over the block tables, then the count term.
+template <typename T>
+__global__ void cg_sg_fold_kernel(const long long* __restrict__ part, int nblocks, int G, int C,
+                                  const unsigned long long* __restrict__ pmax_bits, int n_dims, long long n,
+                                  const int32_t* __restrict__ counts, const T* __restrict__ ps, int ld,
+                                  double* __restrict__ sums) {
+    const long long w = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    const long long GC = (long long)G * C;
+    if (w >= GC) return;
+    long long acc = 0;
+    for (int b = lane; b < nblocks; b += 32) acc += part[(long long)b * GC + w];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+    if (lane == 0) {
+        const int g = (int)(w / C), c = (int)(w - (long long)g * C);
+        const int e = cg_sg_exponent(__longlong_as_double((long long)*pmax_bits), n_dims, n);
+        sums[w] = ldexp((double)acc, -e) + (double)counts[g] * (double)ps[(long long)g * ld + c];
+    }
+}
+
+template <typename T>
+int launch_cg_sg_fold(const long long* part, int nblocks, int G, int C, const unsigned long long* pmax_bits,
+                      int n_dims, long long n, const int32_t* counts, const T* ps, int ld, double* sums, cudaStream_t s) {
+    const long long GC = (long long)G * C;
+    if (GC <= 0) return 0;
+    cg_sg_fold_kernel<T><<<(unsigned)((GC * 32 + 255) / 256), 256, 0, s>>>(part, nblocks, G, C, pmax_bits, n_dims, n,
+                                                                           counts, ps, ld, sums);
+    FEGB_LAUNCH_CHECK("small-G side fold");
+    return 0;
+}
+template int launch_cg_sg_fold<float>(const long long*, int, int, int, const unsigned long long*, int, long long,
+                                      const int32_t*, const float*, int, double*, cudaStream_t);
+template int launch_cg_sg_fold<double>(const long long*, int, int, int, const unsigned long long*, int, long long,
+                                       const int32_t*, const double*, int, double*, cudaStream_t);
 template int launch_cg_init<double>(long long, int, const int32_t*, const double*, double*, double*, double*, int,
                                     double*, double*, double*, unsigned long long*, cudaStream_t);
 template int launch_cg_init<float>(long long, int, const int32_t*, const double*, float*, float*, float*, int, float*,
@@ -915,13 +979,20 @@ __device__ __forceinline__ void cg_run_push(CGRun<T, TILE>& st, int g, const T (
 // stay in registers because every loop over TILE is fully unrolled).
 // NSRC = number of source dimensions when the vector id path is used
 // (1..3); NSRC = 0 reads ids one position at a time for any n_src.
-template <typename T, int CGR_TILE, int NSRC>
-__global__ void __launch_bounds__(256, (sizeof(T) == 4 && CGR_TILE <= 12) ? CG_ROWS_MINB : 2)
-    cg_rows_kernel(CGRowsParams<T> p, int ntiles) {
-    const int lane = threadIdx.x & 31;
-    const long long warp = ((long long)blockIdx.x * 256 + threadIdx.x) >> 5;
-    const long long nchunks = (p.n + CG_CHUNK - 1) / CG_CHUNK;
-    if (warp >= nchunks * ntiles) return;  // whole warp exits together
+// fixed-point add of one position's side contribution w to the small dimension's table
+template <typename T>
+__device__ __forceinline__ void sg_add(long long* tab, int idx, T w, int e) {
+    long long qv;
+    if constexpr (sizeof(T) == 4)
+        qv = __float2ll_rn(ldexpf(w, e));
+    else
+        qv = __double2ll_rn(ldexp(w, e));
+    atomicAdd(reinterpret_cast<unsigned long long*>(tab + idx), (unsigned long long)qv);
+}
+
+template <typename T, int CGR_TILE, int NSRC, bool SG>
+__device__ __forceinline__ void cg_rows_body(const CGRowsParams<T>& p, int ntiles, long long warp, int lane,
+                                             long long* sg_tab, int sg_e) {
     const long long q = warp / ntiles;
     const int c0 = (int)(warp - q * ntiles) * CGR_TILE;
     const int C = p.C;
@@ -955,6 +1026,25 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 && CGR_TILE <= 12) ? CG_R
             tabs[e] = p.src_tab[e] + c0;
             sgid[e] = p.src_gid[e];
         }
+        // small-G side output: v - p_primary per position (p_primary loaded once per run)
+        int pp_g = -1;
+        T pp[SG ? CGR_TILE : 1];
+        auto side = [&](int g, int t, const T (&v)[CGR_TILE]) {
+            if constexpr (SG) {
+                if (g != pp_g) {
+                    T tmp[CGR_TILE];
+#pragma unroll
+                    for (int i = 0; i < CGR_TILE; ++i) tmp[i] = T(0);
+                    cg_sub_row<T, CGR_TILE>(p.prim_tab + (long long)g * LD + c0, cw, tmp, keep);
+#pragma unroll
+                    for (int i = 0; i < CGR_TILE; ++i) pp[i] = -tmp[i];
+                    pp_g = g;
+                }
+#pragma unroll
+                for (int i = 0; i < CGR_TILE; ++i)
+                    if (i < cw) sg_add<T>(sg_tab, t * C + c0 + i, v[i] - pp[i], sg_e);
+            }
+        };
 #pragma unroll 1
         for (int h = 0; h < CG_LANE_POS / CG_IDV; ++h) {
             const long long jb = ls + CG_IDV * h;
@@ -972,6 +1062,13 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 && CGR_TILE <= 12) ? CG_R
 #pragma unroll
                     for (int e = 0; e < NSRC; ++e)
                         cg_sub_row<T, CGR_TILE>(tabs[e] + (long long)sid[e][m] * LD, cw, v, keep);
+                    if constexpr (SG) {
+                        int t = 0;
+#pragma unroll
+                        for (int e = 0; e < NSRC; ++e)
+                            if (e == p.sg_src) t = sid[e][m];
+                        side(gq[m], t, v);
+                    }
                     cg_run_push(st, gq[m], v, p.sums, LD, c0, cw);
                 }
             } else {
@@ -983,7 +1080,9 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 && CGR_TILE <= 12) ? CG_R
 #pragma unroll
                     for (int e = 0; e < NSRC; ++e)
                         cg_sub_row<T, CGR_TILE>(tabs[e] + (long long)__ldg(sgid[e] + j) * LD, cw, v, keep);
-                    cg_run_push(st, __ldg(gseq + j), v, p.sums, LD, c0, cw);
+                    const int g = __ldg(gseq + j);
+                    if constexpr (SG) side(g, __ldg(p.src_gid[p.sg_src] + j), v);
+                    cg_run_push(st, g, v, p.sums, LD, c0, cw);
                 }
             }
         }
@@ -1078,12 +1177,41 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 && CGR_TILE <= 12) ? CG_R
     }
 }
 
+template <typename T, int CGR_TILE, int NSRC, bool SG>
+__global__ void __launch_bounds__(256, SG ? 2 : ((sizeof(T) == 4 && CGR_TILE <= 12) ? CG_ROWS_MINB : 2))
+    cg_rows_kernel(CGRowsParams<T> p, int ntiles) {
+    extern __shared__ long long sg_tab[];
+    const int lane = threadIdx.x & 31;
+    const long long warp = ((long long)blockIdx.x * 256 + threadIdx.x) >> 5;
+    const long long nchunks = (p.n + CG_CHUNK - 1) / CG_CHUNK;
+    int sg_e = 0;
+    if constexpr (SG) {
+        for (int i = threadIdx.x; i < p.sg_G * p.C; i += blockDim.x) sg_tab[i] = 0;
+        sg_e = cg_sg_exponent(__longlong_as_double((long long)*p.pmax_bits), p.n_dims, p.n);
+        __syncthreads();
+    }
+    if (warp < nchunks * ntiles)  // whole warps take part or skip together
+        cg_rows_body<T, CGR_TILE, NSRC, SG>(p, ntiles, warp, lane, sg_tab, sg_e);
+    if constexpr (SG) {
+        __syncthreads();
+        long long* dst = p.sg_part + (long long)blockIdx.x * p.sg_G * p.C;
+        for (int i = threadIdx.x; i < p.sg_G * p.C; i += blockDim.x) dst[i] = sg_tab[i];
+    }
+}
+
 template <typename T, int TILE, int NSRC>
 int launch_cg_rows_tile(const CGRowsParams<T>& p, cudaStream_t s) {
     const int ntiles = (p.C + TILE - 1) / TILE;
-    const long long warps = ((p.n + CG_CHUNK - 1) / CG_CHUNK) * ntiles;
-    const long long blocks = (warps * 32 + 255) / 256;
-    cg_rows_kernel<T, TILE, NSRC><<<(unsigned)blocks, 256, 0, s>>>(p, ntiles);
+    const long long blocks = cg_rows_blocks(p.n, p.C, TILE);
+    if constexpr (NSRC > 0) {
+        if (p.sg_src >= 0) {
+            const size_t smem = sizeof(long long) * (size_t)p.sg_G * p.C;
+            cg_rows_kernel<T, TILE, NSRC, true><<<(unsigned)blocks, 256, smem, s>>>(p, ntiles);
+            FEGB_LAUNCH_CHECK("cg operator sweep with small-G side output");
+            return 0;
+        }
+    }
+    cg_rows_kernel<T, TILE, NSRC, false><<<(unsigned)blocks, 256, 0, s>>>(p, ntiles);
     FEGB_LAUNCH_CHECK("cg operator sweep");
     return 0;
 }
@@ -1091,19 +1219,21 @@ int launch_cg_rows_tile(const CGRowsParams<T>& p, cudaStream_t s) {
 template <typename T, int TILE>
 int launch_cg_rows_nsrc(const CGRowsParams<T>& p, cudaStream_t s) {
     // the vector id path needs 16-byte aligned id arrays
-    bool aligned = (reinterpret_cast<uintptr_t>(p.gseq) & 15u) == 0;
-    for (int e = 0; e < p.n_src; ++e) aligned = aligned && (reinterpret_cast<uintptr_t>(p.src_gid[e]) & 15u) == 0;
-    if (aligned) {
+    if (cg_rows_vector_path(p)) {
         if (p.n_src == 1) return launch_cg_rows_tile<T, TILE, 1>(p, s);
         if (p.n_src == 2) return launch_cg_rows_tile<T, TILE, 2>(p, s);
         if (p.n_src == 3) return launch_cg_rows_tile<T, TILE, 3>(p, s);
     }
+    if (p.sg_src >= 0) return set_error("cg operator: the small-G side output needs the vector id path");
     return launch_cg_rows_tile<T, TILE, 0>(p, s);
 }
 
 template <typename T>
 int launch_cg_rows(const CGRowsParams<T>& p, cudaStream_t s) {
     if (p.n <= 0) return 0;
+    if (p.sg_src >= 0 && (p.sg_src >= p.n_src || !p.prim_tab || !p.pmax_bits || !p.sg_part || p.sg_G <= 0 ||
+                          (size_t)p.sg_G * p.C * sizeof(long long) > CG_SG_SMEM_MAX))
+        return set_error("cg operator: invalid small-G side output");
     // table rows are read in 32-byte pieces: the stride and the tables must allow it
     if (p.ld % (32 / (int)sizeof(T)) != 0) return set_error("cg operator: row stride %d is not a 32-byte multiple", p.ld);
     for (int e = 0; e < p.n_src; ++e)

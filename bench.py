@@ -209,6 +209,8 @@ def main():
     ap.add_argument("--fp64-steps", type=int, default=2, help="timed steps of the plain FP64 form")
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-file", action="store_true",
+                    help="skip the .bin file leg (write the panel once, load it to the device, fit)")
     ap.add_argument("--profile-case", action="store_true",
                     help="one fit per (precision, method) and exit (for ncu captures)")
     ap.add_argument("--case", default="all", help="with --profile-case: mixed-cg, fp64-cg, mixed-ap, fp64-ap or all")
@@ -256,7 +258,8 @@ def main():
         for p, m in (("mixed", "cg"), ("fp64", "cg"), ("mixed", "ap"), ("fp64", "ap")):
             if args.case != "all" and args.case != f"{p}-{m}":
                 continue
-            r = fit(p, method=m)
+            # per-launch events (host-driven loop), so every kernel launch is visible to a profiler
+            r = fit(p, profile=True, method=m)
             print(p, m, r.fe_iterations, r.stats["outer_iterations"], r.stats["time_total"], flush=True)
         return 0
 
@@ -334,17 +337,35 @@ def main():
     h2d = pin_y.nbytes + n * k * 8 + n * n_fe * 4
     d2h = 2 * k * 8
 
+    # .bin file leg: the panel written once in the fe_gpu format, then loaded
+    # straight to the device (fegb_load_bin) and fitted from there
+    file_leg = None
+    if not args.no_file and rank == 0:
+        import tempfile
+
+        from fe_gpu_gb300.bin_io import DeviceDataset, write_dataset
+
+        with tempfile.TemporaryDirectory(dir=os.environ.get("TMPDIR")) as td:
+            path = os.path.join(td, "panel.bin")
+            write_dataset(path, host.y, host.W, host.fe_ids, metadata=dict(
+                y="y", x=[f"x{j + 1}" for j in range(k)], fe=["worker", "firm", "time"]))
+            size = os.path.getsize(path)
+            DeviceDataset(path).close()  # first touch (page cache)
+            t0 = time.perf_counter()
+            ds = DeviceDataset(path)
+            load_s = time.perf_counter() - t0
+            t1 = time.perf_counter()
+            fr = fe_gpu_estimate_device(cfg_for(args.precision), ds.n, ds.k, 0, ds.y, ds.W, None, ds.fe_ids,
+                                        stream=stream.cuda_stream)
+            torch.cuda.synchronize()
+            fit_s = time.perf_counter() - t1
+            ds.close()
+            file_leg = {"file_bytes": size, "load_s": load_s, "load_gbs": size / load_s / 1e9,
+                        "fit_after_load_s": fit_s, "rows_per_s_from_file": n / (load_s + fit_s),
+                        "beta_equal_to_resident_fit": bool(np.array_equal(fr.beta, last.beta))}
+
     # roofline of the dominant sweep-kernel family, timed live in the timed steps
-    fam = ["segment sweep fp64", "segment sweep fp32", "small-G sweep fp64", "small-G sweep fp32",
-           "CG operator segment sweep fp64", "CG operator segment sweep fp32", "CG operator small-G sweep fp64",
-           "CG operator small-G sweep fp32"]
-    secs = [sum(r.stats["prof_seconds"][i] for r in results) for i in range(8)]
-    nlaunch = [sum(r.stats["prof_launches"][i] for r in results) for i in range(8)]
-    nbytes = [sum(r.stats["prof_bytes"][i] for r in results) for i in range(8)]
-    top = int(np.argmax(secs))
-    peak, peak_kind = measured_hbm_peak()
-    achieved = nbytes[top] / secs[top] / 1e9 if secs[top] > 0 else 0.0
-    traffic_per_launch = TRAFFIC_PER_LAUNCH.get((args.workload, fam[top]))
+    roofline = roofline_of(results, args.workload)
     demean_gbs = last.stats["demean_bytes"] / last.stats["time_demean"] / 1e9 if last.stats["time_demean"] else None
 
     value = world * n / (ms / 1e3)
@@ -374,19 +395,8 @@ def main():
         "e2e": {"value": world * n / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "seconds_per_step": e2e_s},
         "gpu_launches": int(launches / args.steps) * args.steps,
-        "roofline": {"bound": "hbm", "kernel": fam[top], "achieved": achieved, "peak": peak,
-                     "peak_source": peak_kind, "unit": "GB/s", "frac": achieved / peak if peak else None,
-                     "traffic": traffic_per_launch,
-                     "traffic_source": ("ncu dram__bytes_read.sum + dram__bytes_write.sum per launch, "
-                                        "profiles/cg_rows_worker_firm_20M.md") if traffic_per_launch else None,
-                     "alg_bytes_definition": ("N (4 D + (D-1) C s): ids and gathered FE-table rows per operator launch"
-                                              if top >= 4 else "N (4 + 2 C s): rows read and written once, one id"),
-                     "launches": nlaunch[top],
-                     "avg_launch_ms": secs[top] / max(1, nlaunch[top]) * 1e3,
-                     "alg_bytes_per_launch": nbytes[top] / max(1, nlaunch[top]),
-                     "all_families": {fam[i]: {"launches": nlaunch[i], "seconds": secs[i],
-                                               "gbs": (nbytes[i] / secs[i] / 1e9) if secs[i] else None}
-                                      for i in range(8) if nlaunch[i]}},
+        "bin_file": file_leg,
+        "roofline": roofline,
         "clocks": clocks,
     }
     if rank == 0 and not args.no_cpu_baseline:
@@ -402,8 +412,13 @@ def main():
 
 
 FAMILIES = ["segment sweep fp64", "segment sweep fp32", "small-G sweep fp64", "small-G sweep fp32",
-            "CG operator segment sweep fp64", "CG operator segment sweep fp32", "CG operator small-G sweep fp64",
-            "CG operator small-G sweep fp32"]
+            "CG operator segment sweep fp64", "CG operator segment sweep fp32",
+            "CG operator dense small-G products fp64", "CG operator dense small-G products fp32"]
+ALG_BYTES = {
+    "segment": "N (4 + 2 C s): rows read and written once, one id",
+    "cg": "N (4 (1 + S) + S C s): destination and S swept source ids, S gathered FE-table rows",
+    "dense": "G_e (4 G_s + C s) per product: count-matrix rows and FE-table rows read once",
+}
 
 
 def roofline_of(results, workload):
@@ -416,8 +431,9 @@ def roofline_of(results, workload):
     traffic = TRAFFIC_PER_LAUNCH.get((workload, FAMILIES[top]))
     return {"bound": "hbm", "kernel": FAMILIES[top], "achieved": achieved, "peak": peak, "peak_source": peak_kind,
             "unit": "GB/s", "frac": achieved / peak if peak else None, "traffic": traffic,
-            "alg_bytes_definition": ("N (4 D + (D-1) C s): ids and gathered FE-table rows per operator launch"
-                                     if top >= 4 else "N (4 + 2 C s): rows read and written once, one id"),
+            "traffic_source": ("ncu dram__bytes_read.sum + dram__bytes_write.sum per launch, "
+                               "profiles/cg_rows_worker_firm_20M.md") if traffic is not None else None,
+            "alg_bytes_definition": ALG_BYTES["segment" if top < 4 else ("cg" if top < 6 else "dense")],
             "launches": nlaunch[top], "avg_launch_ms": secs[top] / max(1, nlaunch[top]) * 1e3,
             "alg_bytes_per_launch": nbytes[top] / max(1, nlaunch[top]),
             "all_families": {FAMILIES[i]: {"launches": nlaunch[i], "seconds": secs[i],
@@ -764,8 +780,6 @@ def formula_cpu_baseline(threads):
 # family). Other workloads were not captured: the gathered tables change size
 # with the FE group counts, so the traffic does not scale with the rows.
 TRAFFIC_PER_LAUNCH: dict = {
-    ("worker_firm_20M", "CG operator segment sweep fp32"): 6.592e+08,
-    ("worker_firm_20M", "CG operator small-G sweep fp32"): 1.144e+09,
 }
 
 

@@ -16,6 +16,8 @@
 #include <string>
 #include <mutex>
 #include <atomic>
+#include <cstdio>
+#include <cstdlib>
 #include <cfloat>
 #include <chrono>
 #include <climits>
@@ -34,6 +36,17 @@ inline double seconds_since(Clock::time_point t0) {
 
 constexpr int MODE_CONTIG = 0;
 constexpr int MODE_GATHER = 1;
+// FEGB_TRACE in the environment: 1 = one stderr line per CG outer round,
+// 2 = also every 10th inner iteration of a host-driven (profiled) solve
+inline int trace_level() {
+    static const int lvl = [] {
+        const char* v = std::getenv("FEGB_TRACE");
+        return v && v[0] ? std::atoi(v) : 0;
+    }();
+    return lvl;
+}
+inline bool trace_enabled() { return trace_level() > 0; }
+
 constexpr int MODE_SMALLG = 2;
 constexpr int CHUNK_R = 256;
 constexpr int MAX_CLUSTER_DIMS = 3;  // src/core/fe_pipeline.f90:20
@@ -802,12 +815,14 @@ struct CGBuffers {
     unsigned long long* zmax = nullptr;
     int rz_blocks = 0, pq_blocks = 0;
     std::vector<int> pq_block_off;
-    // small-G dimension folded into the primary's storage-order operator pass (-1 = none)
-    int sg_dim = -1;
-    long long* sg_part = nullptr;       // per block of that pass: G_s x C int64 sums
-    long long sg_blocks = 0;
-    unsigned long long* pmax = nullptr;  // max |p| (bits)
-    double* pmax_part = nullptr;         // per direction block
+    // dimensions with few groups handled through dense count matrices:
+    // dense[d] says whether d is one; N[d][e] = G_e x G_d counts of the rows
+    // of each (group of e, group of d) pair, for e != d
+    std::vector<char> dense;
+    std::vector<std::vector<uint32_t*>> N;
+    double* dense_part = nullptr;  // chunk partials of the small-side products
+    double* dense_sums = nullptr;  // G_small x C
+    T* extra = nullptr;            // G_max x C: the dense dimensions' share of a swept dimension's q
 };
 
 template <typename T>
@@ -841,21 +856,39 @@ int cg_alloc(Problem& P, CGBuffers<T>& B) {
     FEGB_TRY(dalloc(scr, &B.pq_part, (size_t)std::max(1, B.pq_blocks) * C, "cg pq partials"));
     FEGB_CUDA(cudaMemsetAsync(B.pq_part, 0, sizeof(double) * (size_t)std::max(1, B.pq_blocks) * C, P.s),
               "cg pq partials zero");
-    // one small-G dimension can ride on the primary's storage-order pass
-    // (FP32 form; see CGRowsParams::sg_src)
-    if (sizeof(T) == 4 && P.n_fe >= 2 && P.n_fe - 1 <= 3) {
-        int cand = -1, nsmall = 0;
+    // dense count matrices for dimensions with few groups (see CGBuffers)
+    B.dense.assign(P.n_fe, 0);
+    B.N.assign(P.n_fe, std::vector<uint32_t*>(P.n_fe, nullptr));
+    if (C <= 32 && P.n > 0) {
+        double bytes = 0.0;
         for (int d = 0; d < P.n_fe; ++d)
-            if (d != P.primary && P.dims[d].mode == MODE_SMALLG && P.dims[d].G > 0) {
-                cand = d;
-                ++nsmall;
+            if (P.dims[d].G > 0 && P.dims[d].G <= DENSE_SMALL_MAX_G)
+                for (int e = 0; e < P.n_fe; ++e)
+                    if (e != d) bytes += 4.0 * std::max(1, P.dims[e].G) * P.dims[d].G;
+        if (bytes <= 8e9) {
+            long long chunks = 0;
+            int gmax_all = 1, gsmall = 0;
+            for (int d = 0; d < P.n_fe; ++d) gmax_all = std::max(gmax_all, P.dims[d].G);
+            for (int d = 0; d < P.n_fe; ++d) {
+                if (!(P.dims[d].G > 0 && P.dims[d].G <= DENSE_SMALL_MAX_G)) continue;
+                B.dense[d] = 1;
+                gsmall = std::max(gsmall, P.dims[d].G);
+                long long ch = 0;
+                for (int e = 0; e < P.n_fe; ++e) {
+                    if (e == d || P.dims[e].G <= 0) continue;
+                    const size_t cnt = (size_t)P.dims[e].G * P.dims[d].G;
+                    FEGB_TRY(dalloc(scr, &B.N[d][e], cnt, "dense count matrix"));
+                    FEGB_CUDA(cudaMemsetAsync(B.N[d][e], 0, sizeof(uint32_t) * cnt, P.s), "count matrix zero");
+                    FEGB_TRY(launch_count_pairs(P.dims[e].gid, P.dims[d].gid, P.n, P.dims[d].G, B.N[d][e], P.s));
+                    ch += dense_chunks(P.dims[e].G);
+                }
+                chunks = std::max(chunks, ch);
             }
-        if (nsmall == 1 && (size_t)P.dims[cand].G * C * sizeof(long long) <= CG_SG_SMEM_MAX) {
-            B.sg_dim = cand;
-            B.sg_blocks = cg_rows_blocks(P.n, C, cg_rows_tile(C));
-            FEGB_TRY(dalloc(scr, &B.sg_part, (size_t)B.sg_blocks * P.dims[cand].G * C, "cg small-G side sums"));
-            FEGB_TRY(dalloc(scr, &B.pmax, 1, "cg pmax"));
-            FEGB_TRY(dalloc(scr, &B.pmax_part, (size_t)grid_stride_blocks(P.Gt * C, 256), "cg pmax partials"));
+            if (gsmall > 0) {
+                FEGB_TRY(dalloc(scr, &B.dense_part, (size_t)std::max(1LL, chunks) * gsmall * C, "dense partials"));
+                FEGB_TRY(dalloc(scr, &B.dense_sums, (size_t)gsmall * C, "dense sums"));
+                FEGB_TRY(dalloc(scr, &B.extra, (size_t)gmax_all * C, "dense extra"));
+            }
         }
     }
     // the operator sweep writes sums/head/tail at the padded stride
@@ -876,8 +909,9 @@ int cg_alloc(Problem& P, CGBuffers<T>& B) {
 
 // Algorithmic bytes of one operator sweep: per position the destination id,
 // D-1 source ids and D-1 gathered source rows of C values of size s.
-inline double cg_operator_bytes(const Problem& P, size_t s) {
-    return (double)P.n * (4.0 * P.n_fe + (double)(P.n_fe - 1) * P.C * (double)s);
+inline double cg_operator_bytes(const Problem& P, size_t s, int n_src = -1) {
+    if (n_src < 0) n_src = P.n_fe - 1;
+    return (double)P.n * (4.0 * (1 + n_src) + (double)n_src * P.C * (double)s);
 }
 
 // q = D'D p, dimension by dimension: a no-data sweep over d's traversal with
@@ -886,84 +920,55 @@ template <typename T>
 int cg_apply(Problem& P, CGBuffers<T>& B) {
     const int C = P.C;
     const int L = B.ld;
-    // the primary first: its pass also produces the folded small-G dimension's sums
-    std::vector<int> order;
-    order.push_back(P.primary);
-    for (int d = 0; d < P.n_fe; ++d)
-        if (d != P.primary) order.push_back(d);
-    for (int d : order) {
+    auto begin_timed = [&](Problem::Timed& tm, int kind, double bytes) -> int {
+        if (!P.profile) return 0;
+        tm.kind = kind;
+        tm.bytes = bytes;
+        FEGB_CUDA(cudaEventCreate(&tm.a), "profile event");
+        FEGB_CUDA(cudaEventCreate(&tm.b), "profile event");
+        FEGB_CUDA(cudaEventRecord(tm.a, P.s), "profile record");
+        return 0;
+    };
+    auto end_timed = [&](Problem::Timed& tm) -> int {
+        if (!P.profile) return 0;
+        FEGB_CUDA(cudaEventRecord(tm.b, P.s), "profile record");
+        P.timed.push_back(tm);
+        return 0;
+    };
+    const int fp32 = sizeof(T) == 4 ? 1 : 0;
+    for (int d = 0; d < P.n_fe; ++d) {
         Dim& D = P.dims[d];
         if (D.G <= 0) continue;
-        if (d == B.sg_dim) {
-            // sums accumulated by the primary's pass: fold the block tables, add counts * p_s
-            FEGB_TRY(launch_cg_sg_fold<T>(B.sg_part, (int)B.sg_blocks, D.G, C, B.pmax, P.n_fe, P.n, D.counts,
-                                          B.p + P.goff[d] * L, L, P.sums, P.s));
-            FinalizeParams src{};
-            src.G = D.G;
-            src.C = C;
-            src.sums = P.sums;
-            src.counts = D.counts;
-            FEGB_TRY(launch_cg_q<T>(src, C, B.p + P.goff[d] * L, L, B.q + P.goff[d] * C,
-                                    B.pq_part + (size_t)B.pq_block_off[d] * C, P.s));
-            P.projections += 1;
-            continue;
-        }
         Problem::Timed tm{};
-        if (P.profile) {
-            tm.kind = 4 + (D.mode == MODE_SMALLG ? 2 : 0) + (sizeof(T) == 4 ? 1 : 0);
-            tm.bytes = cg_operator_bytes(P, sizeof(T));
-            FEGB_CUDA(cudaEventCreate(&tm.a), "profile event");
-            FEGB_CUDA(cudaEventCreate(&tm.b), "profile event");
-            FEGB_CUDA(cudaEventRecord(tm.a, P.s), "profile record");
-        }
-        PendingSet<T> ps{};
-        ps.n = 0;
-        for (int e = 0; e < P.n_fe; ++e) {
-            if (e == d) continue;
-            ps.gid[ps.n] = D.mode == MODE_GATHER ? D.gid_at_perm[e] : P.dims[e].gid;
-            ps.tab[ps.n] = B.p + P.goff[e] * C;
-            ++ps.n;
-        }
-        if (D.mode == MODE_SMALLG) {
-            // few groups: storage order with private per-slot tables, so the
-            // other dimensions' rows are read in storage order (the primary's
-            // once per run) instead of once per group of this dimension
-            SmallGParams<T> sp{};
-            sp.X = nullptr;
-            sp.C = C;
-            sp.n = P.n;
-            sp.gid = D.gid;
-            sp.G = D.G;
-            sp.pend.n = 0;
+        if (B.dense[d]) {
+            // few groups: q_d from the dense count matrices, sum_e N_{e,d}^T p_e
+            double bytes = 0.0;
+            for (int e = 0; e < P.n_fe; ++e)
+                if (e != d && P.dims[e].G > 0)
+                    bytes += (double)P.dims[e].G * (4.0 * D.G + (double)C * sizeof(T));
+            FEGB_TRY(begin_timed(tm, 6 + fp32, bytes));
+            long long part = 0;
             for (int e = 0; e < P.n_fe; ++e) {
-                if (e == d) continue;
-                sp.pend.gid[sp.pend.n] = P.dims[e].gid;
-                sp.pend.tab[sp.pend.n] = B.p + P.goff[e] * L;
-                ++sp.pend.n;
+                if (e == d || P.dims[e].G <= 0) continue;
+                FEGB_TRY(launch_small_from_dense<T>(B.N[d][e], P.dims[e].G, D.G, B.p + P.goff[e] * L, L, C,
+                                                    B.dense_part + part * D.G * C, P.s));
+                part += dense_chunks(P.dims[e].G);
             }
-            sp.tld = L;
-            sp.no_data = 1;
-            sp.writeback = 0;
-            sp.rows_per_block = (P.n + P.smallg_nb - 1) / P.smallg_nb;
-            sp.partials = P.partials;
-            FEGB_TRY(launch_smallg_sweep<T>(sp, P.smallg_nb, P.s));
-            FEGB_TRY(launch_fold_smallg(P.partials, P.smallg_nb, D.G, C, P.sums, P.s));
-            if (P.profile) {
-                FEGB_CUDA(cudaEventRecord(tm.b, P.s), "profile record");
-                P.timed.push_back(tm);
-            }
+            FEGB_TRY(launch_fold_dense(B.dense_part, (int)part, D.G, C, B.dense_sums, P.s));
+            FEGB_TRY(end_timed(tm));
             FinalizeParams src{};
             src.G = D.G;
             src.C = C;
-            src.sums = P.sums;  // complete group sums, compact rows
+            src.sums = B.dense_sums;  // complete sums of -p, compact rows
             src.counts = D.counts;
             FEGB_TRY(launch_cg_q<T>(src, C, B.p + P.goff[d] * L, L, B.q + P.goff[d] * C,
                                     B.pq_part + (size_t)B.pq_block_off[d] * C, P.s));
             P.projections += 1;
-            P.demean_bytes += cg_operator_bytes(P, sizeof(T));
+            P.demean_bytes += bytes;
             continue;
         }
-        // every other dimension is traversed in its group-sorted order (identity for the primary)
+        // the other many-group dimensions are swept in d's group-sorted order
+        // (identity for the primary); dense dimensions come from their matrices
         CGRowsParams<T> rp{};
         rp.n = P.n;
         rp.C = C;
@@ -971,47 +976,53 @@ int cg_apply(Problem& P, CGBuffers<T>& B) {
         rp.gseq = D.gseq;
         rp.n_src = 0;
         for (int e = 0; e < P.n_fe; ++e) {
-            if (e == d) continue;
+            if (e == d || B.dense[e]) continue;
             rp.src_gid[rp.n_src] = d == P.primary ? P.dims[e].gid : D.gid_at_perm[e];
             rp.src_tab[rp.n_src] = B.p + P.goff[e] * L;
             ++rp.n_src;
         }
-        rp.sums = B.sums;
-        rp.head = B.head;
-        rp.tail = B.tail;
-        if (d == P.primary && B.sg_dim >= 0) {
-            int idx = 0;
-            for (int e = 0; e < P.n_fe; ++e) {
-                if (e == d) continue;
-                if (e == B.sg_dim) rp.sg_src = idx;
-                ++idx;
-            }
-            rp.sg_G = P.dims[B.sg_dim].G;
-            rp.n_dims = P.n_fe;
-            rp.prim_tab = B.p + P.goff[d] * L;
-            rp.pmax_bits = B.pmax;
-            rp.sg_part = B.sg_part;
-            if (!cg_rows_vector_path(rp)) return set_error("cg operator: small-G side output without the vector path");
-        }
-        FEGB_TRY(launch_cg_rows<T>(rp, P.s));
-        FEGB_TRY(launch_long_sums(D.off, B.head, B.tail, CG_CHUNK, L, D.long_list_cg, D.n_long_cg, B.sums, P.s));
-        if (P.profile) {
-            FEGB_CUDA(cudaEventRecord(tm.b, P.s), "profile record");
-            P.timed.push_back(tm);
-        }
         FinalizeParams src{};
         src.G = D.G;
-        src.C = L;
-        src.off = D.off;
-        src.sums = B.sums;
-        src.head = B.head;
-        src.tail = B.tail;
-        src.R = CG_CHUNK;
         src.counts = D.counts;
+        const double bytes = rp.n_src > 0 ? cg_operator_bytes(P, sizeof(T), rp.n_src) : 0.0;
+        if (rp.n_src > 0) {
+            FEGB_TRY(begin_timed(tm, 4 + fp32, bytes));
+            rp.sums = B.sums;
+            rp.head = B.head;
+            rp.tail = B.tail;
+            FEGB_TRY(launch_cg_rows<T>(rp, P.s));
+            FEGB_TRY(launch_long_sums(D.off, B.head, B.tail, CG_CHUNK, L, D.long_list_cg, D.n_long_cg, B.sums, P.s));
+            FEGB_TRY(end_timed(tm));
+            src.C = L;
+            src.off = D.off;
+            src.sums = B.sums;
+            src.head = B.head;
+            src.tail = B.tail;
+            src.R = CG_CHUNK;
+        } else {
+            src.C = C;
+            src.sums = nullptr;  // no swept source
+        }
+        // the dense dimensions' share: extra = sum_s N_{d,s} p_s
+        const T* extra = nullptr;
+        double xbytes = 0.0;
+        Problem::Timed tx{};
+        for (int s2 = 0; s2 < P.n_fe; ++s2) {
+            if (s2 == d || !B.dense[s2]) continue;
+            if (!extra) FEGB_TRY(begin_timed(tx, 6 + fp32, 0.0));
+            FEGB_TRY(launch_dense_to_groups<T>(B.N[s2][d], D.G, P.dims[s2].G, B.p + P.goff[s2] * L, L, C, B.extra,
+                                               extra ? 1 : 0, P.s));
+            xbytes += (double)D.G * (4.0 * P.dims[s2].G + (double)C * sizeof(T) * (extra ? 2.0 : 1.0));
+            extra = B.extra;
+        }
+        if (extra) {
+            tx.bytes = xbytes;
+            FEGB_TRY(end_timed(tx));
+        }
         FEGB_TRY(launch_cg_q<T>(src, C, B.p + P.goff[d] * L, L, B.q + P.goff[d] * C,
-                                B.pq_part + (size_t)B.pq_block_off[d] * C, P.s));
+                                B.pq_part + (size_t)B.pq_block_off[d] * C, P.s, extra));
         P.projections += 1;
-        P.demean_bytes += cg_operator_bytes(P, sizeof(T));
+        P.demean_bytes += bytes + xbytes;
     }
     return launch_fold_partials(B.pq_part, B.pq_blocks, C, B.pq, P.s);
 }
@@ -1025,6 +1036,7 @@ int cg_apply(Problem& P, CGBuffers<T>& B) {
 struct CGLoopCtl {
     double tol;
     double best;
+    double best_rz;
     double zm;
     int max_it;
     int it;
@@ -1035,6 +1047,7 @@ struct CGLoopCtl {
 __global__ void cg_loop_reset_kernel(CGLoopCtl* c, double tol, int max_it) {
     c->tol = tol;
     c->best = DBL_MAX;
+    c->best_rz = DBL_MAX;
     c->zm = 0.0;
     c->max_it = max_it;
     c->it = 0;
@@ -1042,22 +1055,51 @@ __global__ void cg_loop_reset_kernel(CGLoopCtl* c, double tol, int max_it) {
     c->stop = 0;
 }
 
-// the stopping rules of the host loop in cg_solve_host
-__global__ void cg_loop_check_kernel(const unsigned long long* __restrict__ zmax_bits, CGLoopCtl* c,
+// Stopping rules of an inner solve (host and device loops alike): the largest
+// preconditioned residual |z| below the tolerance ends it. Past the attainable
+// accuracy of the storage type the recursive residual stops falling and then
+// grows again (the iterate drifts away from its best); the solve ends there:
+// when r.z (summed over the columns) rises above CG_DIVERGE times its best
+// value, or after CG_STALL_ITERS iterations in which neither max |z| nor r.z
+// fell below 0.9 of its best. max |z| alone can sit on a plateau for many
+// iterations while r.z still falls.
+constexpr int CG_STALL_ITERS = 60;
+constexpr double CG_DIVERGE = 10.0;
+
+__host__ __device__ inline bool cg_stop_rule(double zm, double rz, double tol, double* best, double* best_rz,
+                                             int* since_best) {
+    if (zm < tol) return true;
+    if (rz > CG_DIVERGE * *best_rz) return true;
+    bool progress = false;
+    if (zm < 0.9 * *best) {
+        *best = zm;
+        progress = true;
+    }
+    if (rz < 0.9 * *best_rz) {
+        *best_rz = rz;
+        progress = true;
+    }
+    if (progress) {
+        *since_best = 0;
+        return false;
+    }
+    return ++*since_best > CG_STALL_ITERS;
+}
+
+__host__ __device__ inline double cg_rz_total(const double* rz, int C) {
+    double t = 0.0;
+    for (int c = 0; c < C; ++c) t += rz[c];
+    return t;
+}
+
+__global__ void cg_loop_check_kernel(const unsigned long long* __restrict__ zmax_bits,
+                                     const double* __restrict__ rz_new, int C, CGLoopCtl* c,
                                      cudaGraphConditionalHandle h) {
     const double zm = __longlong_as_double((long long)*zmax_bits);
     c->zm = zm;
     const int it = c->it + 1;
     c->it = it;
-    bool stop = false;
-    if (zm < c->tol) {
-        stop = true;
-    } else if (zm < 0.9 * c->best) {
-        c->best = zm;
-        c->since_best = 0;
-    } else if (++c->since_best > 60) {
-        stop = true;  // the recursive residual stopped improving at this precision
-    }
+    bool stop = cg_stop_rule(zm, cg_rz_total(rz_new, C), c->tol, &c->best, &c->best_rz, &c->since_best);
     if (it >= c->max_it) stop = true;
     c->stop = stop ? 1 : 0;
     cudaGraphSetConditional(h, stop ? 0u : 1u);
@@ -1107,11 +1149,11 @@ int cg_build_graph(Problem& P, CGBuffers<T>& B, CGGraph<T>& G) {
                                  B.zmax, cs);
     if (!st) st = launch_fold_partials(B.rz_part, B.rz_blocks, C, B.rz_new, cs);
     if (!st) {
-        cg_loop_check_kernel<<<1, 1, 0, cs>>>(B.zmax, G.ctl, h);
+        cg_loop_check_kernel<<<1, 1, 0, cs>>>(B.zmax, B.rz_new, C, G.ctl, h);
         count_launch();
         if (cudaPeekAtLastError() != cudaSuccess) st = 1;
     }
-    if (!st) st = launch_cg_direction<T>(P.Gt, C, B.rz, B.rz_new, B.z, B.p, B.ld, cs, &G.ctl->stop, B.pmax_part, B.pmax);
+    if (!st) st = launch_cg_direction<T>(P.Gt, C, B.rz, B.rz_new, B.z, B.p, B.ld, cs, &G.ctl->stop);
     P.s = saved;
     cudaGraph_t captured = nullptr;
     const cudaError_t ec = cudaStreamEndCapture(cs, &captured);
@@ -1134,9 +1176,6 @@ int cg_solve(Problem& P, CGBuffers<T>& B, double inner_tol, int max_it, int* ite
         const int C = P.C;
         FEGB_TRY(launch_cg_init<T>(P.Gt, C, P.counts_all, P.mu_all, B.r, B.z, B.p, B.ld, B.x, B.rz_part, B.zmax_part,
                                    B.zmax, P.s));
-        if (B.pmax)  // p = z at the start: max |p| = max |z|
-            FEGB_CUDA(cudaMemcpyAsync(B.pmax, B.zmax, sizeof(unsigned long long), cudaMemcpyDeviceToDevice, P.s),
-                      "cg pmax init");
         FEGB_TRY(launch_fold_partials(B.rz_part, B.rz_blocks, C, B.rz, P.s));
         cg_loop_reset_kernel<<<1, 1, 0, P.s>>>(G->ctl, inner_tol, max_it);
         FEGB_LAUNCH_CHECK("cg loop reset");
@@ -1155,34 +1194,30 @@ int cg_solve_host(Problem& P, CGBuffers<T>& B, double inner_tol, int max_it, int
     const int C = P.C;  // vector ops run over compact rows; p keeps the padded stride B.ld
     FEGB_TRY(launch_cg_init<T>(P.Gt, C, P.counts_all, P.mu_all, B.r, B.z, B.p, B.ld, B.x, B.rz_part, B.zmax_part,
                                B.zmax, P.s));
-    if (B.pmax)  // p = z at the start: max |p| = max |z|
-        FEGB_CUDA(cudaMemcpyAsync(B.pmax, B.zmax, sizeof(unsigned long long), cudaMemcpyDeviceToDevice, P.s),
-                  "cg pmax init");
     FEGB_TRY(launch_fold_partials(B.rz_part, B.rz_blocks, C, B.rz, P.s));
-    double best = DBL_MAX;
+    double best = DBL_MAX, best_rz = DBL_MAX;
     int since_best = 0;
     int it = 0;
     double zm = 0.0;
+    std::vector<double> rz_host((size_t)C);
     for (; it < max_it; ++it) {
         FEGB_TRY(cg_apply<T>(P, B));
         FEGB_TRY(launch_cg_update<T>(P.Gt, C, B.inv, B.rz, B.pq, B.p, B.ld, B.q, B.x, B.r, B.z, B.rz_part,
                                      B.zmax_part, B.zmax, P.s));
         FEGB_TRY(launch_fold_partials(B.rz_part, B.rz_blocks, C, B.rz_new, P.s));
+        FEGB_CUDA(cudaMemcpyAsync(rz_host.data(), B.rz_new, sizeof(double) * C, cudaMemcpyDeviceToHost, P.s),
+                  "cg r.z copy");
         unsigned long long bits = 0;
         FEGB_TRY(d2h_sync(&bits, B.zmax, sizeof(bits), P.s, "cg zmax copy"));
         zm = bits_to_double(bits);
-        if (zm < inner_tol) {
+        if (trace_level() >= 2 && it % 10 == 0)
+            std::fprintf(stderr, "fegb cg:   iteration %d max |z| %.3e r.z %.3e\n", it, zm,
+                         cg_rz_total(rz_host.data(), C));
+        if (cg_stop_rule(zm, cg_rz_total(rz_host.data(), C), inner_tol, &best, &best_rz, &since_best)) {
             ++it;
             break;
         }
-        if (zm < 0.9 * best) {
-            best = zm;
-            since_best = 0;
-        } else if (++since_best > 60) {
-            ++it;
-            break;  // the recursive residual stopped improving at this precision
-        }
-        FEGB_TRY(launch_cg_direction<T>(P.Gt, C, B.rz, B.rz_new, B.z, B.p, B.ld, P.s, nullptr, B.pmax_part, B.pmax));
+        FEGB_TRY(launch_cg_direction<T>(P.Gt, C, B.rz, B.rz_new, B.z, B.p, B.ld, P.s));
     }
     *iters = it;
     *zmax_out = zm;
@@ -1217,6 +1252,8 @@ int demean_cg(Problem& P, double tol, int max_iter, int* iterations, int* conver
     for (int round = 0; round < max_outer; ++round) {
         FEGB_TRY(fp64_mean_pass(P, apply_alpha, &mu));
         *outer = round + 1;
+        if (trace_enabled() && (mu < tol || round + 1 == max_outer))
+            std::fprintf(stderr, "fegb cg: outer %d max group mean %.3e (tolerance %.1e)\n", round + 1, mu, tol);
         if (mu < tol) {
             hit = 1;
             break;
@@ -1229,6 +1266,9 @@ int demean_cg(Problem& P, double tol, int max_iter, int* iterations, int* conver
         int it = 0;
         double zm = 0.0;
         FEGB_TRY(cg_solve<T>(P, B, inner_tol, max_iter - total, &it, &zm, use_graph ? &G : nullptr));
+        if (trace_enabled())
+            std::fprintf(stderr, "fegb cg: outer %d max group mean %.3e inner tol %.3e: %d iterations, max |z| %.3e\n",
+                         round + 1, mu, inner_tol, it, zm);
         total += it;
         apply_alpha = true;
     }

@@ -203,7 +203,7 @@ __device__ __forceinline__ double source_sum(const FinalizeParams& p, int g, int
     if (p.partials) {
         for (int b = 0; b < p.nblocks; ++b) sum += p.partials[(long long)b * total + idx];
     } else if (!p.off) {
-        sum = p.sums[idx];
+        sum = p.sums ? p.sums[idx] : 0.0;  // null: no swept source contributes
     } else {
         const int s = p.off[g], e = p.off[g + 1];
         if (e > s) {
@@ -330,7 +330,8 @@ __device__ __forceinline__ void column_partials(A prod, long long base, int C, A
 
 template <typename T>
 __global__ void __launch_bounds__(FIN_THREADS) cg_q_kernel(FinalizeParams src, int C, const T* __restrict__ p,
-                                                            int pld, T* __restrict__ q, double* __restrict__ pq_partials) {
+                                                            int pld, T* __restrict__ q, double* __restrict__ pq_partials,
+                                                            const T* __restrict__ extra) {
     // compact elements (g, c < C); the sweep sums use the padded stride src.C, p uses pld
     __shared__ T smem[FIN_THREADS];
     const long long total = (long long)src.G * C;
@@ -343,7 +344,8 @@ __global__ void __launch_bounds__(FIN_THREADS) cg_q_kernel(FinalizeParams src, i
         const double ssum = source_sum(src, g, c, (long long)g * src.C + c, (long long)src.G * src.C);
         const T pv = p[(long long)g * pld + c];
         // ssum = -(sum over the group's rows of the other dimensions' p)
-        const T qv = (T)src.counts[g] * pv - (T)ssum;
+        T qv = (T)src.counts[g] * pv - (T)ssum;
+        if (extra) qv += extra[idx];
         q[idx] = qv;
         prod = pv * qv;
     }
@@ -462,11 +464,9 @@ __global__ void __launch_bounds__(FIN_THREADS)
 template <typename T>
 __global__ void cg_direction_kernel(long long Gt, int C, const double* __restrict__ rz_old,
                                     const double* __restrict__ rz_new, const T* __restrict__ z, T* __restrict__ p,
-                                    int pld, const int* __restrict__ skip, double* __restrict__ pmax_partials) {
+                                    int pld, const int* __restrict__ skip) {
     if (skip && *skip) return;  // the loop has stopped (graph-driven loop)
     __shared__ double beta[64];
-    __shared__ double red[8];
-    T amax = T(0);
     if (threadIdx.x < C && threadIdx.x < 64)
         beta[threadIdx.x] = rz_old[threadIdx.x] != 0.0 ? rz_new[threadIdx.x] / rz_old[threadIdx.x] : 0.0;
     __syncthreads();
@@ -481,24 +481,12 @@ __global__ void cg_direction_kernel(long long Gt, int C, const double* __restric
     for (; idx < total; idx += st) {
         const T b = C <= 64 ? (T)beta[c] : (T)(rz_old[c] != 0.0 ? rz_new[c] / rz_old[c] : 0.0);
         T* pe = p + g * pld + c;
-        const T pv = z[idx] + b * *pe;
-        *pe = pv;
-        const T ap = pv < T(0) ? -pv : pv;
-        amax = ap > amax ? ap : amax;
+        *pe = z[idx] + b * *pe;
         g += gstep;
         c += cstep;
         if (c >= C) {
             c -= C;
             ++g;
-        }
-    }
-    if (pmax_partials) {
-        double m = warp_max((double)amax);
-        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            for (int w = 1; w < (int)(blockDim.x >> 5); ++w) m = fmax(m, red[w]);
-            pmax_partials[blockIdx.x] = fmax(m, red[0]);
         }
     }
 }
@@ -667,10 +655,11 @@ int launch_convert_f64_f32(const double* src, float* dst, long long n, cudaStrea
 int cg_partial_blocks(long long gc) { return (int)((gc + FIN_THREADS - 1) / FIN_THREADS); }
 
 template <typename T>
-int launch_cg_q(const FinalizeParams& src, int C, const T* p, int pld, T* q, double* pq_partials, cudaStream_t s) {
+int launch_cg_q(const FinalizeParams& src, int C, const T* p, int pld, T* q, double* pq_partials, cudaStream_t s,
+                const T* extra) {
     long long total = (long long)src.G * C;
     if (total <= 0) return 0;
-    cg_q_kernel<T><<<cg_partial_blocks(total), FIN_THREADS, 0, s>>>(src, C, p, pld, q, pq_partials);
+    cg_q_kernel<T><<<cg_partial_blocks(total), FIN_THREADS, 0, s>>>(src, C, p, pld, q, pq_partials, extra);
     FEGB_LAUNCH_CHECK("cg q");
     return 0;
 }
@@ -735,16 +724,12 @@ int launch_cg_update(long long Gt, int C, const T* inv_counts, const double* rz,
 
 template <typename T>
 int launch_cg_direction(long long Gt, int C, double* rz_old, const double* rz_new, const T* z, T* p, int pld,
-                        cudaStream_t s, const int* skip, double* pmax_partials, unsigned long long* pmax_bits) {
+                        cudaStream_t s, const int* skip) {
     long long total = Gt * C;
     if (total > 0) {
-        const unsigned nb = grid_stride_blocks(total, 256);
-        cg_direction_kernel<T><<<nb, 256, 0, s>>>(Gt, C, rz_old, rz_new, z, p, pld, skip, pmax_partials);
+        cg_direction_kernel<T><<<grid_stride_blocks(total, 256), 256, 0, s>>>(Gt, C, rz_old, rz_new, z, p, pld,
+                                                                             skip);
         FEGB_LAUNCH_CHECK("cg direction");
-        if (pmax_partials && pmax_bits) {
-            fold_max_kernel<<<1, FIN_THREADS, 0, s>>>(pmax_partials, (int)nb, pmax_bits);
-            FEGB_LAUNCH_CHECK("cg pmax fold");
-        }
     }
     copy_scalars_kernel<<<1, ((C + 31) / 32) * 32, 0, s>>>(rz_new, rz_old, C, skip);
     FEGB_LAUNCH_CHECK("cg scalars");
@@ -764,8 +749,158 @@ int launch_cg_init(long long Gt, int C, const int32_t* counts, const double* mu,
     return 0;
 }
 
-template int launch_cg_q<double>(const FinalizeParams&, int, const double*, int, double*, double*, cudaStream_t);
-template int launch_cg_q<float>(const FinalizeParams&, int, const float*, int, float*, double*, cudaStream_t);
+template int launch_cg_q<double>(const FinalizeParams&, int, const double*, int, double*, double*, cudaStream_t,
+                                 const double*);
+template int launch_cg_q<float>(const FinalizeParams&, int, const float*, int, float*, double*, cudaStream_t,
+                                const float*);
+
+// ---- dense count matrices of small-G dimensions ----
+
+__global__ void count_pairs_kernel(const int32_t* __restrict__ ge, const int32_t* __restrict__ gs, long long n,
+                                   int Gs, uint32_t* __restrict__ N) {
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long st = (long long)gridDim.x * blockDim.x;
+    for (; i < n; i += st) atomicAdd(N + (long long)ge[i] * Gs + gs[i], 1u);  // integer: order-free
+}
+
+int launch_count_pairs(const int32_t* gid_e, const int32_t* gid_s, long long n, int Gs, uint32_t* N, cudaStream_t s) {
+    if (n <= 0) return 0;
+    count_pairs_kernel<<<grid_stride_blocks(n, 256), 256, 0, s>>>(gid_e, gid_s, n, Gs, N);
+    FEGB_LAUNCH_CHECK("count pairs");
+    return 0;
+}
+
+// Block b covers groups [b * per, (b + 1) * per) of e in tiles of
+// DENSE_TILE groups: the tile's count rows and p rows are staged in shared
+// memory, thread tc (t = tc / C, c = tc % C; up to DENSE_MAX_TC / 256 per
+// thread) sums the tile in the storage type and adds the tile total to an
+// FP64 accumulator. One partial per block, in a fixed order.
+template <typename T>
+__global__ void __launch_bounds__(256) small_from_dense_kernel(const uint32_t* __restrict__ N, long long Ge, int Gs,
+                                                               const T* __restrict__ pe, int ld, int C, long long per,
+                                                               double* __restrict__ partials) {
+    extern __shared__ __align__(16) unsigned char dense_smem[];
+    uint32_t* sN = reinterpret_cast<uint32_t*>(dense_smem);              // DENSE_TILE x Gs
+    T* sP = reinterpret_cast<T*>(dense_smem + sizeof(uint32_t) * DENSE_TILE * Gs);  // DENSE_TILE x C
+    constexpr int R = DENSE_MAX_TC / 256;
+    const int TC = Gs * C;
+    double acc[R];
+    int tt[R], cc[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+        acc[r] = 0.0;
+        const int tc = threadIdx.x + r * 256;
+        tt[r] = tc / C;
+        cc[r] = tc - tt[r] * C;
+    }
+    const long long g0 = (long long)blockIdx.x * per;
+    const long long g1 = min(Ge, g0 + per);
+    for (long long tile = g0; tile < g1; tile += DENSE_TILE) {
+        const int nt = (int)min((long long)DENSE_TILE, g1 - tile);
+        __syncthreads();  // the previous tile is consumed
+        for (int i = threadIdx.x; i < nt * Gs; i += 256) sN[i] = N[tile * Gs + i];
+        for (int i = threadIdx.x; i < nt * C; i += 256) {
+            const int gl = i / C;
+            sP[i] = pe[(tile + gl) * ld + (i - gl * C)];
+        }
+        __syncthreads();
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            if (threadIdx.x + r * 256 >= TC) break;  // past the last output
+            const uint32_t* nr = sN + tt[r];
+            const T* pr = sP + cc[r];
+            T a = T(0);
+            for (int g = 0; g < nt; ++g) a += (T)nr[g * Gs] * pr[g * C];
+            acc[r] += (double)a;
+        }
+    }
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+        const int tc = threadIdx.x + r * 256;
+        if (tc < TC) partials[(long long)blockIdx.x * TC + tc] = acc[r];
+    }
+}
+
+template <typename T>
+int launch_small_from_dense(const uint32_t* N, long long Ge, int Gs, const T* pe, int ld, int C, double* partials,
+                            cudaStream_t s) {
+    if (Ge <= 0) return 0;
+    if (Gs * C > DENSE_MAX_TC) return set_error("dense small-G product: %d x %d outputs exceed %d", Gs, C, DENSE_MAX_TC);
+    const int nb = dense_chunks(Ge);
+    const long long per = (Ge + nb - 1) / nb;
+    const size_t smem = (sizeof(uint32_t) * Gs + sizeof(T) * C) * DENSE_TILE;
+    small_from_dense_kernel<T><<<nb, 256, smem, s>>>(N, Ge, Gs, pe, ld, C, per, partials);
+    FEGB_LAUNCH_CHECK("small-G dense product");
+    return 0;
+}
+template int launch_small_from_dense<float>(const uint32_t*, long long, int, const float*, int, int, double*,
+                                            cudaStream_t);
+template int launch_small_from_dense<double>(const uint32_t*, long long, int, const double*, int, int, double*,
+                                             cudaStream_t);
+
+// One warp per (t, c): strided fold over the parts, fixed shuffle tree.
+__global__ void fold_dense_kernel(const double* __restrict__ partials, int nparts, int TC, double* __restrict__ sums) {
+    const long long w = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (w >= TC) return;
+    double acc = 0.0;
+    for (int b = lane; b < nparts; b += 32) acc += partials[(long long)b * TC + w];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+    if (lane == 0) sums[w] = -acc;  // sums of -p, the sweep convention
+}
+
+int launch_fold_dense(const double* partials, int nparts, int Gs, int C, double* sums, cudaStream_t s) {
+    const int TC = Gs * C;
+    if (TC <= 0) return 0;
+    fold_dense_kernel<<<(unsigned)((TC * 32 + 255) / 256), 256, 0, s>>>(partials, nparts, TC, sums);
+    FEGB_LAUNCH_CHECK("small-G dense fold");
+    return 0;
+}
+
+// extra[g * C + c] (+)= sum_t N[g][t] ps[t][c]. A block takes DENSE_TILE
+// groups of d: their count rows are staged in shared memory (coalesced), ps
+// as well; thread (g, c) then reads both from shared memory.
+template <typename T>
+__global__ void __launch_bounds__(256) dense_to_groups_kernel(const uint32_t* __restrict__ N, long long Gd, int Gs,
+                                                              const T* __restrict__ ps, int ld, int C,
+                                                              T* __restrict__ extra, int accumulate) {
+    __shared__ T sps[DENSE_SMALL_MAX_G * 32];
+    __shared__ uint32_t sN[DENSE_TILE * DENSE_SMALL_MAX_G];
+    const long long g0 = (long long)blockIdx.x * DENSE_TILE;
+    const int nt = (int)min((long long)DENSE_TILE, Gd - g0);
+    for (int i = threadIdx.x; i < Gs * C; i += blockDim.x) {
+        const int t = i / C;
+        sps[i] = ps[(long long)t * ld + (i - t * C)];
+    }
+    for (int i = threadIdx.x; i < nt * Gs; i += blockDim.x) sN[i] = N[g0 * Gs + i];
+    __syncthreads();
+    for (int i = threadIdx.x; i < nt * C; i += blockDim.x) {
+        const int gl = i / C;
+        const int c = i - gl * C;
+        const uint32_t* row = sN + gl * Gs;
+        T acc = T(0);
+        for (int t = 0; t < Gs; ++t) acc += (T)row[t] * sps[t * C + c];
+        const long long o = g0 * C + i;
+        extra[o] = accumulate ? extra[o] + acc : acc;
+    }
+}
+
+template <typename T>
+int launch_dense_to_groups(const uint32_t* N, long long Gd, int Gs, const T* ps, int ld, int C, T* extra,
+                           int accumulate, cudaStream_t s) {
+    const long long total = Gd * C;
+    if (total <= 0) return 0;
+    if (Gs > DENSE_SMALL_MAX_G || C > 32) return set_error("dense small-G product: Gs=%d C=%d too large", Gs, C);
+    const long long nb = (Gd + DENSE_TILE - 1) / DENSE_TILE;
+    dense_to_groups_kernel<T><<<(unsigned)nb, 256, 0, s>>>(N, Gd, Gs, ps, ld, C, extra, accumulate);
+    FEGB_LAUNCH_CHECK("small-G dense to groups");
+    return 0;
+}
+template int launch_dense_to_groups<float>(const uint32_t*, long long, int, const float*, int, int, float*, int,
+                                           cudaStream_t);
+template int launch_dense_to_groups<double>(const uint32_t*, long long, int, const double*, int, int, double*, int,
+                                            cudaStream_t);
 template int launch_cg_update<double>(long long, int, const double*, const double*, const double*, const double*, int,
                                       const double*, double*, double*, double*, double*, double*,
                                       unsigned long long*, cudaStream_t);
@@ -794,51 +929,9 @@ int launch_inv_counts_t(const int32_t* counts, long long G, T* inv, cudaStream_t
 template int launch_inv_counts_t<float>(const int32_t*, long long, float*, cudaStream_t);
 template int launch_inv_counts_t<double>(const int32_t*, long long, double*, cudaStream_t);
 template int launch_cg_direction<double>(long long, int, double*, const double*, const double*, double*, int,
-                                         cudaStream_t, const int*, double*, unsigned long long*);
+                                         cudaStream_t, const int*);
 template int launch_cg_direction<float>(long long, int, double*, const double*, const float*, float*, int,
-                                        cudaStream_t, const int*, double*, unsigned long long*);
-
-int launch_fold_max(const double* partials, int nb, unsigned long long* out, cudaStream_t s) {
-    fold_max_kernel<<<1, FIN_THREADS, 0, s>>>(partials, nb, out);
-    FEGB_LAUNCH_CHECK("max fold");
-    return 0;
-}
-
-// One warp per (g, c): exact int64 sum over the block tables, then the count term.
-template <typename T>
-__global__ void cg_sg_fold_kernel(const long long* __restrict__ part, int nblocks, int G, int C,
-                                  const unsigned long long* __restrict__ pmax_bits, int n_dims, long long n,
-                                  const int32_t* __restrict__ counts, const T* __restrict__ ps, int ld,
-                                  double* __restrict__ sums) {
-    const long long w = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int lane = threadIdx.x & 31;
-    const long long GC = (long long)G * C;
-    if (w >= GC) return;
-    long long acc = 0;
-    for (int b = lane; b < nblocks; b += 32) acc += part[(long long)b * GC + w];
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
-    if (lane == 0) {
-        const int g = (int)(w / C), c = (int)(w - (long long)g * C);
-        const int e = cg_sg_exponent(__longlong_as_double((long long)*pmax_bits), n_dims, n);
-        sums[w] = ldexp((double)acc, -e) + (double)counts[g] * (double)ps[(long long)g * ld + c];
-    }
-}
-
-template <typename T>
-int launch_cg_sg_fold(const long long* part, int nblocks, int G, int C, const unsigned long long* pmax_bits,
-                      int n_dims, long long n, const int32_t* counts, const T* ps, int ld, double* sums, cudaStream_t s) {
-    const long long GC = (long long)G * C;
-    if (GC <= 0) return 0;
-    cg_sg_fold_kernel<T><<<(unsigned)((GC * 32 + 255) / 256), 256, 0, s>>>(part, nblocks, G, C, pmax_bits, n_dims, n,
-                                                                           counts, ps, ld, sums);
-    FEGB_LAUNCH_CHECK("small-G side fold");
-    return 0;
-}
-template int launch_cg_sg_fold<float>(const long long*, int, int, int, const unsigned long long*, int, long long,
-                                      const int32_t*, const float*, int, double*, cudaStream_t);
-template int launch_cg_sg_fold<double>(const long long*, int, int, int, const unsigned long long*, int, long long,
-                                       const int32_t*, const double*, int, double*, cudaStream_t);
+                                        cudaStream_t, const int*);
 template int launch_cg_init<double>(long long, int, const int32_t*, const double*, double*, double*, double*, int,
                                     double*, double*, double*, unsigned long long*, cudaStream_t);
 template int launch_cg_init<float>(long long, int, const int32_t*, const double*, float*, float*, float*, int, float*,
@@ -979,20 +1072,13 @@ __device__ __forceinline__ void cg_run_push(CGRun<T, TILE>& st, int g, const T (
 // stay in registers because every loop over TILE is fully unrolled).
 // NSRC = number of source dimensions when the vector id path is used
 // (1..3); NSRC = 0 reads ids one position at a time for any n_src.
-// fixed-point add of one position's side contribution w to the small dimension's table
-template <typename T>
-__device__ __forceinline__ void sg_add(long long* tab, int idx, T w, int e) {
-    long long qv;
-    if constexpr (sizeof(T) == 4)
-        qv = __float2ll_rn(ldexpf(w, e));
-    else
-        qv = __double2ll_rn(ldexp(w, e));
-    atomicAdd(reinterpret_cast<unsigned long long*>(tab + idx), (unsigned long long)qv);
-}
-
-template <typename T, int CGR_TILE, int NSRC, bool SG>
-__device__ __forceinline__ void cg_rows_body(const CGRowsParams<T>& p, int ntiles, long long warp, int lane,
-                                             long long* sg_tab, int sg_e) {
+template <typename T, int CGR_TILE, int NSRC>
+__global__ void __launch_bounds__(256, (sizeof(T) == 4 && CGR_TILE <= 12) ? CG_ROWS_MINB : 2)
+    cg_rows_kernel(CGRowsParams<T> p, int ntiles) {
+    const int lane = threadIdx.x & 31;
+    const long long warp = ((long long)blockIdx.x * 256 + threadIdx.x) >> 5;
+    const long long nchunks = (p.n + CG_CHUNK - 1) / CG_CHUNK;
+    if (warp >= nchunks * ntiles) return;  // whole warp exits together
     const long long q = warp / ntiles;
     const int c0 = (int)(warp - q * ntiles) * CGR_TILE;
     const int C = p.C;
@@ -1026,25 +1112,6 @@ __device__ __forceinline__ void cg_rows_body(const CGRowsParams<T>& p, int ntile
             tabs[e] = p.src_tab[e] + c0;
             sgid[e] = p.src_gid[e];
         }
-        // small-G side output: v - p_primary per position (p_primary loaded once per run)
-        int pp_g = -1;
-        T pp[SG ? CGR_TILE : 1];
-        auto side = [&](int g, int t, const T (&v)[CGR_TILE]) {
-            if constexpr (SG) {
-                if (g != pp_g) {
-                    T tmp[CGR_TILE];
-#pragma unroll
-                    for (int i = 0; i < CGR_TILE; ++i) tmp[i] = T(0);
-                    cg_sub_row<T, CGR_TILE>(p.prim_tab + (long long)g * LD + c0, cw, tmp, keep);
-#pragma unroll
-                    for (int i = 0; i < CGR_TILE; ++i) pp[i] = -tmp[i];
-                    pp_g = g;
-                }
-#pragma unroll
-                for (int i = 0; i < CGR_TILE; ++i)
-                    if (i < cw) sg_add<T>(sg_tab, t * C + c0 + i, v[i] - pp[i], sg_e);
-            }
-        };
 #pragma unroll 1
         for (int h = 0; h < CG_LANE_POS / CG_IDV; ++h) {
             const long long jb = ls + CG_IDV * h;
@@ -1062,13 +1129,6 @@ __device__ __forceinline__ void cg_rows_body(const CGRowsParams<T>& p, int ntile
 #pragma unroll
                     for (int e = 0; e < NSRC; ++e)
                         cg_sub_row<T, CGR_TILE>(tabs[e] + (long long)sid[e][m] * LD, cw, v, keep);
-                    if constexpr (SG) {
-                        int t = 0;
-#pragma unroll
-                        for (int e = 0; e < NSRC; ++e)
-                            if (e == p.sg_src) t = sid[e][m];
-                        side(gq[m], t, v);
-                    }
                     cg_run_push(st, gq[m], v, p.sums, LD, c0, cw);
                 }
             } else {
@@ -1080,9 +1140,7 @@ __device__ __forceinline__ void cg_rows_body(const CGRowsParams<T>& p, int ntile
 #pragma unroll
                     for (int e = 0; e < NSRC; ++e)
                         cg_sub_row<T, CGR_TILE>(tabs[e] + (long long)__ldg(sgid[e] + j) * LD, cw, v, keep);
-                    const int g = __ldg(gseq + j);
-                    if constexpr (SG) side(g, __ldg(p.src_gid[p.sg_src] + j), v);
-                    cg_run_push(st, g, v, p.sums, LD, c0, cw);
+                    cg_run_push(st, __ldg(gseq + j), v, p.sums, LD, c0, cw);
                 }
             }
         }
@@ -1177,41 +1235,12 @@ __device__ __forceinline__ void cg_rows_body(const CGRowsParams<T>& p, int ntile
     }
 }
 
-template <typename T, int CGR_TILE, int NSRC, bool SG>
-__global__ void __launch_bounds__(256, SG ? 2 : ((sizeof(T) == 4 && CGR_TILE <= 12) ? CG_ROWS_MINB : 2))
-    cg_rows_kernel(CGRowsParams<T> p, int ntiles) {
-    extern __shared__ long long sg_tab[];
-    const int lane = threadIdx.x & 31;
-    const long long warp = ((long long)blockIdx.x * 256 + threadIdx.x) >> 5;
-    const long long nchunks = (p.n + CG_CHUNK - 1) / CG_CHUNK;
-    int sg_e = 0;
-    if constexpr (SG) {
-        for (int i = threadIdx.x; i < p.sg_G * p.C; i += blockDim.x) sg_tab[i] = 0;
-        sg_e = cg_sg_exponent(__longlong_as_double((long long)*p.pmax_bits), p.n_dims, p.n);
-        __syncthreads();
-    }
-    if (warp < nchunks * ntiles)  // whole warps take part or skip together
-        cg_rows_body<T, CGR_TILE, NSRC, SG>(p, ntiles, warp, lane, sg_tab, sg_e);
-    if constexpr (SG) {
-        __syncthreads();
-        long long* dst = p.sg_part + (long long)blockIdx.x * p.sg_G * p.C;
-        for (int i = threadIdx.x; i < p.sg_G * p.C; i += blockDim.x) dst[i] = sg_tab[i];
-    }
-}
-
 template <typename T, int TILE, int NSRC>
 int launch_cg_rows_tile(const CGRowsParams<T>& p, cudaStream_t s) {
     const int ntiles = (p.C + TILE - 1) / TILE;
-    const long long blocks = cg_rows_blocks(p.n, p.C, TILE);
-    if constexpr (NSRC > 0) {
-        if (p.sg_src >= 0) {
-            const size_t smem = sizeof(long long) * (size_t)p.sg_G * p.C;
-            cg_rows_kernel<T, TILE, NSRC, true><<<(unsigned)blocks, 256, smem, s>>>(p, ntiles);
-            FEGB_LAUNCH_CHECK("cg operator sweep with small-G side output");
-            return 0;
-        }
-    }
-    cg_rows_kernel<T, TILE, NSRC, false><<<(unsigned)blocks, 256, 0, s>>>(p, ntiles);
+    const long long warps = ((p.n + CG_CHUNK - 1) / CG_CHUNK) * ntiles;
+    const long long blocks = (warps * 32 + 255) / 256;
+    cg_rows_kernel<T, TILE, NSRC><<<(unsigned)blocks, 256, 0, s>>>(p, ntiles);
     FEGB_LAUNCH_CHECK("cg operator sweep");
     return 0;
 }
@@ -1219,21 +1248,19 @@ int launch_cg_rows_tile(const CGRowsParams<T>& p, cudaStream_t s) {
 template <typename T, int TILE>
 int launch_cg_rows_nsrc(const CGRowsParams<T>& p, cudaStream_t s) {
     // the vector id path needs 16-byte aligned id arrays
-    if (cg_rows_vector_path(p)) {
+    bool aligned = (reinterpret_cast<uintptr_t>(p.gseq) & 15u) == 0;
+    for (int e = 0; e < p.n_src; ++e) aligned = aligned && (reinterpret_cast<uintptr_t>(p.src_gid[e]) & 15u) == 0;
+    if (aligned) {
         if (p.n_src == 1) return launch_cg_rows_tile<T, TILE, 1>(p, s);
         if (p.n_src == 2) return launch_cg_rows_tile<T, TILE, 2>(p, s);
         if (p.n_src == 3) return launch_cg_rows_tile<T, TILE, 3>(p, s);
     }
-    if (p.sg_src >= 0) return set_error("cg operator: the small-G side output needs the vector id path");
     return launch_cg_rows_tile<T, TILE, 0>(p, s);
 }
 
 template <typename T>
 int launch_cg_rows(const CGRowsParams<T>& p, cudaStream_t s) {
     if (p.n <= 0) return 0;
-    if (p.sg_src >= 0 && (p.sg_src >= p.n_src || !p.prim_tab || !p.pmax_bits || !p.sg_part || p.sg_G <= 0 ||
-                          (size_t)p.sg_G * p.C * sizeof(long long) > CG_SG_SMEM_MAX))
-        return set_error("cg operator: invalid small-G side output");
     // table rows are read in 32-byte pieces: the stride and the tables must allow it
     if (p.ld % (32 / (int)sizeof(T)) != 0) return set_error("cg operator: row stride %d is not a 32-byte multiple", p.ld);
     for (int e = 0; e < p.n_src; ++e)

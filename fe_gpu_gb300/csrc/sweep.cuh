@@ -78,7 +78,7 @@ struct FinalizeParams {
     // source of the group sums: segments (off/sums/head/tail, chunk size R) or
     // small-G block partials (partials, nblocks)
     // source of the group sums: off == null && partials == null means sums[]
-    // already holds complete group sums
+    // already holds complete group sums (sums == null: all zero)
     const int32_t* off;
     const double* sums;
     const double* head;
@@ -169,65 +169,10 @@ struct CGRowsParams {
     double* sums;
     double* head;
     double* tail;
-    // Optional side output of the storage-order (primary) pass: the operator
-    // sums of one small-G dimension, accumulated in fixed point (int64, so
-    // the result does not depend on the order of the adds). For each
-    // position the pass adds v - p_primary (v = its own contribution) to the
-    // small dimension's group; cg_sg_fold adds count * p_small afterwards.
-    int sg_src = -1;              // index of the small dimension among the sources; -1 = none
-    int sg_G = 0;                 // its groups
-    int n_dims = 0;               // FE dimensions (bounds |v - p_primary| by n_dims * pmax)
-    const T* prim_tab = nullptr;  // primary dimension's p rows (stride ld)
-    const unsigned long long* pmax_bits = nullptr;  // max |p| (bits of a non-negative double)
-    long long* sg_part = nullptr;  // per block: sg_G x C int64 sums
 };
 
 template <typename T>
 int launch_cg_rows(const CGRowsParams<T>& p, cudaStream_t s);
-
-// shared memory limit of the small-G side table (sg_G x C int64)
-constexpr size_t CG_SG_SMEM_MAX = 40 * 1024;
-
-// blocks of one operator launch over n positions and C columns with column tile `tile`
-inline long long cg_rows_blocks(long long n, int C, int tile) {
-    const int ntiles = (C + tile - 1) / tile;
-    const long long warps = ((n + CG_CHUNK - 1) / CG_CHUNK) * ntiles;
-    return (warps * 32 + 255) / 256;
-}
-// the column tile launch_cg_rows picks for C columns
-inline int cg_rows_tile(int C) { return C <= 4 ? 4 : C <= 8 ? 8 : C == 9 ? 9 : C <= 12 ? 12 : 16; }
-
-// the vector id path (needed by the small-G side output): 1..3 sources and
-// 16-byte aligned id arrays
-template <typename T>
-inline bool cg_rows_vector_path(const CGRowsParams<T>& p) {
-    if (p.n_src < 1 || p.n_src > 3) return false;
-    bool aligned = (reinterpret_cast<uintptr_t>(p.gseq) & 15u) == 0;
-    for (int e = 0; e < p.n_src; ++e) aligned = aligned && (reinterpret_cast<uintptr_t>(p.src_gid[e]) & 15u) == 0;
-    return aligned;
-}
-
-// Fixed-point exponent of the small-G side output: values are scaled by
-// 2^e so that n sums of |v| <= n_dims * pmax stay below 2^62.
-__host__ __device__ inline int cg_sg_exponent(double pmax, int n_dims, long long n) {
-    double b = (double)(n_dims > 0 ? n_dims : 1) * pmax;
-    if (!(b > 0.0)) b = 1.0;
-    int eb = 0;
-    frexp(b, &eb);  // b < 2^eb
-    int en = 1;
-    while (en < 62 && (1LL << en) <= n) ++en;  // n < 2^en
-    int e = 62 - en - eb;
-    return e > 100 ? 100 : (e < -100 ? -100 : e);
-}
-
-// sums[g * C + c] = sum over blocks of part (exact int64) / 2^e + counts[g] * ps[g * ld + c]:
-// the small dimension's operator sums (sums of -p over the other dimensions).
-template <typename T>
-int launch_cg_sg_fold(const long long* part, int nblocks, int G, int C, const unsigned long long* pmax_bits,
-                      int n_dims, long long n, const int32_t* counts, const T* ps, int ld, double* sums, cudaStream_t s);
-
-// max |p| over the G-space direction (bits of a non-negative double), from per-block maxima.
-int launch_fold_max(const double* partials, int nb, unsigned long long* out, cudaStream_t s);
 
 // Row stride of the CG G-space vectors: rows padded to 32-byte multiples (a
 // multiple of 16 columns above 16) so that table rows load as 256-bit vectors.
@@ -249,8 +194,37 @@ inline int cg_row_stride(int C, int elem_bytes) {
 // with pending tables {p_e, e != d} (sums of -p_e over the rows of each
 // group). Also writes per-block partials of p.q per column.
 // src.C is the padded row stride of the sweep sums; q is compact (C columns).
+// extra (optional, G x C compact): added to q (contributions computed apart
+// from the sweep, e.g. from dense small-G count matrices).
 template <typename T>
-int launch_cg_q(const FinalizeParams& src, int C, const T* p, int pld, T* q, double* pq_partials, cudaStream_t s);
+int launch_cg_q(const FinalizeParams& src, int C, const T* p, int pld, T* q, double* pq_partials, cudaStream_t s,
+                const T* extra = nullptr);
+
+// ---- dense count matrices of small-G dimensions ----
+// For a dimension s with few groups and any other dimension e, the operator
+// coupling D_s' D_e is the G_e x G_s count matrix N (rows of each (group of e,
+// group of s) pair), built once. N[g * Gs + t] counts the rows with gid_e = g
+// and gid_s = t.
+constexpr int DENSE_SMALL_MAX_G = 64;
+constexpr int DENSE_TILE = 64;          // groups per shared-memory tile of the dense products
+constexpr int DENSE_MAX_BLOCKS = 1024;  // partial blocks of a small-side product (fixed: same sums on any GPU)
+constexpr int DENSE_MAX_TC = DENSE_SMALL_MAX_G * 32;
+int launch_count_pairs(const int32_t* gid_e, const int32_t* gid_s, long long n, int Gs, uint32_t* N, cudaStream_t s);
+// number of partial blocks of a small-side product over Ge groups
+inline int dense_chunks(long long Ge) {
+    const long long tiles = (Ge + DENSE_TILE - 1) / DENSE_TILE;
+    return (int)(tiles < DENSE_MAX_BLOCKS ? tiles : DENSE_MAX_BLOCKS);
+}
+// partials[block][t][c] = sum over the block's groups g of N[g][t] * pe[g * ld + c]
+template <typename T>
+int launch_small_from_dense(const uint32_t* N, long long Ge, int Gs, const T* pe, int ld, int C, double* partials,
+                            cudaStream_t s);
+// sums[t * C + c] = -(sum over parts of partials[part][t][c]), parts in order
+int launch_fold_dense(const double* partials, int nparts, int Gs, int C, double* sums, cudaStream_t s);
+// extra[g * C + c] (+)= sum_t N[g][t] * ps[t * ld + c]  (accumulate = 0 overwrites)
+template <typename T>
+int launch_dense_to_groups(const uint32_t* N, long long Gd, int Gs, const T* ps, int ld, int C, T* extra,
+                           int accumulate, cudaStream_t s);
 int cg_partial_blocks(long long gc);
 
 // out[c] = sum_b partials[b * C + c] for b < nb (fixed order)
@@ -271,14 +245,11 @@ template <typename T>
 int launch_inv_counts_t(const int32_t* counts, long long G, T* inv, cudaStream_t s);
 
 // b = rz_new / rz_old per column; p = z + b p; rz_old = rz_new
-template <typename T>
 // skip (device, optional): when *skip != 0 both kernels return at once (the
 // direction step of a graph-driven loop that has stopped).
-// pmax_partials (optional): per-block max |p| after the update (grid_stride_blocks(Gt * C, 256) entries),
-// folded into pmax_bits.
+template <typename T>
 int launch_cg_direction(long long Gt, int C, double* rz_old, const double* rz_new, const T* z, T* p, int pld,
-                        cudaStream_t s, const int* skip = nullptr, double* pmax_partials = nullptr,
-                        unsigned long long* pmax_bits = nullptr);
+                        cudaStream_t s, const int* skip = nullptr);
 
 // r = counts * mu, z = p = mu (cast to T); partials of r.z and max |z|
 // inv_counts[g] = 1 / counts[g] (0 for empty groups)

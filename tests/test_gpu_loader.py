@@ -38,8 +38,8 @@ def test_device_load_matches_host_reader(built, tmp_path, case):
     W = rng.standard_normal((n, k))
     Z = rng.standard_normal((n, c["l"])) if c["l"] else None
     fe = np.vstack([rng.integers(1, g, n) for g in (500, 40, 7)]).astype(np.int32)
-    meta = dict(depvar="y", regressors=[f"x{j}" for j in range(k)], instruments=[f"z{j}" for j in range(c["l"])],
-                fe=["a", "b", "c"], cluster="", weight="") if c["meta"] else None
+    meta = dict(y="y", x=[f"x{j}" for j in range(k)], iv=[f"z{j}" for j in range(c["l"])],
+                fe=["a", "b", "c"]) if c["meta"] else None
     path = tmp_path / "d.bin"
     write_dataset(str(path), y, W, fe, Z=Z, cluster=fe[0] if c["cluster"] else None,
                   weights=np.abs(y) if c["weights"] else None, precision_flag=c["precision_flag"], metadata=meta,
@@ -50,6 +50,8 @@ def test_device_load_matches_host_reader(built, tmp_path, case):
         assert (ds.n, ds.k, ds.l, ds.n_fe) == (hdr.n_obs, hdr.n_regressors, hdr.n_instruments, hdr.n_fe)
         assert ds.header.precision_flag == hdr.precision_flag
         assert ds.header.regressor_names == hdr.regressor_names and ds.header.fe_names == hdr.fe_names
+        if c["meta"]:
+            assert ds.header.fe_names == ["a", "b", "c"] and ds.header.regressor_names[0] == "x0"
         assert np.array_equal(_back(ds.y, np.float64, n), host.y)
         assert np.array_equal(_back(ds.W, np.float64, n * k).reshape(k, n).T, host.W)
         if hdr.n_instruments:

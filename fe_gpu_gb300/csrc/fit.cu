@@ -64,6 +64,8 @@ struct Dim {
     int n_long = 0;
     int32_t* long_list_cg = nullptr;    // the same for the CG operator's chunk size
     int n_long_cg = 0;
+    int32_t* multi_list_cg = nullptr;   // groups crossing 1..SEG_LONG_SPAN CG chunk boundaries
+    int n_multi_cg = 0;
     double* prev = nullptr;
     double* pend64 = nullptr;
     float* pend32 = nullptr;
@@ -425,6 +427,8 @@ int build_problem(Problem& P, long long n_in, int k, int l, int n_fe, const doub
                 if (sorted_all) {
                     FEGB_TRY(dalloc(scr, &D.long_list_cg, (size_t)D.G, "long groups (cg)"));
                     FEGB_TRY(find_long_groups(D.off, D.G, CG_CHUNK, D.long_list_cg, &D.n_long_cg, s));
+                    FEGB_TRY(dalloc(scr, &D.multi_list_cg, (size_t)D.G, "multi-chunk groups (cg)"));
+                    FEGB_TRY(find_multi_groups(D.off, D.G, CG_CHUNK, D.multi_list_cg, &D.n_multi_cg, s));
                 }
             }
         }
@@ -811,18 +815,23 @@ struct CGBuffers {
     int ld = 0;  // padded row stride of the G-space vectors
     double *rz = nullptr, *rz_new = nullptr, *pq = nullptr;
     double *rz_part = nullptr, *pq_part = nullptr, *zmax_part = nullptr;
-    double *sums = nullptr, *head = nullptr, *tail = nullptr;
+    T* sums = nullptr;  // operator sweep: complete-run group sums (G_max x C, storage type)
+    double *head = nullptr, *tail = nullptr;  // and chunk head/tail partials (chunks x C)
     unsigned long long* zmax = nullptr;
     int rz_blocks = 0, pq_blocks = 0;
     std::vector<int> pq_block_off;
     // dimensions with few groups handled through dense count matrices:
-    // dense[d] says whether d is one; N[d][e] = G_e x G_d counts of the rows
-    // of each (group of e, group of d) pair, for e != d
+    // dense[s] says whether s is one; N8[s][e] / N32[s][e] = G_e x G_s counts
+    // of the rows of each (group of e, group of s) pair, e != s (uint8 when
+    // every count is below 256)
     std::vector<char> dense;
-    std::vector<std::vector<uint32_t*>> N;
-    double* dense_part = nullptr;  // chunk partials of the small-side products
-    double* dense_sums = nullptr;  // G_small x C
-    T* extra = nullptr;            // G_max x C: the dense dimensions' share of a swept dimension's q
+    std::vector<std::vector<uint8_t*>> N8;
+    std::vector<std::vector<uint32_t*>> N32;
+    std::vector<long long> dpart_off, dsum_off;  // per dense s: its partial blocks, its sums
+    double* dense_part = nullptr;
+    double* dense_sums = nullptr;
+    T* extra = nullptr;  // Gt x C: the dense dimensions' share of each swept dimension's q
+    bool any_dense = false;
 };
 
 template <typename T>
@@ -846,10 +855,10 @@ int cg_alloc(Problem& P, CGBuffers<T>& B) {
     FEGB_TRY(dalloc(scr, &B.rz_new, (size_t)C, "cg rz new"));
     FEGB_TRY(dalloc(scr, &B.pq, (size_t)C, "cg pq"));
     FEGB_TRY(dalloc(scr, &B.zmax, 1, "cg zmax"));
-    B.rz_blocks = cg_partial_blocks(P.Gt * C);
+    B.rz_blocks = cg_partial_blocks(P.Gt, C);
     B.pq_block_off.assign(P.n_fe + 1, 0);
     for (int d = 0; d < P.n_fe; ++d)
-        B.pq_block_off[d + 1] = B.pq_block_off[d] + cg_partial_blocks((long long)std::max(1, P.dims[d].G) * C);
+        B.pq_block_off[d + 1] = B.pq_block_off[d] + cg_partial_blocks(std::max(1, P.dims[d].G), C);
     B.pq_blocks = B.pq_block_off[P.n_fe];
     FEGB_TRY(dalloc(scr, &B.rz_part, (size_t)B.rz_blocks * C, "cg rz partials"));
     FEGB_TRY(dalloc(scr, &B.zmax_part, (size_t)B.rz_blocks, "cg zmax partials"));
@@ -858,51 +867,65 @@ int cg_alloc(Problem& P, CGBuffers<T>& B) {
               "cg pq partials zero");
     // dense count matrices for dimensions with few groups (see CGBuffers)
     B.dense.assign(P.n_fe, 0);
-    B.N.assign(P.n_fe, std::vector<uint32_t*>(P.n_fe, nullptr));
+    B.N8.assign(P.n_fe, std::vector<uint8_t*>(P.n_fe, nullptr));
+    B.N32.assign(P.n_fe, std::vector<uint32_t*>(P.n_fe, nullptr));
+    B.dpart_off.assign(P.n_fe, 0);
+    B.dsum_off.assign(P.n_fe, 0);
     if (C <= 32 && P.n > 0) {
-        double bytes = 0.0;
+        double bytes = 0.0;  // worst case: uint32 counts
         for (int d = 0; d < P.n_fe; ++d)
             if (P.dims[d].G > 0 && P.dims[d].G <= DENSE_SMALL_MAX_G)
                 for (int e = 0; e < P.n_fe; ++e)
                     if (e != d) bytes += 4.0 * std::max(1, P.dims[e].G) * P.dims[d].G;
         if (bytes <= 8e9) {
-            long long chunks = 0;
-            int gmax_all = 1, gsmall = 0;
-            for (int d = 0; d < P.n_fe; ++d) gmax_all = std::max(gmax_all, P.dims[d].G);
+            long long parts = 0, sums = 0;
+            unsigned* mx = nullptr;
+            FEGB_TRY(dalloc(scr, &mx, 1, "count max"));
             for (int d = 0; d < P.n_fe; ++d) {
                 if (!(P.dims[d].G > 0 && P.dims[d].G <= DENSE_SMALL_MAX_G)) continue;
                 B.dense[d] = 1;
-                gsmall = std::max(gsmall, P.dims[d].G);
-                long long ch = 0;
+                B.any_dense = true;
+                B.dpart_off[d] = parts;
+                B.dsum_off[d] = sums;
+                sums += (long long)P.dims[d].G * C;
                 for (int e = 0; e < P.n_fe; ++e) {
                     if (e == d || P.dims[e].G <= 0) continue;
                     const size_t cnt = (size_t)P.dims[e].G * P.dims[d].G;
-                    FEGB_TRY(dalloc(scr, &B.N[d][e], cnt, "dense count matrix"));
-                    FEGB_CUDA(cudaMemsetAsync(B.N[d][e], 0, sizeof(uint32_t) * cnt, P.s), "count matrix zero");
-                    FEGB_TRY(launch_count_pairs(P.dims[e].gid, P.dims[d].gid, P.n, P.dims[d].G, B.N[d][e], P.s));
-                    ch += dense_chunks(P.dims[e].G);
+                    Scratch tmp(P.s);  // the uint32 counts, released once narrowed or copied
+                    uint32_t* N = nullptr;
+                    FEGB_TRY(tmp.alloc(&N, cnt, "count matrix"));
+                    FEGB_CUDA(cudaMemsetAsync(N, 0, sizeof(uint32_t) * cnt, P.s), "count matrix zero");
+                    FEGB_TRY(launch_count_pairs(P.dims[e].gid, P.dims[d].gid, P.n, P.dims[d].G, N, P.s));
+                    FEGB_TRY(launch_count_max(N, (long long)cnt, mx, P.s));
+                    unsigned hmx = 0;
+                    FEGB_TRY(d2h_sync(&hmx, mx, sizeof(hmx), P.s, "count max copy"));
+                    if (hmx < 256) {
+                        FEGB_TRY(dalloc(scr, &B.N8[d][e], cnt, "count matrix (uint8)"));
+                        FEGB_TRY(launch_narrow_counts(N, (long long)cnt, B.N8[d][e], P.s));
+                    } else {
+                        FEGB_TRY(dalloc(scr, &B.N32[d][e], cnt, "count matrix (uint32)"));
+                        FEGB_CUDA(cudaMemcpyAsync(B.N32[d][e], N, sizeof(uint32_t) * cnt, cudaMemcpyDeviceToDevice,
+                                                  P.s),
+                                  "count matrix copy");
+                    }
+                    parts += (long long)dense_chunks(P.dims[e].G) * P.dims[d].G * C;
                 }
-                chunks = std::max(chunks, ch);
             }
-            if (gsmall > 0) {
-                FEGB_TRY(dalloc(scr, &B.dense_part, (size_t)std::max(1LL, chunks) * gsmall * C, "dense partials"));
-                FEGB_TRY(dalloc(scr, &B.dense_sums, (size_t)gsmall * C, "dense sums"));
-                FEGB_TRY(dalloc(scr, &B.extra, (size_t)gmax_all * C, "dense extra"));
+            if (B.any_dense) {
+                FEGB_TRY(dalloc(scr, &B.dense_part, (size_t)std::max(1LL, parts), "dense partials"));
+                FEGB_TRY(dalloc(scr, &B.dense_sums, (size_t)std::max(1LL, sums), "dense sums"));
+                FEGB_TRY(dalloc(scr, &B.extra, (size_t)std::max(1LL, P.Gt) * C, "dense extra"));
             }
         }
     }
-    // the operator sweep writes sums/head/tail at the padded stride
-    if (L > P.C) {
-        long long nchunks = std::max(1LL, seg_nchunks(P.n, CG_CHUNK));
+    // the operator sweep's sums / head / tail, compact rows of C
+    {
+        const long long nchunks = std::max(1LL, seg_nchunks(P.n, CG_CHUNK));
         int gmax = 1;
         for (int d = 0; d < P.n_fe; ++d) gmax = std::max(gmax, P.dims[d].G);
-        FEGB_TRY(dalloc(scr, &B.sums, (size_t)gmax * L, "cg sums"));
-        FEGB_TRY(dalloc(scr, &B.head, (size_t)nchunks * L, "cg heads"));
-        FEGB_TRY(dalloc(scr, &B.tail, (size_t)nchunks * L, "cg tails"));
-    } else {
-        B.sums = P.sums;
-        B.head = P.head;
-        B.tail = P.tail;
+        FEGB_TRY(dalloc(scr, &B.sums, (size_t)gmax * C, "cg sums"));
+        FEGB_TRY(dalloc(scr, &B.head, (size_t)nchunks * C, "cg heads"));
+        FEGB_TRY(dalloc(scr, &B.tail, (size_t)nchunks * C, "cg tails"));
     }
     return 0;
 }
@@ -936,39 +959,52 @@ int cg_apply(Problem& P, CGBuffers<T>& B) {
         return 0;
     };
     const int fp32 = sizeof(T) == 4 ? 1 : 0;
-    for (int d = 0; d < P.n_fe; ++d) {
-        Dim& D = P.dims[d];
-        if (D.G <= 0) continue;
+    // 1. dimensions with few groups: one pass over each count matrix gives the
+    // small dimension's sums and the other dimension's share (extra)
+    if (B.any_dense) {
         Problem::Timed tm{};
-        if (B.dense[d]) {
-            // few groups: q_d from the dense count matrices, sum_e N_{e,d}^T p_e
-            double bytes = 0.0;
-            for (int e = 0; e < P.n_fe; ++e)
-                if (e != d && P.dims[e].G > 0)
-                    bytes += (double)P.dims[e].G * (4.0 * D.G + (double)C * sizeof(T));
-            FEGB_TRY(begin_timed(tm, 6 + fp32, bytes));
-            long long part = 0;
+        double bytes = 0.0;
+        for (int sd = 0; sd < P.n_fe; ++sd) {
+            if (!B.dense[sd]) continue;
             for (int e = 0; e < P.n_fe; ++e) {
-                if (e == d || P.dims[e].G <= 0) continue;
-                FEGB_TRY(launch_small_from_dense<T>(B.N[d][e], P.dims[e].G, D.G, B.p + P.goff[e] * L, L, C,
-                                                    B.dense_part + part * D.G * C, P.s));
+                if (e == sd || P.dims[e].G <= 0) continue;
+                const double cb = B.N8[sd][e] ? 1.0 : 4.0;
+                bytes += (double)P.dims[e].G * (cb * P.dims[sd].G + (double)C * sizeof(T) * (B.dense[e] ? 1.0 : 2.0));
+            }
+        }
+        FEGB_TRY(begin_timed(tm, 6 + fp32, bytes));
+        std::vector<char> written(P.n_fe, 0);
+        for (int sd = 0; sd < P.n_fe; ++sd) {
+            if (!B.dense[sd]) continue;
+            const int Gs = P.dims[sd].G;
+            long long part = 0;
+            double* pbase = B.dense_part + B.dpart_off[sd];
+            for (int e = 0; e < P.n_fe; ++e) {
+                if (e == sd || P.dims[e].G <= 0) continue;
+                T* ex = B.dense[e] ? nullptr : B.extra + P.goff[e] * C;
+                const int acc = ex && written[e] ? 1 : 0;
+                const T* pe = B.p + P.goff[e] * L;
+                const T* ps = B.p + P.goff[sd] * L;
+                if (B.N8[sd][e])
+                    FEGB_TRY((launch_dense_pair<T, uint8_t>(B.N8[sd][e], P.dims[e].G, Gs, pe, ps, L, C,
+                                                            pbase + part * Gs * C, ex, acc, P.s)));
+                else
+                    FEGB_TRY((launch_dense_pair<T, uint32_t>(B.N32[sd][e], P.dims[e].G, Gs, pe, ps, L, C,
+                                                             pbase + part * Gs * C, ex, acc, P.s)));
+                if (ex) written[e] = 1;
                 part += dense_chunks(P.dims[e].G);
             }
-            FEGB_TRY(launch_fold_dense(B.dense_part, (int)part, D.G, C, B.dense_sums, P.s));
-            FEGB_TRY(end_timed(tm));
-            FinalizeParams src{};
-            src.G = D.G;
-            src.C = C;
-            src.sums = B.dense_sums;  // complete sums of -p, compact rows
-            src.counts = D.counts;
-            FEGB_TRY(launch_cg_q<T>(src, C, B.p + P.goff[d] * L, L, B.q + P.goff[d] * C,
-                                    B.pq_part + (size_t)B.pq_block_off[d] * C, P.s));
-            P.projections += 1;
-            P.demean_bytes += bytes;
-            continue;
+            FEGB_TRY(launch_fold_dense(pbase, (int)part, Gs, C, B.dense_sums + B.dsum_off[sd], P.s));
         }
-        // the other many-group dimensions are swept in d's group-sorted order
-        // (identity for the primary); dense dimensions come from their matrices
+        FEGB_TRY(end_timed(tm));
+        P.demean_bytes += bytes;
+    }
+    // 2. the many-group dimensions: each is swept in its group-sorted order
+    // (identity for the primary) over the other many-group dimensions
+    for (int d = 0; d < P.n_fe; ++d) {
+        Dim& D = P.dims[d];
+        if (D.G <= 0 || B.dense[d]) continue;
+        Problem::Timed tm{};
         CGRowsParams<T> rp{};
         rp.n = P.n;
         rp.C = C;
@@ -984,45 +1020,42 @@ int cg_apply(Problem& P, CGBuffers<T>& B) {
         FinalizeParams src{};
         src.G = D.G;
         src.counts = D.counts;
-        const double bytes = rp.n_src > 0 ? cg_operator_bytes(P, sizeof(T), rp.n_src) : 0.0;
         if (rp.n_src > 0) {
+            const double bytes = cg_operator_bytes(P, sizeof(T), rp.n_src);
             FEGB_TRY(begin_timed(tm, 4 + fp32, bytes));
             rp.sums = B.sums;
             rp.head = B.head;
             rp.tail = B.tail;
             FEGB_TRY(launch_cg_rows<T>(rp, P.s));
-            FEGB_TRY(launch_long_sums(D.off, B.head, B.tail, CG_CHUNK, L, D.long_list_cg, D.n_long_cg, B.sums, P.s));
+            FEGB_TRY(launch_group_sums<T>(D.off, B.head, B.tail, CG_CHUNK, C, D.long_list_cg, D.n_long_cg,
+                                          D.multi_list_cg, D.n_multi_cg, B.sums, P.s));
             FEGB_TRY(end_timed(tm));
-            src.C = L;
-            src.off = D.off;
-            src.sums = B.sums;
-            src.head = B.head;
-            src.tail = B.tail;
-            src.R = CG_CHUNK;
+            P.demean_bytes += bytes;
+            src.C = C;  // complete sums, compact rows
+            if constexpr (sizeof(T) == 4)
+                src.sums32 = reinterpret_cast<const float*>(B.sums);
+            else
+                src.sums = reinterpret_cast<const double*>(B.sums);
         } else {
             src.C = C;
             src.sums = nullptr;  // no swept source
         }
-        // the dense dimensions' share: extra = sum_s N_{d,s} p_s
-        const T* extra = nullptr;
-        double xbytes = 0.0;
-        Problem::Timed tx{};
-        for (int s2 = 0; s2 < P.n_fe; ++s2) {
-            if (s2 == d || !B.dense[s2]) continue;
-            if (!extra) FEGB_TRY(begin_timed(tx, 6 + fp32, 0.0));
-            FEGB_TRY(launch_dense_to_groups<T>(B.N[s2][d], D.G, P.dims[s2].G, B.p + P.goff[s2] * L, L, C, B.extra,
-                                               extra ? 1 : 0, P.s));
-            xbytes += (double)D.G * (4.0 * P.dims[s2].G + (double)C * sizeof(T) * (extra ? 2.0 : 1.0));
-            extra = B.extra;
-        }
-        if (extra) {
-            tx.bytes = xbytes;
-            FEGB_TRY(end_timed(tx));
-        }
         FEGB_TRY(launch_cg_q<T>(src, C, B.p + P.goff[d] * L, L, B.q + P.goff[d] * C,
-                                B.pq_part + (size_t)B.pq_block_off[d] * C, P.s, extra));
+                                B.pq_part + (size_t)B.pq_block_off[d] * C, P.s,
+                                B.any_dense ? B.extra + P.goff[d] * C : nullptr));
         P.projections += 1;
-        P.demean_bytes += bytes + xbytes;
+    }
+    // 3. the dimensions with few groups, from their complete sums
+    for (int sd = 0; sd < P.n_fe; ++sd) {
+        if (!B.dense[sd]) continue;
+        FinalizeParams src{};
+        src.G = P.dims[sd].G;
+        src.C = C;
+        src.sums = B.dense_sums + B.dsum_off[sd];  // complete sums of -p, compact rows
+        src.counts = P.dims[sd].counts;
+        FEGB_TRY(launch_cg_q<T>(src, C, B.p + P.goff[sd] * L, L, B.q + P.goff[sd] * C,
+                                B.pq_part + (size_t)B.pq_block_off[sd] * C, P.s));
+        P.projections += 1;
     }
     return launch_fold_partials(B.pq_part, B.pq_blocks, C, B.pq, P.s);
 }
@@ -1658,6 +1691,9 @@ int estimate_on_problem(Problem& P, const fegb_config& cfg, const int* G_all, lo
         FEGB_CUDA(cudaMemsetAsync(acc, 0, sizeof(double) * kk * kk, s), "acc zero");
         const int ncd = (int)cdims.size();
         long long min_single = LLONG_MAX;
+        // subsets whose clusters are single rows, and the meat S'S they all share
+        std::vector<int> row_masks;
+        double* meat_rows = nullptr;
         for (int mask = 1; mask < (1 << ncd) && cluster_ok; ++mask) {
             std::vector<int> sd;
             for (int j = 0; j < ncd; ++j)
@@ -1666,7 +1702,11 @@ int estimate_on_problem(Problem& P, const fegb_config& cfg, const int* G_all, lo
             Scratch sub(s);
             const int32_t *perm = nullptr, *gseq = nullptr, *off = nullptr;
             int n_cl = 0;
-            if (m == 1 && P.dims[sd[0]].mode != MODE_SMALLG) {
+            bool rows = false;  // every cluster of this subset is one row
+            for (int u : row_masks) rows = rows || (mask & u) == u;
+            if (rows && m > 1) {
+                n_cl = (int)n;  // a refinement of single-row clusters: no sort needed
+            } else if (m == 1 && P.dims[sd[0]].mode != MODE_SMALLG) {
                 const Dim& D = P.dims[sd[0]];
                 perm = D.mode == MODE_GATHER ? D.perm : nullptr;
                 gseq = D.gseq;
@@ -1728,11 +1768,26 @@ int estimate_on_problem(Problem& P, const fegb_config& cfg, const int* G_all, lo
                 }
                 min_single = std::min(min_single, nc1);
             }
-            double* Sc = nullptr;
-            FEGB_TRY(sub.alloc(&Sc, (size_t)n_cl * ns, "cluster scores"));
-            FEGB_TRY(cluster_score_sums(P, S, ns, perm, gseq, off, n_cl, Sc, sub));
-            MatView sv{Sc, ns, 1, ns};
-            FEGB_TRY(crossprod_auto(sv, sv, n_cl, true, false, 1.0, 0.0, meat, ns, s, sub));
+            if (m > 1 && !rows && n_cl == n) {
+                rows = true;
+                row_masks.push_back(mask);
+            }
+            if (rows) {
+                // cluster sums of single-row clusters are the score rows: meat = S'S
+                if (!meat_rows) {
+                    FEGB_TRY(scr.alloc(&meat_rows, (size_t)ns * ns, "meat of single-row clusters"));
+                    MatView sv{S, ns, 1, ns};
+                    FEGB_TRY(crossprod_auto(sv, sv, n, true, false, 1.0, 0.0, meat_rows, ns, s, sub));
+                }
+                FEGB_CUDA(cudaMemcpyAsync(meat, meat_rows, sizeof(double) * ns * ns, cudaMemcpyDeviceToDevice, s),
+                          "meat copy");
+            } else {
+                double* Sc = nullptr;
+                FEGB_TRY(sub.alloc(&Sc, (size_t)n_cl * ns, "cluster scores"));
+                FEGB_TRY(cluster_score_sums(P, S, ns, perm, gseq, off, n_cl, Sc, sub));
+                MatView sv{Sc, ns, 1, ns};
+                FEGB_TRY(crossprod_auto(sv, sv, n_cl, true, false, 1.0, 0.0, meat, ns, s, sub));
+            }
             const double* Mk = meat;
             int ldm = ns;
             if (use_iv) {

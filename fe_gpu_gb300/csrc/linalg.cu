@@ -517,105 +517,143 @@ int crossprod(const MatView& A, const MatView& B, long long n, bool gram, bool u
 
 namespace {
 
-constexpr int DS_TR = 64;   // rows per shared-memory tile (and per FP64 fold)
-constexpr int DS_PPT = 4;   // output entries per thread
+constexpr int DS_TR_MAX = 256;  // rows per shared-memory tile (and per FP64 fold), at most
+constexpr int DS_SMEM = 48 * 1024;  // tile bytes aimed at (several blocks per SM)
+constexpr int DS_PPT = 4;       // output entries per thread
 constexpr int DS_PAIRS_PER_BLOCK = CP_THREADS * DS_PPT;
 
-// Largest magnitude the split path accepts: products and 64-row partial sums
+// Largest magnitude the split path accepts: products and 256-row partial sums
 // stay far inside the FP32 range (2^127).
-constexpr double DS_MAX_ABS = 1152921504606846976.0;  // 2^60
-
-// dst[r * w + c] = (hi, lo) of src element (r, c): hi = fl32(x), lo = fl32(x - hi)
-// (x - hi is exact in FP64). *bad is set when a value is not finite or exceeds
-// DS_MAX_ABS; the caller then uses the FP64 path.
-__global__ void split_fp32_kernel(const double* __restrict__ src, long long rs, long long cs, int w, long long n,
-                                  float2* __restrict__ dst, int* __restrict__ bad) {
-    const long long total = n * w;
-    long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    const long long st = (long long)gridDim.x * blockDim.x;
-    bool out_of_range = false;
-    for (; e < total; e += st) {
-        const long long r = e / w;
-        const int c = (int)(e - r * w);
-        const double x = src[r * rs + (long long)c * cs];
-        out_of_range |= !(fabs(x) <= DS_MAX_ABS);
-        const float hi = __double2float_rn(x);
-        const float lo = __double2float_rn(x - (double)hi);
-        dst[e] = make_float2(hi, lo);
-    }
-    if (__any_sync(0xffffffffu, out_of_range) && (threadIdx.x & 31) == 0) atomicOr(bad, 1);
-}
+constexpr double DS_MAX_ABS = 72057594037927936.0;  // 2^56
 
 struct DSParams {
-    const float2* A;  // n x a, row-major
+    const double* A;  // FP64 source, element (r, c) at A[r * ars + c * acs]
+    long long ars, acs;
     int a;
-    const float2* B;  // n x b, row-major (== A for a Gram)
+    const double* B;  // == A for a Gram
+    long long brs, bcs;
     int b;
     long long n;
     int gram;
     long long p0;     // first pair of this launch
     int npairs;
+    int phases;       // row phases (PPT == 1)
     long long rows_per_block;
+    int tr;            // rows per tile
     double* partials;  // row blocks x npairs
+    int* bad;          // set when a value is not finite or exceeds DS_MAX_ABS
 };
 
+// Tile rows [row0, row0 + rows) of an FP64 source into shared memory as
+// (hi, lo) FP32 pairs: hi = fl32(x), lo = fl32(x - hi) (x - hi is exact in FP64).
+__device__ __forceinline__ bool load_split_tile(float2* dst, const double* src, long long rs, long long cs, int width,
+                                                long long row0, int rows) {
+    const int total = rows * width;
+    bool out_of_range = false;
+    for (int e = threadIdx.x; e < total; e += blockDim.x) {
+        int r, c;
+        if (rs == 1) {  // column-major source: consecutive threads walk rows
+            r = e % rows;
+            c = e / rows;
+        } else {
+            r = e / width;
+            c = e - r * width;
+        }
+        const double x = src[(row0 + r) * rs + (long long)c * cs];
+        out_of_range |= !(fabs(x) <= DS_MAX_ABS);
+        const float hi = __double2float_rn(x);
+        dst[r * width + c] = make_float2(hi, __double2float_rn(x - (double)hi));
+    }
+    return out_of_range;
+}
+
+// acc_hi/acc_lo (+)= x * y in double-single arithmetic:
+// (xh + xl)(yh + yl) = ph + pe + cross with ph + pe exact (TwoProd by FMA);
+// TwoSum of the running high part and ph, its rounding error into the low part.
+// (The _rn intrinsics are never contracted into FMAs, which TwoSum relies on.)
+__device__ __forceinline__ void ds_fma(float2 x, float2 y, float& sh, float& sl) {
+    const float ph = __fmul_rn(x.x, y.x);
+    const float pe = fmaf(x.x, y.x, -ph);
+    const float cr = fmaf(x.x, y.y, x.y * y.x);
+    const float s1 = __fadd_rn(sh, ph);
+    const float bb = __fsub_rn(s1, sh);
+    const float err = __fadd_rn(__fsub_rn(sh, __fsub_rn(s1, bb)), __fsub_rn(ph, bb));
+    sh = s1;
+    sl += err + (pe + cr);
+}
+
+// PPT output entries per thread; PPT == 1: few pairs, the threads of a block
+// split each tile's rows into p.phases row phases (folded in a fixed order).
+// Each tile's double-single sums are folded into FP64 accumulators.
+template <int PPT>
 __global__ void __launch_bounds__(CP_THREADS) crossprod_split_kernel(DSParams p) {
     extern __shared__ float2 dsm[];
     float2* sA = dsm;
-    float2* sB = p.gram ? dsm : dsm + DS_TR * p.a;
+    float2* sB = p.gram ? dsm : dsm + p.tr * p.a;
     const int t = threadIdx.x;
-    const int chunk0 = blockIdx.y * DS_PAIRS_PER_BLOCK;
-    int pi[DS_PPT], pj[DS_PPT];
-    bool pv[DS_PPT];
-    float sh[DS_PPT], sl[DS_PPT];
-    double acc[DS_PPT];
+    const int chunk0 = PPT == 1 ? 0 : blockIdx.y * CP_THREADS * PPT;
+    int pi[PPT], pj[PPT];
+    bool pv[PPT];
+    double acc[PPT];
+    int phase = 0;
+    if (PPT == 1) {
+        const int local = t % p.npairs;
+        phase = t / p.npairs;
+        pv[0] = phase < p.phases;
+        pair_ij(p.p0 + local, p.gram, p.a, pi[0], pj[0]);
+        acc[0] = 0.0;
+    } else {
 #pragma unroll
-    for (int s = 0; s < DS_PPT; ++s) {
-        const int local = chunk0 + t + s * CP_THREADS;
-        pv[s] = local < p.npairs;
-        pair_ij(p.p0 + (pv[s] ? local : 0), p.gram, p.a, pi[s], pj[s]);
-        sh[s] = 0.f;
-        sl[s] = 0.f;
-        acc[s] = 0.0;
+        for (int s = 0; s < PPT; ++s) {
+            const int local = chunk0 + t + s * CP_THREADS;
+            pv[s] = local < p.npairs;
+            pair_ij(p.p0 + (pv[s] ? local : 0), p.gram, p.a, pi[s], pj[s]);
+            acc[s] = 0.0;
+        }
     }
+    bool bad = false;
     const long long r0 = (long long)blockIdx.x * p.rows_per_block;
     const long long r1 = min(p.n, r0 + p.rows_per_block);
-    for (long long tile = r0; tile < r1; tile += DS_TR) {
-        const int rows = (int)min((long long)DS_TR, r1 - tile);
-        for (int e = t; e < rows * p.a; e += CP_THREADS) sA[e] = p.A[tile * p.a + e];
-        if (!p.gram)
-            for (int e = t; e < rows * p.b; e += CP_THREADS) sB[e] = p.B[tile * p.b + e];
+    for (long long tile = r0; tile < r1; tile += p.tr) {
+        const int rows = (int)min((long long)p.tr, r1 - tile);
+        bad |= load_split_tile(sA, p.A, p.ars, p.acs, p.a, tile, rows);
+        if (!p.gram) bad |= load_split_tile(sB, p.B, p.brs, p.bcs, p.b, tile, rows);
         __syncthreads();
-        for (int r = 0; r < rows; ++r) {
-#pragma unroll
-            for (int s = 0; s < DS_PPT; ++s) {
-                if (!pv[s]) continue;
-                const float2 x = sA[r * p.a + pi[s]];
-                const float2 y = sB[r * p.b + pj[s]];
-                // (xh + xl)(yh + yl) = ph + pe + cross, ph + pe exact (TwoProd by FMA)
-                // (the _rn intrinsics are never contracted into FMAs, which TwoSum relies on)
-                const float ph = __fmul_rn(x.x, y.x);
-                const float pe = fmaf(x.x, y.x, -ph);
-                const float cr = fmaf(x.x, y.y, x.y * y.x);
-                // TwoSum of the running high part and ph; the rounding error goes to sl
-                const float s1 = __fadd_rn(sh[s], ph);
-                const float bb = __fsub_rn(s1, sh[s]);
-                const float err = __fadd_rn(__fsub_rn(sh[s], __fsub_rn(s1, bb)), __fsub_rn(ph, bb));
-                sh[s] = s1;
-                sl[s] += err + (pe + cr);
+        if (PPT == 1) {
+            if (pv[0]) {
+                float sh = 0.f, sl = 0.f;
+                for (int r = phase; r < rows; r += p.phases) ds_fma(sA[r * p.a + pi[0]], sB[r * p.b + pj[0]], sh, sl);
+                acc[0] += (double)sh + (double)sl;
             }
-        }
+        } else {
+            float sh[PPT], sl[PPT];
 #pragma unroll
-        for (int s = 0; s < DS_PPT; ++s) {
-            acc[s] += (double)sh[s] + (double)sl[s];
-            sh[s] = 0.f;
-            sl[s] = 0.f;
+            for (int s = 0; s < PPT; ++s) sh[s] = sl[s] = 0.f;
+            for (int r = 0; r < rows; ++r) {
+#pragma unroll
+                for (int s = 0; s < PPT; ++s)
+                    if (pv[s]) ds_fma(sA[r * p.a + pi[s]], sB[r * p.b + pj[s]], sh[s], sl[s]);
+            }
+#pragma unroll
+            for (int s = 0; s < PPT; ++s) acc[s] += (double)sh[s] + (double)sl[s];
         }
         __syncthreads();
     }
+    if (__any_sync(0xffffffffu, bad) && (t & 31) == 0) atomicOr(p.bad, 1);
+    if (PPT == 1) {
+        __shared__ double fold[CP_THREADS];
+        fold[t] = pv[0] ? acc[0] : 0.0;
+        __syncthreads();
+        if (t < p.npairs) {
+            double v = 0.0;
+            for (int ph = 0; ph < p.phases; ++ph) v += fold[ph * p.npairs + t];
+            p.partials[(long long)blockIdx.x * p.npairs + t] = v;
+        }
+    } else {
 #pragma unroll
-    for (int s = 0; s < DS_PPT; ++s)
-        if (pv[s]) p.partials[(long long)blockIdx.x * p.npairs + chunk0 + t + s * CP_THREADS] = acc[s];
+        for (int s = 0; s < PPT; ++s)
+            if (pv[s]) p.partials[(long long)blockIdx.x * p.npairs + chunk0 + t + s * CP_THREADS] = acc[s];
+    }
 }
 
 }  // namespace
@@ -625,61 +663,74 @@ int crossprod_split(const MatView& A, const MatView& B, long long n, bool gram, 
     const int a = A.cols, b = gram ? A.cols : B.cols;
     if (a <= 0 || b <= 0) return 0;
     if (n <= 0) return crossprod(A, B, n, gram, upper_only, alpha, beta, out, ldo, s, scr);
-    const size_t smem = sizeof(float2) * DS_TR * (gram ? a : a + b);
-    if (smem > 200 * 1024) return crossprod(A, B, n, gram, upper_only, alpha, beta, out, ldo, s, scr);
-    static const cudaError_t attr_status =
-        cudaFuncSetAttribute(crossprod_split_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    const int width = gram ? a : a + b;
+    if (sizeof(float2) * 16 * (size_t)width > 200 * 1024)
+        return crossprod(A, B, n, gram, upper_only, alpha, beta, out, ldo, s, scr);
+    const int tr = std::max(16, std::min(DS_TR_MAX, (int)(DS_SMEM / (sizeof(float2) * width)) / 16 * 16));
+    const size_t smem = sizeof(float2) * (size_t)tr * width;
+    static const cudaError_t attr_status = []() {
+        cudaError_t e = cudaFuncSetAttribute(crossprod_split_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             200 * 1024);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(crossprod_split_kernel<DS_PPT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     200 * 1024);
+        return e;
+    }();
     if (attr_status != cudaSuccess) return set_cuda_error(attr_status, "split crossprod attr");
-    float2 *sa = nullptr, *sb = nullptr;
     int* bad = nullptr;
     FEGB_TRY(scr.alloc(&bad, 1, "split range flag"));
     FEGB_CUDA(cudaMemsetAsync(bad, 0, sizeof(int), s), "split flag reset");
-    FEGB_TRY(scr.alloc(&sa, (size_t)n * a, "split A"));
-    split_fp32_kernel<<<grid_stride_blocks(n * a, 256), 256, 0, s>>>(A.ptr, A.rs, A.cs, a, n, sa, bad);
-    FEGB_LAUNCH_CHECK("split A");
-    if (!gram) {
-        FEGB_TRY(scr.alloc(&sb, (size_t)n * b, "split B"));
-        split_fp32_kernel<<<grid_stride_blocks(n * b, 256), 256, 0, s>>>(B.ptr, B.rs, B.cs, b, n, sb, bad);
-        FEGB_LAUNCH_CHECK("split B");
-    }
-    int hbad = 0;
-    FEGB_CUDA(cudaMemcpyAsync(&hbad, bad, sizeof(int), cudaMemcpyDeviceToHost, s), "split flag copy");
-    FEGB_CUDA(cudaStreamSynchronize(s), "split flag sync");
-    if (hbad) return crossprod(A, B, n, gram, upper_only, alpha, beta, out, ldo, s, scr);
     const long long total_pairs = gram ? (long long)a * (a + 1) / 2 : (long long)a * b;
-    long long nb = std::min<long long>((n + DS_TR - 1) / DS_TR, (long long)num_sms() * 4);
+    long long nb = std::min<long long>((n + tr - 1) / tr, (long long)num_sms() * 8);
     long long rpb = (n + nb - 1) / nb;
-    rpb = ((rpb + DS_TR - 1) / DS_TR) * DS_TR;
+    rpb = ((rpb + tr - 1) / tr) * tr;
     nb = (n + rpb - 1) / rpb;
     for (long long p0 = 0; p0 < total_pairs; p0 += CP_MAXPAIRS_LAUNCH) {
         const int np = (int)std::min<long long>(CP_MAXPAIRS_LAUNCH, total_pairs - p0);
         double* partials = nullptr;
         FEGB_TRY(scr.alloc(&partials, (size_t)nb * np, "split crossprod partials"));
         DSParams p;
-        p.A = sa;
+        p.A = A.ptr;
+        p.ars = A.rs;
+        p.acs = A.cs;
         p.a = a;
-        p.B = gram ? sa : sb;
+        p.B = gram ? A.ptr : B.ptr;
+        p.brs = gram ? A.rs : B.rs;
+        p.bcs = gram ? A.cs : B.cs;
         p.b = b;
         p.n = n;
         p.gram = gram ? 1 : 0;
         p.p0 = p0;
         p.npairs = np;
+        p.phases = np <= 128 ? CP_THREADS / np : 1;
         p.rows_per_block = rpb;
+        p.tr = tr;
         p.partials = partials;
-        dim3 grid((unsigned)nb, (unsigned)((np + DS_PAIRS_PER_BLOCK - 1) / DS_PAIRS_PER_BLOCK));
-        crossprod_split_kernel<<<grid, CP_THREADS, smem, s>>>(p);
+        p.bad = bad;
+        if (np <= 128) {
+            crossprod_split_kernel<1><<<(unsigned)nb, CP_THREADS, smem, s>>>(p);
+        } else {
+            dim3 grid((unsigned)nb, (unsigned)((np + DS_PAIRS_PER_BLOCK - 1) / DS_PAIRS_PER_BLOCK));
+            crossprod_split_kernel<DS_PPT><<<grid, CP_THREADS, smem, s>>>(p);
+        }
         FEGB_LAUNCH_CHECK("split crossprod");
         crossprod_reduce_kernel<<<(np + 255) / 256, 256, 0, s>>>(partials, (int)nb, np, p0, gram, upper_only, a, alpha,
                                                                   beta, out, ldo);
         FEGB_LAUNCH_CHECK("split crossprod reduce");
     }
+    int hbad = 0;
+    FEGB_CUDA(cudaMemcpyAsync(&hbad, bad, sizeof(int), cudaMemcpyDeviceToHost, s), "split flag copy");
+    FEGB_CUDA(cudaStreamSynchronize(s), "split flag sync");
+    // a value outside the split range: the whole product again in FP64
+    if (hbad) return crossprod(A, B, n, gram, upper_only, alpha, beta, out, ldo, s, scr);
     return 0;
 }
 
 int crossprod_auto(const MatView& A, const MatView& B, long long n, bool gram, bool upper_only, double alpha,
                    double beta, double* out, int ldo, cudaStream_t s, Scratch& scr) {
     const long long pairs = gram ? (long long)A.cols * (A.cols + 1) / 2 : (long long)A.cols * B.cols;
-    if (pairs >= CROSSPROD_SPLIT_MIN_PAIRS && n >= 4096)
+    const long long cols = gram ? A.cols : (long long)A.cols + B.cols;
+    if (pairs >= CROSSPROD_SPLIT_PAIRS_PER_COL * cols && n >= 4096)
         return crossprod_split(A, B, n, gram, upper_only, alpha, beta, out, ldo, s, scr);
     return crossprod(A, B, n, gram, upper_only, alpha, beta, out, ldo, s, scr);
 }

@@ -28,9 +28,11 @@ int crossprod(const MatView& A, const MatView& B, long long n, bool gram, bool u
 // (TwoProd by FMA plus the cross terms), summed with TwoSum into an FP32 pair
 // per output and folded into FP64 every tile of rows. Relative error per term
 // about 2^-47, against 2^-53 for FP64 products; GB300 issues FP32 at about 60x
-// its FP64 rate, so wide cross products run several times faster. Used by the
-// estimator when an output has at least CROSSPROD_SPLIT_MIN_PAIRS entries.
-constexpr long long CROSSPROD_SPLIT_MIN_PAIRS = 300;
+// its FP64 rate, so cross products whose FP64 form is bound by the FP64 pipe
+// (outputs at least CROSSPROD_SPLIT_PAIRS_PER_COL times the input columns)
+// run several times faster. The FP64 values are split while a tile is loaded;
+// a value beyond the split range sends the whole product to the FP64 path.
+constexpr long long CROSSPROD_SPLIT_PAIRS_PER_COL = 3;
 int crossprod_split(const MatView& A, const MatView& B, long long n, bool gram, bool upper_only, double alpha,
                     double beta, double* out, int ldo, cudaStream_t s, Scratch& scr);
 // crossprod_split when the output is large enough, else crossprod.

@@ -203,13 +203,14 @@ __device__ __forceinline__ double source_sum(const FinalizeParams& p, int g, int
     if (p.partials) {
         for (int b = 0; b < p.nblocks; ++b) sum += p.partials[(long long)b * total + idx];
     } else if (!p.off) {
-        sum = p.sums ? p.sums[idx] : 0.0;  // null: no swept source contributes
+        // null: no swept source contributes
+        sum = p.sums32 ? (double)p.sums32[idx] : (p.sums ? p.sums[idx] : 0.0);
     } else {
         const int s = p.off[g], e = p.off[g + 1];
         if (e > s) {
             const long long qs = s / p.R, qe = (e - 1) / p.R;
             if (qs == qe || qe - qs > SEG_LONG_SPAN) {
-                sum = p.sums[idx];  // complete run, or folded by launch_long_sums
+                sum = p.sums32 ? (double)p.sums32[idx] : p.sums[idx];  // complete run, or folded by launch_long_sums
             } else {
                 sum = p.tail[qs * p.C + c];
                 for (long long q = qs + 1; q <= qe; ++q) sum += p.head[q * p.C + c];
@@ -328,11 +329,152 @@ __device__ __forceinline__ void column_partials(A prod, long long base, int C, A
     }
 }
 
+// ---- row-tiled CG vector kernels ----
+// A block covers VEC_STEPS steps of rps = 256 / C rows of a G x C table
+// (C <= 256); thread t handles column c = t % C of rows g0 + t / C + rps * k,
+// so its column is fixed: products accumulate in one register per thread (in
+// T, VEC_STEPS terms at most) and each block writes one FP64 partial per
+// column, folded in row order. 32-bit index arithmetic per thread.
+struct VecLane {
+    int c;       // column
+    int rr;      // row within a step
+    int rps;     // rows per step
+    bool active;
+};
+
+__device__ __forceinline__ VecLane vec_lane(int C) {
+    VecLane v;
+    v.rps = 256 / C;
+    v.rr = (int)threadIdx.x / C;
+    v.c = (int)threadIdx.x - v.rr * C;
+    v.active = v.rr < v.rps;
+    return v;
+}
+
+// partial[c] of this block = sum over its threads of column c (rows in order)
+__device__ __forceinline__ void vec_column_partials(double prod, const VecLane& v, int C, double* red, double* out) {
+    red[threadIdx.x] = v.active ? prod : 0.0;
+    __syncthreads();
+    if ((int)threadIdx.x < C) {
+        double acc = 0.0;
+        for (int j = 0; j < v.rps; ++j) acc += red[j * C + threadIdx.x];
+        out[(long long)blockIdx.x * C + threadIdx.x] = acc;
+    }
+}
+
+__device__ __forceinline__ void vec_block_max(double m, double* red8, double* out) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) red8[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double mm = red8[0];
+        for (int w = 1; w < 8; ++w) mm = fmax(mm, red8[w]);
+        out[blockIdx.x] = mm;
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) cg_q_rows_kernel(FinalizeParams src, int C, const T* __restrict__ p, int pld,
+                                                        T* __restrict__ q, double* __restrict__ pq_partials,
+                                                        const T* __restrict__ extra) {
+    __shared__ double red[256];
+    const VecLane v = vec_lane(C);
+    T prod = T(0);
+    if (v.active) {
+        const long long g0 = (long long)blockIdx.x * v.rps * VEC_STEPS + v.rr;
+#pragma unroll 4
+        for (int k = 0; k < VEC_STEPS; ++k) {
+            const long long gl = g0 + (long long)k * v.rps;
+            if (gl >= src.G) break;
+            const int g = (int)gl;
+            const long long idx = gl * C + v.c;
+            const int cnt = src.counts[g];
+            // ssum = -(sum over the group's rows of the other dimensions' p); a group
+            // without rows has none (and no sum written)
+            const double ssum = cnt > 0 ? source_sum(src, g, v.c, gl * src.C + v.c, (long long)src.G * src.C) : 0.0;
+            const T pv = p[gl * pld + v.c];
+            T qv = (T)cnt * pv - (T)ssum;
+            if (extra) qv += extra[idx];
+            q[idx] = qv;
+            prod += pv * qv;
+        }
+    }
+    vec_column_partials((double)prod, v, C, red, pq_partials);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) cg_update_rows_kernel(long long Gt, int C, const T* __restrict__ inv_counts,
+                                                             const double* __restrict__ rz,
+                                                             const double* __restrict__ pq, const T* __restrict__ p,
+                                                             int pld, const T* __restrict__ q, T* __restrict__ x,
+                                                             T* __restrict__ r, T* __restrict__ z,
+                                                             double* __restrict__ rz_partials,
+                                                             double* __restrict__ zmax_partials) {
+    __shared__ double red[256];
+    __shared__ double red8[8];
+    const VecLane v = vec_lane(C);
+    T prod = T(0), az = T(0);
+    if (v.active) {
+        const double den = pq[v.c];
+        const T a = (T)(den != 0.0 ? rz[v.c] / den : 0.0);
+        const long long g0 = (long long)blockIdx.x * v.rps * VEC_STEPS + v.rr;
+#pragma unroll 4
+        for (int k = 0; k < VEC_STEPS; ++k) {
+            const long long g = g0 + (long long)k * v.rps;
+            if (g >= Gt) break;
+            const long long idx = g * C + v.c;
+            x[idx] += a * p[g * pld + v.c];
+            const T rv = r[idx] - a * q[idx];
+            const T zv = rv * inv_counts[g];
+            r[idx] = rv;
+            z[idx] = zv;
+            prod += rv * zv;
+            const T m = zv < T(0) ? -zv : zv;
+            az = m > az ? m : az;
+        }
+    }
+    vec_column_partials((double)prod, v, C, red, rz_partials);
+    vec_block_max((double)az, red8, zmax_partials);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) cg_init_rows_kernel(long long Gt, int C, const int32_t* __restrict__ counts,
+                                                           const double* __restrict__ mu, T* __restrict__ r,
+                                                           T* __restrict__ z, T* __restrict__ p, int pld,
+                                                           T* __restrict__ x, double* __restrict__ rz_partials,
+                                                           double* __restrict__ zmax_partials) {
+    __shared__ double red[256];
+    __shared__ double red8[8];
+    const VecLane v = vec_lane(C);
+    T prod = T(0), az = T(0);
+    if (v.active) {
+        const long long g0 = (long long)blockIdx.x * v.rps * VEC_STEPS + v.rr;
+        for (int k = 0; k < VEC_STEPS; ++k) {
+            const long long g = g0 + (long long)k * v.rps;
+            if (g >= Gt) break;
+            const long long idx = g * C + v.c;
+            const int cnt = counts[g];
+            const T m = cnt > 0 ? (T)mu[idx] : T(0);
+            const T rv = (T)cnt * m;
+            r[idx] = rv;
+            z[idx] = m;
+            p[g * pld + v.c] = m;
+            x[idx] = T(0);
+            prod += rv * m;
+            const T am = m < T(0) ? -m : m;
+            az = am > az ? am : az;
+        }
+    }
+    vec_column_partials((double)prod, v, C, red, rz_partials);
+    vec_block_max((double)az, red8, zmax_partials);
+}
+
 template <typename T>
 __global__ void __launch_bounds__(FIN_THREADS) cg_q_kernel(FinalizeParams src, int C, const T* __restrict__ p,
                                                             int pld, T* __restrict__ q, double* __restrict__ pq_partials,
                                                             const T* __restrict__ extra) {
-    // compact elements (g, c < C); the sweep sums use the padded stride src.C, p uses pld
+    // compact elements (g, c < C); p uses the padded stride pld
     __shared__ T smem[FIN_THREADS];
     const long long total = (long long)src.G * C;
     const long long base = (long long)blockIdx.x * FIN_THREADS;
@@ -379,10 +521,11 @@ __global__ void __launch_bounds__(FIN_THREADS)
 
 // One block per long group: tail of its first chunk plus the heads of the
 // following chunks, for every column.
+template <typename S>
 __global__ void __launch_bounds__(FIN_THREADS)
     long_sums_kernel(const int32_t* __restrict__ off, const double* __restrict__ head,
                      const double* __restrict__ tail, int R, int C, const int32_t* __restrict__ list,
-                     double* __restrict__ sums) {
+                     S* __restrict__ sums) {
     __shared__ double smem[FIN_THREADS];
     const int g = list[blockIdx.x];
     const long long qs = off[g] / R, qe = (off[g + 1] - 1) / R;
@@ -390,7 +533,7 @@ __global__ void __launch_bounds__(FIN_THREADS)
         double acc = 0.0;
         for (long long q = qs + 1 + threadIdx.x; q <= qe; q += FIN_THREADS) acc += head[q * C + c];
         double t = block_tree_sum(acc, smem);
-        if (threadIdx.x == 0) sums[(long long)g * C + c] = tail[qs * C + c] + t;
+        if (threadIdx.x == 0) sums[(long long)g * C + c] = (S)(tail[qs * C + c] + t);
     }
 }
 
@@ -414,6 +557,49 @@ __global__ void find_long_kernel(const int32_t* __restrict__ off, int G, int R, 
     if (g >= G) return;
     const int s = off[g], e = off[g + 1];
     if (e > s && (long long)((e - 1) / R) - (long long)(s / R) > SEG_LONG_SPAN) list[atomicAdd(count, 1)] = g;
+}
+
+// groups whose segment run crosses 1..SEG_LONG_SPAN chunk boundaries
+__global__ void find_multi_kernel(const int32_t* __restrict__ off, int G, int R, int32_t* __restrict__ list,
+                                  int* __restrict__ count) {
+    int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= G) return;
+    const int s = off[g], e = off[g + 1];
+    if (e <= s) return;
+    const long long span = (long long)((e - 1) / R) - (long long)(s / R);
+    if (span >= 1 && span <= SEG_LONG_SPAN) list[atomicAdd(count, 1)] = g;
+}
+
+// Completes the sums of the groups whose run crosses chunk boundaries: blocks
+// [0, n_long) take one long group each (block tree over its chunk heads),
+// later blocks take 8 multi-chunk groups, one warp each (lane = column,
+// heads in chunk order). sums[g * C + c] = tail[qs] + head[qs + 1] + ... + head[qe].
+template <typename S>
+__global__ void __launch_bounds__(FIN_THREADS)
+    group_sums_kernel(const int32_t* __restrict__ off, const double* __restrict__ head,
+                      const double* __restrict__ tail, int R, int C, const int32_t* __restrict__ long_list,
+                      int n_long, const int32_t* __restrict__ multi_list, int n_multi, S* __restrict__ sums) {
+    __shared__ double smem[FIN_THREADS];
+    if ((int)blockIdx.x < n_long) {
+        const int g = long_list[blockIdx.x];
+        const long long qs = off[g] / R, qe = (off[g + 1] - 1) / R;
+        for (int c = 0; c < C; ++c) {
+            double acc = 0.0;
+            for (long long q = qs + 1 + threadIdx.x; q <= qe; q += FIN_THREADS) acc += head[q * C + c];
+            const double t = block_tree_sum(acc, smem);
+            if (threadIdx.x == 0) sums[(long long)g * C + c] = (S)(tail[qs * C + c] + t);
+        }
+        return;
+    }
+    const long long w = (long long)(blockIdx.x - n_long) * (FIN_THREADS / 32) + (threadIdx.x >> 5);
+    if (w >= n_multi) return;
+    const int g = multi_list[w];
+    const long long qs = off[g] / R, qe = (off[g + 1] - 1) / R;
+    for (int c = threadIdx.x & 31; c < C; c += 32) {
+        double acc = tail[qs * C + c];
+        for (long long q = qs + 1; q <= qe; ++q) acc += head[q * C + c];
+        sums[(long long)g * C + c] = (S)acc;
+    }
 }
 
 template <typename T>
@@ -652,14 +838,24 @@ int launch_convert_f64_f32(const double* src, float* dst, long long n, cudaStrea
 }
 
 
-int cg_partial_blocks(long long gc) { return (int)((gc + FIN_THREADS - 1) / FIN_THREADS); }
+int cg_partial_blocks(long long G, int C) {
+    if (C <= 256) {
+        const long long rows = (long long)(256 / C) * VEC_STEPS;
+        return (int)((G + rows - 1) / rows);
+    }
+    return (int)((G * C + FIN_THREADS - 1) / FIN_THREADS);
+}
 
 template <typename T>
 int launch_cg_q(const FinalizeParams& src, int C, const T* p, int pld, T* q, double* pq_partials, cudaStream_t s,
                 const T* extra) {
     long long total = (long long)src.G * C;
     if (total <= 0) return 0;
-    cg_q_kernel<T><<<cg_partial_blocks(total), FIN_THREADS, 0, s>>>(src, C, p, pld, q, pq_partials, extra);
+    const int nb = cg_partial_blocks(src.G, C);
+    if (C <= 256)
+        cg_q_rows_kernel<T><<<nb, 256, 0, s>>>(src, C, p, pld, q, pq_partials, extra);
+    else
+        cg_q_kernel<T><<<nb, FIN_THREADS, 0, s>>>(src, C, p, pld, q, pq_partials, extra);
     FEGB_LAUNCH_CHECK("cg q");
     return 0;
 }
@@ -669,6 +865,36 @@ int launch_fold_partials(const double* partials, int nb, int C, double* out, cud
     FEGB_LAUNCH_CHECK("fold partials");
     return 0;
 }
+
+int find_multi_groups(const int32_t* off, int G, int R, int32_t* list, int* n_multi, cudaStream_t s) {
+    *n_multi = 0;
+    if (G <= 0) return 0;
+    int* cnt = nullptr;
+    FEGB_CUDA(cudaMallocAsync(&cnt, sizeof(int), s), "multi groups counter");
+    FEGB_CUDA(cudaMemsetAsync(cnt, 0, sizeof(int), s), "multi groups reset");
+    find_multi_kernel<<<(G + 255) / 256, 256, 0, s>>>(off, G, R, list, cnt);
+    FEGB_LAUNCH_CHECK("find multi-chunk groups");
+    FEGB_CUDA(cudaMemcpyAsync(n_multi, cnt, sizeof(int), cudaMemcpyDeviceToHost, s), "multi groups count");
+    FEGB_CUDA(cudaFreeAsync(cnt, s), "multi groups free");
+    FEGB_CUDA(cudaStreamSynchronize(s), "multi groups sync");
+    return 0;
+}
+
+template <typename S>
+int launch_group_sums(const int32_t* off, const double* head, const double* tail, int R, int C,
+                      const int32_t* long_list, int n_long, const int32_t* multi_list, int n_multi, S* sums,
+                      cudaStream_t s) {
+    const long long nb = (long long)n_long + ((long long)n_multi + FIN_THREADS / 32 - 1) / (FIN_THREADS / 32);
+    if (nb <= 0) return 0;
+    group_sums_kernel<S><<<(unsigned)nb, FIN_THREADS, 0, s>>>(off, head, tail, R, C, long_list, n_long, multi_list,
+                                                              n_multi, sums);
+    FEGB_LAUNCH_CHECK("group sums across chunks");
+    return 0;
+}
+template int launch_group_sums<float>(const int32_t*, const double*, const double*, int, int, const int32_t*, int,
+                                      const int32_t*, int, float*, cudaStream_t);
+template int launch_group_sums<double>(const int32_t*, const double*, const double*, int, int, const int32_t*, int,
+                                       const int32_t*, int, double*, cudaStream_t);
 
 int find_long_groups(const int32_t* off, int G, int R, int32_t* list, int* n_long, cudaStream_t s) {
     *n_long = 0;
@@ -684,12 +910,23 @@ int find_long_groups(const int32_t* off, int G, int R, int32_t* list, int* n_lon
     return 0;
 }
 
-int launch_long_sums(const int32_t* off, const double* head, const double* tail, int R, int C, const int32_t* list,
-                     int n_long, double* sums, cudaStream_t s) {
+template <typename S>
+int long_sums_t(const int32_t* off, const double* head, const double* tail, int R, int C, const int32_t* list,
+                int n_long, S* sums, cudaStream_t s) {
     if (n_long <= 0) return 0;
-    long_sums_kernel<<<n_long, FIN_THREADS, 0, s>>>(off, head, tail, R, C, list, sums);
+    long_sums_kernel<S><<<n_long, FIN_THREADS, 0, s>>>(off, head, tail, R, C, list, sums);
     FEGB_LAUNCH_CHECK("long group sums");
     return 0;
+}
+
+int launch_long_sums(const int32_t* off, const double* head, const double* tail, int R, int C, const int32_t* list,
+                     int n_long, double* sums, cudaStream_t s) {
+    return long_sums_t<double>(off, head, tail, R, C, list, n_long, sums, s);
+}
+
+int launch_long_sums(const int32_t* off, const double* head, const double* tail, int R, int C, const int32_t* list,
+                     int n_long, float* sums, cudaStream_t s) {
+    return long_sums_t<float>(off, head, tail, R, C, list, n_long, sums, s);
 }
 
 int launch_fold_smallg(const double* partials, int nblocks, int G, int C, double* sums, cudaStream_t s) {
@@ -713,9 +950,13 @@ int launch_cg_update(long long Gt, int C, const T* inv_counts, const double* rz,
                      unsigned long long* zmax, cudaStream_t s) {
     long long total = Gt * C;
     if (total <= 0) return 0;
-    const int nb = cg_partial_blocks(total);
-    cg_update_kernel<T><<<nb, FIN_THREADS, 0, s>>>(Gt, C, inv_counts, rz, pq, p, pld, q, x, r, z, rz_partials,
-                                                   zmax_partials);
+    const int nb = cg_partial_blocks(Gt, C);
+    if (C <= 256)
+        cg_update_rows_kernel<T><<<nb, 256, 0, s>>>(Gt, C, inv_counts, rz, pq, p, pld, q, x, r, z, rz_partials,
+                                                    zmax_partials);
+    else
+        cg_update_kernel<T><<<nb, FIN_THREADS, 0, s>>>(Gt, C, inv_counts, rz, pq, p, pld, q, x, r, z, rz_partials,
+                                                       zmax_partials);
     FEGB_LAUNCH_CHECK("cg update");
     fold_max_kernel<<<1, FIN_THREADS, 0, s>>>(zmax_partials, nb, zmax);
     FEGB_LAUNCH_CHECK("cg max fold");
@@ -741,8 +982,12 @@ int launch_cg_init(long long Gt, int C, const int32_t* counts, const double* mu,
                    double* rz_partials, double* zmax_partials, unsigned long long* zmax, cudaStream_t s) {
     long long total = Gt * C;
     if (total <= 0) return 0;
-    const int nb = cg_partial_blocks(total);
-    cg_init_kernel<T><<<nb, FIN_THREADS, 0, s>>>(Gt, C, counts, mu, r, z, p, pld, x, rz_partials, zmax_partials);
+    const int nb = cg_partial_blocks(Gt, C);
+    if (C <= 256)
+        cg_init_rows_kernel<T><<<nb, 256, 0, s>>>(Gt, C, counts, mu, r, z, p, pld, x, rz_partials, zmax_partials);
+    else
+        cg_init_kernel<T><<<nb, FIN_THREADS, 0, s>>>(Gt, C, counts, mu, r, z, p, pld, x, rz_partials,
+                                                     zmax_partials);
     FEGB_LAUNCH_CHECK("cg init");
     fold_max_kernel<<<1, FIN_THREADS, 0, s>>>(zmax_partials, nb, zmax);
     FEGB_LAUNCH_CHECK("cg max fold");
@@ -770,73 +1015,257 @@ int launch_count_pairs(const int32_t* gid_e, const int32_t* gid_s, long long n, 
     return 0;
 }
 
-// Block b covers groups [b * per, (b + 1) * per) of e in tiles of
-// DENSE_TILE groups: the tile's count rows and p rows are staged in shared
-// memory, thread tc (t = tc / C, c = tc % C; up to DENSE_MAX_TC / 256 per
-// thread) sums the tile in the storage type and adds the tile total to an
-// FP64 accumulator. One partial per block, in a fixed order.
+__global__ void count_max_kernel(const uint32_t* __restrict__ N, long long cnt, unsigned* __restrict__ mx) {
+    unsigned m = 0;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < cnt; i += (long long)gridDim.x * blockDim.x)
+        m = max(m, N[i]);
+    for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(mx, m);  // integer max: order-free
+}
+
+__global__ void narrow_counts_kernel(const uint32_t* __restrict__ N, long long cnt, uint8_t* __restrict__ out) {
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < cnt; i += (long long)gridDim.x * blockDim.x)
+        out[i] = (uint8_t)N[i];
+}
+
+int launch_count_max(const uint32_t* N, long long cnt, unsigned* mx, cudaStream_t s) {
+    FEGB_CUDA(cudaMemsetAsync(mx, 0, sizeof(unsigned), s), "count max reset");
+    if (cnt <= 0) return 0;
+    count_max_kernel<<<grid_stride_blocks(cnt, 256), 256, 0, s>>>(N, cnt, mx);
+    FEGB_LAUNCH_CHECK("count max");
+    return 0;
+}
+
+int launch_narrow_counts(const uint32_t* N, long long cnt, uint8_t* out, cudaStream_t s) {
+    if (cnt <= 0) return 0;
+    narrow_counts_kernel<<<grid_stride_blocks(cnt, 256), 256, 0, s>>>(N, cnt, out);
+    FEGB_LAUNCH_CHECK("narrow counts");
+    return 0;
+}
+
+namespace {
+
+constexpr int DENSE_WARPS = 8;
+
+// 16-byte vector of T (4 floats or 2 doubles)
 template <typename T>
-__global__ void __launch_bounds__(256) small_from_dense_kernel(const uint32_t* __restrict__ N, long long Ge, int Gs,
-                                                               const T* __restrict__ pe, int ld, int C, long long per,
-                                                               double* __restrict__ partials) {
-    extern __shared__ __align__(16) unsigned char dense_smem[];
-    uint32_t* sN = reinterpret_cast<uint32_t*>(dense_smem);              // DENSE_TILE x Gs
-    T* sP = reinterpret_cast<T*>(dense_smem + sizeof(uint32_t) * DENSE_TILE * Gs);  // DENSE_TILE x C
-    constexpr int R = DENSE_MAX_TC / 256;
-    const int TC = Gs * C;
-    double acc[R];
-    int tt[R], cc[R];
+struct Vec16;
+template <>
+struct Vec16<float> {
+    using type = float4;
+    static constexpr int n = 4;
+};
+template <>
+struct Vec16<double> {
+    using type = double2;
+    static constexpr int n = 2;
+};
+
+// acc[c] += m * row[c] for c < NC (NC a multiple of 4; row 16-byte aligned)
+template <typename T, int NC>
+__device__ __forceinline__ void fma_row(T m, const T* __restrict__ row, T* acc) {
+    using V = typename Vec16<T>::type;
+    constexpr int W = Vec16<T>::n;
 #pragma unroll
-    for (int r = 0; r < R; ++r) {
-        acc[r] = 0.0;
-        const int tc = threadIdx.x + r * 256;
-        tt[r] = tc / C;
-        cc[r] = tc - tt[r] * C;
-    }
-    const long long g0 = (long long)blockIdx.x * per;
-    const long long g1 = min(Ge, g0 + per);
-    for (long long tile = g0; tile < g1; tile += DENSE_TILE) {
-        const int nt = (int)min((long long)DENSE_TILE, g1 - tile);
-        __syncthreads();  // the previous tile is consumed
-        for (int i = threadIdx.x; i < nt * Gs; i += 256) sN[i] = N[tile * Gs + i];
-        for (int i = threadIdx.x; i < nt * C; i += 256) {
-            const int gl = i / C;
-            sP[i] = pe[(tile + gl) * ld + (i - gl * C)];
+    for (int c = 0; c < NC; c += W) {
+        const V v = *reinterpret_cast<const V*>(row + c);
+        if constexpr (W == 4) {
+            acc[c] = fmaf(m, v.x, acc[c]);
+            acc[c + 1] = fmaf(m, v.y, acc[c + 1]);
+            acc[c + 2] = fmaf(m, v.z, acc[c + 2]);
+            acc[c + 3] = fmaf(m, v.w, acc[c + 3]);
+        } else {
+            acc[c] = fma(m, v.x, acc[c]);
+            acc[c + 1] = fma(m, v.y, acc[c + 1]);
         }
-        __syncthreads();
-#pragma unroll
-        for (int r = 0; r < R; ++r) {
-            if (threadIdx.x + r * 256 >= TC) break;  // past the last output
-            const uint32_t* nr = sN + tt[r];
-            const T* pr = sP + cc[r];
-            T a = T(0);
-            for (int g = 0; g < nt; ++g) a += (T)nr[g * Gs] * pr[g * C];
-            acc[r] += (double)a;
-        }
-    }
-#pragma unroll
-    for (int r = 0; r < R; ++r) {
-        const int tc = threadIdx.x + r * 256;
-        if (tc < TC) partials[(long long)blockIdx.x * TC + tc] = acc[r];
     }
 }
 
-template <typename T>
-int launch_small_from_dense(const uint32_t* N, long long Ge, int Gs, const T* pe, int ld, int C, double* partials,
-                            cudaStream_t s) {
-    if (Ge <= 0) return 0;
-    if (Gs * C > DENSE_MAX_TC) return set_error("dense small-G product: %d x %d outputs exceed %d", Gs, C, DENSE_MAX_TC);
+// 16-byte global -> shared copy that completes asynchronously (L2 only)
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_prev() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
+
+// Stage the count rows and pe rows of groups [tile, tile + nt) into one
+// shared-memory buffer: whole 16-byte pieces asynchronously; a count tail
+// that is not a whole piece (the last tile of a range) with plain loads,
+// done by the caller through dense_tail.
+template <typename T, typename CT>
+__device__ __forceinline__ void dense_issue(const CT* __restrict__ M, const T* __restrict__ pe, int Gs, int ld,
+                                            long long tile, int nt, CT* sM, T* sP) {
+    const long long mbytes = (long long)nt * Gs * sizeof(CT);
+    const char* gm = reinterpret_cast<const char*>(M + tile * Gs);
+    for (long long o = (long long)threadIdx.x * 16; o + 16 <= mbytes; o += 256 * 16)
+        cp_async16(reinterpret_cast<char*>(sM) + o, gm + o);
+    const long long pbytes = (long long)nt * ld * sizeof(T);
+    const char* gp = reinterpret_cast<const char*>(pe + tile * ld);
+    for (long long o = (long long)threadIdx.x * 16; o < pbytes; o += 256 * 16)
+        cp_async16(reinterpret_cast<char*>(sP) + o, gp + o);
+}
+
+template <typename CT>
+__device__ __forceinline__ void dense_tail(const CT* __restrict__ M, int Gs, long long tile, int nt, CT* sM) {
+    const long long n = (long long)nt * Gs;
+    const long long whole = (n * (long long)sizeof(CT)) / 16 * 16 / (long long)sizeof(CT);
+    for (long long i = whole + threadIdx.x; i < n; i += 256) sM[i] = M[tile * Gs + i];
+}
+
+// Dense pair product of a small dimension s (Gs groups) and a dimension e
+// (Ge groups) through their count matrix M (Ge x Gs, row g: the rows of each
+// group of s within group g of e):
+//   partials[block][t][c] = sum over the block's groups g of M[g][t] pe[g][c]
+//   extra[g][c] (+)= sum_t M[g][t] ps[t][c]                 (extra != null)
+// Block b covers groups [b * per, (b + 1) * per) (per a multiple of
+// DENSE_TILE) in tiles of DENSE_TILE groups, double-buffered in shared memory
+// by asynchronous copies (the next tile loads while this one is used). Small
+// side: warp w takes the tile's groups g = w mod 8, lane = group t of s (and
+// t + 32 when TWO), all columns in registers, pe rows read as 16-byte
+// broadcasts; the 8 warps' sums are folded in warp order into FP64 at the
+// end. Extra side: thread = (group of e, quad of 4 columns).
+template <typename T, typename CT, int CQ, bool TWO>
+__global__ void __launch_bounds__(256) dense_pair_kernel(const CT* __restrict__ M, long long Ge, int Gs,
+                                                         const T* __restrict__ pe, const T* __restrict__ ps, int ld,
+                                                         int C, long long per, double* __restrict__ partials,
+                                                         T* __restrict__ extra, int accumulate) {
+    extern __shared__ __align__(16) unsigned char dense_smem[];
+    // layout: sS (Gs x CQ) | 2 x [sP (DENSE_TILE x ld) | sM (DENSE_TILE x Gs, padded to 16 bytes)]
+    T* sS = reinterpret_cast<T*>(dense_smem);
+    const size_t s_bytes = sizeof(T) * (size_t)DENSE_SMALL_MAX_G * CQ;
+    const size_t p_bytes = sizeof(T) * (size_t)DENSE_TILE * ld;
+    const size_t m_bytes = ((sizeof(CT) * (size_t)DENSE_TILE * Gs + 15) / 16) * 16;
+    unsigned char* const buf0 = dense_smem + s_bytes;
+    unsigned char* const buf1 = buf0 + p_bytes + m_bytes;
+    double* red = reinterpret_cast<double*>(dense_smem);  // Gs x C (after the tiles)
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (extra)
+        for (int i = threadIdx.x; i < Gs * CQ; i += 256) {
+            const int t = i / CQ, c = i - t * CQ;
+            sS[i] = c < C ? ps[(long long)t * ld + c] : T(0);
+        }
+    T acc0[CQ], acc1[TWO ? CQ : 1];
+#pragma unroll
+    for (int c = 0; c < CQ; ++c) acc0[c] = T(0);
+#pragma unroll
+    for (int c = 0; c < (TWO ? CQ : 1); ++c) acc1[c] = T(0);
+    const long long g0 = (long long)blockIdx.x * per;
+    const long long g1 = min(Ge, g0 + per);
+    if (g0 < g1)
+        dense_issue<T, CT>(M, pe, Gs, ld, g0, (int)min((long long)DENSE_TILE, g1 - g0),
+                           reinterpret_cast<CT*>(buf0 + p_bytes), reinterpret_cast<T*>(buf0));
+    cp_async_commit();
+    bool odd = false;
+    for (long long tile = g0; tile < g1; tile += DENSE_TILE, odd = !odd) {
+        unsigned char* const cur = odd ? buf1 : buf0;
+        unsigned char* const nxt = odd ? buf0 : buf1;
+        const int nt = (int)min((long long)DENSE_TILE, g1 - tile);
+        const long long next = tile + DENSE_TILE;
+        if (next < g1)
+            dense_issue<T, CT>(M, pe, Gs, ld, next, (int)min((long long)DENSE_TILE, g1 - next),
+                               reinterpret_cast<CT*>(nxt + p_bytes), reinterpret_cast<T*>(nxt));
+        cp_async_commit();
+        cp_async_wait_prev();  // this tile's copies are done (the next tile's may be in flight)
+        CT* const m = reinterpret_cast<CT*>(cur + p_bytes);
+        const T* const pt = reinterpret_cast<const T*>(cur);
+        dense_tail<CT>(M, Gs, tile, nt, m);
+        __syncthreads();
+        for (int gl = warp; gl < nt; gl += DENSE_WARPS) {
+            const T* prow = pt + gl * ld;
+            if (lane < Gs) fma_row<T, CQ>((T)m[gl * Gs + lane], prow, acc0);
+            if constexpr (TWO)
+                if (lane + 32 < Gs) fma_row<T, CQ>((T)m[gl * Gs + lane + 32], prow, acc1);
+        }
+        if (extra) {
+            constexpr int QN = CQ / 4;
+            for (int i = threadIdx.x; i < nt * QN; i += 256) {
+                const int gl = i / QN, c0 = (i - gl * QN) * 4;
+                T a[4] = {T(0), T(0), T(0), T(0)};
+                const CT* mr = m + gl * Gs;
+                for (int t = 0; t < Gs; ++t) fma_row<T, 4>((T)mr[t], sS + t * CQ + c0, a);
+                T* o = extra + (tile + gl) * C + c0;
+#pragma unroll
+                for (int c = 0; c < 4; ++c)
+                    if (c0 + c < C) o[c] = accumulate ? o[c] + a[c] : a[c];
+            }
+        }
+        __syncthreads();  // this buffer is refilled two tiles on
+    }
+    // fold the warps' small-side sums in warp order (FP64); red overlays sS
+    __syncthreads();
+    for (int w = 0; w < DENSE_WARPS; ++w) {
+        if (warp == w) {
+#pragma unroll
+            for (int c = 0; c < CQ; ++c) {
+                if (c >= C) break;
+                if (lane < Gs) red[lane * C + c] = (w ? red[lane * C + c] : 0.0) + (double)acc0[c];
+                if constexpr (TWO)
+                    if (lane + 32 < Gs) red[(lane + 32) * C + c] = (w ? red[(lane + 32) * C + c] : 0.0) + (double)acc1[c];
+            }
+        }
+        __syncthreads();
+    }
+    for (int i = threadIdx.x; i < Gs * C; i += 256) partials[(long long)blockIdx.x * Gs * C + i] = red[i];
+}
+
+template <typename T, typename CT, int CQ, bool TWO>
+int dense_pair_cq(const CT* M, long long Ge, int Gs, const T* pe, const T* ps, int ld, int C, double* partials,
+                  T* extra, int accumulate, cudaStream_t s) {
+    static const cudaError_t attr = cudaFuncSetAttribute(dense_pair_kernel<T, CT, CQ, TWO>,
+                                                         cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
+    if (attr != cudaSuccess) return set_cuda_error(attr, "dense pair attr");
     const int nb = dense_chunks(Ge);
-    const long long per = (Ge + nb - 1) / nb;
-    const size_t smem = (sizeof(uint32_t) * Gs + sizeof(T) * C) * DENSE_TILE;
-    small_from_dense_kernel<T><<<nb, 256, smem, s>>>(N, Ge, Gs, pe, ld, C, per, partials);
-    FEGB_LAUNCH_CHECK("small-G dense product");
+    long long per = (Ge + nb - 1) / nb;
+    per = (per + DENSE_TILE - 1) / DENSE_TILE * DENSE_TILE;  // tiles (and their copies) start on 16 bytes
+    const size_t p_bytes = sizeof(T) * (size_t)DENSE_TILE * ld;
+    const size_t m_bytes = ((sizeof(CT) * (size_t)DENSE_TILE * Gs + 15) / 16) * 16;
+    const size_t smem = std::max(sizeof(T) * (size_t)DENSE_SMALL_MAX_G * CQ + 2 * (p_bytes + m_bytes),
+                                 sizeof(double) * (size_t)Gs * C);
+    dense_pair_kernel<T, CT, CQ, TWO><<<nb, 256, smem, s>>>(M, Ge, Gs, pe, ps, ld, C, per, partials, extra,
+                                                            accumulate);
+    FEGB_LAUNCH_CHECK("dense small-G pair product");
     return 0;
 }
-template int launch_small_from_dense<float>(const uint32_t*, long long, int, const float*, int, int, double*,
-                                            cudaStream_t);
-template int launch_small_from_dense<double>(const uint32_t*, long long, int, const double*, int, int, double*,
-                                             cudaStream_t);
+
+template <typename T, typename CT, int CQ>
+int dense_pair_two(const CT* M, long long Ge, int Gs, const T* pe, const T* ps, int ld, int C, double* partials,
+                   T* extra, int accumulate, cudaStream_t s) {
+    if (Gs > 32) return dense_pair_cq<T, CT, CQ, true>(M, Ge, Gs, pe, ps, ld, C, partials, extra, accumulate, s);
+    return dense_pair_cq<T, CT, CQ, false>(M, Ge, Gs, pe, ps, ld, C, partials, extra, accumulate, s);
+}
+
+}  // namespace
+
+template <typename T, typename CT>
+int launch_dense_pair(const CT* M, long long Ge, int Gs, const T* pe, const T* ps, int ld, int C, double* partials,
+                      T* extra, int accumulate, cudaStream_t s) {
+    if (Ge <= 0 || Gs <= 0 || C <= 0) return 0;
+    if (Gs > DENSE_SMALL_MAX_G || C > 32) return set_error("dense small-G product: Gs=%d C=%d too large", Gs, C);
+    // pe and ps rows are copied whole (ld values, 16-byte pieces) and read CQ wide
+    if (ld % (16 / (int)sizeof(T)) != 0 || (reinterpret_cast<uintptr_t>(pe) & 15u) != 0 ||
+        (reinterpret_cast<uintptr_t>(M) & 15u) != 0)
+        return set_error("dense small-G product: unaligned rows (ld %d)", ld);
+    if (C <= 4 && ld >= 4) return dense_pair_two<T, CT, 4>(M, Ge, Gs, pe, ps, ld, C, partials, extra, accumulate, s);
+    if (C <= 8 && ld >= 8) return dense_pair_two<T, CT, 8>(M, Ge, Gs, pe, ps, ld, C, partials, extra, accumulate, s);
+    if (C <= 12 && ld >= 12)
+        return dense_pair_two<T, CT, 12>(M, Ge, Gs, pe, ps, ld, C, partials, extra, accumulate, s);
+    if (C <= 16 && ld >= 16)
+        return dense_pair_two<T, CT, 16>(M, Ge, Gs, pe, ps, ld, C, partials, extra, accumulate, s);
+    if (C <= 24 && ld >= 24)
+        return dense_pair_two<T, CT, 24>(M, Ge, Gs, pe, ps, ld, C, partials, extra, accumulate, s);
+    if (C <= 32 && ld >= 32)
+        return dense_pair_two<T, CT, 32>(M, Ge, Gs, pe, ps, ld, C, partials, extra, accumulate, s);
+    return set_error("dense small-G product: row stride %d below the %d-column read", ld, C);
+}
+template int launch_dense_pair<float, uint8_t>(const uint8_t*, long long, int, const float*, const float*, int, int,
+                                               double*, float*, int, cudaStream_t);
+template int launch_dense_pair<float, uint32_t>(const uint32_t*, long long, int, const float*, const float*, int, int,
+                                                double*, float*, int, cudaStream_t);
+template int launch_dense_pair<double, uint8_t>(const uint8_t*, long long, int, const double*, const double*, int, int,
+                                                double*, double*, int, cudaStream_t);
+template int launch_dense_pair<double, uint32_t>(const uint32_t*, long long, int, const double*, const double*, int,
+                                                 int, double*, double*, int, cudaStream_t);
 
 // One warp per (t, c): strided fold over the parts, fixed shuffle tree.
 __global__ void fold_dense_kernel(const double* __restrict__ partials, int nparts, int TC, double* __restrict__ sums) {
@@ -858,49 +1287,6 @@ int launch_fold_dense(const double* partials, int nparts, int Gs, int C, double*
     return 0;
 }
 
-// extra[g * C + c] (+)= sum_t N[g][t] ps[t][c]. A block takes DENSE_TILE
-// groups of d: their count rows are staged in shared memory (coalesced), ps
-// as well; thread (g, c) then reads both from shared memory.
-template <typename T>
-__global__ void __launch_bounds__(256) dense_to_groups_kernel(const uint32_t* __restrict__ N, long long Gd, int Gs,
-                                                              const T* __restrict__ ps, int ld, int C,
-                                                              T* __restrict__ extra, int accumulate) {
-    __shared__ T sps[DENSE_SMALL_MAX_G * 32];
-    __shared__ uint32_t sN[DENSE_TILE * DENSE_SMALL_MAX_G];
-    const long long g0 = (long long)blockIdx.x * DENSE_TILE;
-    const int nt = (int)min((long long)DENSE_TILE, Gd - g0);
-    for (int i = threadIdx.x; i < Gs * C; i += blockDim.x) {
-        const int t = i / C;
-        sps[i] = ps[(long long)t * ld + (i - t * C)];
-    }
-    for (int i = threadIdx.x; i < nt * Gs; i += blockDim.x) sN[i] = N[g0 * Gs + i];
-    __syncthreads();
-    for (int i = threadIdx.x; i < nt * C; i += blockDim.x) {
-        const int gl = i / C;
-        const int c = i - gl * C;
-        const uint32_t* row = sN + gl * Gs;
-        T acc = T(0);
-        for (int t = 0; t < Gs; ++t) acc += (T)row[t] * sps[t * C + c];
-        const long long o = g0 * C + i;
-        extra[o] = accumulate ? extra[o] + acc : acc;
-    }
-}
-
-template <typename T>
-int launch_dense_to_groups(const uint32_t* N, long long Gd, int Gs, const T* ps, int ld, int C, T* extra,
-                           int accumulate, cudaStream_t s) {
-    const long long total = Gd * C;
-    if (total <= 0) return 0;
-    if (Gs > DENSE_SMALL_MAX_G || C > 32) return set_error("dense small-G product: Gs=%d C=%d too large", Gs, C);
-    const long long nb = (Gd + DENSE_TILE - 1) / DENSE_TILE;
-    dense_to_groups_kernel<T><<<(unsigned)nb, 256, 0, s>>>(N, Gd, Gs, ps, ld, C, extra, accumulate);
-    FEGB_LAUNCH_CHECK("small-G dense to groups");
-    return 0;
-}
-template int launch_dense_to_groups<float>(const uint32_t*, long long, int, const float*, int, int, float*, int,
-                                           cudaStream_t);
-template int launch_dense_to_groups<double>(const uint32_t*, long long, int, const double*, int, int, double*, int,
-                                            cudaStream_t);
 template int launch_cg_update<double>(long long, int, const double*, const double*, const double*, const double*, int,
                                       const double*, double*, double*, double*, double*, double*,
                                       unsigned long long*, cudaStream_t);
@@ -1038,8 +1424,8 @@ struct CGRun {
 
 // Adds one position (group g, contribution v) to the lane's run state.
 template <typename T, int TILE>
-__device__ __forceinline__ void cg_run_push(CGRun<T, TILE>& st, int g, const T (&v)[TILE], double* __restrict__ sums,
-                                            int LD, int c0, int cw) {
+__device__ __forceinline__ void cg_run_push(CGRun<T, TILE>& st, int g, const T (&v)[TILE], T* __restrict__ sums,
+                                            int SC, int c0, int cw) {
     if (!st.started) {
         st.started = true;
         st.firstg = st.cur = g;
@@ -1054,10 +1440,10 @@ __device__ __forceinline__ void cg_run_push(CGRun<T, TILE>& st, int g, const T (
             st.single = false;
         } else {
             // a run that starts and ends inside this lane is complete
-            double* dst = sums + (long long)st.cur * LD + c0;
+            T* dst = sums + (long long)st.cur * SC + c0;
 #pragma unroll
             for (int i = 0; i < TILE; ++i)
-                if (i < cw) dst[i] = (double)st.run[i];
+                if (i < cw) dst[i] = st.run[i];
         }
         st.cur = g;
 #pragma unroll
@@ -1129,7 +1515,7 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 && CGR_TILE <= 12) ? CG_R
 #pragma unroll
                     for (int e = 0; e < NSRC; ++e)
                         cg_sub_row<T, CGR_TILE>(tabs[e] + (long long)sid[e][m] * LD, cw, v, keep);
-                    cg_run_push(st, gq[m], v, p.sums, LD, c0, cw);
+                    cg_run_push(st, gq[m], v, p.sums, C, c0, cw);
                 }
             } else {
                 // ragged end of the last chunk
@@ -1140,7 +1526,7 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 && CGR_TILE <= 12) ? CG_R
 #pragma unroll
                     for (int e = 0; e < NSRC; ++e)
                         cg_sub_row<T, CGR_TILE>(tabs[e] + (long long)__ldg(sgid[e] + j) * LD, cw, v, keep);
-                    cg_run_push(st, __ldg(gseq + j), v, p.sums, LD, c0, cw);
+                    cg_run_push(st, __ldg(gseq + j), v, p.sums, C, c0, cw);
                 }
             }
         }
@@ -1151,7 +1537,7 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 && CGR_TILE <= 12) ? CG_R
             for (int i = 0; i < CGR_TILE; ++i) v[i] = T(0);
             for (int e = 0; e < p.n_src; ++e)
                 cg_sub_row<T, CGR_TILE>(p.src_tab[e] + (long long)__ldcs(p.src_gid[e] + j) * LD + c0, cw, v, keep);
-            cg_run_push(st, __ldcs(gseq + j), v, p.sums, LD, c0, cw);
+            cg_run_push(st, __ldcs(gseq + j), v, p.sums, C, c0, cw);
         }
     }
     const int firstg = st.firstg;
@@ -1216,21 +1602,21 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 && CGR_TILE <= 12) ? CG_R
         const long long col = c0 + i;
         if (!empty && !single) {
             // head run of a multi-run lane ends inside this lane
-            const double val = (double)((cont ? in : T(0)) + st.head[i]);
+            const T val = (cont ? in : T(0)) + st.head[i];
             if (head_from_start && before)
-                p.head[q * LD + col] = val;
+                p.head[q * C + col] = (double)val;
             else
-                p.sums[(long long)fg * LD + col] = val;
+                p.sums[(long long)fg * C + col] = val;
         }
         if (tail_ends_here) {
             const bool from_start = sgl && head_from_start;
             const bool at_end = lane == lane_end;
             if (from_start && before)
-                p.head[q * LD + col] = (double)out;
+                p.head[q * C + col] = (double)out;
             else if (at_end && after)
-                p.tail[q * LD + col] = (double)out;
+                p.tail[q * C + col] = (double)out;
             else
-                p.sums[(long long)lg * LD + col] = (double)out;
+                p.sums[(long long)lg * C + col] = out;
         }
     }
 }

@@ -81,6 +81,7 @@ struct FinalizeParams {
     // already holds complete group sums (sums == null: all zero)
     const int32_t* off;
     const double* sums;
+    const float* sums32;  // FP32 complete sums, used instead of sums when set
     const double* head;
     const double* tail;
     int R;
@@ -118,9 +119,20 @@ constexpr int SEG_LONG_SPAN = 32;
 
 // Lists the long groups of a segment traversal (device list, count on host).
 int find_long_groups(const int32_t* off, int G, int R, int32_t* list, int* n_long, cudaStream_t s);
+// Groups whose run crosses 1..SEG_LONG_SPAN chunk boundaries (list order unspecified).
+int find_multi_groups(const int32_t* off, int G, int R, int32_t* list, int* n_multi, cudaStream_t s);
+// Completes sums[g * C + c] of the listed long and multi-chunk groups from the
+// chunk tail/head partials (each group summed in chunk order), so that sums
+// then holds every group's complete sum.
+template <typename S>
+int launch_group_sums(const int32_t* off, const double* head, const double* tail, int R, int C,
+                      const int32_t* long_list, int n_long, const int32_t* multi_list, int n_multi, S* sums,
+                      cudaStream_t s);
 // sums[g][c] = tail[qs][c] + sum_{qs<q<=qe} head[q][c] for the listed groups.
 int launch_long_sums(const int32_t* off, const double* head, const double* tail, int R, int C, const int32_t* list,
                      int n_long, double* sums, cudaStream_t s);
+int launch_long_sums(const int32_t* off, const double* head, const double* tail, int R, int C, const int32_t* list,
+                     int n_long, float* sums, cudaStream_t s);
 // sums[g][c] = sum_b partials[b][g][c] (small-G block partials, fixed tree order).
 int launch_fold_smallg(const double* partials, int nblocks, int G, int C, double* sums, cudaStream_t s);
 
@@ -161,12 +173,14 @@ template <typename T>
 struct CGRowsParams {
     long long n;
     int C;                 // real columns
-    int ld;                // row stride of the tables and of sums/head/tail (see cg_row_stride)
+    int ld;                // row stride of the gathered tables (see cg_row_stride)
     const int32_t* gseq;
     int n_src;
     const int32_t* src_gid[SWEEP_MAXP];
     const T* src_tab[SWEEP_MAXP];
-    double* sums;
+    // outputs at the compact stride C: complete-run sums in the storage type
+    // (runs are summed in T), chunk head/tail partials in FP64
+    T* sums;
     double* head;
     double* tail;
 };
@@ -204,28 +218,35 @@ int launch_cg_q(const FinalizeParams& src, int C, const T* p, int pld, T* q, dou
 // For a dimension s with few groups and any other dimension e, the operator
 // coupling D_s' D_e is the G_e x G_s count matrix N (rows of each (group of e,
 // group of s) pair), built once. N[g * Gs + t] counts the rows with gid_e = g
-// and gid_s = t.
+// and gid_s = t; stored as uint8 when every count is below 256.
 constexpr int DENSE_SMALL_MAX_G = 64;
 constexpr int DENSE_TILE = 64;          // groups per shared-memory tile of the dense products
-constexpr int DENSE_MAX_BLOCKS = 1024;  // partial blocks of a small-side product (fixed: same sums on any GPU)
-constexpr int DENSE_MAX_TC = DENSE_SMALL_MAX_G * 32;
+constexpr int DENSE_MAX_BLOCKS = 608;   // partial blocks of a product (fixed: the same sums on any GPU)
 int launch_count_pairs(const int32_t* gid_e, const int32_t* gid_s, long long n, int Gs, uint32_t* N, cudaStream_t s);
-// number of partial blocks of a small-side product over Ge groups
+// *mx = max of N[0..cnt)
+int launch_count_max(const uint32_t* N, long long cnt, unsigned* mx, cudaStream_t s);
+// out = (uint8) N
+int launch_narrow_counts(const uint32_t* N, long long cnt, uint8_t* out, cudaStream_t s);
+// number of partial blocks of a product over Ge groups
 inline int dense_chunks(long long Ge) {
     const long long tiles = (Ge + DENSE_TILE - 1) / DENSE_TILE;
     return (int)(tiles < DENSE_MAX_BLOCKS ? tiles : DENSE_MAX_BLOCKS);
 }
-// partials[block][t][c] = sum over the block's groups g of N[g][t] * pe[g * ld + c]
-template <typename T>
-int launch_small_from_dense(const uint32_t* N, long long Ge, int Gs, const T* pe, int ld, int C, double* partials,
-                            cudaStream_t s);
+// One pass over the count matrix M (Ge x Gs) of a small dimension s and a
+// dimension e: partials[block][t][c] = sum over the block's groups g of
+// M[g][t] * pe[g * ld + c] (dense_chunks(Ge) blocks), and, when extra is not
+// null, extra[g * C + c] (+)= sum_t M[g][t] * ps[t * ld + c] (accumulate = 0
+// overwrites). pe and M start on 16 bytes and ld is a multiple of 16 bytes.
+template <typename T, typename CT>
+int launch_dense_pair(const CT* M, long long Ge, int Gs, const T* pe, const T* ps, int ld, int C, double* partials,
+                      T* extra, int accumulate, cudaStream_t s);
 // sums[t * C + c] = -(sum over parts of partials[part][t][c]), parts in order
 int launch_fold_dense(const double* partials, int nparts, int Gs, int C, double* sums, cudaStream_t s);
-// extra[g * C + c] (+)= sum_t N[g][t] * ps[t * ld + c]  (accumulate = 0 overwrites)
-template <typename T>
-int launch_dense_to_groups(const uint32_t* N, long long Gd, int Gs, const T* ps, int ld, int C, T* extra,
-                           int accumulate, cudaStream_t s);
-int cg_partial_blocks(long long gc);
+// Partial blocks (one FP64 partial per column each) of the CG vector kernels
+// over a G x C table: VEC_STEPS steps of 256 / C rows per block (C <= 256),
+// else one block per 256 elements.
+constexpr int VEC_STEPS = 16;
+int cg_partial_blocks(long long G, int C);
 
 // out[c] = sum_b partials[b * C + c] for b < nb (fixed order)
 int launch_fold_partials(const double* partials, int nb, int C, double* out, cudaStream_t s);

@@ -207,6 +207,28 @@ __global__ void gather_i32_kernel(const int32_t* __restrict__ src, const int32_t
     for (; i < n; i += st) out[i] = src[idx[i]];
 }
 
+// Distinct id tuples of the swept dimensions: tuple k covers the key-sorted
+// rows [off[k], off[k + 1]); its weight is that row count and its ids are
+// those of its first row.
+__global__ void tuple_build_kernel(const int32_t* __restrict__ off, const int32_t* __restrict__ perm, long long m,
+                                   int nd, const int32_t* const* __restrict__ gids, int32_t* const* __restrict__ tgid,
+                                   float* __restrict__ weight) {
+    long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long st = (long long)gridDim.x * blockDim.x;
+    for (; k < m; k += st) {
+        const int r = perm[off[k]];
+        weight[k] = (float)(off[k + 1] - off[k]);
+        for (int j = 0; j < nd; ++j) tgid[j][k] = gids[j][r];
+    }
+}
+
+__global__ void gather_f32_kernel(const float* __restrict__ src, const int32_t* __restrict__ idx, long long n,
+                                  float* __restrict__ out) {
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long st = (long long)gridDim.x * blockDim.x;
+    for (; i < n; i += st) out[i] = src[idx[i]];
+}
+
 __global__ void counts_from_offsets_kernel(const int32_t* __restrict__ off, int G, int32_t* __restrict__ counts) {
     int g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g < G) counts[g] = off[g + 1] - off[g];
@@ -832,7 +854,145 @@ struct CGBuffers {
     double* dense_sums = nullptr;
     T* extra = nullptr;  // Gt x C: the dense dimensions' share of each swept dimension's q
     bool any_dense = false;
+    // the operator sweep of each many-group dimension d: positions in d's group
+    // order, either the rows or (compressed) the distinct id tuples of the
+    // many-group dimensions, each weighted by its row count
+    struct Stream {
+        long long m = 0;
+        const int32_t* gseq = nullptr;
+        const int32_t* off = nullptr;  // G_d + 1 offsets over the positions
+        int n_src = 0;
+        const int32_t* src_gid[SWEEP_MAXP] = {};
+        int src_dim[SWEEP_MAXP] = {};
+        const float* weight = nullptr;
+        const int32_t* long_list = nullptr;
+        int n_long = 0;
+        const int32_t* multi_list = nullptr;
+        int n_multi = 0;
+    };
+    std::vector<Stream> stream;
+    bool compressed = false;
 };
+
+// Position streams of the CG operator sweeps (see CGBuffers::Stream). The
+// rows are compressed into distinct id tuples of the many-group dimensions
+// when that removes at least a quarter of the positions: the operator carries
+// no row data, so rows with equal ids contribute equally (weight x one row).
+template <typename T>
+int cg_streams(Problem& P, CGBuffers<T>& B) {
+    Scratch& scr = *P.scr;
+    cudaStream_t s = P.s;
+    const long long n = P.n;
+    std::vector<int> sw;  // swept dimensions, the primary last (most significant key part)
+    for (int d = 0; d < P.n_fe; ++d)
+        if (P.dims[d].G > 0 && !B.dense[d] && d != P.primary) sw.push_back(d);
+    if (P.primary >= 0 && P.dims[P.primary].G > 0 && !B.dense[P.primary]) sw.push_back(P.primary);
+    B.stream.assign(P.n_fe, typename CGBuffers<T>::Stream());
+    // rows, in each dimension's group order
+    for (int d : sw) {
+        Dim& D = P.dims[d];
+        auto& st = B.stream[d];
+        st.m = n;
+        st.gseq = D.gseq;
+        st.off = D.off;
+        for (int e : sw) {
+            if (e == d) continue;
+            st.src_dim[st.n_src] = e;
+            st.src_gid[st.n_src++] = d == P.primary ? P.dims[e].gid : D.gid_at_perm[e];
+        }
+        st.long_list = D.long_list_cg;
+        st.n_long = D.n_long_cg;
+        st.multi_list = D.multi_list_cg;
+        st.n_multi = D.n_multi_cg;
+    }
+    if (sw.size() < 2 || n < 4096) return 0;
+    std::vector<const int32_t*> ptrs;
+    std::vector<unsigned long long> strides;
+    unsigned long long stride = 1;
+    for (int d : sw) {
+        const unsigned long long Gd = (unsigned long long)P.dims[d].G;
+        if (stride > (1ULL << 62) / Gd) return 0;  // key does not fit: keep the rows
+        ptrs.push_back(P.dims[d].gid);
+        strides.push_back(stride);
+        stride *= Gd;
+    }
+    int m = 0;
+    int32_t *perm = nullptr, *toff = nullptr;
+    {
+        Scratch tmp(s);  // the row-level sort, released once the tuples are built
+        FEGB_TRY(tmp.alloc(&perm, (size_t)n, "tuple perm"));
+        FEGB_TRY(tmp.alloc(&toff, (size_t)n + 1, "tuple offsets"));
+        FEGB_TRY(cluster_ids_by_key(ptrs.data(), strides.data(), (int)sw.size(), n, bits_for(stride), nullptr, &m,
+                                    perm, toff, s, tmp, true, nullptr));
+        if (m <= 0 || (double)m > 0.75 * (double)n) return 0;
+        std::vector<int32_t*> tg(sw.size());
+        for (size_t j = 0; j < sw.size(); ++j) FEGB_TRY(dalloc(scr, &tg[j], (size_t)m, "tuple ids"));
+        float* w = nullptr;
+        FEGB_TRY(dalloc(scr, &w, (size_t)m, "tuple weights"));
+        int32_t** dg = nullptr;
+        const int32_t** dsrc = nullptr;
+        FEGB_TRY(tmp.alloc(&dg, sw.size(), "tuple id table"));
+        FEGB_TRY(tmp.alloc(&dsrc, sw.size(), "tuple source table"));
+        FEGB_CUDA(cudaMemcpyAsync(dg, tg.data(), sizeof(int32_t*) * sw.size(), cudaMemcpyHostToDevice, s),
+                  "tuple id table");
+        FEGB_CUDA(cudaMemcpyAsync(dsrc, ptrs.data(), sizeof(int32_t*) * sw.size(), cudaMemcpyHostToDevice, s),
+                  "tuple source table");
+        tuple_build_kernel<<<grid_stride_blocks(m, 256), 256, 0, s>>>(toff, perm, m, (int)sw.size(), dsrc, dg, w);
+        FEGB_LAUNCH_CHECK("tuple build");
+        FEGB_CUDA(cudaStreamSynchronize(s), "tuple build sync");  // host tables above are stack arrays
+        // per swept dimension: the tuples in its group order
+        for (size_t jd = 0; jd < sw.size(); ++jd) {
+            const int d = sw[jd];
+            const int G = P.dims[d].G;
+            auto& st = B.stream[d];
+            st = typename CGBuffers<T>::Stream();
+            st.m = m;
+            int32_t* order = nullptr;  // tuple index at each position (null: identity)
+            if (d == P.primary) {
+                st.gseq = tg[jd];  // the primary is the most significant key part: already in order
+                st.weight = w;
+            } else {
+                uint32_t* sorted = nullptr;
+                float* wd = nullptr;
+                FEGB_TRY(dalloc(scr, &sorted, (size_t)m, "tuple gseq"));
+                FEGB_TRY(tmp.alloc(&order, (size_t)m, "tuple order"));
+                FEGB_TRY(radix_sort_u32(reinterpret_cast<const uint32_t*>(tg[jd]), nullptr, sorted, order, m,
+                                        bits_for((unsigned long long)G), s, tmp));
+                FEGB_TRY(dalloc(scr, &wd, (size_t)m, "tuple weights (sorted)"));
+                gather_f32_kernel<<<grid_stride_blocks(m, 256), 256, 0, s>>>(w, order, m, wd);
+                FEGB_LAUNCH_CHECK("tuple weight gather");
+                st.gseq = reinterpret_cast<int32_t*>(sorted);
+                st.weight = wd;
+            }
+            for (size_t je = 0; je < sw.size(); ++je) {
+                if (je == jd) continue;
+                if (!order) {
+                    st.src_gid[st.n_src] = tg[je];
+                } else {
+                    int32_t* gj = nullptr;
+                    FEGB_TRY(dalloc(scr, &gj, (size_t)m, "tuple source ids"));
+                    gather_i32_kernel<<<grid_stride_blocks(m, 256), 256, 0, s>>>(tg[je], order, m, gj);
+                    FEGB_LAUNCH_CHECK("tuple id gather");
+                    st.src_gid[st.n_src] = gj;
+                }
+                st.src_dim[st.n_src++] = sw[je];
+            }
+            int32_t *off = nullptr, *ll = nullptr, *ml = nullptr;
+            FEGB_TRY(dalloc(scr, &off, (size_t)G + 1, "tuple group offsets"));
+            FEGB_TRY(segment_offsets(reinterpret_cast<const uint32_t*>(st.gseq), m, G, off, s));
+            FEGB_TRY(dalloc(scr, &ll, (size_t)G, "tuple long groups"));
+            FEGB_TRY(find_long_groups(off, G, CG_CHUNK, ll, &st.n_long, s));
+            FEGB_TRY(dalloc(scr, &ml, (size_t)G, "tuple multi-chunk groups"));
+            FEGB_TRY(find_multi_groups(off, G, CG_CHUNK, ml, &st.n_multi, s));
+            st.off = off;
+            st.long_list = ll;
+            st.multi_list = ml;
+        }
+        FEGB_CUDA(cudaStreamSynchronize(s), "tuple streams sync");
+    }
+    B.compressed = true;
+    return 0;
+}
 
 template <typename T>
 int cg_alloc(Problem& P, CGBuffers<T>& B) {
@@ -918,6 +1078,7 @@ int cg_alloc(Problem& P, CGBuffers<T>& B) {
             }
         }
     }
+    FEGB_TRY(cg_streams(P, B));
     // the operator sweep's sums / head / tail, compact rows of C
     {
         const long long nchunks = std::max(1LL, seg_nchunks(P.n, CG_CHUNK));
@@ -928,13 +1089,6 @@ int cg_alloc(Problem& P, CGBuffers<T>& B) {
         FEGB_TRY(dalloc(scr, &B.tail, (size_t)nchunks * C, "cg tails"));
     }
     return 0;
-}
-
-// Algorithmic bytes of one operator sweep: per position the destination id,
-// D-1 source ids and D-1 gathered source rows of C values of size s.
-inline double cg_operator_bytes(const Problem& P, size_t s, int n_src = -1) {
-    if (n_src < 0) n_src = P.n_fe - 1;
-    return (double)P.n * (4.0 * (1 + n_src) + (double)n_src * P.C * (double)s);
 }
 
 // q = D'D p, dimension by dimension: a no-data sweep over d's traversal with
@@ -1005,30 +1159,32 @@ int cg_apply(Problem& P, CGBuffers<T>& B) {
         Dim& D = P.dims[d];
         if (D.G <= 0 || B.dense[d]) continue;
         Problem::Timed tm{};
+        const auto& st = B.stream[d];
         CGRowsParams<T> rp{};
-        rp.n = P.n;
+        rp.n = st.m;
         rp.C = C;
         rp.ld = L;
-        rp.gseq = D.gseq;
-        rp.n_src = 0;
-        for (int e = 0; e < P.n_fe; ++e) {
-            if (e == d || B.dense[e]) continue;
-            rp.src_gid[rp.n_src] = d == P.primary ? P.dims[e].gid : D.gid_at_perm[e];
-            rp.src_tab[rp.n_src] = B.p + P.goff[e] * L;
-            ++rp.n_src;
+        rp.gseq = st.gseq;
+        rp.n_src = st.n_src;
+        for (int i = 0; i < st.n_src; ++i) {
+            rp.src_gid[i] = st.src_gid[i];
+            rp.src_tab[i] = B.p + P.goff[st.src_dim[i]] * L;
         }
+        rp.weight = st.weight;
         FinalizeParams src{};
         src.G = D.G;
         src.counts = D.counts;
         if (rp.n_src > 0) {
-            const double bytes = cg_operator_bytes(P, sizeof(T), rp.n_src);
+            // per position: destination id, source ids, weight, gathered source rows
+            const double bytes = (double)st.m * (4.0 * (1 + rp.n_src) + (st.weight ? 4.0 : 0.0) +
+                                                 (double)rp.n_src * C * sizeof(T));
             FEGB_TRY(begin_timed(tm, 4 + fp32, bytes));
             rp.sums = B.sums;
             rp.head = B.head;
             rp.tail = B.tail;
             FEGB_TRY(launch_cg_rows<T>(rp, P.s));
-            FEGB_TRY(launch_group_sums<T>(D.off, B.head, B.tail, CG_CHUNK, C, D.long_list_cg, D.n_long_cg,
-                                          D.multi_list_cg, D.n_multi_cg, B.sums, P.s));
+            FEGB_TRY(launch_group_sums<T>(st.off, B.head, B.tail, CG_CHUNK, C, st.long_list, st.n_long,
+                                          st.multi_list, st.n_multi, B.sums, P.s));
             FEGB_TRY(end_timed(tm));
             P.demean_bytes += bytes;
             src.C = C;  // complete sums, compact rows

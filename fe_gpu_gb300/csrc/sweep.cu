@@ -1352,6 +1352,12 @@ __device__ __forceinline__ void ld_ids(const int32_t* ptr, int (&o)[CG_IDV], uns
                  : "l"(ptr), "l"(pol));
 }
 
+__device__ __forceinline__ void ld_weights(const float* ptr, float (&o)[CG_IDV], unsigned long long pol) {
+    asm("ld.global.nc.L1::no_allocate.L2::cache_hint.v4.f32 {%0,%1,%2,%3}, [%4], %5;"
+                 : "=f"(o[0]), "=f"(o[1]), "=f"(o[2]), "=f"(o[3])
+                 : "l"(ptr), "l"(pol));
+}
+
 // Pieces of a table row: NE consecutive elements at an address aligned to
 // the piece's vector size (pieces start at 32-byte boundaries of the row).
 template <int NE>
@@ -1504,9 +1510,11 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 && CGR_TILE <= 12) ? CG_R
             if (jb + CG_IDV <= le) {
                 int gq[CG_IDV];
                 int sid[NSRC][CG_IDV];
+                float wq[CG_IDV];
                 ld_ids(gseq + jb, gq, stream);
 #pragma unroll
                 for (int e = 0; e < NSRC; ++e) ld_ids(sgid[e] + jb, sid[e], stream);
+                if (p.weight) ld_weights(p.weight + jb, wq, stream);
 #pragma unroll
                 for (int m = 0; m < CG_IDV; ++m) {
                     T v[CGR_TILE];
@@ -1515,6 +1523,11 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 && CGR_TILE <= 12) ? CG_R
 #pragma unroll
                     for (int e = 0; e < NSRC; ++e)
                         cg_sub_row<T, CGR_TILE>(tabs[e] + (long long)sid[e][m] * LD, cw, v, keep);
+                    if (p.weight) {
+                        const T w = (T)wq[m];
+#pragma unroll
+                        for (int i = 0; i < CGR_TILE; ++i) v[i] *= w;
+                    }
                     cg_run_push(st, gq[m], v, p.sums, C, c0, cw);
                 }
             } else {
@@ -1526,6 +1539,11 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 && CGR_TILE <= 12) ? CG_R
 #pragma unroll
                     for (int e = 0; e < NSRC; ++e)
                         cg_sub_row<T, CGR_TILE>(tabs[e] + (long long)__ldg(sgid[e] + j) * LD, cw, v, keep);
+                    if (p.weight) {
+                        const T w = (T)__ldg(p.weight + j);
+#pragma unroll
+                        for (int i = 0; i < CGR_TILE; ++i) v[i] *= w;
+                    }
                     cg_run_push(st, __ldg(gseq + j), v, p.sums, C, c0, cw);
                 }
             }
@@ -1537,6 +1555,11 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 && CGR_TILE <= 12) ? CG_R
             for (int i = 0; i < CGR_TILE; ++i) v[i] = T(0);
             for (int e = 0; e < p.n_src; ++e)
                 cg_sub_row<T, CGR_TILE>(p.src_tab[e] + (long long)__ldcs(p.src_gid[e] + j) * LD + c0, cw, v, keep);
+            if (p.weight) {
+                const T w = (T)__ldcs(p.weight + j);
+#pragma unroll
+                for (int i = 0; i < CGR_TILE; ++i) v[i] *= w;
+            }
             cg_run_push(st, __ldcs(gseq + j), v, p.sums, C, c0, cw);
         }
     }
@@ -1634,7 +1657,7 @@ int launch_cg_rows_tile(const CGRowsParams<T>& p, cudaStream_t s) {
 template <typename T, int TILE>
 int launch_cg_rows_nsrc(const CGRowsParams<T>& p, cudaStream_t s) {
     // the vector id path needs 16-byte aligned id arrays
-    bool aligned = (reinterpret_cast<uintptr_t>(p.gseq) & 15u) == 0;
+    bool aligned = (reinterpret_cast<uintptr_t>(p.gseq) & 15u) == 0 && (reinterpret_cast<uintptr_t>(p.weight) & 15u) == 0;
     for (int e = 0; e < p.n_src; ++e) aligned = aligned && (reinterpret_cast<uintptr_t>(p.src_gid[e]) & 15u) == 0;
     if (aligned) {
         if (p.n_src == 1) return launch_cg_rows_tile<T, TILE, 1>(p, s);

@@ -178,6 +178,9 @@ struct CGRowsParams {
     int n_src;
     const int32_t* src_gid[SWEEP_MAXP];
     const T* src_tab[SWEEP_MAXP];
+    // optional multiplicity of each position (a position then stands for that
+    // many rows with the same ids); 16-byte aligned like the id arrays
+    const float* weight;
     // outputs at the compact stride C: complete-run sums in the storage type
     // (runs are summed in T), chunk head/tail partials in FP64
     T* sums;

@@ -774,12 +774,13 @@ def formula_cpu_baseline(threads):
 
 
 # DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of the
-# dominant kernel families, from the ncu capture summarised in
-# profiles/cg_rows_worker_firm_20M.md (first operator launches of one fit:
-# worker and firm dimensions for the segment family, time for the small-G
-# family). Other workloads were not captured: the gathered tables change size
-# with the FE group counts, so the traffic does not scale with the rows.
+# dominant kernel family, from the ncu capture summarised in
+# profiles/cg_rows_worker_firm_20M.md (mean of the worker and firm operator
+# sweeps of one fit). Other workloads were not captured: the gathered tables
+# change size with the FE group counts, so the traffic does not scale with the
+# rows.
 TRAFFIC_PER_LAUNCH: dict = {
+    ("worker_firm_20M", "CG operator segment sweep fp32"): 1.027e+08,
 }
 
 

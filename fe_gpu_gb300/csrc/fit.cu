@@ -229,6 +229,21 @@ __global__ void gather_f32_kernel(const float* __restrict__ src, const int32_t* 
     for (; i < n; i += st) out[i] = src[idx[i]];
 }
 
+// Sets *hit when two rows share both their group of a and their group of b
+// (b has at most 64 groups): one 64-bit mask of seen groups of b per group
+// of a. The outcome does not depend on the order of the atomic updates.
+__global__ void pair_collision_kernel(const int32_t* __restrict__ ga, const int32_t* __restrict__ gb, long long n,
+                                      unsigned long long* __restrict__ seen, int* __restrict__ hit) {
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long st = (long long)gridDim.x * blockDim.x;
+    bool h = false;
+    for (; i < n; i += st) {
+        const unsigned long long bit = 1ULL << gb[i];
+        h |= (atomicOr(seen + ga[i], bit) & bit) != 0;
+    }
+    if (__any_sync(0xffffffffu, h) && (threadIdx.x & 31) == 0) atomicOr(hit, 1);
+}
+
 __global__ void counts_from_offsets_kernel(const int32_t* __restrict__ off, int G, int32_t* __restrict__ counts) {
     int g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g < G) counts[g] = off[g + 1] - off[g];
@@ -1547,6 +1562,13 @@ int compute_tss_dev(const double* y, long long n, double* out, cudaStream_t s, S
 
 // Cluster-score sums of S (n x ns AoS, storage order) over the groups of one
 // cluster subset; writes Sc (n_cl x ns).
+// bit of FE dimension d (0-based) in a cluster-subset mask over cdims (1-based dims)
+inline int ia_mask_bit(const std::vector<int>& cdims, int d) {
+    for (size_t j = 0; j < cdims.size(); ++j)
+        if (cdims[j] - 1 == d) return (int)j;
+    return 0;
+}
+
 int cluster_score_sums(Problem& P, const double* S, int ns, const int32_t* perm, const int32_t* gseq,
                        const int32_t* off, int n_cl, double* Sc, Scratch& scr) {
     SegSweepParams<double> sp{};
@@ -1860,8 +1882,35 @@ int estimate_on_problem(Problem& P, const fegb_config& cfg, const int* G_all, lo
             int n_cl = 0;
             bool rows = false;  // every cluster of this subset is one row
             for (int u : row_masks) rows = rows || (mask & u) == u;
+            if (!rows && m > 1) {
+                // a pair with a dimension of at most 64 groups: one pass tells whether its pairs are unique
+                for (int ia = 0; ia < m && !rows; ++ia)
+                    for (int ib = 0; ib < m && !rows; ++ib) {
+                        const int a = sd[ia], b = sd[ib];
+                        if (a == b || P.dims[b].G > 64 || P.dims[a].G <= 0) continue;
+                        unsigned long long* seen = nullptr;
+                        int* hit = nullptr;
+                        FEGB_TRY(sub.alloc(&seen, (size_t)P.dims[a].G, "pair masks"));
+                        FEGB_TRY(sub.alloc(&hit, 1, "pair hit"));
+                        FEGB_CUDA(cudaMemsetAsync(seen, 0, sizeof(unsigned long long) * P.dims[a].G, s), "pair masks");
+                        FEGB_CUDA(cudaMemsetAsync(hit, 0, sizeof(int), s), "pair hit");
+                        pair_collision_kernel<<<grid_stride_blocks(n, 256), 256, 0, s>>>(P.dims[a].gid, P.dims[b].gid,
+                                                                                         n, seen, hit);
+                        FEGB_LAUNCH_CHECK("pair uniqueness");
+                        int h = 1;
+                        FEGB_TRY(d2h_sync(&h, hit, sizeof(int), s, "pair hit copy"));
+                        if (!h) {
+                            rows = true;
+                            row_masks.push_back((1 << ia_mask_bit(cdims, a)) | (1 << ia_mask_bit(cdims, b)));
+                        }
+                    }
+            }
+            const bool smallg_single = m == 1 && !rows && P.dims[sd[0]].mode == MODE_SMALLG &&
+                                       smallg_eligible(P.dims[sd[0]].G, ns);
             if (rows && m > 1) {
                 n_cl = (int)n;  // a refinement of single-row clusters: no sort needed
+            } else if (smallg_single) {
+                n_cl = P.dims[sd[0]].G;  // sums from per-block tables in storage order, no sort
             } else if (m == 1 && P.dims[sd[0]].mode != MODE_SMALLG) {
                 const Dim& D = P.dims[sd[0]];
                 perm = D.mode == MODE_GATHER ? D.perm : nullptr;
@@ -1915,7 +1964,7 @@ int estimate_on_problem(Problem& P, const fegb_config& cfg, const int* G_all, lo
             }
             if (m == 1) {
                 long long nc1 = n_cl;
-                if (cpu_conv && P.dims[sd[0]].mode != MODE_SMALLG) {
+                if (cpu_conv && (P.dims[sd[0]].mode != MODE_SMALLG || smallg_single)) {
                     // the CPU path counts distinct ids (cluster_id_builder ranks)
                     std::vector<int32_t> hc(P.dims[sd[0]].G);
                     FEGB_TRY(d2h_sync(hc.data(), P.dims[sd[0]].counts, sizeof(int32_t) * hc.size(), s, "counts copy"));
@@ -1940,7 +1989,22 @@ int estimate_on_problem(Problem& P, const fegb_config& cfg, const int* G_all, lo
             } else {
                 double* Sc = nullptr;
                 FEGB_TRY(sub.alloc(&Sc, (size_t)n_cl * ns, "cluster scores"));
-                FEGB_TRY(cluster_score_sums(P, S, ns, perm, gseq, off, n_cl, Sc, sub));
+                if (smallg_single) {
+                    const Dim& D = P.dims[sd[0]];
+                    SmallGParams<double> sp{};
+                    sp.X = S;
+                    sp.C = ns;
+                    sp.n = n;
+                    sp.gid = D.gid;
+                    sp.G = D.G;
+                    sp.pend.n = 0;
+                    sp.rows_per_block = (n + P.smallg_nb - 1) / P.smallg_nb;
+                    FEGB_TRY(sub.alloc(&sp.partials, (size_t)P.smallg_nb * D.G * ns, "cluster score partials"));
+                    FEGB_TRY(launch_smallg_sweep<double>(sp, P.smallg_nb, s));
+                    FEGB_TRY(launch_fold_smallg(sp.partials, P.smallg_nb, D.G, ns, Sc, s));
+                } else {
+                    FEGB_TRY(cluster_score_sums(P, S, ns, perm, gseq, off, n_cl, Sc, sub));
+                }
                 MatView sv{Sc, ns, 1, ns};
                 FEGB_TRY(crossprod_auto(sv, sv, n_cl, true, false, 1.0, 0.0, meat, ns, s, sub));
             }

@@ -119,13 +119,19 @@ __global__ void __launch_bounds__(CP_THREADS) crossprod_kernel(CPParams p) {
     }
 }
 
+// One warp per output entry: lanes take the row blocks b = lane, lane + 32, ...
+// in order, then a fixed shuffle tree.
 __global__ void crossprod_reduce_kernel(const double* __restrict__ partials, int nblocks, int npairs, long long p0,
                                         int gram, int upper_only, int a, double alpha, double beta, double* out,
                                         int ldo) {
-    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const long long t = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
     if (t >= npairs) return;
     double v = 0.0;
-    for (int b = 0; b < nblocks; ++b) v += partials[(long long)b * npairs + t];
+    for (int b = lane; b < nblocks; b += 32) v += partials[(long long)b * npairs + t];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if (lane != 0) return;
     int i, j;
     pair_ij(p0 + t, gram, a, i, j);
     double* o = out + i + (long long)j * ldo;
@@ -135,6 +141,8 @@ __global__ void crossprod_reduce_kernel(const double* __restrict__ partials, int
         *o2 = alpha * v + (beta != 0.0 ? beta * (*o2) : 0.0);
     }
 }
+
+inline unsigned reduce_blocks(long long npairs) { return (unsigned)((npairs * 32 + 255) / 256); }
 
 constexpr int RS_THREADS = 256;
 
@@ -449,7 +457,7 @@ int crossprod(const MatView& A, const MatView& B, long long n, bool gram, bool u
             double* zeros = nullptr;
             FEGB_TRY(scr.alloc(&zeros, (size_t)np, "crossprod zeros"));
             FEGB_CUDA(cudaMemsetAsync(zeros, 0, sizeof(double) * np, s), "crossprod zero");
-            crossprod_reduce_kernel<<<(np + 255) / 256, 256, 0, s>>>(zeros, 1, np, p0, gram, upper_only, a, alpha,
+            crossprod_reduce_kernel<<<reduce_blocks(np), 256, 0, s>>>(zeros, 1, np, p0, gram, upper_only, a, alpha,
                                                                       beta, out, ldo);
             FEGB_LAUNCH_CHECK("crossprod zero reduce");
         }
@@ -506,7 +514,7 @@ int crossprod(const MatView& A, const MatView& B, long long n, bool gram, bool u
         else
             crossprod_kernel<32><<<(unsigned)nb, CP_THREADS, smem, s>>>(p);
         FEGB_LAUNCH_CHECK("crossprod");
-        crossprod_reduce_kernel<<<(np + 255) / 256, 256, 0, s>>>(partials, (int)nb, np, p0, gram, upper_only, a, alpha,
+        crossprod_reduce_kernel<<<reduce_blocks(np), 256, 0, s>>>(partials, (int)nb, np, p0, gram, upper_only, a, alpha,
                                                                   beta, out, ldo);
         FEGB_LAUNCH_CHECK("crossprod reduce");
     }
@@ -522,9 +530,9 @@ constexpr int DS_SMEM = 48 * 1024;  // tile bytes aimed at (several blocks per S
 constexpr int DS_PPT = 4;       // output entries per thread
 constexpr int DS_PAIRS_PER_BLOCK = CP_THREADS * DS_PPT;
 
-// Largest magnitude the split path accepts: products and 256-row partial sums
-// stay far inside the FP32 range (2^127).
-constexpr double DS_MAX_ABS = 72057594037927936.0;  // 2^56
+// The split path accepts magnitudes in [2^-60, 2^57) (and zero): products
+// and 256-row partial sums then stay inside the FP32 range (2^127) and the
+// low parts stay normal (see split_bits).
 
 struct DSParams {
     const double* A;  // FP64 source, element (r, c) at A[r * ars + c * acs]
@@ -541,8 +549,31 @@ struct DSParams {
     long long rows_per_block;
     int tr;            // rows per tile
     double* partials;  // row blocks x npairs
-    int* bad;          // set when a value is not finite or exceeds DS_MAX_ABS
+    int* bad;          // set when a value is outside the split range (split_bits)
 };
+
+// (hi, lo) FP32 pair of an FP64 value from its IEEE-754 fields, without the
+// FP64 pipe: hi = the leading 24 significant bits (truncated), lo = the
+// remaining 29 bits times their power of two (rounded to 24 bits by the
+// integer conversion, scaled exactly), so |v - hi - lo| <= 2^-48 |v|. Zero
+// maps to (0, 0); a value outside [2^-60, 2^57) in magnitude (or not finite,
+// or subnormal) sets bad.
+__device__ __forceinline__ float2 split_bits(double v, bool& bad) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+    if ((b << 1) == 0ULL) return make_float2(0.f, 0.f);
+    const int e = (int)((b >> 52) & 0x7FF);
+    if (e < 1023 - 60 || e > 1023 + 56) {
+        bad = true;
+        return make_float2(0.f, 0.f);
+    }
+    const unsigned sign = (unsigned)(b >> 63) << 31;
+    const unsigned long long mant = b & ((1ULL << 52) - 1ULL);
+    const float hi = __uint_as_float(sign | ((unsigned)(e - 1023 + 127) << 23) | (unsigned)(mant >> 29));
+    const unsigned rem = (unsigned)(mant & ((1ULL << 29) - 1ULL));
+    const float scale = __uint_as_float((unsigned)(e - 1075 + 127) << 23);  // 2^(e - 1075), a normal float here
+    const float lo = __uint_as_float(__float_as_uint((float)rem * scale) | sign);
+    return make_float2(hi, lo);
+}
 
 // Tile rows [row0, row0 + rows) of an FP64 source into shared memory as
 // (hi, lo) FP32 pairs: hi = fl32(x), lo = fl32(x - hi) (x - hi is exact in FP64).
@@ -559,10 +590,7 @@ __device__ __forceinline__ bool load_split_tile(float2* dst, const double* src, 
             r = e / width;
             c = e - r * width;
         }
-        const double x = src[(row0 + r) * rs + (long long)c * cs];
-        out_of_range |= !(fabs(x) <= DS_MAX_ABS);
-        const float hi = __double2float_rn(x);
-        dst[r * width + c] = make_float2(hi, __double2float_rn(x - (double)hi));
+        dst[r * width + c] = split_bits(src[(row0 + r) * rs + (long long)c * cs], out_of_range);
     }
     return out_of_range;
 }
@@ -656,6 +684,106 @@ __global__ void __launch_bounds__(CP_THREADS) crossprod_split_kernel(DSParams p)
     }
 }
 
+// Thin Gram products (A <= DS_ROWS_MAX_A columns): each row is handled by
+// SPLIT threads (one per warp of a warp group), thread part q holding the
+// pairs [q NPP, (q + 1) NPP) in registers as double-single sums; each thread
+// sums at most DS_ROWS_PER_THREAD rows, so the FP32 parts stay in range. The
+// threads' FP64 totals are reduced per block in a fixed order (warp shuffle
+// tree, then the row groups in order). Pair p = j (j + 1) / 2 + i, i <= j.
+constexpr int DS_ROWS_GROUPS = 2;        // row groups (of 32 rows) per block
+constexpr int DS_ROWS_PER_THREAD = 64;
+constexpr int DS_ROWS_MAX_A = 10;
+
+__host__ __device__ constexpr int ds_rows_split(int A) { return A * (A + 1) / 2 <= 16 ? 1 : (A * (A + 1) / 2 + 15) / 16; }
+
+template <int A, int SPLIT, int PART>
+__device__ __forceinline__ void split_rows_part(const double* __restrict__ X, long long rs, long long r0,
+                                                long long r1, int lane, double (*red)[A * (A + 1) / 2], int rg,
+                                                bool& oor) {
+    constexpr int NP = A * (A + 1) / 2;
+    constexpr int NPP = (NP + SPLIT - 1) / SPLIT;
+    constexpr int LO = PART * NPP;
+    constexpr int HI = (LO + NPP < NP) ? LO + NPP : NP;
+    float sh[NPP], sl[NPP];
+#pragma unroll
+    for (int q = 0; q < NPP; ++q) sh[q] = sl[q] = 0.f;
+    for (long long r = r0 + lane; r < r1; r += 32) {
+        float2 x[A];
+#pragma unroll
+        for (int i = 0; i < A; ++i) x[i] = split_bits(X[r * rs + i], oor);
+        int q = 0;
+#pragma unroll
+        for (int j = 0; j < A; ++j)
+#pragma unroll
+            for (int i = 0; i <= j; ++i, ++q)
+                if (q >= LO && q < HI) ds_fma(x[i], x[j], sh[q - LO], sl[q - LO]);
+    }
+#pragma unroll
+    for (int q = LO; q < HI; ++q) {
+        double v = (double)sh[q - LO] + (double)sl[q - LO];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if (lane == 0) red[rg][q] = v;
+    }
+}
+
+template <int A, int SPLIT, int PART>
+__device__ __forceinline__ void split_rows_select(int part, const double* X, long long rs, long long r0, long long r1,
+                                                  int lane, double (*red)[A * (A + 1) / 2], int rg, bool& oor) {
+    if constexpr (PART < SPLIT) {
+        if (part == PART)
+            split_rows_part<A, SPLIT, PART>(X, rs, r0, r1, lane, red, rg, oor);
+        else
+            split_rows_select<A, SPLIT, PART + 1>(part, X, rs, r0, r1, lane, red, rg, oor);
+    }
+}
+
+template <int A>
+__global__ void __launch_bounds__(32 * ds_rows_split(A) * DS_ROWS_GROUPS)
+    crossprod_split_rows_kernel(const double* __restrict__ X, long long rs, long long n, double* __restrict__ partials,
+                                int* __restrict__ bad) {
+    constexpr int NP = A * (A + 1) / 2;
+    constexpr int SPLIT = ds_rows_split(A);
+    __shared__ double red[DS_ROWS_GROUPS][NP];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int part = warp % SPLIT, rg = warp / SPLIT;
+    const long long rows_rg = 32LL * DS_ROWS_PER_THREAD;
+    const long long r0 = ((long long)blockIdx.x * DS_ROWS_GROUPS + rg) * rows_rg;
+    const long long r1 = min(n, r0 + rows_rg);
+    bool oor = false;
+    split_rows_select<A, SPLIT, 0>(part, X, rs, r0, r1, lane, red, rg, oor);
+    if (__any_sync(0xffffffffu, oor) && lane == 0) atomicOr(bad, 1);
+    __syncthreads();
+    for (int q = threadIdx.x; q < NP; q += blockDim.x) {
+        double v = 0.0;
+        for (int g = 0; g < DS_ROWS_GROUPS; ++g) v += red[g][q];
+        partials[(long long)blockIdx.x * NP + q] = v;
+    }
+}
+
+template <int A>
+int split_rows_launch(const double* X, long long rs, long long n, double* partials, int* bad, int nb, cudaStream_t s) {
+    crossprod_split_rows_kernel<A><<<nb, 32 * ds_rows_split(A) * DS_ROWS_GROUPS, 0, s>>>(X, rs, n, partials, bad);
+    FEGB_LAUNCH_CHECK("split crossprod (rows)");
+    return 0;
+}
+
+int split_rows_dispatch(int a, const double* X, long long rs, long long n, double* partials, int* bad, int nb,
+                        cudaStream_t s) {
+    switch (a) {
+        case 2: return split_rows_launch<2>(X, rs, n, partials, bad, nb, s);
+        case 3: return split_rows_launch<3>(X, rs, n, partials, bad, nb, s);
+        case 4: return split_rows_launch<4>(X, rs, n, partials, bad, nb, s);
+        case 5: return split_rows_launch<5>(X, rs, n, partials, bad, nb, s);
+        case 6: return split_rows_launch<6>(X, rs, n, partials, bad, nb, s);
+        case 7: return split_rows_launch<7>(X, rs, n, partials, bad, nb, s);
+        case 8: return split_rows_launch<8>(X, rs, n, partials, bad, nb, s);
+        case 9: return split_rows_launch<9>(X, rs, n, partials, bad, nb, s);
+        case 10: return split_rows_launch<10>(X, rs, n, partials, bad, nb, s);
+        default: return set_error("split crossprod (rows): %d columns", a);
+    }
+}
+
 }  // namespace
 
 int crossprod_split(const MatView& A, const MatView& B, long long n, bool gram, bool upper_only, double alpha,
@@ -681,6 +809,22 @@ int crossprod_split(const MatView& A, const MatView& B, long long n, bool gram, 
     FEGB_TRY(scr.alloc(&bad, 1, "split range flag"));
     FEGB_CUDA(cudaMemsetAsync(bad, 0, sizeof(int), s), "split flag reset");
     const long long total_pairs = gram ? (long long)a * (a + 1) / 2 : (long long)a * b;
+    if (gram && A.cs == 1 && A.rs >= a && a >= 2 && a <= DS_ROWS_MAX_A) {
+        const long long rows_pb = 32LL * DS_ROWS_GROUPS * DS_ROWS_PER_THREAD;
+        const long long nb = (n + rows_pb - 1) / rows_pb;
+        if (nb > 0x7fffffffLL) return crossprod(A, B, n, gram, upper_only, alpha, beta, out, ldo, s, scr);
+        double* partials = nullptr;
+        FEGB_TRY(scr.alloc(&partials, (size_t)nb * total_pairs, "split crossprod partials"));
+        FEGB_TRY(split_rows_dispatch(a, A.ptr, A.rs, n, partials, bad, (int)nb, s));
+        crossprod_reduce_kernel<<<reduce_blocks(total_pairs), 256, 0, s>>>(
+            partials, (int)nb, (int)total_pairs, 0, 1, upper_only, a, alpha, beta, out, ldo);
+        FEGB_LAUNCH_CHECK("split crossprod reduce");
+        int hbad = 0;
+        FEGB_CUDA(cudaMemcpyAsync(&hbad, bad, sizeof(int), cudaMemcpyDeviceToHost, s), "split flag copy");
+        FEGB_CUDA(cudaStreamSynchronize(s), "split flag sync");
+        if (hbad) return crossprod(A, B, n, gram, upper_only, alpha, beta, out, ldo, s, scr);
+        return 0;
+    }
     long long nb = std::min<long long>((n + tr - 1) / tr, (long long)num_sms() * 8);
     long long rpb = (n + nb - 1) / nb;
     rpb = ((rpb + tr - 1) / tr) * tr;
@@ -714,7 +858,7 @@ int crossprod_split(const MatView& A, const MatView& B, long long n, bool gram, 
             crossprod_split_kernel<DS_PPT><<<grid, CP_THREADS, smem, s>>>(p);
         }
         FEGB_LAUNCH_CHECK("split crossprod");
-        crossprod_reduce_kernel<<<(np + 255) / 256, 256, 0, s>>>(partials, (int)nb, np, p0, gram, upper_only, a, alpha,
+        crossprod_reduce_kernel<<<reduce_blocks(np), 256, 0, s>>>(partials, (int)nb, np, p0, gram, upper_only, a, alpha,
                                                                   beta, out, ldo);
         FEGB_LAUNCH_CHECK("split crossprod reduce");
     }
@@ -883,7 +1027,7 @@ extern "C" int fe_gpu_syrk_noalloc(int n_rows, int n_cols, double alpha, const d
         FEGB_LAUNCH_CHECK("syrk noalloc");
     }
     // nb = 0 (no rows) leaves Q = beta Q on the upper triangle
-    crossprod_reduce_kernel<<<(npairs + 255) / 256, 256, 0, s>>>(partials, nb, npairs, 0, 1, 1, n_cols, alpha, beta, Q,
+    crossprod_reduce_kernel<<<reduce_blocks(npairs), 256, 0, s>>>(partials, nb, npairs, 0, 1, 1, n_cols, alpha, beta, Q,
                                                                   n_cols);
     FEGB_LAUNCH_CHECK("syrk noalloc reduce");
     FEGB_CUDA(cudaStreamSynchronize(s), "syrk noalloc sync");

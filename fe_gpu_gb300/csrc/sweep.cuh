@@ -157,16 +157,17 @@ int launch_apply_pending(T* X, int C, long long n, const PendingSet<T>& pend, cu
 // dst (float) = (float) src (double), n elements
 int launch_convert_f64_f32(const double* src, float* dst, long long n, cudaStream_t s);
 
-// ---- row-per-lane operator sweep for the CG normal-equation operator ----
-// Position j of a dimension's group-sorted order has destination group
-// gseq[j] and source ids src_gid[e][j] for the other dimensions; the sweep
-// forms, per destination group, sum over its positions of
-// -(sum_e src_tab[e][src_gid[e][j]]) (no row data). Each warp owns a chunk of
-// CG_CHUNK = 32 x 16 positions; each lane accumulates its 16 positions (runs
-// of equal destination in registers, storage type T); runs that cross lanes
-// are combined by a warp scan in FP64. Output layout as the segment sweep
-// (sums / head / tail with chunk size CG_CHUNK).
-constexpr int CG_LANE_POS = 16;
+// ---- position sweep for the CG normal-equation operator ----
+// Position j of a dimension's group-sorted stream has destination group
+// gseq[j], source ids src_gid[e][j] for the other swept dimensions and an
+// optional weight w[j] (the rows it stands for); the sweep forms, per
+// destination group, the sum over its positions of
+// -w[j] (sum_e src_tab[e][src_gid[e][j]]) (no row data). Each warp owns a
+// chunk of CG_CHUNK = 32 x CG_LANE_POS positions; each lane accumulates its
+// positions (runs of equal destination in registers, storage type T); runs
+// that cross lanes are combined by a flag-precomputed warp scan in T. Output:
+// complete-run sums (T) and chunk head/tail partials (FP64), compact rows.
+constexpr int CG_LANE_POS = 8;
 constexpr int CG_CHUNK = 32 * CG_LANE_POS;
 
 template <typename T>

@@ -887,6 +887,16 @@ struct CGBuffers {
     };
     std::vector<Stream> stream;
     bool compressed = false;
+    // Schur-complement form: the primary (largest) dimension is eliminated, the
+    // CG vectors span the other dimensions only (off[d]: their rows, Gv in all),
+    // and the primary's slot of p (at off[primary]) holds -u = -(1/n) D_P'D_R x,
+    // the primary's response to the other dimensions' x
+    bool schur = false;
+    int prim = -1;
+    std::vector<long long> off;
+    long long Gv = 0;
+    int32_t* counts_v = nullptr;  // group sizes in the CG layout
+    double* mu_v = nullptr;       // FP64 group means in the CG layout (Schur form)
 };
 
 // Position streams of the CG operator sweeps (see CGBuffers::Stream). The
@@ -1015,25 +1025,65 @@ int cg_alloc(Problem& P, CGBuffers<T>& B) {
     // r, z, q, x: compact rows of C; p (gathered by the operator sweep): rows padded to B.ld
     B.ld = cg_row_stride(P.C, (int)sizeof(T));
     const int C = P.C;
-    const size_t nc = (size_t)std::max(1LL, P.Gt) * C;
-    const size_t np = (size_t)std::max(1LL, P.Gt) * B.ld;
+    // layout: the Schur form when the primary is swept (more than DENSE_SMALL_MAX_G
+    // groups, or too many columns for the dense path) and another dimension exists
+    B.prim = P.primary;
+    {
+        int others = 0;
+        for (int d = 0; d < P.n_fe; ++d)
+            if (d != P.primary && P.dims[d].G > 0) ++others;
+        const bool prim_dense = P.primary < 0 || (P.dims[P.primary].G <= DENSE_SMALL_MAX_G && C <= 32);
+        B.schur = !prim_dense && others > 0 && P.dims[P.primary].G > 0;
+    }
+    B.off.assign(P.n_fe, 0);
+    long long prows = 0;  // rows of p
+    if (B.schur) {
+        long long o = 0;
+        for (int d = 0; d < P.n_fe; ++d) {
+            if (d == B.prim) continue;
+            B.off[d] = o;
+            o += std::max(1, P.dims[d].G);
+        }
+        B.Gv = o;
+        B.off[B.prim] = o;
+        prows = o + std::max(1, P.dims[B.prim].G);
+    } else {
+        for (int d = 0; d < P.n_fe; ++d) B.off[d] = P.goff[d];
+        B.Gv = P.Gt;
+        prows = P.Gt;
+    }
+    const size_t nc = (size_t)std::max(1LL, B.Gv) * C;
+    const size_t np = (size_t)std::max(1LL, prows) * B.ld;
     FEGB_TRY(dalloc(scr, &B.r, nc, "cg r"));
     FEGB_TRY(dalloc(scr, &B.z, nc, "cg z"));
     FEGB_TRY(dalloc(scr, &B.p, np, "cg p"));
     FEGB_CUDA(cudaMemsetAsync(B.p, 0, sizeof(T) * np, P.s), "cg p padding zero");
     FEGB_TRY(dalloc(scr, &B.q, nc, "cg q"));
     FEGB_TRY(dalloc(scr, &B.x, nc, "cg solution"));
-    FEGB_TRY(dalloc(scr, &B.inv, (size_t)std::max(1LL, P.Gt), "cg inverse counts"));
-    FEGB_TRY(launch_inv_counts_t<T>(P.counts_all, P.Gt, B.inv, P.s));
+    if (B.schur) {
+        FEGB_TRY(dalloc(scr, &B.counts_v, (size_t)std::max(1LL, B.Gv), "cg counts"));
+        FEGB_TRY(dalloc(scr, &B.mu_v, nc, "cg group means"));
+        FEGB_CUDA(cudaMemsetAsync(B.counts_v, 0, sizeof(int32_t) * (size_t)std::max(1LL, B.Gv), P.s), "cg counts");
+        for (int d = 0; d < P.n_fe; ++d)
+            if (d != B.prim && P.dims[d].G > 0)
+                FEGB_CUDA(cudaMemcpyAsync(B.counts_v + B.off[d], P.counts_all + P.goff[d],
+                                          sizeof(int32_t) * P.dims[d].G, cudaMemcpyDeviceToDevice, P.s),
+                          "cg counts copy");
+    } else {
+        B.counts_v = P.counts_all;
+    }
+    FEGB_TRY(dalloc(scr, &B.inv, (size_t)std::max(1LL, B.Gv), "cg inverse counts"));
+    FEGB_TRY(launch_inv_counts_t<T>(B.counts_v, B.Gv, B.inv, P.s));
     const int L = B.ld;
     FEGB_TRY(dalloc(scr, &B.rz, (size_t)C, "cg rz"));
     FEGB_TRY(dalloc(scr, &B.rz_new, (size_t)C, "cg rz new"));
     FEGB_TRY(dalloc(scr, &B.pq, (size_t)C, "cg pq"));
     FEGB_TRY(dalloc(scr, &B.zmax, 1, "cg zmax"));
-    B.rz_blocks = cg_partial_blocks(P.Gt, C);
+    B.rz_blocks = cg_partial_blocks(B.Gv, C);
     B.pq_block_off.assign(P.n_fe + 1, 0);
     for (int d = 0; d < P.n_fe; ++d)
-        B.pq_block_off[d + 1] = B.pq_block_off[d] + cg_partial_blocks(std::max(1, P.dims[d].G), C);
+        B.pq_block_off[d + 1] =
+            B.pq_block_off[d] + (B.schur && d == B.prim ? 0 : cg_partial_blocks(std::max(1, P.dims[d].G), C));
     B.pq_blocks = B.pq_block_off[P.n_fe];
     FEGB_TRY(dalloc(scr, &B.rz_part, (size_t)B.rz_blocks * C, "cg rz partials"));
     FEGB_TRY(dalloc(scr, &B.zmax_part, (size_t)B.rz_blocks, "cg zmax partials"));
@@ -1089,7 +1139,7 @@ int cg_alloc(Problem& P, CGBuffers<T>& B) {
             if (B.any_dense) {
                 FEGB_TRY(dalloc(scr, &B.dense_part, (size_t)std::max(1LL, parts), "dense partials"));
                 FEGB_TRY(dalloc(scr, &B.dense_sums, (size_t)std::max(1LL, sums), "dense sums"));
-                FEGB_TRY(dalloc(scr, &B.extra, (size_t)std::max(1LL, P.Gt) * C, "dense extra"));
+                FEGB_TRY(dalloc(scr, &B.extra, (size_t)std::max(1LL, prows) * C, "dense extra"));
             }
         }
     }
@@ -1106,42 +1156,131 @@ int cg_alloc(Problem& P, CGBuffers<T>& B) {
     return 0;
 }
 
-// q = D'D p, dimension by dimension: a no-data sweep over d's traversal with
-// the other dimensions' p as pending tables, then q_d = counts_d p_d - sums.
-template <typename T>
-int cg_apply(Problem& P, CGBuffers<T>& B) {
-    const int C = P.C;
-    const int L = B.ld;
-    auto begin_timed = [&](Problem::Timed& tm, int kind, double bytes) -> int {
+// Profile events around a group of launches (no-ops unless P.profile).
+struct CGTimer {
+    Problem& P;
+    Problem::Timed tm{};
+    bool on = false;
+    explicit CGTimer(Problem& p) : P(p) {}
+    int begin(int kind, double bytes) {
         if (!P.profile) return 0;
         tm.kind = kind;
         tm.bytes = bytes;
         FEGB_CUDA(cudaEventCreate(&tm.a), "profile event");
         FEGB_CUDA(cudaEventCreate(&tm.b), "profile event");
         FEGB_CUDA(cudaEventRecord(tm.a, P.s), "profile record");
+        on = true;
         return 0;
-    };
-    auto end_timed = [&](Problem::Timed& tm) -> int {
-        if (!P.profile) return 0;
+    }
+    int end() {
+        if (!on) return 0;
         FEGB_CUDA(cudaEventRecord(tm.b, P.s), "profile record");
         P.timed.push_back(tm);
+        on = false;
         return 0;
-    };
-    const int fp32 = sizeof(T) == 4 ? 1 : 0;
-    // 1. dimensions with few groups: one pass over each count matrix gives the
-    // small dimension's sums and the other dimension's share (extra)
+    }
+};
+
+// The operator sweep of swept dimension d over its stream: complete group sums
+// of -(sum of the sources' rows, weighted) into B.sums (storage type, stride C).
+// Returns the number of swept sources (0: no sweep, B.sums untouched).
+template <typename T>
+int cg_sweep(Problem& P, CGBuffers<T>& B, int d, int* n_src) {
+    const int C = P.C;
+    const int L = B.ld;
+    const auto& st = B.stream[d];
+    *n_src = st.n_src;
+    if (st.n_src == 0) return 0;
+    CGRowsParams<T> rp{};
+    rp.n = st.m;
+    rp.C = C;
+    rp.ld = L;
+    rp.gseq = st.gseq;
+    rp.n_src = st.n_src;
+    for (int i = 0; i < st.n_src; ++i) {
+        rp.src_gid[i] = st.src_gid[i];
+        rp.src_tab[i] = B.p + B.off[st.src_dim[i]] * L;
+    }
+    rp.weight = st.weight;
+    rp.sums = B.sums;
+    rp.head = B.head;
+    rp.tail = B.tail;
+    // per position: destination id, source ids, weight, gathered source rows
+    const double bytes =
+        (double)st.m * (4.0 * (1 + rp.n_src) + (st.weight ? 4.0 : 0.0) + (double)rp.n_src * C * sizeof(T));
+    CGTimer tm(P);
+    FEGB_TRY(tm.begin(4 + (sizeof(T) == 4 ? 1 : 0), bytes));
+    FEGB_TRY(launch_cg_rows<T>(rp, P.s));
+    FEGB_TRY(launch_group_sums<T>(st.off, B.head, B.tail, CG_CHUNK, C, st.long_list, st.n_long, st.multi_list,
+                                  st.n_multi, B.sums, P.s));
+    FEGB_TRY(tm.end());
+    P.demean_bytes += bytes;
+    return 0;
+}
+
+// Schur form, step 1: the primary's slot of p = -u with
+// u = (1/n_P) (D_P'D_R x), x = the other dimensions' rows of p: the primary's
+// stream sweep gives -(sum over its rows of the swept dimensions' x), the dense
+// count matrices the small dimensions' share.
+template <typename T>
+int cg_schur_u(Problem& P, CGBuffers<T>& B) {
+    const int C = P.C;
+    const int L = B.ld;
+    const int pd = B.prim;
+    const Dim& D = P.dims[pd];
+    int n_src = 0;
+    FEGB_TRY(cg_sweep<T>(P, B, pd, &n_src));
+    if (n_src == 0) FEGB_CUDA(cudaMemsetAsync(B.sums, 0, sizeof(T) * (size_t)D.G * C, P.s), "schur sums zero");
+    T* ex = nullptr;
     if (B.any_dense) {
-        Problem::Timed tm{};
+        CGTimer tm(P);
+        double bytes = 0.0;
+        bool first = true;
+        FEGB_TRY(tm.begin(6 + (sizeof(T) == 4 ? 1 : 0), 0.0));
+        for (int sd = 0; sd < P.n_fe; ++sd) {
+            if (!B.dense[sd]) continue;
+            ex = B.extra + B.off[pd] * C;
+            const T* ps = B.p + B.off[sd] * L;
+            if (B.N8[sd][pd])
+                FEGB_TRY((launch_dense_pair<T, uint8_t>(B.N8[sd][pd], D.G, P.dims[sd].G, nullptr, ps, L, C, nullptr,
+                                                        ex, first ? 0 : 1, P.s)));
+            else
+                FEGB_TRY((launch_dense_pair<T, uint32_t>(B.N32[sd][pd], D.G, P.dims[sd].G, nullptr, ps, L, C,
+                                                         nullptr, ex, first ? 0 : 1, P.s)));
+            bytes += (double)D.G * ((B.N8[sd][pd] ? 1.0 : 4.0) * P.dims[sd].G + (double)C * sizeof(T) * (first ? 1 : 2));
+            first = false;
+        }
+        tm.tm.bytes = bytes;
+        FEGB_TRY(tm.end());
+        P.demean_bytes += bytes;
+    }
+    return launch_schur_u<T>(B.sums, ex, D.counts, D.G, C, B.p + B.off[pd] * L, L, P.s);
+}
+
+// q = D'D p over the CG dimensions, given p (and, in the Schur form, the
+// primary's slot of p): (1) one pass over each count matrix of a small
+// dimension, (2) the operator sweep of each many-group dimension, (3) q of
+// the small dimensions from their complete sums. In the Schur form the primary
+// is a source of the sweeps and of the count-matrix passes but has no q.
+template <typename T>
+int cg_apply_rest(Problem& P, CGBuffers<T>& B) {
+    const int C = P.C;
+    const int L = B.ld;
+    const int fp32 = sizeof(T) == 4 ? 1 : 0;
+    auto in_cg = [&](int d) { return P.dims[d].G > 0 && !(B.schur && d == B.prim); };
+    if (B.any_dense) {
+        CGTimer tm(P);
         double bytes = 0.0;
         for (int sd = 0; sd < P.n_fe; ++sd) {
             if (!B.dense[sd]) continue;
             for (int e = 0; e < P.n_fe; ++e) {
                 if (e == sd || P.dims[e].G <= 0) continue;
                 const double cb = B.N8[sd][e] ? 1.0 : 4.0;
-                bytes += (double)P.dims[e].G * (cb * P.dims[sd].G + (double)C * sizeof(T) * (B.dense[e] ? 1.0 : 2.0));
+                const bool ext = !B.dense[e] && in_cg(e);
+                bytes += (double)P.dims[e].G * (cb * P.dims[sd].G + (double)C * sizeof(T) * (ext ? 2.0 : 1.0));
             }
         }
-        FEGB_TRY(begin_timed(tm, 6 + fp32, bytes));
+        FEGB_TRY(tm.begin(6 + fp32, bytes));
         std::vector<char> written(P.n_fe, 0);
         for (int sd = 0; sd < P.n_fe; ++sd) {
             if (!B.dense[sd]) continue;
@@ -1150,10 +1289,11 @@ int cg_apply(Problem& P, CGBuffers<T>& B) {
             double* pbase = B.dense_part + B.dpart_off[sd];
             for (int e = 0; e < P.n_fe; ++e) {
                 if (e == sd || P.dims[e].G <= 0) continue;
-                T* ex = B.dense[e] ? nullptr : B.extra + P.goff[e] * C;
+                // the small side always; the other side only for a swept CG dimension
+                T* ex = (B.dense[e] || !in_cg(e)) ? nullptr : B.extra + B.off[e] * C;
                 const int acc = ex && written[e] ? 1 : 0;
-                const T* pe = B.p + P.goff[e] * L;
-                const T* ps = B.p + P.goff[sd] * L;
+                const T* pe = B.p + B.off[e] * L;
+                const T* ps = B.p + B.off[sd] * L;
                 if (B.N8[sd][e])
                     FEGB_TRY((launch_dense_pair<T, uint8_t>(B.N8[sd][e], P.dims[e].G, Gs, pe, ps, L, C,
                                                             pbase + part * Gs * C, ex, acc, P.s)));
@@ -1165,70 +1305,94 @@ int cg_apply(Problem& P, CGBuffers<T>& B) {
             }
             FEGB_TRY(launch_fold_dense(pbase, (int)part, Gs, C, B.dense_sums + B.dsum_off[sd], P.s));
         }
-        FEGB_TRY(end_timed(tm));
+        FEGB_TRY(tm.end());
         P.demean_bytes += bytes;
     }
-    // 2. the many-group dimensions: each is swept in its group-sorted order
-    // (identity for the primary) over the other many-group dimensions
     for (int d = 0; d < P.n_fe; ++d) {
         Dim& D = P.dims[d];
-        if (D.G <= 0 || B.dense[d]) continue;
-        Problem::Timed tm{};
-        const auto& st = B.stream[d];
-        CGRowsParams<T> rp{};
-        rp.n = st.m;
-        rp.C = C;
-        rp.ld = L;
-        rp.gseq = st.gseq;
-        rp.n_src = st.n_src;
-        for (int i = 0; i < st.n_src; ++i) {
-            rp.src_gid[i] = st.src_gid[i];
-            rp.src_tab[i] = B.p + P.goff[st.src_dim[i]] * L;
-        }
-        rp.weight = st.weight;
+        if (!in_cg(d) || B.dense[d]) continue;
+        int n_src = 0;
+        FEGB_TRY(cg_sweep<T>(P, B, d, &n_src));
         FinalizeParams src{};
         src.G = D.G;
         src.counts = D.counts;
-        if (rp.n_src > 0) {
-            // per position: destination id, source ids, weight, gathered source rows
-            const double bytes = (double)st.m * (4.0 * (1 + rp.n_src) + (st.weight ? 4.0 : 0.0) +
-                                                 (double)rp.n_src * C * sizeof(T));
-            FEGB_TRY(begin_timed(tm, 4 + fp32, bytes));
-            rp.sums = B.sums;
-            rp.head = B.head;
-            rp.tail = B.tail;
-            FEGB_TRY(launch_cg_rows<T>(rp, P.s));
-            FEGB_TRY(launch_group_sums<T>(st.off, B.head, B.tail, CG_CHUNK, C, st.long_list, st.n_long,
-                                          st.multi_list, st.n_multi, B.sums, P.s));
-            FEGB_TRY(end_timed(tm));
-            P.demean_bytes += bytes;
-            src.C = C;  // complete sums, compact rows
+        src.C = C;  // complete sums, compact rows (none without a swept source)
+        if (n_src > 0) {
             if constexpr (sizeof(T) == 4)
                 src.sums32 = reinterpret_cast<const float*>(B.sums);
             else
                 src.sums = reinterpret_cast<const double*>(B.sums);
-        } else {
-            src.C = C;
-            src.sums = nullptr;  // no swept source
         }
-        FEGB_TRY(launch_cg_q<T>(src, C, B.p + P.goff[d] * L, L, B.q + P.goff[d] * C,
+        FEGB_TRY(launch_cg_q<T>(src, C, B.p + B.off[d] * L, L, B.q + B.off[d] * C,
                                 B.pq_part + (size_t)B.pq_block_off[d] * C, P.s,
-                                B.any_dense ? B.extra + P.goff[d] * C : nullptr));
+                                B.any_dense ? B.extra + B.off[d] * C : nullptr));
         P.projections += 1;
     }
-    // 3. the dimensions with few groups, from their complete sums
     for (int sd = 0; sd < P.n_fe; ++sd) {
-        if (!B.dense[sd]) continue;
+        if (!B.dense[sd] || !in_cg(sd)) continue;
         FinalizeParams src{};
         src.G = P.dims[sd].G;
         src.C = C;
         src.sums = B.dense_sums + B.dsum_off[sd];  // complete sums of -p, compact rows
         src.counts = P.dims[sd].counts;
-        FEGB_TRY(launch_cg_q<T>(src, C, B.p + P.goff[sd] * L, L, B.q + P.goff[sd] * C,
+        FEGB_TRY(launch_cg_q<T>(src, C, B.p + B.off[sd] * L, L, B.q + B.off[sd] * C,
                                 B.pq_part + (size_t)B.pq_block_off[sd] * C, P.s));
         P.projections += 1;
     }
-    return launch_fold_partials(B.pq_part, B.pq_blocks, C, B.pq, P.s);
+    return 0;
+}
+
+// One operator application q = A p with the p.q partials folded into B.pq:
+// A = D'D, or in the Schur form A = D_R'(I - P_P) D_R over the non-primary
+// dimensions R (P_P: projection on the primary's group means).
+template <typename T>
+int cg_apply(Problem& P, CGBuffers<T>& B) {
+    if (B.schur) FEGB_TRY(cg_schur_u<T>(P, B));
+    FEGB_TRY(cg_apply_rest<T>(P, B));
+    return launch_fold_partials(B.pq_part, B.pq_blocks, P.C, B.pq, P.s);
+}
+
+// Start of an inner solve from the current FP64 group means (mu_all):
+// standard form r = D'r_data = counts * mu; Schur form
+// r = D_R'(I - P_P) r_data = counts_R * mu_R - D_R'D_P mu_P, obtained from the
+// operator with x = 0 and the primary's slot of p = -mu_P.
+template <typename T>
+int cg_start(Problem& P, CGBuffers<T>& B) {
+    const int C = P.C;
+    const int L = B.ld;
+    if (!B.schur)
+        return launch_cg_init<T>(P.Gt, C, P.counts_all, P.mu_all, B.r, B.z, B.p, L, B.x, B.rz_part, B.zmax_part,
+                                 B.zmax, P.s);
+    const int pd = B.prim;
+    FEGB_CUDA(cudaMemsetAsync(B.p, 0, sizeof(T) * (size_t)B.Gv * L, P.s), "cg p zero");
+    FEGB_TRY(launch_table_from_f64<T>(P.mu_all + P.goff[pd] * C, P.dims[pd].G, C, -1.0, B.p + B.off[pd] * L, L,
+                                      P.s));
+    FEGB_TRY(cg_apply_rest<T>(P, B));
+    for (int d = 0; d < P.n_fe; ++d)
+        if (d != pd && P.dims[d].G > 0)
+            FEGB_CUDA(cudaMemcpyAsync(B.mu_v + B.off[d] * C, P.mu_all + P.goff[d] * C,
+                                      sizeof(double) * (size_t)P.dims[d].G * C, cudaMemcpyDeviceToDevice, P.s),
+                      "cg means copy");
+    return launch_cg_init_rhs<T>(B.Gv, C, B.counts_v, B.mu_v, B.q, B.inv, B.r, B.z, B.p, L, B.x, B.rz_part,
+                                 B.zmax_part, B.zmax, P.s);
+}
+
+// End of an inner solve: the FE increments of x become the FP64 table applied
+// by the next FP64 pass; in the Schur form the primary's increment is
+// mu_P - u(x) (the group means of the residual after the others' increments).
+template <typename T>
+int cg_finish(Problem& P, CGBuffers<T>& B) {
+    const int C = P.C;
+    const int L = B.ld;
+    if (!B.schur) return launch_to_f64<T>(B.x, C, P.alpha_all, C, P.Gt, P.s);
+    const int pd = B.prim;
+    for (int d = 0; d < P.n_fe; ++d)
+        if (d != pd && P.dims[d].G > 0)
+            FEGB_TRY(launch_to_f64<T>(B.x + B.off[d] * C, C, P.alpha_all + P.goff[d] * C, C, P.dims[d].G, P.s));
+    FEGB_TRY(launch_table_from_compact<T>(B.x, B.Gv, C, B.p, L, P.s));
+    FEGB_TRY(cg_schur_u<T>(P, B));
+    return launch_alpha_primary<T>(P.mu_all + P.goff[pd] * C, B.p + B.off[pd] * L, P.dims[pd].G, C, L,
+                                   P.alpha_all + P.goff[pd] * C, P.s);
 }
 
 // ---- graph-driven CG loop ----
@@ -1349,7 +1513,7 @@ int cg_build_graph(Problem& P, CGBuffers<T>& B, CGGraph<T>& G) {
     const int C = P.C;
     int st = cg_apply<T>(P, B);
     if (!st)
-        st = launch_cg_update<T>(P.Gt, C, B.inv, B.rz, B.pq, B.p, B.ld, B.q, B.x, B.r, B.z, B.rz_part, B.zmax_part,
+        st = launch_cg_update<T>(B.Gv, C, B.inv, B.rz, B.pq, B.p, B.ld, B.q, B.x, B.r, B.z, B.rz_part, B.zmax_part,
                                  B.zmax, cs);
     if (!st) st = launch_fold_partials(B.rz_part, B.rz_blocks, C, B.rz_new, cs);
     if (!st) {
@@ -1357,7 +1521,7 @@ int cg_build_graph(Problem& P, CGBuffers<T>& B, CGGraph<T>& G) {
         count_launch();
         if (cudaPeekAtLastError() != cudaSuccess) st = 1;
     }
-    if (!st) st = launch_cg_direction<T>(P.Gt, C, B.rz, B.rz_new, B.z, B.p, B.ld, cs, &G.ctl->stop);
+    if (!st) st = launch_cg_direction<T>(B.Gv, C, B.rz, B.rz_new, B.z, B.p, B.ld, cs, &G.ctl->stop);
     P.s = saved;
     cudaGraph_t captured = nullptr;
     const cudaError_t ec = cudaStreamEndCapture(cs, &captured);
@@ -1378,8 +1542,7 @@ int cg_solve(Problem& P, CGBuffers<T>& B, double inner_tol, int max_it, int* ite
              CGGraph<T>* G = nullptr) {
     if (G && G->exec && max_it > 0) {
         const int C = P.C;
-        FEGB_TRY(launch_cg_init<T>(P.Gt, C, P.counts_all, P.mu_all, B.r, B.z, B.p, B.ld, B.x, B.rz_part, B.zmax_part,
-                                   B.zmax, P.s));
+        FEGB_TRY(cg_start<T>(P, B));
         FEGB_TRY(launch_fold_partials(B.rz_part, B.rz_blocks, C, B.rz, P.s));
         cg_loop_reset_kernel<<<1, 1, 0, P.s>>>(G->ctl, inner_tol, max_it);
         FEGB_LAUNCH_CHECK("cg loop reset");
@@ -1388,7 +1551,7 @@ int cg_solve(Problem& P, CGBuffers<T>& B, double inner_tol, int max_it, int* ite
         FEGB_TRY(d2h_sync(&h, G->ctl, sizeof(h), P.s, "cg loop state copy"));
         *iters = h.it;
         *zmax_out = h.zm;
-        return launch_to_f64<T>(B.x, P.C, P.alpha_all, P.C, P.Gt, P.s);
+        return cg_finish<T>(P, B);
     }
     return cg_solve_host<T>(P, B, inner_tol, max_it, iters, zmax_out);
 }
@@ -1396,8 +1559,7 @@ int cg_solve(Problem& P, CGBuffers<T>& B, double inner_tol, int max_it, int* ite
 template <typename T>
 int cg_solve_host(Problem& P, CGBuffers<T>& B, double inner_tol, int max_it, int* iters, double* zmax_out) {
     const int C = P.C;  // vector ops run over compact rows; p keeps the padded stride B.ld
-    FEGB_TRY(launch_cg_init<T>(P.Gt, C, P.counts_all, P.mu_all, B.r, B.z, B.p, B.ld, B.x, B.rz_part, B.zmax_part,
-                               B.zmax, P.s));
+    FEGB_TRY(cg_start<T>(P, B));
     FEGB_TRY(launch_fold_partials(B.rz_part, B.rz_blocks, C, B.rz, P.s));
     double best = DBL_MAX, best_rz = DBL_MAX;
     int since_best = 0;
@@ -1406,7 +1568,7 @@ int cg_solve_host(Problem& P, CGBuffers<T>& B, double inner_tol, int max_it, int
     std::vector<double> rz_host((size_t)C);
     for (; it < max_it; ++it) {
         FEGB_TRY(cg_apply<T>(P, B));
-        FEGB_TRY(launch_cg_update<T>(P.Gt, C, B.inv, B.rz, B.pq, B.p, B.ld, B.q, B.x, B.r, B.z, B.rz_part,
+        FEGB_TRY(launch_cg_update<T>(B.Gv, C, B.inv, B.rz, B.pq, B.p, B.ld, B.q, B.x, B.r, B.z, B.rz_part,
                                      B.zmax_part, B.zmax, P.s));
         FEGB_TRY(launch_fold_partials(B.rz_part, B.rz_blocks, C, B.rz_new, P.s));
         FEGB_CUDA(cudaMemcpyAsync(rz_host.data(), B.rz_new, sizeof(double) * C, cudaMemcpyDeviceToHost, P.s),
@@ -1421,12 +1583,11 @@ int cg_solve_host(Problem& P, CGBuffers<T>& B, double inner_tol, int max_it, int
             ++it;
             break;
         }
-        FEGB_TRY(launch_cg_direction<T>(P.Gt, C, B.rz, B.rz_new, B.z, B.p, B.ld, P.s));
+        FEGB_TRY(launch_cg_direction<T>(B.Gv, C, B.rz, B.rz_new, B.z, B.p, B.ld, P.s));
     }
     *iters = it;
     *zmax_out = zm;
-    // the increment of this solve becomes the FP64 table applied by the next FP64 pass
-    return launch_to_f64<T>(B.x, P.C, P.alpha_all, P.C, P.Gt, P.s);
+    return cg_finish<T>(P, B);
 }
 
 // FP64 refinement loop around a CG inner solve in storage type T.

@@ -471,6 +471,39 @@ __global__ void __launch_bounds__(256) cg_init_rows_kernel(long long Gt, int C, 
 }
 
 template <typename T>
+__global__ void __launch_bounds__(256) cg_init_rhs_rows_kernel(long long Gt, int C, const int32_t* __restrict__ counts,
+                                                               const double* __restrict__ mu, const T* __restrict__ qb,
+                                                               const T* __restrict__ inv, T* __restrict__ r,
+                                                               T* __restrict__ z, T* __restrict__ p, int pld,
+                                                               T* __restrict__ x, double* __restrict__ rz_partials,
+                                                               double* __restrict__ zmax_partials) {
+    __shared__ double red[256];
+    __shared__ double red8[8];
+    const VecLane v = vec_lane(C);
+    T prod = T(0), az = T(0);
+    if (v.active) {
+        const long long g0 = (long long)blockIdx.x * v.rps * VEC_STEPS + v.rr;
+        for (int k = 0; k < VEC_STEPS; ++k) {
+            const long long g = g0 + (long long)k * v.rps;
+            if (g >= Gt) break;
+            const long long idx = g * C + v.c;
+            const int cnt = counts[g];
+            const T rv = cnt > 0 ? (T)((double)cnt * mu[idx] + (double)qb[idx]) : T(0);
+            const T zv = rv * inv[g];
+            r[idx] = rv;
+            z[idx] = zv;
+            p[g * pld + v.c] = zv;
+            x[idx] = T(0);
+            prod += rv * zv;
+            const T am = zv < T(0) ? -zv : zv;
+            az = am > az ? am : az;
+        }
+    }
+    vec_column_partials((double)prod, v, C, red, rz_partials);
+    vec_block_max((double)az, red8, zmax_partials);
+}
+
+template <typename T>
 __global__ void __launch_bounds__(FIN_THREADS) cg_q_kernel(FinalizeParams src, int C, const T* __restrict__ p,
                                                             int pld, T* __restrict__ q, double* __restrict__ pq_partials,
                                                             const T* __restrict__ extra) {
@@ -994,6 +1027,27 @@ int launch_cg_init(long long Gt, int C, const int32_t* counts, const double* mu,
     return 0;
 }
 
+template <typename T>
+int launch_cg_init_rhs(long long Gt, int C, const int32_t* counts, const double* mu, const T* qb, const T* inv, T* r,
+                       T* z, T* p, int pld, T* x, double* rz_partials, double* zmax_partials, unsigned long long* zmax,
+                       cudaStream_t s) {
+    if (Gt * C <= 0) return 0;
+    if (C > 256) return set_error("cg: %d columns exceed the right-hand-side initialisation", C);
+    const int nb = cg_partial_blocks(Gt, C);
+    cg_init_rhs_rows_kernel<T><<<nb, 256, 0, s>>>(Gt, C, counts, mu, qb, inv, r, z, p, pld, x, rz_partials,
+                                                  zmax_partials);
+    FEGB_LAUNCH_CHECK("cg init (rhs)");
+    fold_max_kernel<<<1, FIN_THREADS, 0, s>>>(zmax_partials, nb, zmax);
+    FEGB_LAUNCH_CHECK("cg max fold");
+    return 0;
+}
+template int launch_cg_init_rhs<float>(long long, int, const int32_t*, const double*, const float*, const float*,
+                                       float*, float*, float*, int, float*, double*, double*, unsigned long long*,
+                                       cudaStream_t);
+template int launch_cg_init_rhs<double>(long long, int, const int32_t*, const double*, const double*, const double*,
+                                        double*, double*, double*, int, double*, double*, double*,
+                                        unsigned long long*, cudaStream_t);
+
 template int launch_cg_q<double>(const FinalizeParams&, int, const double*, int, double*, double*, cudaStream_t,
                                  const double*);
 template int launch_cg_q<float>(const FinalizeParams&, int, const float*, int, float*, double*, cudaStream_t,
@@ -1100,6 +1154,7 @@ __device__ __forceinline__ void dense_issue(const CT* __restrict__ M, const T* _
     const char* gm = reinterpret_cast<const char*>(M + tile * Gs);
     for (long long o = (long long)threadIdx.x * 16; o + 16 <= mbytes; o += 256 * 16)
         cp_async16(reinterpret_cast<char*>(sM) + o, gm + o);
+    if (!pe) return;
     const long long pbytes = (long long)nt * ld * sizeof(T);
     const char* gp = reinterpret_cast<const char*>(pe + tile * ld);
     for (long long o = (long long)threadIdx.x * 16; o < pbytes; o += 256 * 16)
@@ -1152,8 +1207,9 @@ __global__ void __launch_bounds__(256) dense_pair_kernel(const CT* __restrict__ 
     for (int c = 0; c < (TWO ? CQ : 1); ++c) acc1[c] = T(0);
     const long long g0 = (long long)blockIdx.x * per;
     const long long g1 = min(Ge, g0 + per);
+    const bool small_side = partials != nullptr;  // else only the extra side (pe is not read)
     if (g0 < g1)
-        dense_issue<T, CT>(M, pe, Gs, ld, g0, (int)min((long long)DENSE_TILE, g1 - g0),
+        dense_issue<T, CT>(M, small_side ? pe : nullptr, Gs, ld, g0, (int)min((long long)DENSE_TILE, g1 - g0),
                            reinterpret_cast<CT*>(buf0 + p_bytes), reinterpret_cast<T*>(buf0));
     cp_async_commit();
     bool odd = false;
@@ -1163,7 +1219,7 @@ __global__ void __launch_bounds__(256) dense_pair_kernel(const CT* __restrict__ 
         const int nt = (int)min((long long)DENSE_TILE, g1 - tile);
         const long long next = tile + DENSE_TILE;
         if (next < g1)
-            dense_issue<T, CT>(M, pe, Gs, ld, next, (int)min((long long)DENSE_TILE, g1 - next),
+            dense_issue<T, CT>(M, small_side ? pe : nullptr, Gs, ld, next, (int)min((long long)DENSE_TILE, g1 - next),
                                reinterpret_cast<CT*>(nxt + p_bytes), reinterpret_cast<T*>(nxt));
         cp_async_commit();
         cp_async_wait_prev();  // this tile's copies are done (the next tile's may be in flight)
@@ -1171,7 +1227,7 @@ __global__ void __launch_bounds__(256) dense_pair_kernel(const CT* __restrict__ 
         const T* const pt = reinterpret_cast<const T*>(cur);
         dense_tail<CT>(M, Gs, tile, nt, m);
         __syncthreads();
-        for (int gl = warp; gl < nt; gl += DENSE_WARPS) {
+        for (int gl = warp; small_side && gl < nt; gl += DENSE_WARPS) {
             const T* prow = pt + gl * ld;
             if (lane < Gs) fma_row<T, CQ>((T)m[gl * Gs + lane], prow, acc0);
             if constexpr (TWO)
@@ -1206,7 +1262,8 @@ __global__ void __launch_bounds__(256) dense_pair_kernel(const CT* __restrict__ 
         }
         __syncthreads();
     }
-    for (int i = threadIdx.x; i < Gs * C; i += 256) partials[(long long)blockIdx.x * Gs * C + i] = red[i];
+    if (small_side)
+        for (int i = threadIdx.x; i < Gs * C; i += 256) partials[(long long)blockIdx.x * Gs * C + i] = red[i];
 }
 
 template <typename T, typename CT, int CQ, bool TWO>
@@ -1243,7 +1300,7 @@ int launch_dense_pair(const CT* M, long long Ge, int Gs, const T* pe, const T* p
     if (Ge <= 0 || Gs <= 0 || C <= 0) return 0;
     if (Gs > DENSE_SMALL_MAX_G || C > 32) return set_error("dense small-G product: Gs=%d C=%d too large", Gs, C);
     // pe and ps rows are copied whole (ld values, 16-byte pieces) and read CQ wide
-    if (ld % (16 / (int)sizeof(T)) != 0 || (reinterpret_cast<uintptr_t>(pe) & 15u) != 0 ||
+    if (ld % (16 / (int)sizeof(T)) != 0 || (reinterpret_cast<uintptr_t>(pe) & 15u) != 0 || (!partials && !extra) ||
         (reinterpret_cast<uintptr_t>(M) & 15u) != 0)
         return set_error("dense small-G product: unaligned rows (ld %d)", ld);
     if (C <= 4 && ld >= 4) return dense_pair_two<T, CT, 4>(M, Ge, Gs, pe, ps, ld, C, partials, extra, accumulate, s);
@@ -1266,6 +1323,101 @@ template int launch_dense_pair<double, uint8_t>(const uint8_t*, long long, int, 
                                                 double*, double*, int, cudaStream_t);
 template int launch_dense_pair<double, uint32_t>(const uint32_t*, long long, int, const double*, const double*, int,
                                                  int, double*, double*, int, cudaStream_t);
+
+// ---- Schur-complement CG helpers ----
+
+// table[g * L + c] = (sums[g * C + c] - extra[g * C + c]) / counts[g] (0 for an
+// empty group); extra may be null.
+template <typename T>
+__global__ void schur_u_kernel(const T* __restrict__ sums, const T* __restrict__ extra,
+                               const int32_t* __restrict__ counts, long long G, int C, T* __restrict__ table, int L) {
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long st = (long long)gridDim.x * blockDim.x;
+    for (; i < G * C; i += st) {
+        const long long g = i / C;
+        const int c = (int)(i - g * C);
+        const int n = counts[g];
+        T v = sums[i];
+        if (extra) v -= extra[i];
+        table[g * L + c] = n > 0 ? v / (T)n : T(0);
+    }
+}
+
+template <typename T>
+int launch_schur_u(const T* sums, const T* extra, const int32_t* counts, long long G, int C, T* table, int L,
+                   cudaStream_t s) {
+    if (G <= 0) return 0;
+    schur_u_kernel<T><<<grid_stride_blocks(G * C, 256), 256, 0, s>>>(sums, extra, counts, G, C, table, L);
+    FEGB_LAUNCH_CHECK("schur u");
+    return 0;
+}
+template int launch_schur_u<float>(const float*, const float*, const int32_t*, long long, int, float*, int,
+                                   cudaStream_t);
+template int launch_schur_u<double>(const double*, const double*, const int32_t*, long long, int, double*, int,
+                                    cudaStream_t);
+
+// table[g * L + c] = (T)(scale * src[g * C + c])
+template <typename T>
+__global__ void table_from_f64_kernel(const double* __restrict__ src, long long G, int C, double scale,
+                                      T* __restrict__ table, int L) {
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long st = (long long)gridDim.x * blockDim.x;
+    for (; i < G * C; i += st) {
+        const long long g = i / C;
+        table[g * L + (i - g * C)] = (T)(scale * src[i]);
+    }
+}
+
+// table[g * L + c] = src[g * C + c]
+template <typename T>
+__global__ void table_from_compact_kernel(const T* __restrict__ src, long long G, int C, T* __restrict__ table, int L) {
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long st = (long long)gridDim.x * blockDim.x;
+    for (; i < G * C; i += st) {
+        const long long g = i / C;
+        table[g * L + (i - g * C)] = src[i];
+    }
+}
+
+// alpha[g * C + c] = mu[g * C + c] + table[g * L + c]
+template <typename T>
+__global__ void alpha_primary_kernel(const double* __restrict__ mu, const T* __restrict__ table, long long G, int C,
+                                     int L, double* __restrict__ alpha) {
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long st = (long long)gridDim.x * blockDim.x;
+    for (; i < G * C; i += st) {
+        const long long g = i / C;
+        alpha[i] = mu[i] + (double)table[g * L + (i - g * C)];
+    }
+}
+
+template <typename T>
+int launch_table_from_f64(const double* src, long long G, int C, double scale, T* table, int L, cudaStream_t s) {
+    if (G <= 0) return 0;
+    table_from_f64_kernel<T><<<grid_stride_blocks(G * C, 256), 256, 0, s>>>(src, G, C, scale, table, L);
+    FEGB_LAUNCH_CHECK("table from fp64");
+    return 0;
+}
+template <typename T>
+int launch_table_from_compact(const T* src, long long G, int C, T* table, int L, cudaStream_t s) {
+    if (G <= 0) return 0;
+    table_from_compact_kernel<T><<<grid_stride_blocks(G * C, 256), 256, 0, s>>>(src, G, C, table, L);
+    FEGB_LAUNCH_CHECK("table from compact");
+    return 0;
+}
+template <typename T>
+int launch_alpha_primary(const double* mu, const T* table, long long G, int C, int L, double* alpha, cudaStream_t s) {
+    if (G <= 0) return 0;
+    alpha_primary_kernel<T><<<grid_stride_blocks(G * C, 256), 256, 0, s>>>(mu, table, G, C, L, alpha);
+    FEGB_LAUNCH_CHECK("primary increment");
+    return 0;
+}
+template int launch_table_from_f64<float>(const double*, long long, int, double, float*, int, cudaStream_t);
+template int launch_table_from_f64<double>(const double*, long long, int, double, double*, int, cudaStream_t);
+template int launch_table_from_compact<float>(const float*, long long, int, float*, int, cudaStream_t);
+template int launch_table_from_compact<double>(const double*, long long, int, double*, int, cudaStream_t);
+template int launch_alpha_primary<float>(const double*, const float*, long long, int, int, double*, cudaStream_t);
+template int launch_alpha_primary<double>(const double*, const double*, long long, int, int, double*, cudaStream_t);
 
 // One warp per (t, c): strided fold over the parts, fixed shuffle tree.
 __global__ void fold_dense_kernel(const double* __restrict__ partials, int nparts, int TC, double* __restrict__ sums) {

@@ -240,10 +240,25 @@ inline int dense_chunks(long long Ge) {
 // dimension e: partials[block][t][c] = sum over the block's groups g of
 // M[g][t] * pe[g * ld + c] (dense_chunks(Ge) blocks), and, when extra is not
 // null, extra[g * C + c] (+)= sum_t M[g][t] * ps[t * ld + c] (accumulate = 0
-// overwrites). pe and M start on 16 bytes and ld is a multiple of 16 bytes.
+// overwrites). partials null: only the extra side (pe is not read). pe and M
+// start on 16 bytes and ld is a multiple of 16 bytes.
 template <typename T, typename CT>
 int launch_dense_pair(const CT* M, long long Ge, int Gs, const T* pe, const T* ps, int ld, int C, double* partials,
                       T* extra, int accumulate, cudaStream_t s);
+// Schur-complement CG helpers (the primary dimension eliminated):
+// table[g * L + c] = (sums[g * C + c] - extra[g * C + c]) / counts[g] (extra optional)
+template <typename T>
+int launch_schur_u(const T* sums, const T* extra, const int32_t* counts, long long G, int C, T* table, int L,
+                   cudaStream_t s);
+// table[g * L + c] = (T)(scale * src[g * C + c])
+template <typename T>
+int launch_table_from_f64(const double* src, long long G, int C, double scale, T* table, int L, cudaStream_t s);
+// table[g * L + c] = src[g * C + c]
+template <typename T>
+int launch_table_from_compact(const T* src, long long G, int C, T* table, int L, cudaStream_t s);
+// alpha[g * C + c] = mu[g * C + c] + table[g * L + c]
+template <typename T>
+int launch_alpha_primary(const double* mu, const T* table, long long G, int C, int L, double* alpha, cudaStream_t s);
 // sums[t * C + c] = -(sum over parts of partials[part][t][c]), parts in order
 int launch_fold_dense(const double* partials, int nparts, int Gs, int C, double* sums, cudaStream_t s);
 // Partial blocks (one FP64 partial per column each) of the CG vector kernels
@@ -276,6 +291,12 @@ template <typename T>
 int launch_cg_direction(long long Gt, int C, double* rz_old, const double* rz_new, const T* z, T* p, int pld,
                         cudaStream_t s, const int* skip = nullptr);
 
+// r = counts * mu + qb (in FP64, cast to T), z = inv * r, p = z, x = 0; partials
+// of r.z and max |z| (the start of a solve from a right-hand side counts * mu + qb)
+template <typename T>
+int launch_cg_init_rhs(long long Gt, int C, const int32_t* counts, const double* mu, const T* qb, const T* inv, T* r,
+                       T* z, T* p, int pld, T* x, double* rz_partials, double* zmax_partials, unsigned long long* zmax,
+                       cudaStream_t s);
 // r = counts * mu, z = p = mu (cast to T); partials of r.z and max |z|
 // inv_counts[g] = 1 / counts[g] (0 for empty groups)
 int launch_inv_counts(const int32_t* counts, long long G, double* inv_counts, cudaStream_t s);

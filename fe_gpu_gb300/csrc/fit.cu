@@ -1222,15 +1222,49 @@ int cg_sweep(Problem& P, CGBuffers<T>& B, int d, int* n_src) {
 // u = (1/n_P) (D_P'D_R x), x = the other dimensions' rows of p: the primary's
 // stream sweep gives -(sum over its rows of the swept dimensions' x), the dense
 // count matrices the small dimensions' share.
+// With exactly one small dimension s, one pass over the primary's count matrix
+// both forms -u and the small side of s for the primary (*prim_small_done).
 template <typename T>
-int cg_schur_u(Problem& P, CGBuffers<T>& B) {
+int cg_schur_u(Problem& P, CGBuffers<T>& B, bool* prim_small_done = nullptr) {
     const int C = P.C;
     const int L = B.ld;
     const int pd = B.prim;
     const Dim& D = P.dims[pd];
+    if (prim_small_done) *prim_small_done = false;
     int n_src = 0;
     FEGB_TRY(cg_sweep<T>(P, B, pd, &n_src));
     if (n_src == 0) FEGB_CUDA(cudaMemsetAsync(B.sums, 0, sizeof(T) * (size_t)D.G * C, P.s), "schur sums zero");
+    int n_dense = 0, sd1 = -1;
+    for (int d = 0; d < P.n_fe; ++d)
+        if (B.dense[d]) {
+            ++n_dense;
+            sd1 = d;
+        }
+    if (n_dense == 1 && prim_small_done) {
+        const int Gs = P.dims[sd1].G;
+        long long part = 0;  // the primary's block of sd1's partials (cg_apply_rest's order)
+        for (int e = 0; e < pd; ++e)
+            if (e != sd1 && P.dims[e].G > 0) part += dense_chunks(P.dims[e].G);
+        DenseSchur<T> sch;
+        sch.sums = B.sums;
+        sch.counts = D.counts;
+        sch.table = B.p + B.off[pd] * L;
+        double* pb = B.dense_part + B.dpart_off[sd1] + part * Gs * C;
+        const T* ps = B.p + B.off[sd1] * L;
+        const double bytes = (double)D.G * ((B.N8[sd1][pd] ? 1.0 : 4.0) * Gs + 2.0 * C * sizeof(T) + 4.0);
+        CGTimer tm(P);
+        FEGB_TRY(tm.begin(6 + (sizeof(T) == 4 ? 1 : 0), bytes));
+        if (B.N8[sd1][pd])
+            FEGB_TRY((launch_dense_pair<T, uint8_t>(B.N8[sd1][pd], D.G, Gs, nullptr, ps, L, C, pb, nullptr, 0, P.s,
+                                                    sch)));
+        else
+            FEGB_TRY((launch_dense_pair<T, uint32_t>(B.N32[sd1][pd], D.G, Gs, nullptr, ps, L, C, pb, nullptr, 0,
+                                                     P.s, sch)));
+        FEGB_TRY(tm.end());
+        P.demean_bytes += bytes;
+        *prim_small_done = true;
+        return 0;
+    }
     T* ex = nullptr;
     if (B.any_dense) {
         CGTimer tm(P);
@@ -1263,7 +1297,7 @@ int cg_schur_u(Problem& P, CGBuffers<T>& B) {
 // the small dimensions from their complete sums. In the Schur form the primary
 // is a source of the sweeps and of the count-matrix passes but has no q.
 template <typename T>
-int cg_apply_rest(Problem& P, CGBuffers<T>& B) {
+int cg_apply_rest(Problem& P, CGBuffers<T>& B, bool prim_small_done = false) {
     const int C = P.C;
     const int L = B.ld;
     const int fp32 = sizeof(T) == 4 ? 1 : 0;
@@ -1274,7 +1308,7 @@ int cg_apply_rest(Problem& P, CGBuffers<T>& B) {
         for (int sd = 0; sd < P.n_fe; ++sd) {
             if (!B.dense[sd]) continue;
             for (int e = 0; e < P.n_fe; ++e) {
-                if (e == sd || P.dims[e].G <= 0) continue;
+                if (e == sd || P.dims[e].G <= 0 || (prim_small_done && e == B.prim)) continue;
                 const double cb = B.N8[sd][e] ? 1.0 : 4.0;
                 const bool ext = !B.dense[e] && in_cg(e);
                 bytes += (double)P.dims[e].G * (cb * P.dims[sd].G + (double)C * sizeof(T) * (ext ? 2.0 : 1.0));
@@ -1289,6 +1323,10 @@ int cg_apply_rest(Problem& P, CGBuffers<T>& B) {
             double* pbase = B.dense_part + B.dpart_off[sd];
             for (int e = 0; e < P.n_fe; ++e) {
                 if (e == sd || P.dims[e].G <= 0) continue;
+                if (prim_small_done && e == B.prim) {  // done with the primary's response
+                    part += dense_chunks(P.dims[e].G);
+                    continue;
+                }
                 // the small side always; the other side only for a swept CG dimension
                 T* ex = (B.dense[e] || !in_cg(e)) ? nullptr : B.extra + B.off[e] * C;
                 const int acc = ex && written[e] ? 1 : 0;
@@ -1347,8 +1385,9 @@ int cg_apply_rest(Problem& P, CGBuffers<T>& B) {
 // dimensions R (P_P: projection on the primary's group means).
 template <typename T>
 int cg_apply(Problem& P, CGBuffers<T>& B) {
-    if (B.schur) FEGB_TRY(cg_schur_u<T>(P, B));
-    FEGB_TRY(cg_apply_rest<T>(P, B));
+    bool prim_small_done = false;
+    if (B.schur) FEGB_TRY(cg_schur_u<T>(P, B, &prim_small_done));
+    FEGB_TRY(cg_apply_rest<T>(P, B, prim_small_done));
     return launch_fold_partials(B.pq_part, B.pq_blocks, P.C, B.pq, P.s);
 }
 

@@ -1184,18 +1184,21 @@ template <typename T, typename CT, int CQ, bool TWO>
 __global__ void __launch_bounds__(256) dense_pair_kernel(const CT* __restrict__ M, long long Ge, int Gs,
                                                          const T* __restrict__ pe, const T* __restrict__ ps, int ld,
                                                          int C, long long per, double* __restrict__ partials,
-                                                         T* __restrict__ extra, int accumulate) {
+                                                         T* __restrict__ extra, int accumulate, DenseSchur<T> sch) {
     extern __shared__ __align__(16) unsigned char dense_smem[];
-    // layout: sS (Gs x CQ) | 2 x [sP (DENSE_TILE x ld) | sM (DENSE_TILE x Gs, padded to 16 bytes)]
+    // layout: sS (Gs x CQ) | sU (DENSE_TILE x CQ) |
+    //         2 x [sP (DENSE_TILE x ld) | sM (DENSE_TILE x Gs, padded to 16 bytes)]
     T* sS = reinterpret_cast<T*>(dense_smem);
     const size_t s_bytes = sizeof(T) * (size_t)DENSE_SMALL_MAX_G * CQ;
+    T* sU = reinterpret_cast<T*>(dense_smem + s_bytes);
+    const size_t u_bytes = sizeof(T) * (size_t)DENSE_TILE * CQ;
     const size_t p_bytes = sizeof(T) * (size_t)DENSE_TILE * ld;
     const size_t m_bytes = ((sizeof(CT) * (size_t)DENSE_TILE * Gs + 15) / 16) * 16;
-    unsigned char* const buf0 = dense_smem + s_bytes;
+    unsigned char* const buf0 = dense_smem + s_bytes + u_bytes;
     unsigned char* const buf1 = buf0 + p_bytes + m_bytes;
     double* red = reinterpret_cast<double*>(dense_smem);  // Gs x C (after the tiles)
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    if (extra)
+    if (extra || sch.sums)
         for (int i = threadIdx.x; i < Gs * CQ; i += 256) {
             const int t = i / CQ, c = i - t * CQ;
             sS[i] = c < C ? ps[(long long)t * ld + c] : T(0);
@@ -1207,9 +1210,10 @@ __global__ void __launch_bounds__(256) dense_pair_kernel(const CT* __restrict__ 
     for (int c = 0; c < (TWO ? CQ : 1); ++c) acc1[c] = T(0);
     const long long g0 = (long long)blockIdx.x * per;
     const long long g1 = min(Ge, g0 + per);
+    const bool schur = sch.sums != nullptr;       // the small side's pe rows are computed, not read
     const bool small_side = partials != nullptr;  // else only the extra side (pe is not read)
     if (g0 < g1)
-        dense_issue<T, CT>(M, small_side ? pe : nullptr, Gs, ld, g0, (int)min((long long)DENSE_TILE, g1 - g0),
+        dense_issue<T, CT>(M, small_side && !schur ? pe : nullptr, Gs, ld, g0, (int)min((long long)DENSE_TILE, g1 - g0),
                            reinterpret_cast<CT*>(buf0 + p_bytes), reinterpret_cast<T*>(buf0));
     cp_async_commit();
     bool odd = false;
@@ -1219,7 +1223,7 @@ __global__ void __launch_bounds__(256) dense_pair_kernel(const CT* __restrict__ 
         const int nt = (int)min((long long)DENSE_TILE, g1 - tile);
         const long long next = tile + DENSE_TILE;
         if (next < g1)
-            dense_issue<T, CT>(M, small_side ? pe : nullptr, Gs, ld, next, (int)min((long long)DENSE_TILE, g1 - next),
+            dense_issue<T, CT>(M, small_side && !schur ? pe : nullptr, Gs, ld, next, (int)min((long long)DENSE_TILE, g1 - next),
                                reinterpret_cast<CT*>(nxt + p_bytes), reinterpret_cast<T*>(nxt));
         cp_async_commit();
         cp_async_wait_prev();  // this tile's copies are done (the next tile's may be in flight)
@@ -1227,13 +1231,35 @@ __global__ void __launch_bounds__(256) dense_pair_kernel(const CT* __restrict__ 
         const T* const pt = reinterpret_cast<const T*>(cur);
         dense_tail<CT>(M, Gs, tile, nt, m);
         __syncthreads();
+        if (schur) {
+            // u = (sums - sum_t M[g][t] ps[t]) / counts for the tile's groups: written to the
+            // primary's table and kept in shared memory as this tile's pe rows
+            constexpr int QN = CQ / 4;
+            for (int i = threadIdx.x; i < nt * QN; i += 256) {
+                const int gl = i / QN, c0 = (i - gl * QN) * 4;
+                const long long g = tile + gl;
+                T a[4] = {T(0), T(0), T(0), T(0)};
+                const CT* mr = m + gl * Gs;
+                for (int t = 0; t < Gs; ++t) fma_row<T, 4>((T)mr[t], sS + t * CQ + c0, a);
+                const int n = sch.counts[g];
+#pragma unroll
+                for (int c = 0; c < 4; ++c) {
+                    const int col = c0 + c;
+                    T u = T(0);
+                    if (col < C && n > 0) u = (sch.sums[g * C + col] - a[c]) / (T)n;
+                    sU[gl * CQ + col] = u;
+                    if (col < C) sch.table[g * ld + col] = u;
+                }
+            }
+            __syncthreads();
+        }
         for (int gl = warp; small_side && gl < nt; gl += DENSE_WARPS) {
-            const T* prow = pt + gl * ld;
+            const T* prow = schur ? sU + gl * CQ : pt + gl * ld;
             if (lane < Gs) fma_row<T, CQ>((T)m[gl * Gs + lane], prow, acc0);
             if constexpr (TWO)
                 if (lane + 32 < Gs) fma_row<T, CQ>((T)m[gl * Gs + lane + 32], prow, acc1);
         }
-        if (extra) {
+        if (extra && !schur) {
             constexpr int QN = CQ / 4;
             for (int i = threadIdx.x; i < nt * QN; i += 256) {
                 const int gl = i / QN, c0 = (i - gl * QN) * 4;
@@ -1268,7 +1294,7 @@ __global__ void __launch_bounds__(256) dense_pair_kernel(const CT* __restrict__ 
 
 template <typename T, typename CT, int CQ, bool TWO>
 int dense_pair_cq(const CT* M, long long Ge, int Gs, const T* pe, const T* ps, int ld, int C, double* partials,
-                  T* extra, int accumulate, cudaStream_t s) {
+                  T* extra, int accumulate, const DenseSchur<T>& sch, cudaStream_t s) {
     static const cudaError_t attr = cudaFuncSetAttribute(dense_pair_kernel<T, CT, CQ, TWO>,
                                                          cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
     if (attr != cudaSuccess) return set_cuda_error(attr, "dense pair attr");
@@ -1277,52 +1303,53 @@ int dense_pair_cq(const CT* M, long long Ge, int Gs, const T* pe, const T* ps, i
     per = (per + DENSE_TILE - 1) / DENSE_TILE * DENSE_TILE;  // tiles (and their copies) start on 16 bytes
     const size_t p_bytes = sizeof(T) * (size_t)DENSE_TILE * ld;
     const size_t m_bytes = ((sizeof(CT) * (size_t)DENSE_TILE * Gs + 15) / 16) * 16;
-    const size_t smem = std::max(sizeof(T) * (size_t)DENSE_SMALL_MAX_G * CQ + 2 * (p_bytes + m_bytes),
+    const size_t smem = std::max(sizeof(T) * (size_t)(DENSE_SMALL_MAX_G + DENSE_TILE) * CQ + 2 * (p_bytes + m_bytes),
                                  sizeof(double) * (size_t)Gs * C);
     dense_pair_kernel<T, CT, CQ, TWO><<<nb, 256, smem, s>>>(M, Ge, Gs, pe, ps, ld, C, per, partials, extra,
-                                                            accumulate);
+                                                            accumulate, sch);
     FEGB_LAUNCH_CHECK("dense small-G pair product");
     return 0;
 }
 
 template <typename T, typename CT, int CQ>
 int dense_pair_two(const CT* M, long long Ge, int Gs, const T* pe, const T* ps, int ld, int C, double* partials,
-                   T* extra, int accumulate, cudaStream_t s) {
-    if (Gs > 32) return dense_pair_cq<T, CT, CQ, true>(M, Ge, Gs, pe, ps, ld, C, partials, extra, accumulate, s);
-    return dense_pair_cq<T, CT, CQ, false>(M, Ge, Gs, pe, ps, ld, C, partials, extra, accumulate, s);
+                   T* extra, int accumulate, const DenseSchur<T>& sch, cudaStream_t s) {
+    if (Gs > 32) return dense_pair_cq<T, CT, CQ, true>(M, Ge, Gs, pe, ps, ld, C, partials, extra, accumulate, sch, s);
+    return dense_pair_cq<T, CT, CQ, false>(M, Ge, Gs, pe, ps, ld, C, partials, extra, accumulate, sch, s);
 }
 
 }  // namespace
 
 template <typename T, typename CT>
 int launch_dense_pair(const CT* M, long long Ge, int Gs, const T* pe, const T* ps, int ld, int C, double* partials,
-                      T* extra, int accumulate, cudaStream_t s) {
+                      T* extra, int accumulate, cudaStream_t s, const DenseSchur<T>& sch) {
     if (Ge <= 0 || Gs <= 0 || C <= 0) return 0;
     if (Gs > DENSE_SMALL_MAX_G || C > 32) return set_error("dense small-G product: Gs=%d C=%d too large", Gs, C);
     // pe and ps rows are copied whole (ld values, 16-byte pieces) and read CQ wide
-    if (ld % (16 / (int)sizeof(T)) != 0 || (reinterpret_cast<uintptr_t>(pe) & 15u) != 0 || (!partials && !extra) ||
-        (reinterpret_cast<uintptr_t>(M) & 15u) != 0)
-        return set_error("dense small-G product: unaligned rows (ld %d)", ld);
-    if (C <= 4 && ld >= 4) return dense_pair_two<T, CT, 4>(M, Ge, Gs, pe, ps, ld, C, partials, extra, accumulate, s);
-    if (C <= 8 && ld >= 8) return dense_pair_two<T, CT, 8>(M, Ge, Gs, pe, ps, ld, C, partials, extra, accumulate, s);
+    if (ld % (16 / (int)sizeof(T)) != 0 || (reinterpret_cast<uintptr_t>(pe) & 15u) != 0 ||
+        (!partials && !extra) || (reinterpret_cast<uintptr_t>(M) & 15u) != 0 ||
+        (sch.sums && (extra || !partials || !sch.counts || !sch.table)))
+        return set_error("dense small-G product: invalid arguments (ld %d)", ld);
+    if (C <= 4 && ld >= 4) return dense_pair_two<T, CT, 4>(M, Ge, Gs, pe, ps, ld, C, partials, extra, accumulate, sch, s);
+    if (C <= 8 && ld >= 8) return dense_pair_two<T, CT, 8>(M, Ge, Gs, pe, ps, ld, C, partials, extra, accumulate, sch, s);
     if (C <= 12 && ld >= 12)
-        return dense_pair_two<T, CT, 12>(M, Ge, Gs, pe, ps, ld, C, partials, extra, accumulate, s);
+        return dense_pair_two<T, CT, 12>(M, Ge, Gs, pe, ps, ld, C, partials, extra, accumulate, sch, s);
     if (C <= 16 && ld >= 16)
-        return dense_pair_two<T, CT, 16>(M, Ge, Gs, pe, ps, ld, C, partials, extra, accumulate, s);
+        return dense_pair_two<T, CT, 16>(M, Ge, Gs, pe, ps, ld, C, partials, extra, accumulate, sch, s);
     if (C <= 24 && ld >= 24)
-        return dense_pair_two<T, CT, 24>(M, Ge, Gs, pe, ps, ld, C, partials, extra, accumulate, s);
+        return dense_pair_two<T, CT, 24>(M, Ge, Gs, pe, ps, ld, C, partials, extra, accumulate, sch, s);
     if (C <= 32 && ld >= 32)
-        return dense_pair_two<T, CT, 32>(M, Ge, Gs, pe, ps, ld, C, partials, extra, accumulate, s);
+        return dense_pair_two<T, CT, 32>(M, Ge, Gs, pe, ps, ld, C, partials, extra, accumulate, sch, s);
     return set_error("dense small-G product: row stride %d below the %d-column read", ld, C);
 }
 template int launch_dense_pair<float, uint8_t>(const uint8_t*, long long, int, const float*, const float*, int, int,
-                                               double*, float*, int, cudaStream_t);
+                                               double*, float*, int, cudaStream_t, const DenseSchur<float>&);
 template int launch_dense_pair<float, uint32_t>(const uint32_t*, long long, int, const float*, const float*, int, int,
-                                                double*, float*, int, cudaStream_t);
+                                                double*, float*, int, cudaStream_t, const DenseSchur<float>&);
 template int launch_dense_pair<double, uint8_t>(const uint8_t*, long long, int, const double*, const double*, int, int,
-                                                double*, double*, int, cudaStream_t);
+                                                double*, double*, int, cudaStream_t, const DenseSchur<double>&);
 template int launch_dense_pair<double, uint32_t>(const uint32_t*, long long, int, const double*, const double*, int,
-                                                 int, double*, double*, int, cudaStream_t);
+                                                 int, double*, double*, int, cudaStream_t, const DenseSchur<double>&);
 
 // ---- Schur-complement CG helpers ----
 

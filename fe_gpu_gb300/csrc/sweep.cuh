@@ -242,9 +242,19 @@ inline int dense_chunks(long long Ge) {
 // null, extra[g * C + c] (+)= sum_t M[g][t] * ps[t * ld + c] (accumulate = 0
 // overwrites). partials null: only the extra side (pe is not read). pe and M
 // start on 16 bytes and ld is a multiple of 16 bytes.
+// Schur form of the pass over the primary's count matrix (one small dimension):
+// with sums set, each group g of e gets u = (sums[g * C + c] - sum_t M[g][t] ps[t])
+// / counts[g], written to table (row stride ld), and u is the pe of the small
+// side (extra must be null). Zero-initialised = the plain pass.
+template <typename T>
+struct DenseSchur {
+    const T* sums = nullptr;
+    const int32_t* counts = nullptr;
+    T* table = nullptr;
+};
 template <typename T, typename CT>
 int launch_dense_pair(const CT* M, long long Ge, int Gs, const T* pe, const T* ps, int ld, int C, double* partials,
-                      T* extra, int accumulate, cudaStream_t s);
+                      T* extra, int accumulate, cudaStream_t s, const DenseSchur<T>& sch = DenseSchur<T>());
 // Schur-complement CG helpers (the primary dimension eliminated):
 // table[g * L + c] = (sums[g * C + c] - extra[g * C + c]) / counts[g] (extra optional)
 template <typename T>

@@ -728,4 +728,68 @@ int fe_build_cluster_ids(const int32_t* fe_ids, int ld_fe, long long n_obs, cons
     return 0;
 }
 
+// Self-test of one dense count-matrix pass of the CG operator on host data
+// (FP32 storage, uint8 counts); see include/fegb.h.
+int fegb_test_dense_pair(const uint8_t* counts, long long Ge, int Gs, const float* pe, const float* ps, int ld, int C,
+                         const float* sums, const int32_t* group_counts, int accumulate, int tensor_cores,
+                         double* out_small, float* out_extra, float* out_table) {
+    using namespace fegb;
+    if (Ge <= 0 || Gs <= 0 || Gs > DENSE_SMALL_MAX_G || C <= 0 || C > 32 || ld < C || !counts || !ps)
+        return set_error("fegb_test_dense_pair: invalid sizes");
+    const bool schur = sums != nullptr;
+    if (schur && (!group_counts || !out_table || out_extra))
+        return set_error("fegb_test_dense_pair: the Schur form needs group counts and a table, and no extra");
+    Scratch scr(kLegacy);
+    uint8_t* dM = nullptr;
+    float *dpe = nullptr, *dps = nullptr, *dsums = nullptr, *dextra = nullptr, *dtab = nullptr;
+    int32_t* dcnt = nullptr;
+    double *dpart = nullptr, *dsmall = nullptr;
+    const size_t nm = (size_t)Ge * Gs;
+    FEGB_TRY(scr.alloc(&dM, nm, "test counts"));
+    FEGB_TRY(scr.alloc(&dps, (size_t)Gs * ld, "test ps"));
+    FEGB_CUDA(cudaMemcpy(dM, counts, nm, cudaMemcpyHostToDevice), "test counts copy");
+    FEGB_CUDA(cudaMemcpy(dps, ps, sizeof(float) * Gs * ld, cudaMemcpyHostToDevice), "test ps copy");
+    if (pe) {
+        FEGB_TRY(scr.alloc(&dpe, (size_t)Ge * ld, "test pe"));
+        FEGB_CUDA(cudaMemcpy(dpe, pe, sizeof(float) * Ge * ld, cudaMemcpyHostToDevice), "test pe copy");
+    }
+    DenseSchur<float> sch;
+    if (schur) {
+        FEGB_TRY(scr.alloc(&dsums, (size_t)Ge * C, "test sums"));
+        // the group counts start one element past an aligned address (a primary
+        // that is not the first dimension): the pass must not stage them asynchronously
+        FEGB_TRY(scr.alloc(&dcnt, (size_t)Ge + 1, "test group counts"));
+        dcnt += 1;
+        FEGB_TRY(scr.alloc(&dtab, (size_t)Ge * ld, "test table"));
+        FEGB_CUDA(cudaMemcpy(dsums, sums, sizeof(float) * Ge * C, cudaMemcpyHostToDevice), "test sums copy");
+        FEGB_CUDA(cudaMemcpy(dcnt, group_counts, sizeof(int32_t) * Ge, cudaMemcpyHostToDevice), "test counts copy");
+        FEGB_CUDA(cudaMemset(dtab, 0, sizeof(float) * Ge * ld), "test table zero");
+        sch.sums = dsums;
+        sch.counts = dcnt;
+        sch.table = dtab;
+    }
+    if (out_extra) {
+        FEGB_TRY(scr.alloc(&dextra, (size_t)Ge * C, "test extra"));
+        FEGB_CUDA(cudaMemcpy(dextra, out_extra, sizeof(float) * Ge * C, cudaMemcpyHostToDevice), "test extra copy");
+    }
+    const int nparts = dense_chunks(Ge);
+    if (out_small) {
+        FEGB_TRY(scr.alloc(&dpart, (size_t)nparts * Gs * C, "test partials"));
+        FEGB_TRY(scr.alloc(&dsmall, (size_t)Gs * C, "test small sums"));
+    }
+    dense_force_mode(tensor_cores ? 1 : 0);
+    const int st = launch_dense_pair<float, uint8_t>(dM, Ge, Gs, schur ? nullptr : dpe, dps, ld, C, dpart, dextra,
+                                                     accumulate, kLegacy, sch);
+    dense_force_mode(-1);
+    FEGB_TRY(st);
+    if (out_small) FEGB_TRY(launch_fold_dense(dpart, nparts, Gs, C, dsmall, kLegacy));
+    FEGB_CUDA(cudaDeviceSynchronize(), "test sync");
+    if (out_small) FEGB_CUDA(cudaMemcpy(out_small, dsmall, sizeof(double) * Gs * C, cudaMemcpyDeviceToHost), "test out");
+    if (out_extra)
+        FEGB_CUDA(cudaMemcpy(out_extra, dextra, sizeof(float) * Ge * C, cudaMemcpyDeviceToHost), "test extra out");
+    if (schur)
+        FEGB_CUDA(cudaMemcpy(out_table, dtab, sizeof(float) * Ge * ld, cudaMemcpyDeviceToHost), "test table out");
+    return 0;
+}
+
 }  // extern "C"

@@ -143,6 +143,21 @@ int fegb_group_sizes(const int* const* d_fe_ids, int n_fe, long long n, int* siz
 /* Number of kernel launches issued by this library since it was loaded. */
 long long fegb_kernel_launches(void);
 
+/* Self-test of one dense count-matrix pass of the CG operator (FP32 storage,
+ * uint8 counts), on host arrays. counts: Ge x Gs row-major (rows of each pair
+ * of a group g of a many-group dimension and a group t of a small dimension);
+ * pe: Ge x ld and ps: Gs x ld rows (first C columns used). Outputs:
+ *   out_small[t*C+c] = -sum_g counts[g][t] pe[g][c]        (null: not formed)
+ *   out_extra[g*C+c] (+)= sum_t counts[g][t] ps[t][c]      (null: not formed;
+ *                       accumulate = 1 adds to the values passed in)
+ * Schur form (sums non-null, Ge x C; group_counts Ge; pe unused; out_extra
+ * null): out_table[g*ld+c] = (sums[g][c] - sum_t counts[g][t] ps[t][c]) /
+ * group_counts[g] and out_small uses those rows as pe. tensor_cores = 1: the
+ * tensor-core (TF32 split) form, 0: the FP32 form. */
+int fegb_test_dense_pair(const unsigned char* counts, long long Ge, int Gs, const float* pe, const float* ps, int ld,
+                         int C, const float* sums, const int* group_counts, int accumulate, int tensor_cores,
+                         double* out_small, float* out_extra, float* out_table);
+
 /* FE reconstruction of --save-fe (reconstruct_and_save_fixed_effects,
  * src/core/fe_pipeline.f90:1619-1733): forward Gauss-Seidel sweeps of the
  * residual y - W beta (beta: host, k values), dimension by dimension, each

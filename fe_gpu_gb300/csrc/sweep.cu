@@ -1,6 +1,8 @@
 // Alternating-projection sweep kernels (see sweep.cuh for the scheme).
 #include "sweep.cuh"
 
+#include <cstdlib>
+
 #include <type_traits>
 
 namespace fegb {
@@ -1373,7 +1375,14 @@ namespace {
 thread_local int t_dense_mode = -1;  // -1 (default) and 0: the FP32 form; 1: the tensor-core form
 }  // namespace
 
-bool dense_use_mma() { return t_dense_mode > 0; }
+bool dense_use_mma() {
+    if (t_dense_mode >= 0) return t_dense_mode > 0;
+    static const bool env = [] {  // FEGB_DENSE_TENSOR=1: the tensor-core form by default
+        const char* v = std::getenv("FEGB_DENSE_TENSOR");
+        return v && v[0] == '1';
+    }();
+    return env;
+}
 void dense_force_mode(int mode) { t_dense_mode = mode; }
 
 namespace {

@@ -256,7 +256,8 @@ template <typename T, typename CT>
 int launch_dense_pair(const CT* M, long long Ge, int Gs, const T* pe, const T* ps, int ld, int C, double* partials,
                       T* extra, int accumulate, cudaStream_t s, const DenseSchur<T>& sch = DenseSchur<T>());
 // Form of the uint8 / FP32 dense pair pass on the calling host thread: the
-// FP32 form by default (mode -1 or 0), the tensor-core (TF32 split) form with
+// FP32 form by default (mode -1 or 0; FEGB_DENSE_TENSOR=1 in the environment
+// makes mode -1 the tensor-core form), the tensor-core (TF32 split) form with
 // mode 1. The TF32 split keeps about 2^-22 relative precision per product
 // against 2^-24 for FP32 FMAs, which cost the FP32 inner CG a few iterations
 // per solve on the worker-firm panels, so the FP32 form stays the default.

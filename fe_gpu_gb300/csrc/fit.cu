@@ -1019,6 +1019,66 @@ int cg_streams(Problem& P, CGBuffers<T>& B) {
     return 0;
 }
 
+__global__ void counts_to_f64_kernel(const int32_t* __restrict__ counts, long long G, double* __restrict__ out) {
+    const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (g < G) out[g] = (double)counts[g];
+}
+
+// Schur form: Jacobi preconditioner from the diagonal of
+// S = D_R'(I - P_P)D_R, S_gg = n_g - sum_w n_{w,g}^2 / n_w (only groups of the
+// primary spread over several groups of the dimension contribute), instead of
+// the group counts n_g. Needs each (group, primary group) pair as one
+// position of the dimension's stream (compressed streams over the primary and
+// at most one other many-group dimension); otherwise the counts stay.
+template <typename T>
+int cg_schur_precond(Problem& P, CGBuffers<T>& B) {
+    const int pd = B.prim;
+    std::vector<int> swept;
+    for (int d = 0; d < P.n_fe; ++d)
+        if (d != pd && P.dims[d].G > 0 && !B.dense[d]) swept.push_back(d);
+    if (swept.size() > 1 || (swept.size() == 1 && !B.compressed)) return 0;
+    Scratch tmp(P.s);
+    double* diag = nullptr;
+    FEGB_TRY(tmp.alloc(&diag, (size_t)std::max(1LL, B.Gv), "schur diagonal"));
+    counts_to_f64_kernel<<<(unsigned)((B.Gv + 255) / 256), 256, 0, P.s>>>(B.counts_v, B.Gv, diag);
+    FEGB_LAUNCH_CHECK("schur diagonal init");
+    for (int e : swept) {
+        const auto& st = B.stream[e];
+        const int32_t* pid = nullptr;
+        for (int i = 0; i < st.n_src; ++i)
+            if (st.src_dim[i] == pd) pid = st.src_gid[i];
+        if (!pid) return 0;
+        FEGB_TRY(launch_schur_diag_stream(st.off, P.dims[e].G, st.weight, pid, P.dims[pd].counts, diag + B.off[e],
+                                          P.s));
+    }
+    for (int sd = 0; sd < P.n_fe; ++sd) {
+        if (!B.dense[sd] || sd == pd || P.dims[sd].G <= 0) continue;
+        const int Gs = P.dims[sd].G;
+        const int nparts = dense_chunks(P.dims[pd].G);
+        double *part = nullptr, *folded = nullptr;
+        FEGB_TRY(tmp.alloc(&part, (size_t)nparts * Gs, "schur diagonal partials"));
+        FEGB_TRY(tmp.alloc(&folded, (size_t)Gs, "schur diagonal sums"));
+        if (B.N8[sd][pd])
+            FEGB_TRY(launch_schur_diag_dense<uint8_t>(B.N8[sd][pd], P.dims[pd].G, Gs, P.dims[pd].counts, part, nparts,
+                                                      P.s));
+        else
+            FEGB_TRY(launch_schur_diag_dense<uint32_t>(B.N32[sd][pd], P.dims[pd].G, Gs, P.dims[pd].counts, part,
+                                                       nparts, P.s));
+        FEGB_TRY(launch_fold_dense(part, nparts, Gs, 1, folded, P.s));  // folded = -sum
+        std::vector<double> hd(Gs), hf(Gs);
+        FEGB_CUDA(cudaMemcpyAsync(hd.data(), diag + B.off[sd], sizeof(double) * Gs, cudaMemcpyDeviceToHost, P.s),
+                  "schur diagonal copy");
+        FEGB_TRY(d2h_sync(hf.data(), folded, sizeof(double) * Gs, P.s, "schur diagonal copy"));
+        for (int t = 0; t < Gs; ++t) hd[t] += hf[t];
+        FEGB_CUDA(cudaMemcpyAsync(diag + B.off[sd], hd.data(), sizeof(double) * Gs, cudaMemcpyHostToDevice, P.s),
+                  "schur diagonal copy");
+        FEGB_CUDA(cudaStreamSynchronize(P.s), "schur diagonal sync");
+    }
+    FEGB_TRY(launch_inv_diag<T>(diag, B.counts_v, B.Gv, B.inv, P.s));
+    FEGB_CUDA(cudaStreamSynchronize(P.s), "schur diagonal sync");
+    return 0;
+}
+
 template <typename T>
 int cg_alloc(Problem& P, CGBuffers<T>& B) {
     Scratch& scr = *P.scr;
@@ -1144,6 +1204,7 @@ int cg_alloc(Problem& P, CGBuffers<T>& B) {
         }
     }
     FEGB_TRY(cg_streams(P, B));
+    if (B.schur) FEGB_TRY(cg_schur_precond(P, B));
     // the operator sweep's sums / head / tail, compact rows of C
     {
         const long long nchunks = std::max(1LL, seg_nchunks(P.n, CG_CHUNK));

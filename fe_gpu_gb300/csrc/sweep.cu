@@ -1745,6 +1745,88 @@ template int launch_table_from_compact<double>(const double*, long long, int, do
 template int launch_alpha_primary<float>(const double*, const float*, long long, int, int, double*, cudaStream_t);
 template int launch_alpha_primary<double>(const double*, const double*, long long, int, int, double*, cudaStream_t);
 
+// ---- diagonal of the Schur complement (the CG's Jacobi preconditioner) ----
+
+// diag[g] -= sum over positions j in [off[g], off[g+1]) of w[j]^2 / n_P[pid[j]]
+// (a stream in which each (group of e, group of P) pair is one position). One
+// warp per group: lane l takes positions l, l + 32, ... in order, then a fixed
+// shuffle tree (groups of a Pareto-sized dimension can hold 1e5 positions).
+__global__ void schur_diag_stream_kernel(const int32_t* __restrict__ off, int G, const float* __restrict__ w,
+                                         const int32_t* __restrict__ pid, const int32_t* __restrict__ nP,
+                                         double* __restrict__ diag) {
+    const long long g = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (g >= G) return;
+    double acc = 0.0;
+    for (int j = off[g] + lane; j < off[g + 1]; j += 32) {
+        const double wj = w ? (double)w[j] : 1.0;
+        const int n = nP[pid[j]];
+        if (n > 0) acc += wj * wj / (double)n;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+    if (lane == 0) diag[g] -= acc;
+}
+
+// partials[block][t] = sum over the block's groups g of N[g][t]^2 / n[g]
+// (DENSE_TILE-row blocks as the dense passes; one thread per t, groups in order)
+template <typename CT>
+__global__ void schur_diag_dense_kernel(const CT* __restrict__ N, long long Ge, int Gs, const int32_t* __restrict__ n,
+                                        long long per, double* __restrict__ partials) {
+    const long long g0 = (long long)blockIdx.x * per;
+    const long long g1 = min(Ge, g0 + per);
+    for (int t = threadIdx.x; t < Gs; t += blockDim.x) {
+        double acc = 0.0;
+        for (long long g = g0; g < g1; ++g) {
+            const double m = (double)N[g * Gs + t];
+            if (m != 0.0 && n[g] > 0) acc += m * m / (double)n[g];
+        }
+        partials[(long long)blockIdx.x * Gs + t] = acc;
+    }
+}
+
+// inv[g] = diag[g] > tiny * counts[g] ? 1 / diag[g] : 0 (an unidentified group gets 0)
+template <typename T>
+__global__ void inv_diag_kernel(const double* __restrict__ diag, const int32_t* __restrict__ counts, long long G,
+                                T* __restrict__ inv) {
+    const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= G) return;
+    const double d = diag[g];
+    inv[g] = (counts[g] > 0 && d > 1e-9 * (double)counts[g]) ? (T)(1.0 / d) : T(0);
+}
+
+int launch_schur_diag_stream(const int32_t* off, int G, const float* w, const int32_t* pid, const int32_t* nP,
+                             double* diag, cudaStream_t s) {
+    if (G <= 0) return 0;
+    schur_diag_stream_kernel<<<(unsigned)(((long long)G * 32 + 255) / 256), 256, 0, s>>>(off, G, w, pid, nP, diag);
+    FEGB_LAUNCH_CHECK("schur diagonal (stream)");
+    return 0;
+}
+
+template <typename CT>
+int launch_schur_diag_dense(const CT* N, long long Ge, int Gs, const int32_t* n, double* partials, int nparts,
+                            cudaStream_t s) {
+    if (Ge <= 0) return 0;
+    const long long per = (Ge + nparts - 1) / nparts;
+    schur_diag_dense_kernel<CT><<<nparts, 64, 0, s>>>(N, Ge, Gs, n, per, partials);
+    FEGB_LAUNCH_CHECK("schur diagonal (dense)");
+    return 0;
+}
+template int launch_schur_diag_dense<uint8_t>(const uint8_t*, long long, int, const int32_t*, double*, int,
+                                              cudaStream_t);
+template int launch_schur_diag_dense<uint32_t>(const uint32_t*, long long, int, const int32_t*, double*, int,
+                                               cudaStream_t);
+
+template <typename T>
+int launch_inv_diag(const double* diag, const int32_t* counts, long long G, T* inv, cudaStream_t s) {
+    if (G <= 0) return 0;
+    inv_diag_kernel<T><<<(unsigned)((G + 255) / 256), 256, 0, s>>>(diag, counts, G, inv);
+    FEGB_LAUNCH_CHECK("inverse diagonal");
+    return 0;
+}
+template int launch_inv_diag<float>(const double*, const int32_t*, long long, float*, cudaStream_t);
+template int launch_inv_diag<double>(const double*, const int32_t*, long long, double*, cudaStream_t);
+
 // One warp per (t, c): strided fold over the parts, fixed shuffle tree.
 __global__ void fold_dense_kernel(const double* __restrict__ partials, int nparts, int TC, double* __restrict__ sums) {
     const long long w = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;

@@ -765,7 +765,12 @@ int fp64_mean_pass(Problem& P, bool apply_alpha, double* mu_max) {
             }
         }
         if (D.G > 0 && P.n > 0) {
-            FEGB_TRY(sweep_sums<double>(P, d, P.X, ps, first && apply_alpha));
+            if (ps.n > 0) {
+                // the increments in one coalesced element pass, then a read-only sweep
+                FEGB_TRY(launch_apply_pending<double>(P.X, P.C, P.n, ps, P.s));
+                ps = PendingSet<double>{};
+            }
+            FEGB_TRY(sweep_sums<double>(P, d, P.X, ps, false));
             FinalizeParams f = finalize_base(P, d);
             f.mean_out = D.mu;
             f.max_partials = P.max_partials;

@@ -299,12 +299,21 @@ __global__ void apply_pending_kernel(T* __restrict__ X, int C, long long n, Pend
     const long long total = n * (long long)C;
     long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const long long stride = (long long)gridDim.x * blockDim.x;
+    // (row, col) of i advanced incrementally: one 64-bit division per thread, not per element
+    long long row = i / C;
+    int col = (int)(i - row * C);
+    const long long rstep = stride / C;
+    const int cstep = (int)(stride - rstep * C);
     for (; i < total; i += stride) {
-        const long long row = i / C;
-        const int col = (int)(i - row * C);
         T v = X[i];
         for (int e = 0; e < pend.n; ++e) v -= pend.tab[e][(long long)pend.gid[e][row] * C + col];
         X[i] = v;
+        row += rstep;
+        col += cstep;
+        if (col >= C) {
+            col -= C;
+            ++row;
+        }
     }
 }
 

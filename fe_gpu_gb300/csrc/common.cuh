@@ -113,10 +113,42 @@ __device__ __forceinline__ void atomic_max_nonneg(unsigned long long* slot, doub
     atomicMax(slot, dbl_bits(v));
 }
 
+// (hi, lo) FP32 pair of an FP64 value from its IEEE-754 fields, without the
+// FP64 pipe: hi = the leading 24 significant bits (truncated), lo = the
+// remaining 29 bits times their power of two (rounded to 24 bits by the
+// integer conversion, scaled exactly), so |v - hi - lo| <= 2^-48 |v| for
+// 2^-60 <= |v| < 2^(EMAX+1). Below 2^-60 lo is dropped (relative error <= 2^-23
+// of a value that small); below 2^-126 the value counts as zero. From
+// 2^(EMAX+1) up, and for non-finite values, bad is set and (0, 0) returned.
+template <int EMAX>
+__device__ __forceinline__ float2 split_f64(double v, bool& bad) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+    const int e = (int)((b >> 52) & 0x7FF);
+    if (e > 1023 + EMAX) {
+        bad = true;
+        return make_float2(0.f, 0.f);
+    }
+    if (e < 1023 - 126) return make_float2(0.f, 0.f);
+    const unsigned sign = (unsigned)(b >> 63) << 31;
+    const unsigned long long mant = b & ((1ULL << 52) - 1ULL);
+    const float hi = __uint_as_float(sign | ((unsigned)(e - 1023 + 127) << 23) | (unsigned)(mant >> 29));
+    if (e < 1023 - 60) return make_float2(hi, 0.f);
+    const unsigned rem = (unsigned)(mant & ((1ULL << 29) - 1ULL));
+    const float scale = __uint_as_float((unsigned)(e - 1075 + 127) << 23);  // 2^(e - 1075), a normal float here
+    const float lo = __uint_as_float(__float_as_uint((float)rem * scale) | sign);
+    return make_float2(hi, lo);
+}
+
+// Max over the warp of non-negative doubles, taken on their bit patterns: the
+// integer pipe instead of the FP64 one, which is narrow on this part.
 __device__ __forceinline__ double warp_max(double v) {
+    unsigned long long b = dbl_bits(v);
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
-    return v;
+    for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long ob = __shfl_xor_sync(0xffffffffu, b, o);
+        b = ob > b ? ob : b;
+    }
+    return bits_dbl(b);
 }
 
 }  // namespace fegb

@@ -101,6 +101,16 @@ struct Problem {
     double* alpha_all = nullptr;
     double* mu_all = nullptr;
     int smallg_nb = 0;
+    // the CG operator's row sort by distinct id tuples of its swept dimensions
+    // (positions grouped by tuple), kept for the cluster subset over the same
+    // dimensions: tuple t holds sorted positions tuple_off[t] .. tuple_off[t+1]
+    std::vector<int> tuple_dims;            // FE dimensions of the key, ascending
+    std::vector<const int32_t*> tuple_gid;  // their id arrays when the sort ran
+    const int32_t* tuple_perm = nullptr;
+    const int32_t* tuple_off = nullptr;
+    const int32_t* tuple_gseq = nullptr;
+    int tuple_m = 0;
+    long long tuple_n = 0;
     int projections = 0;
     double demean_bytes = 0.0;
     // optional per-launch CUDA-event timing of the sweep kernels
@@ -324,6 +334,22 @@ double bits_to_double(unsigned long long b) {
 // ---------------------------- preparation ---------------------------------
 
 // Builds the storage-order problem from device inputs in the reference layout.
+// Dimensions the CG operator handles through dense count matrices: at most
+// DENSE_SMALL_MAX_G groups, C <= 32, and all matrices together within 8 GB at
+// uint32 counts. Such a dimension needs no row sort of its own.
+std::vector<char> cg_dense_plan(const std::vector<int>& G, int C, long long n) {
+    std::vector<char> dense(G.size(), 0);
+    if (C > 32 || n <= 0) return dense;
+    double bytes = 0.0;  // worst case: uint32 counts
+    for (size_t d = 0; d < G.size(); ++d)
+        if (G[d] > 0 && G[d] <= DENSE_SMALL_MAX_G)
+            for (size_t e = 0; e < G.size(); ++e)
+                if (e != d) bytes += 4.0 * std::max(1, G[e]) * G[d];
+    if (bytes > 8e9) return dense;
+    for (size_t d = 0; d < G.size(); ++d) dense[d] = G[d] > 0 && G[d] <= DENSE_SMALL_MAX_G;
+    return dense;
+}
+
 int build_problem(Problem& P, long long n_in, int k, int l, int n_fe, const double* y, const double* W, const double* Z,
                   const int32_t* const* ids, const int* G_in, bool drop_singletons, bool mixed, long long* n_single,
                   bool sorted_all = false) {
@@ -420,6 +446,12 @@ int build_problem(Problem& P, long long n_in, int k, int l, int n_fe, const doub
     FEGB_CUDA(cudaMemsetAsync(P.counts_all, 0, sizeof(int32_t) * (size_t)std::max(1LL, P.Gt), s), "counts zero");
     FEGB_CUDA(cudaMemsetAsync(P.alpha_all, 0, sizeof(double) * (size_t)std::max(1LL, P.Gt) * C, s), "alpha zero");
     int gmax = 1, gmax_small = 0;
+    // the CG operator sweeps every dimension it does not handle densely
+    std::vector<char> cg_sorted(n_fe, 0);
+    if (sorted_all) {
+        const std::vector<char> dense = cg_dense_plan(G, C, n);
+        for (int d = 0; d < n_fe; ++d) cg_sorted[d] = d != P.primary && !dense[d];
+    }
     for (int d = 0; d < n_fe; ++d) {
         Dim& D = P.dims[d];
         D.counts = P.counts_all + P.goff[d];
@@ -440,7 +472,7 @@ int build_problem(Problem& P, long long n_in, int k, int l, int n_fe, const doub
         } else {
             D.mode = MODE_GATHER;
         }
-        const bool need_sorted = D.mode == MODE_GATHER || (sorted_all && d != P.primary);
+        const bool need_sorted = D.mode == MODE_GATHER || cg_sorted[d];
         if (need_sorted && n > 0) {
             uint32_t* sorted = nullptr;
             FEGB_TRY(dalloc(scr, &sorted, (size_t)n, "gather gseq"));
@@ -461,7 +493,7 @@ int build_problem(Problem& P, long long n_in, int k, int l, int n_fe, const doub
                 FEGB_LAUNCH_CHECK("counts");
                 FEGB_TRY(dalloc(scr, &D.long_list, (size_t)D.G, "long groups"));
                 FEGB_TRY(find_long_groups(D.off, D.G, CHUNK_R, D.long_list, &D.n_long, s));
-                if (sorted_all) {
+                if (cg_sorted[d]) {
                     FEGB_TRY(dalloc(scr, &D.long_list_cg, (size_t)D.G, "long groups (cg)"));
                     FEGB_TRY(find_long_groups(D.off, D.G, CG_CHUNK, D.long_list_cg, &D.n_long_cg, s));
                     FEGB_TRY(dalloc(scr, &D.multi_list_cg, (size_t)D.G, "multi-chunk groups (cg)"));
@@ -491,7 +523,7 @@ int build_problem(Problem& P, long long n_in, int k, int l, int n_fe, const doub
     for (int d = 0; d < n_fe; ++d) {
         Dim& D = P.dims[d];
         D.gid_at_perm.assign(n_fe, nullptr);
-        if (!(D.mode == MODE_GATHER || (sorted_all && d != P.primary)) || n == 0) continue;
+        if (!(D.mode == MODE_GATHER || cg_sorted[d]) || n == 0) continue;
         for (int e = 0; e < n_fe; ++e) {
             if (e == d) continue;
             FEGB_TRY(dalloc(scr, &D.gid_at_perm[e], (size_t)n, "gid at perm"));
@@ -567,13 +599,19 @@ template <typename T>
 int sweep_sums_impl(Problem& P, int d, T* data, const PendingSet<T>& ps, bool writeback);
 
 // One sweep launch (segment or small-G), timed with CUDA events on the fit's
-// stream when profiling is on. Algorithmic bytes per launch: n (4 + 2 C s).
+// stream when profiling is on. Algorithmic bytes per launch: n (4 + C s) for
+// the group ids and the rows read, n C s more when the rows are written back,
+// 4 n for the traversal permutation of a gathered sweep and 4 n per pending
+// table's ids.
 template <typename T>
 int sweep_sums(Problem& P, int d, T* data, const PendingSet<T>& ps, bool writeback) {
     if (!P.profile) return sweep_sums_impl<T>(P, d, data, ps, writeback);
     Problem::Timed t;
     t.kind = (P.dims[d].mode == MODE_SMALLG ? 2 : 0) + (sizeof(T) == 4 ? 1 : 0);
-    t.bytes = (double)P.n * (4.0 + 2.0 * P.C * sizeof(T));
+    const Dim& D = P.dims[d];
+    const bool wb = writeback && D.mode != MODE_GATHER;
+    t.bytes = (double)P.n * (4.0 + (wb ? 2.0 : 1.0) * P.C * sizeof(T) + (D.mode == MODE_GATHER ? 4.0 : 0.0) +
+                             4.0 * ps.n);
     FEGB_CUDA(cudaEventCreate(&t.a), "profile event");
     FEGB_CUDA(cudaEventCreate(&t.b), "profile event");
     FEGB_CUDA(cudaEventRecord(t.a, P.s), "profile record");
@@ -742,44 +780,31 @@ int demean_plain(Problem& P, double tol, int max_iter, int* iterations, int* con
     return 0;
 }
 
-// FP64 group means of the current FP64 residual for every dimension; the
-// first (primary, storage-order) pass also subtracts the FE increments of the
-// previous refinement round and writes the rows back. Returns max |mean|.
+// FP64 group means of the current FP64 residual for every dimension, after
+// subtracting the FE increments of the previous refinement round from the rows
+// (apply_alpha; one element pass, then read-only sweeps). Returns max |mean|.
 int fp64_mean_pass(Problem& P, bool apply_alpha, double* mu_max) {
-    FEGB_CUDA(cudaMemsetAsync(P.max_bits + 1, 0, sizeof(unsigned long long), P.s), "reset mu max");
-    // storage-order pass first
-    std::vector<int> seq;
-    seq.push_back(P.primary);
-    for (int d = 0; d < P.n_fe; ++d)
-        if (d != P.primary) seq.push_back(d);
-    bool first = true;
-    for (int d : seq) {
-        Dim& D = P.dims[d];
+    if (apply_alpha && P.n > 0) {
         PendingSet<double> ps{};
-        ps.n = 0;
-        if (first && apply_alpha) {
-            for (int e = 0; e < P.n_fe; ++e) {
-                ps.gid[ps.n] = P.dims[e].gid;
-                ps.tab[ps.n] = P.dims[e].alpha;
-                ++ps.n;
-            }
+        for (int e = 0; e < P.n_fe; ++e) {
+            ps.gid[ps.n] = P.dims[e].gid;
+            ps.tab[ps.n] = P.dims[e].alpha;
+            ++ps.n;
         }
-        if (D.G > 0 && P.n > 0) {
-            if (ps.n > 0) {
-                // the increments in one coalesced element pass, then a read-only sweep
-                FEGB_TRY(launch_apply_pending<double>(P.X, P.C, P.n, ps, P.s));
-                ps = PendingSet<double>{};
-            }
-            FEGB_TRY(sweep_sums<double>(P, d, P.X, ps, false));
-            FinalizeParams f = finalize_base(P, d);
-            f.mean_out = D.mu;
-            f.max_partials = P.max_partials;
-            f.change_bits = P.max_bits + 1;
-            FEGB_TRY(launch_finalize(f, P.s));
-            bool rw = first && apply_alpha;
-            P.demean_bytes += (double)P.n * ((rw ? 4.0 * (1 + P.n_fe) : 4.0) + (rw ? 16.0 : 8.0) * P.C);
-        }
-        first = false;
+        FEGB_TRY(launch_apply_pending<double>(P.X, P.C, P.n, ps, P.s));
+        P.demean_bytes += (double)P.n * (4.0 * P.n_fe + 16.0 * P.C);
+    }
+    FEGB_CUDA(cudaMemsetAsync(P.max_bits + 1, 0, sizeof(unsigned long long), P.s), "reset mu max");
+    for (int d = 0; d < P.n_fe; ++d) {
+        Dim& D = P.dims[d];
+        if (D.G <= 0 || P.n <= 0) continue;
+        FEGB_TRY(sweep_sums<double>(P, d, P.X, PendingSet<double>{}, false));
+        FinalizeParams f = finalize_base(P, d);
+        f.mean_out = D.mu;
+        f.max_partials = P.max_partials;
+        f.change_bits = P.max_bits + 1;
+        FEGB_TRY(launch_finalize(f, P.s));
+        P.demean_bytes += (double)P.n * (4.0 + 8.0 * P.C);
     }
     unsigned long long b = 0;
     FEGB_TRY(d2h_sync(&b, P.max_bits + 1, sizeof(b), P.s, "mu max copy"));
@@ -947,13 +972,27 @@ int cg_streams(Problem& P, CGBuffers<T>& B) {
         stride *= Gd;
     }
     int m = 0;
-    int32_t *perm = nullptr, *toff = nullptr;
+    int32_t *perm = nullptr, *toff = nullptr, *tseq = nullptr;
     {
-        Scratch tmp(s);  // the row-level sort, released once the tuples are built
-        FEGB_TRY(tmp.alloc(&perm, (size_t)n, "tuple perm"));
-        FEGB_TRY(tmp.alloc(&toff, (size_t)n + 1, "tuple offsets"));
+        Scratch tmp(s);  // the sort's work arrays, released once the tuples are built
+        // the row permutation, offsets and tuple ranks outlive the operator: the
+        // cluster subset over the same dimensions reuses them
+        FEGB_TRY(dalloc(scr, &perm, (size_t)n, "tuple perm"));
+        FEGB_TRY(dalloc(scr, &toff, (size_t)n + 1, "tuple offsets"));
+        FEGB_TRY(dalloc(scr, &tseq, (size_t)n, "tuple ranks"));
         FEGB_TRY(cluster_ids_by_key(ptrs.data(), strides.data(), (int)sw.size(), n, bits_for(stride), nullptr, &m,
-                                    perm, toff, s, tmp, true, nullptr));
+                                    perm, toff, s, tmp, true, tseq));
+        if (m > 0) {
+            P.tuple_dims.assign(sw.begin(), sw.end());
+            std::sort(P.tuple_dims.begin(), P.tuple_dims.end());
+            P.tuple_gid.clear();
+            for (int d : P.tuple_dims) P.tuple_gid.push_back(P.dims[d].gid);
+            P.tuple_perm = perm;
+            P.tuple_off = toff;
+            P.tuple_gseq = tseq;
+            P.tuple_m = m;
+            P.tuple_n = n;
+        }
         if (m <= 0 || (double)m > 0.75 * (double)n) return 0;
         std::vector<int32_t*> tg(sw.size());
         for (size_t j = 0; j < sw.size(); ++j) FEGB_TRY(dalloc(scr, &tg[j], (size_t)m, "tuple ids"));
@@ -1024,11 +1063,6 @@ int cg_streams(Problem& P, CGBuffers<T>& B) {
     return 0;
 }
 
-__global__ void counts_to_f64_kernel(const int32_t* __restrict__ counts, long long G, double* __restrict__ out) {
-    const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (g < G) out[g] = (double)counts[g];
-}
-
 // Schur form: Jacobi preconditioner from the diagonal of
 // S = D_R'(I - P_P)D_R, S_gg = n_g - sum_w n_{w,g}^2 / n_w (only groups of the
 // primary spread over several groups of the dimension contribute), instead of
@@ -1043,43 +1077,28 @@ int cg_schur_precond(Problem& P, CGBuffers<T>& B) {
         if (d != pd && P.dims[d].G > 0 && !B.dense[d]) swept.push_back(d);
     if (swept.size() > 1 || (swept.size() == 1 && !B.compressed)) return 0;
     Scratch tmp(P.s);
-    double* diag = nullptr;
-    FEGB_TRY(tmp.alloc(&diag, (size_t)std::max(1LL, B.Gv), "schur diagonal"));
-    counts_to_f64_kernel<<<(unsigned)((B.Gv + 255) / 256), 256, 0, P.s>>>(B.counts_v, B.Gv, diag);
-    FEGB_LAUNCH_CHECK("schur diagonal init");
+    unsigned long long* acc = nullptr;
+    FEGB_TRY(tmp.alloc(&acc, (size_t)std::max(1LL, B.Gv), "schur diagonal"));
+    FEGB_CUDA(cudaMemsetAsync(acc, 0, sizeof(unsigned long long) * std::max(1LL, B.Gv), P.s), "schur diagonal zero");
     for (int e : swept) {
         const auto& st = B.stream[e];
         const int32_t* pid = nullptr;
         for (int i = 0; i < st.n_src; ++i)
             if (st.src_dim[i] == pd) pid = st.src_gid[i];
         if (!pid) return 0;
-        FEGB_TRY(launch_schur_diag_stream(st.off, P.dims[e].G, st.weight, pid, P.dims[pd].counts, diag + B.off[e],
-                                          P.s));
+        FEGB_TRY(launch_schur_diag_stream(st.gseq, st.m, st.weight, pid, P.dims[pd].counts, acc + B.off[e], P.s));
     }
     for (int sd = 0; sd < P.n_fe; ++sd) {
         if (!B.dense[sd] || sd == pd || P.dims[sd].G <= 0) continue;
         const int Gs = P.dims[sd].G;
-        const int nparts = dense_chunks(P.dims[pd].G);
-        double *part = nullptr, *folded = nullptr;
-        FEGB_TRY(tmp.alloc(&part, (size_t)nparts * Gs, "schur diagonal partials"));
-        FEGB_TRY(tmp.alloc(&folded, (size_t)Gs, "schur diagonal sums"));
         if (B.N8[sd][pd])
-            FEGB_TRY(launch_schur_diag_dense<uint8_t>(B.N8[sd][pd], P.dims[pd].G, Gs, P.dims[pd].counts, part, nparts,
-                                                      P.s));
+            FEGB_TRY(launch_schur_diag_dense<uint8_t>(B.N8[sd][pd], P.dims[pd].G, Gs, P.dims[pd].counts,
+                                                      acc + B.off[sd], P.s));
         else
-            FEGB_TRY(launch_schur_diag_dense<uint32_t>(B.N32[sd][pd], P.dims[pd].G, Gs, P.dims[pd].counts, part,
-                                                       nparts, P.s));
-        FEGB_TRY(launch_fold_dense(part, nparts, Gs, 1, folded, P.s));  // folded = -sum
-        std::vector<double> hd(Gs), hf(Gs);
-        FEGB_CUDA(cudaMemcpyAsync(hd.data(), diag + B.off[sd], sizeof(double) * Gs, cudaMemcpyDeviceToHost, P.s),
-                  "schur diagonal copy");
-        FEGB_TRY(d2h_sync(hf.data(), folded, sizeof(double) * Gs, P.s, "schur diagonal copy"));
-        for (int t = 0; t < Gs; ++t) hd[t] += hf[t];
-        FEGB_CUDA(cudaMemcpyAsync(diag + B.off[sd], hd.data(), sizeof(double) * Gs, cudaMemcpyHostToDevice, P.s),
-                  "schur diagonal copy");
-        FEGB_CUDA(cudaStreamSynchronize(P.s), "schur diagonal sync");
+            FEGB_TRY(launch_schur_diag_dense<uint32_t>(B.N32[sd][pd], P.dims[pd].G, Gs, P.dims[pd].counts,
+                                                       acc + B.off[sd], P.s));
     }
-    FEGB_TRY(launch_inv_diag<T>(diag, B.counts_v, B.Gv, B.inv, P.s));
+    FEGB_TRY(launch_inv_diag<T>(acc, B.counts_v, B.Gv, B.inv, P.s));
     FEGB_CUDA(cudaStreamSynchronize(P.s), "schur diagonal sync");
     return 0;
 }
@@ -1161,18 +1180,16 @@ int cg_alloc(Problem& P, CGBuffers<T>& B) {
     B.N32.assign(P.n_fe, std::vector<uint32_t*>(P.n_fe, nullptr));
     B.dpart_off.assign(P.n_fe, 0);
     B.dsum_off.assign(P.n_fe, 0);
-    if (C <= 32 && P.n > 0) {
-        double bytes = 0.0;  // worst case: uint32 counts
-        for (int d = 0; d < P.n_fe; ++d)
-            if (P.dims[d].G > 0 && P.dims[d].G <= DENSE_SMALL_MAX_G)
-                for (int e = 0; e < P.n_fe; ++e)
-                    if (e != d) bytes += 4.0 * std::max(1, P.dims[e].G) * P.dims[d].G;
-        if (bytes <= 8e9) {
+    std::vector<int> Gd(P.n_fe);
+    for (int d = 0; d < P.n_fe; ++d) Gd[d] = P.dims[d].G;
+    const std::vector<char> plan = cg_dense_plan(Gd, C, P.n);
+    if (std::find(plan.begin(), plan.end(), 1) != plan.end()) {
+        {
             long long parts = 0, sums = 0;
             unsigned* mx = nullptr;
             FEGB_TRY(dalloc(scr, &mx, 1, "count max"));
             for (int d = 0; d < P.n_fe; ++d) {
-                if (!(P.dims[d].G > 0 && P.dims[d].G <= DENSE_SMALL_MAX_G)) continue;
+                if (!plan[d]) continue;
                 B.dense[d] = 1;
                 B.any_dense = true;
                 B.dpart_off[d] = parts;
@@ -1850,22 +1867,16 @@ int cluster_score_sums(Problem& P, const double* S, int ns, const int32_t* perm,
     sp.R = CHUNK_R;
     long long nchunks = std::max(1LL, seg_nchunks(P.n, CHUNK_R));
     double *sums = nullptr, *head = nullptr, *tail = nullptr;
-    int32_t* cnt = nullptr;
     FEGB_TRY(scr.alloc(&sums, (size_t)std::max(1, n_cl) * ns, "score sums"));
     FEGB_TRY(scr.alloc(&head, (size_t)nchunks * ns, "score heads"));
     FEGB_TRY(scr.alloc(&tail, (size_t)nchunks * ns, "score tails"));
-    FEGB_TRY(scr.alloc(&cnt, (size_t)std::max(1, n_cl), "score counts"));
     sp.sums = sums;
     sp.head = head;
     sp.tail = tail;
-    FEGB_TRY(launch_seg_sweep<double>(sp, P.s));
     int32_t* long_list = nullptr;
     int n_long = 0;
     FEGB_TRY(scr.alloc(&long_list, (size_t)std::max(1, n_cl), "score long groups"));
     FEGB_TRY(find_long_groups(off, n_cl, CHUNK_R, long_list, &n_long, P.s));
-    FEGB_TRY(launch_long_sums(off, head, tail, CHUNK_R, ns, long_list, n_long, sums, P.s));
-    counts_from_offsets_kernel<<<(n_cl + 255) / 256, 256, 0, P.s>>>(off, n_cl, cnt);
-    FEGB_LAUNCH_CHECK("score counts");
     FinalizeParams f{};
     f.G = n_cl;
     f.C = ns;
@@ -1874,8 +1885,9 @@ int cluster_score_sums(Problem& P, const double* S, int ns, const int32_t* perm,
     f.head = head;
     f.tail = tail;
     f.R = CHUNK_R;
-    f.counts = cnt;
     f.sum_out = Sc;
+    FEGB_TRY(launch_seg_sweep<double>(sp, P.s));
+    FEGB_TRY(launch_long_sums(off, head, tail, CHUNK_R, ns, long_list, n_long, sums, P.s));
     return launch_finalize(f, P.s);
 }
 
@@ -2173,8 +2185,21 @@ int estimate_on_problem(Problem& P, const fegb_config& cfg, const int* G_all, lo
             }
             const bool smallg_single = m == 1 && !rows && P.dims[sd[0]].mode == MODE_SMALLG &&
                                        smallg_eligible(P.dims[sd[0]].G, ns);
+            bool tuples = m > 1 && P.tuple_m > 0 && P.tuple_n == n && P.tuple_dims.size() == sd.size();
+            if (tuples) {
+                std::vector<int> sds(sd);
+                std::sort(sds.begin(), sds.end());
+                for (size_t j = 0; j < sds.size() && tuples; ++j)
+                    tuples = sds[j] == P.tuple_dims[j] && P.dims[sds[j]].gid == P.tuple_gid[j];
+            }
             if (rows && m > 1) {
                 n_cl = (int)n;  // a refinement of single-row clusters: no sort needed
+            } else if (tuples) {
+                // the clusters are the CG operator's id tuples: its row sort serves
+                perm = P.tuple_perm;
+                gseq = P.tuple_gseq;
+                off = P.tuple_off;
+                n_cl = P.tuple_m;
             } else if (smallg_single) {
                 n_cl = P.dims[sd[0]].G;  // sums from per-block tables in storage order, no sort
             } else if (m == 1 && P.dims[sd[0]].mode != MODE_SMALLG) {

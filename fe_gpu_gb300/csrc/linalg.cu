@@ -551,31 +551,10 @@ struct DSParams {
     int* bad;          // set when a value is outside the split range (split_bits)
 };
 
-// (hi, lo) FP32 pair of an FP64 value from its IEEE-754 fields, without the
-// FP64 pipe: hi = the leading 24 significant bits (truncated), lo = the
-// remaining 29 bits times their power of two (rounded to 24 bits by the
-// integer conversion, scaled exactly), so |v - hi - lo| <= 2^-48 |v| for
-// 2^-60 <= |v| < 2^57. Below 2^-60 (noise-level values, e.g. residuals of a
-// converged projection) lo is dropped (relative error <= 2^-23 of a value that
-// small); below 2^-126 the value counts as zero. From 2^57 up, and for non-finite
-// values, bad is set and the product is formed in FP64 instead.
-__device__ __forceinline__ float2 split_bits(double v, bool& bad) {
-    const unsigned long long b = (unsigned long long)__double_as_longlong(v);
-    const int e = (int)((b >> 52) & 0x7FF);
-    if (e > 1023 + 56) {
-        bad = true;
-        return make_float2(0.f, 0.f);
-    }
-    if (e < 1023 - 126) return make_float2(0.f, 0.f);
-    const unsigned sign = (unsigned)(b >> 63) << 31;
-    const unsigned long long mant = b & ((1ULL << 52) - 1ULL);
-    const float hi = __uint_as_float(sign | ((unsigned)(e - 1023 + 127) << 23) | (unsigned)(mant >> 29));
-    if (e < 1023 - 60) return make_float2(hi, 0.f);
-    const unsigned rem = (unsigned)(mant & ((1ULL << 29) - 1ULL));
-    const float scale = __uint_as_float((unsigned)(e - 1075 + 127) << 23);  // 2^(e - 1075), a normal float here
-    const float lo = __uint_as_float(__float_as_uint((float)rem * scale) | sign);
-    return make_float2(hi, lo);
-}
+// The cross products split values below 2^57 (split_f64): a product and its
+// 256-row partial sums stay inside the FP32 range. Outside it (and for
+// non-finite values) bad is set and the product is formed in FP64 instead.
+__device__ __forceinline__ float2 split_bits(double v, bool& bad) { return split_f64<56>(v, bad); }
 
 // Tile rows [row0, row0 + rows) of an FP64 source into shared memory as
 // (hi, lo) FP32 pairs: hi = fl32(x), lo = fl32(x - hi) (x - hi is exact in FP64).

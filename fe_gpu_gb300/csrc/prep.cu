@@ -284,7 +284,8 @@ struct DimPtrs {
     int zero_based;
 };
 
-__global__ void keys_kernel(DimPtrs dp, long long n, unsigned long long* __restrict__ keys) {
+template <typename K>
+__global__ void keys_kernel(DimPtrs dp, long long n, K* __restrict__ keys) {
     long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     long long st = (long long)gridDim.x * blockDim.x;
     for (; i < n; i += st) {
@@ -296,7 +297,7 @@ __global__ void keys_kernel(DimPtrs dp, long long n, unsigned long long* __restr
             else if (v > 0)
                 key += (unsigned long long)(v - 1) * dp.stride[d];
         }
-        keys[i] = key;
+        keys[i] = (K)key;
     }
 }
 
@@ -490,33 +491,45 @@ int cluster_ids_by_key(const int32_t* const* dims, const unsigned long long* str
         dp.p[d] = dims[d];
         dp.stride[d] = strides[d];
     }
-    unsigned long long *keys = nullptr, *sorted = nullptr;
     int32_t* perm = perm_out;
     uint32_t *flags = nullptr, *excl = nullptr, *total = nullptr;
-    FEGB_TRY(scr.alloc(&keys, (size_t)n, "cluster keys"));
-    FEGB_TRY(scr.alloc(&sorted, (size_t)n, "cluster sorted keys"));
     if (!perm) FEGB_TRY(scr.alloc(&perm, (size_t)n, "cluster perm"));
     FEGB_TRY(scr.alloc(&flags, (size_t)n, "cluster flags"));
     FEGB_TRY(scr.alloc(&excl, (size_t)n, "cluster scan"));
     FEGB_TRY(scr.alloc(&total, 1, "cluster total"));
     unsigned g = grid_stride_blocks(n, 256);
-    keys_kernel<<<g, 256, 0, s>>>(dp, n, keys);
-    FEGB_LAUNCH_CHECK("cluster keys");
-    if (key_bits < 0) {
-        unsigned long long* mx = nullptr;
-        FEGB_TRY(scr.alloc(&mx, 1, "max key"));
-        FEGB_CUDA(cudaMemsetAsync(mx, 0, sizeof(unsigned long long), s), "max key reset");
-        max_u64_kernel<<<g, 256, 0, s>>>(keys, n, mx);
-        FEGB_LAUNCH_CHECK("max key");
-        unsigned long long h = 0;
-        FEGB_CUDA(cudaMemcpyAsync(&h, mx, sizeof(h), cudaMemcpyDeviceToHost, s), "max key copy");
-        FEGB_CUDA(cudaStreamSynchronize(s), "max key sync");
-        key_bits = 0;
-        while (key_bits < 64 && (h >> key_bits) != 0ull) ++key_bits;
+    if (key_bits >= 0 && key_bits <= 32) {
+        // keys that fit 32 bits: half the bytes moved by every radix pass
+        uint32_t *keys = nullptr, *sorted = nullptr;
+        FEGB_TRY(scr.alloc(&keys, (size_t)n, "cluster keys"));
+        FEGB_TRY(scr.alloc(&sorted, (size_t)n, "cluster sorted keys"));
+        keys_kernel<uint32_t><<<g, 256, 0, s>>>(dp, n, keys);
+        FEGB_LAUNCH_CHECK("cluster keys");
+        FEGB_TRY(radix_sort_u32(keys, nullptr, sorted, perm, n, key_bits, s, scr));
+        change_flags_kernel<uint32_t><<<g, 256, 0, s>>>(sorted, n, flags);
+        FEGB_LAUNCH_CHECK("cluster flags");
+    } else {
+        unsigned long long *keys = nullptr, *sorted = nullptr;
+        FEGB_TRY(scr.alloc(&keys, (size_t)n, "cluster keys"));
+        FEGB_TRY(scr.alloc(&sorted, (size_t)n, "cluster sorted keys"));
+        keys_kernel<unsigned long long><<<g, 256, 0, s>>>(dp, n, keys);
+        FEGB_LAUNCH_CHECK("cluster keys");
+        if (key_bits < 0) {
+            unsigned long long* mx = nullptr;
+            FEGB_TRY(scr.alloc(&mx, 1, "max key"));
+            FEGB_CUDA(cudaMemsetAsync(mx, 0, sizeof(unsigned long long), s), "max key reset");
+            max_u64_kernel<<<g, 256, 0, s>>>(keys, n, mx);
+            FEGB_LAUNCH_CHECK("max key");
+            unsigned long long h = 0;
+            FEGB_CUDA(cudaMemcpyAsync(&h, mx, sizeof(h), cudaMemcpyDeviceToHost, s), "max key copy");
+            FEGB_CUDA(cudaStreamSynchronize(s), "max key sync");
+            key_bits = 0;
+            while (key_bits < 64 && (h >> key_bits) != 0ull) ++key_bits;
+        }
+        FEGB_TRY(radix_sort_u64(keys, nullptr, sorted, perm, n, key_bits, s, scr));
+        change_flags_kernel<unsigned long long><<<g, 256, 0, s>>>(sorted, n, flags);
+        FEGB_LAUNCH_CHECK("cluster flags");
     }
-    FEGB_TRY(radix_sort_u64(keys, nullptr, sorted, perm, n, key_bits, s, scr));
-    change_flags_kernel<unsigned long long><<<g, 256, 0, s>>>(sorted, n, flags);
-    FEGB_LAUNCH_CHECK("cluster flags");
     FEGB_TRY(scan_exclusive_u32(flags, excl, n, total, s, scr));
     scatter_ranks_kernel<<<g, 256, 0, s>>>(perm, excl, flags, n, out_ids, offsets_out, gseq_out);
     FEGB_LAUNCH_CHECK("cluster ranks");

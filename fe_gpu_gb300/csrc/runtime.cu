@@ -792,4 +792,74 @@ int fegb_test_dense_pair(const uint8_t* counts, long long Ge, int Gs, const floa
     return 0;
 }
 
+// Self-test of the FP64 group-sum sweeps (segment and small-G forms) on host
+// data; see include/fegb.h.
+int fegb_test_group_sums(const double* X, long long n, int C, const int32_t* gid, int G, int small_g,
+                         double* out_sums) {
+    using namespace fegb;
+    constexpr int kChunk = 256;  // positions per segment-sweep chunk, as the fits use
+    if (n <= 0 || C <= 0 || G <= 0 || !X || !gid || !out_sums) return set_error("fegb_test_group_sums: invalid sizes");
+    if (small_g && !smallg_eligible(G, C)) return set_error("fegb_test_group_sums: G=%d C=%d not small-G", G, C);
+    Scratch scr(kLegacy);
+    double *dX = nullptr, *dsums = nullptr;
+    int32_t* dg = nullptr;
+    FEGB_TRY(scr.alloc(&dX, (size_t)n * C, "test data"));
+    FEGB_TRY(scr.alloc(&dg, (size_t)n, "test ids"));
+    FEGB_TRY(scr.alloc(&dsums, (size_t)G * C, "test sums"));
+    FEGB_CUDA(cudaMemcpy(dX, X, sizeof(double) * n * C, cudaMemcpyHostToDevice), "test data copy");
+    FEGB_CUDA(cudaMemcpy(dg, gid, sizeof(int32_t) * n, cudaMemcpyHostToDevice), "test ids copy");
+    if (small_g) {
+        SmallGParams<double> sp{};
+        const int nb = smallg_nblocks(n);
+        sp.X = dX;
+        sp.C = C;
+        sp.n = n;
+        sp.gid = dg;
+        sp.G = G;
+        sp.rows_per_block = (n + nb - 1) / nb;
+        FEGB_TRY(scr.alloc(&sp.partials, (size_t)nb * G * C, "test partials"));
+        FEGB_TRY(launch_smallg_sweep<double>(sp, nb, kLegacy));
+        FEGB_TRY(launch_fold_smallg(sp.partials, nb, G, C, dsums, kLegacy));
+    } else {
+        // ids must be non-decreasing: storage order is the traversal order
+        const long long nchunks = seg_nchunks(n, kChunk);
+        double *sums = nullptr, *head = nullptr, *tail = nullptr;
+        int32_t *off = nullptr, *longs = nullptr;
+        int n_long = 0;
+        FEGB_TRY(scr.alloc(&sums, (size_t)G * C, "test run sums"));
+        FEGB_TRY(scr.alloc(&head, (size_t)nchunks * C, "test heads"));
+        FEGB_TRY(scr.alloc(&tail, (size_t)nchunks * C, "test tails"));
+        FEGB_TRY(scr.alloc(&off, (size_t)G + 1, "test offsets"));
+        FEGB_TRY(scr.alloc(&longs, (size_t)G, "test long groups"));
+        FEGB_TRY(segment_offsets(reinterpret_cast<const uint32_t*>(dg), n, G, off, kLegacy));
+        FEGB_TRY(find_long_groups(off, G, kChunk, longs, &n_long, kLegacy));
+        SegSweepParams<double> sp{};
+        sp.X = dX;
+        sp.rs = C;
+        sp.cs = 1;
+        sp.C = C;
+        sp.n = n;
+        sp.gseq = dg;
+        sp.R = kChunk;
+        sp.sums = sums;
+        sp.head = head;
+        sp.tail = tail;
+        FEGB_TRY(launch_seg_sweep<double>(sp, kLegacy));
+        FEGB_TRY(launch_long_sums(off, head, tail, kChunk, C, longs, n_long, sums, kLegacy));
+        FinalizeParams f{};
+        f.G = G;
+        f.C = C;
+        f.off = off;
+        f.sums = sums;
+        f.head = head;
+        f.tail = tail;
+        f.R = kChunk;
+        f.sum_out = dsums;
+        FEGB_TRY(launch_finalize(f, kLegacy));
+    }
+    FEGB_CUDA(cudaDeviceSynchronize(), "test sync");
+    FEGB_CUDA(cudaMemcpy(out_sums, dsums, sizeof(double) * G * C, cudaMemcpyDeviceToHost), "test sums out");
+    return 0;
+}
+
 }  // extern "C"

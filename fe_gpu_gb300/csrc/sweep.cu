@@ -25,13 +25,16 @@ inline Geometry geometry(int C) {
     return g;
 }
 
+// Positions per lane loaded ahead of the accumulation: the sweeps are bound by
+// the loads in flight (the FP64 segment sweep is given 80 registers, 3 blocks
+// per SM, to hold 8 without spilling).
 template <typename T>
 struct SweepUnroll {
-    static constexpr int U = sizeof(T) == 4 ? 8 : 4;
+    static constexpr int U = 8;
 };
 
 template <typename T>
-__global__ void __launch_bounds__(SW_THREADS, 4)
+__global__ void __launch_bounds__(SW_THREADS, sizeof(T) == 8 ? 3 : 4)
     seg_sweep_kernel(SegSweepParams<T> p, int L, int P, int CT, long long n_items) {
     constexpr int U = SweepUnroll<T>::U;
     constexpr bool kF32 = sizeof(T) == 4;
@@ -228,11 +231,14 @@ __global__ void __launch_bounds__(FIN_THREADS) finalize_kernel(FinalizeParams p)
     const long long total = (long long)p.G * p.C;
     double amax = 0.0;
     if (idx < total) {
-        const int g = (int)(idx / p.C);
+        // 32-bit division where the element count allows it (FP64-free integer path)
+        const int g = total < 0x7fffffffLL ? (int)idx / p.C : (int)(idx / p.C);
         const int c = (int)(idx - (long long)g * p.C);
         const double sum = source_sum(p, g, c, idx, total);
-        const int cnt = p.counts ? p.counts[g] : 0;
         if (p.sum_out) p.sum_out[idx] = sum;
+        // plain sums (cluster score sums): no mean, no reciprocal
+        if (!(p.mean_out || p.prev || p.pend64 || p.pend32 || p.alpha || p.max_partials)) return;
+        const int cnt = p.counts ? p.counts[g] : 0;
         // reciprocal multiply, as in src/gpu/fe_gpu_runtime.cu:195-200
         const double inv = p.inv_counts ? p.inv_counts[g] : (cnt > 0 ? 1.0 / (double)cnt : 0.0);
         double mean = sum * inv;
@@ -1756,85 +1762,116 @@ template int launch_alpha_primary<double>(const double*, const double*, long lon
 
 // ---- diagonal of the Schur complement (the CG's Jacobi preconditioner) ----
 
-// diag[g] -= sum over positions j in [off[g], off[g+1]) of w[j]^2 / n_P[pid[j]]
-// (a stream in which each (group of e, group of P) pair is one position). One
-// warp per group: lane l takes positions l, l + 32, ... in order, then a fixed
-// shuffle tree (groups of a Pareto-sized dimension can hold 1e5 positions).
-__global__ void schur_diag_stream_kernel(const int32_t* __restrict__ off, int G, const float* __restrict__ w,
-                                         const int32_t* __restrict__ pid, const int32_t* __restrict__ nP,
-                                         double* __restrict__ diag) {
-    const long long g = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int lane = threadIdx.x & 31;
-    if (g >= G) return;
-    double acc = 0.0;
-    for (int j = off[g] + lane; j < off[g + 1]; j += 32) {
-        const double wj = w ? (double)w[j] : 1.0;
-        const int n = nP[pid[j]];
-        if (n > 0) acc += wj * wj / (double)n;
-    }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
-    if (lane == 0) diag[g] -= acc;
+// S_gg = n_g - sum_w n_wg^2 / n_w is accumulated as the sum of the
+// nonnegative terms n_wg (n_w - n_wg) / n_w (the weights n_wg of a group add up
+// to n_g), each term in FP32 and rounded to a fixed-point integer with 20
+// fraction bits: integer sums are exact and independent of the order, so the
+// 64-bit atomics leave the result deterministic, no term cancels another, and a
+// group whose every primary group lies inside it sums to exactly 0. A nonzero
+// term is at least 1/2 (n_wg >= 1, n_w - n_wg >= 1), so 2^-20 is far below the
+// resolution a Jacobi preconditioner needs. Nothing here runs on the FP64 pipe.
+__device__ __forceinline__ unsigned long long schur_term_fixed(float w, int nw) {
+    const int wi = (int)w;
+    if (nw <= 0 || wi >= nw) return 0ull;
+    const float t = w * (float)(nw - wi) / (float)nw;
+    return __float2ull_rn(t * 1048576.0f);
 }
 
-// partials[block][t] = sum over the block's groups g of N[g][t]^2 / n[g]
-// (DENSE_TILE-row blocks as the dense passes; one thread per t, groups in order)
+// acc[gseq[j]] += term(w[j], n_P[pid[j]]) over the positions of a stream in
+// group order; each thread takes SCHUR_RUN consecutive positions and issues one
+// atomic per group run it sees.
+constexpr int SCHUR_RUN = 16;
+__global__ void schur_diag_stream_kernel(const int32_t* __restrict__ gseq, long long m, const float* __restrict__ w,
+                                         const int32_t* __restrict__ pid, const int32_t* __restrict__ nP,
+                                         unsigned long long* __restrict__ acc) {
+    const long long j0 = ((long long)blockIdx.x * blockDim.x + threadIdx.x) * SCHUR_RUN;
+    if (j0 >= m) return;
+    const long long j1 = min(m, j0 + SCHUR_RUN);
+    int g = gseq[j0];
+    unsigned long long a = 0;
+    for (long long j = j0; j < j1; ++j) {
+        const int gj = gseq[j];
+        if (gj != g) {
+            if (a) atomicAdd(acc + g, a);
+            g = gj;
+            a = 0;
+        }
+        a += schur_term_fixed(w ? w[j] : 1.0f, nP[pid[j]]);
+    }
+    if (a) atomicAdd(acc + g, a);
+}
+
+// acc[t] += term(N[g][t], n[g]) over the Ge x Gs count matrix: thread i of the
+// first S = (threads / Gs) * Gs takes elements i, i + S, ... (one column each),
+// folded per block in shared memory, one global atomic per column per block.
 template <typename CT>
 __global__ void schur_diag_dense_kernel(const CT* __restrict__ N, long long Ge, int Gs, const int32_t* __restrict__ n,
-                                        long long per, double* __restrict__ partials) {
-    const long long g0 = (long long)blockIdx.x * per;
-    const long long g1 = min(Ge, g0 + per);
-    for (int t = threadIdx.x; t < Gs; t += blockDim.x) {
-        double acc = 0.0;
-        for (long long g = g0; g < g1; ++g) {
-            const double m = (double)N[g * Gs + t];
-            if (m != 0.0 && n[g] > 0) acc += m * m / (double)n[g];
+                                        unsigned long long* __restrict__ acc) {
+    __shared__ unsigned long long col[DENSE_SMALL_MAX_G];
+    for (int t = threadIdx.x; t < Gs; t += blockDim.x) col[t] = 0ull;
+    __syncthreads();
+    const long long T = (long long)gridDim.x * blockDim.x;
+    const long long S = T - T % Gs;
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < S) {
+        const int t = (int)(i % Gs);
+        const long long gstep = S / Gs;
+        unsigned long long a = 0;
+        for (long long g = i / Gs; g < Ge; g += gstep) {
+            const unsigned mv = (unsigned)N[g * Gs + t];
+            if (mv) a += schur_term_fixed((float)mv, n[g]);
         }
-        partials[(long long)blockIdx.x * Gs + t] = acc;
+        if (a) atomicAdd(col + t, a);
     }
+    __syncthreads();
+    for (int t = threadIdx.x; t < Gs; t += blockDim.x)
+        if (col[t]) atomicAdd(acc + t, col[t]);
 }
 
-// inv[g] = diag[g] > tiny * counts[g] ? 1 / diag[g] : 0 (an unidentified group gets 0)
+// inv[g] = 1 / S_gg, or 0 when S_gg <= 1e-9 counts[g] (no identifying variation)
 template <typename T>
-__global__ void inv_diag_kernel(const double* __restrict__ diag, const int32_t* __restrict__ counts, long long G,
-                                T* __restrict__ inv) {
+__global__ void inv_diag_kernel(const unsigned long long* __restrict__ acc, const int32_t* __restrict__ counts,
+                                long long G, T* __restrict__ inv) {
     const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= G) return;
-    const double d = diag[g];
-    inv[g] = (counts[g] > 0 && d > 1e-9 * (double)counts[g]) ? (T)(1.0 / d) : T(0);
+    const float d = (float)acc[g] * (1.0f / 1048576.0f);
+    inv[g] = (counts[g] > 0 && d > 1e-9f * (float)counts[g]) ? (T)(1.0f / d) : T(0);
 }
 
-int launch_schur_diag_stream(const int32_t* off, int G, const float* w, const int32_t* pid, const int32_t* nP,
-                             double* diag, cudaStream_t s) {
-    if (G <= 0) return 0;
-    schur_diag_stream_kernel<<<(unsigned)(((long long)G * 32 + 255) / 256), 256, 0, s>>>(off, G, w, pid, nP, diag);
+int launch_schur_diag_stream(const int32_t* gseq, long long m, const float* w, const int32_t* pid, const int32_t* nP,
+                             unsigned long long* acc, cudaStream_t s) {
+    if (m <= 0) return 0;
+    const long long threads = (m + SCHUR_RUN - 1) / SCHUR_RUN;
+    schur_diag_stream_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(gseq, m, w, pid, nP, acc);
     FEGB_LAUNCH_CHECK("schur diagonal (stream)");
     return 0;
 }
 
 template <typename CT>
-int launch_schur_diag_dense(const CT* N, long long Ge, int Gs, const int32_t* n, double* partials, int nparts,
+int launch_schur_diag_dense(const CT* N, long long Ge, int Gs, const int32_t* n, unsigned long long* acc,
                             cudaStream_t s) {
-    if (Ge <= 0) return 0;
-    const long long per = (Ge + nparts - 1) / nparts;
-    schur_diag_dense_kernel<CT><<<nparts, 64, 0, s>>>(N, Ge, Gs, n, per, partials);
+    if (Ge <= 0 || Gs <= 0) return 0;
+    if (Gs > DENSE_SMALL_MAX_G) return set_error("schur diagonal: %d columns above %d", Gs, DENSE_SMALL_MAX_G);
+    const long long elems = Ge * Gs;
+    const long long blocks = std::min<long long>(DENSE_MAX_BLOCKS * 2, (elems + 255) / 256);
+    schur_diag_dense_kernel<CT><<<(unsigned)std::max(1LL, blocks), 256, 0, s>>>(N, Ge, Gs, n, acc);
     FEGB_LAUNCH_CHECK("schur diagonal (dense)");
     return 0;
 }
-template int launch_schur_diag_dense<uint8_t>(const uint8_t*, long long, int, const int32_t*, double*, int,
+template int launch_schur_diag_dense<uint8_t>(const uint8_t*, long long, int, const int32_t*, unsigned long long*,
                                               cudaStream_t);
-template int launch_schur_diag_dense<uint32_t>(const uint32_t*, long long, int, const int32_t*, double*, int,
+template int launch_schur_diag_dense<uint32_t>(const uint32_t*, long long, int, const int32_t*, unsigned long long*,
                                                cudaStream_t);
 
 template <typename T>
-int launch_inv_diag(const double* diag, const int32_t* counts, long long G, T* inv, cudaStream_t s) {
+int launch_inv_diag(const unsigned long long* acc, const int32_t* counts, long long G, T* inv, cudaStream_t s) {
     if (G <= 0) return 0;
-    inv_diag_kernel<T><<<(unsigned)((G + 255) / 256), 256, 0, s>>>(diag, counts, G, inv);
+    inv_diag_kernel<T><<<(unsigned)((G + 255) / 256), 256, 0, s>>>(acc, counts, G, inv);
     FEGB_LAUNCH_CHECK("inverse diagonal");
     return 0;
 }
-template int launch_inv_diag<float>(const double*, const int32_t*, long long, float*, cudaStream_t);
-template int launch_inv_diag<double>(const double*, const int32_t*, long long, double*, cudaStream_t);
+template int launch_inv_diag<float>(const unsigned long long*, const int32_t*, long long, float*, cudaStream_t);
+template int launch_inv_diag<double>(const unsigned long long*, const int32_t*, long long, double*, cudaStream_t);
 
 // One warp per (t, c): strided fold over the parts, fixed shuffle tree.
 __global__ void fold_dense_kernel(const double* __restrict__ partials, int nparts, int TC, double* __restrict__ sums) {

@@ -277,18 +277,20 @@ int launch_table_from_compact(const T* src, long long G, int C, T* table, int L,
 // alpha[g * C + c] = mu[g * C + c] + table[g * L + c]
 template <typename T>
 int launch_alpha_primary(const double* mu, const T* table, long long G, int C, int L, double* alpha, cudaStream_t s);
-// Diagonal of the Schur complement D_R'(I - P_P)D_R: diag[g] (= n_g on entry)
-// -= sum over the group's positions of w^2 / n_P[pid] (each (group, primary
-// group) pair one position of the stream; w null = 1)
-int launch_schur_diag_stream(const int32_t* off, int G, const float* w, const int32_t* pid, const int32_t* nP,
-                             double* diag, cudaStream_t s);
-// partials[part][t] = sum over the part's groups g of N[g][t]^2 / n[g] (nparts parts in order)
+// Diagonal of the Schur complement D_R'(I - P_P)D_R as fixed-point sums (20
+// fraction bits) of n_wg (n_w - n_wg) / n_w over the (group, primary group)
+// pairs: acc must be zeroed first. Stream form: one position per pair, in
+// group order (gseq), weight w (null = 1), primary group pid, primary counts nP.
+int launch_schur_diag_stream(const int32_t* gseq, long long m, const float* w, const int32_t* pid, const int32_t* nP,
+                             unsigned long long* acc, cudaStream_t s);
+// Dense form: N is the Ge x Gs count matrix (primary groups x the dimension's
+// Gs <= DENSE_SMALL_MAX_G groups), n the primary counts; adds into acc[0..Gs).
 template <typename CT>
-int launch_schur_diag_dense(const CT* N, long long Ge, int Gs, const int32_t* n, double* partials, int nparts,
+int launch_schur_diag_dense(const CT* N, long long Ge, int Gs, const int32_t* n, unsigned long long* acc,
                             cudaStream_t s);
-// inv[g] = 1 / diag[g], or 0 when diag[g] <= 1e-9 counts[g] (no identifying variation)
+// inv[g] = 1 / S_gg, or 0 when S_gg <= 1e-9 counts[g] (no identifying variation)
 template <typename T>
-int launch_inv_diag(const double* diag, const int32_t* counts, long long G, T* inv, cudaStream_t s);
+int launch_inv_diag(const unsigned long long* acc, const int32_t* counts, long long G, T* inv, cudaStream_t s);
 // sums[t * C + c] = -(sum over parts of partials[part][t][c]), parts in order
 int launch_fold_dense(const double* partials, int nparts, int Gs, int C, double* sums, cudaStream_t s);
 // Partial blocks (one FP64 partial per column each) of the CG vector kernels

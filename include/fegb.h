@@ -158,6 +158,13 @@ int fegb_test_dense_pair(const unsigned char* counts, long long Ge, int Gs, cons
                          int C, const float* sums, const int* group_counts, int accumulate, int tensor_cores,
                          double* out_small, float* out_extra, float* out_table);
 
+/* Self-test of the FP64 group-sum sweeps behind the within-transform's group
+ * means, on host arrays: X is n x C row-major, gid the 0-based group of each
+ * row (non-decreasing for the segment form, small_g = 0; any order for the
+ * small-G form, small_g = 1, which needs G x C to fit its shared-memory
+ * tables). out_sums[g*C+c] = sum of X[i][c] over the rows of group g. */
+int fegb_test_group_sums(const double* X, long long n, int C, const int* gid, int G, int small_g, double* out_sums);
+
 /* FE reconstruction of --save-fe (reconstruct_and_save_fixed_effects,
  * src/core/fe_pipeline.f90:1619-1733): forward Gauss-Seidel sweeps of the
  * residual y - W beta (beta: host, k values), dimension by dimension, each

@@ -161,3 +161,4 @@ def test_deterministic_bitwise(built, method):
     assert a.fe_iterations == b.fe_iterations
     assert np.array_equal(a.beta, b.beta)
     assert np.array_equal(a.se, b.se)
+

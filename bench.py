@@ -43,6 +43,12 @@ WORKLOADS = {
                                   "regressors, FEs worker/firm/time, 3-way clustered SEs"),
     "worker_firm_2M": dict(n_workers=100_000, n_firms=10_000, n_periods=20, switch_prob=0.1, n_reg=8,
                            seed=20261204, desc="small case of the 20M panel for profiling"),
+    "worker_firm_5M": dict(n_workers=250_000, n_firms=25_000, n_periods=20, switch_prob=0.1, n_reg=8,
+                           seed=20261204, desc="quarter-size case of the 20M panel for ncu captures (360 MB of "
+                                                "FP64 rows, above L2)"),
+    "nls_panel": dict(generator="nls", seed=20261203,
+                      desc="nlswork-shaped unbalanced panel: 4,700 ids with U{1..15} consecutive years of 15, "
+                           "13 Zipf(1.1) occupations, 5 regressors, FEs id/occupation/year, 3-way clustered SEs"),
 }
 
 
@@ -72,11 +78,19 @@ def dist_env():
         os.environ.get("LOCAL_RANK", "0"))
 
 
-def make_panel(name):
-    from fe_gpu_gb300.synth import worker_firm_panel
+def make_panel(name, scale=1):
+    """The workload's panel; scale > 1 divides the workers and firms of a
+    worker-firm panel (the bounded CPU sample). The nls panel is small enough
+    to be used whole."""
+    from fe_gpu_gb300.synth import nls_panel, worker_firm_panel
 
     w = dict(WORKLOADS[name])
     w.pop("desc")
+    if w.pop("generator", None) == "nls":
+        return nls_panel(seed=w["seed"])
+    if scale > 1:
+        w["n_workers"] = max(1000, w["n_workers"] // scale)
+        w["n_firms"] = max(100, w["n_firms"] // scale)
     return worker_firm_panel(**w)
 
 
@@ -148,24 +162,30 @@ def measured_hbm_peak():
 def cpu_baseline(name, threads):
     """The oracle (C restatement of the reference CPU estimator) on a bounded
     sample of the workload: the same panel design with 1/5 of the workers and
-    firms (4M rows), fitted with the CPU path's conventions."""
-    from fe_gpu_gb300.synth import worker_firm_panel
+    firms (4M rows of the 20M panel), fitted with the CPU path's conventions;
+    the nls panel whole."""
     from oracle import oracle as O
 
-    w = dict(WORKLOADS[name])
-    w.pop("desc")
-    w["n_workers"] = max(1000, w["n_workers"] // 5)
-    w["n_firms"] = max(100, w["n_firms"] // 5)
-    hdr, host = worker_firm_panel(**w)
+    w = WORKLOADS[name]
+    nls = w.get("generator") == "nls"
+    hdr, host = make_panel(name, scale=1 if nls else 5)
     os.environ["OMP_NUM_THREADS"] = str(threads)
     t0 = time.perf_counter()
     r = O.cpu_estimate(host.y, host.W, host.fe_ids, tol=1e-8, max_iter=100000, cluster_dims=[1, 2, 3])
     dt = time.perf_counter() - t0
     n = host.y.shape[0]
+    what = ("the whole panel" if nls else
+            f"{w['n_workers'] // 5} workers x {w['n_periods']} periods, {w['n_firms'] // 5} firms")
     return {"value": n / dt, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"{n} rows ({w['n_workers']} workers x {w['n_periods']} periods, {w['n_firms']} firms), "
-                      f"whole fit with the reference CPU conventions, {r.stats['fe_iterations']} AP iterations, "
-                      f"{dt:.2f} s", "seconds": dt}
+            "sample": f"{n} rows ({what}), whole fit with the reference CPU conventions, "
+                      f"{r.stats['fe_iterations']} AP iterations, {dt:.2f} s", "seconds": dt}
+
+
+def workload_rows(name):
+    w = WORKLOADS[name]
+    if w.get("generator") == "nls":
+        return make_panel(name)[1].y.shape[0]
+    return w["n_workers"] * w["n_periods"]
 
 
 def run_reference(args):
@@ -182,7 +202,7 @@ def run_reference(args):
             vals.append(cb["value"])
     value = float(np.median(vals)) if vals else cb["value"]
     w = WORKLOADS[args.workload]
-    rows = w["n_workers"] * w["n_periods"]
+    rows = workload_rows(args.workload)
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": rows / value * 1e3, "higher_is_better": True,
@@ -365,7 +385,7 @@ def main():
                         "beta_equal_to_resident_fit": bool(np.array_equal(fr.beta, last.beta))}
 
     # roofline of the dominant sweep-kernel family, timed live in the timed steps
-    roofline = roofline_of(results, args.workload)
+    roofline = roofline_of(results, args.workload, elements_per_sweep=n * (1 + k))
     demean_gbs = last.stats["demean_bytes"] / last.stats["time_demean"] / 1e9 if last.stats["time_demean"] else None
 
     value = world * n / (ms / 1e3)
@@ -415,13 +435,23 @@ FAMILIES = ["segment sweep fp64", "segment sweep fp32", "small-G sweep fp64", "s
             "CG operator segment sweep fp64", "CG operator segment sweep fp32",
             "CG operator dense small-G products fp64", "CG operator dense small-G products fp32"]
 ALG_BYTES = {
-    "segment": "N (4 + 2 C s): rows read and written once, one id",
+    "segment": ("N (4 + C s) per read-only sweep (one id and one row read per position; the FP64 mean passes "
+                "of the mixed form are read-only), N C s more when the rows are written back, 4 N for the "
+                "traversal permutation of a gathered sweep"),
     "cg": "N (4 (1 + S) + S C s): destination and S swept source ids, S gathered FE-table rows",
     "dense": "G_e (4 G_s + C s) per product: count-matrix rows and FE-table rows read once",
 }
 
 
-def roofline_of(results, workload):
+# Nominal dense FP64 rate of the part (1.25 TFLOP/s, an FMA counted as two):
+# an FP64 addition takes one FMA issue slot, so 625 G additions/s.
+FP64_ADDS_PEAK_NOMINAL = 625.0
+
+
+def roofline_of(results, workload, elements_per_sweep=None):
+    """Roofline entry of the dominant sweep family. For the FP64 sweep families
+    (one FP64 addition per element) elements_per_sweep = N x C also gives the
+    FP64-pipe rate, the bound that sits below HBM for them on this part."""
     secs = [sum(r.stats["prof_seconds"][i] for r in results) for i in range(8)]
     nlaunch = [sum(r.stats["prof_launches"][i] for r in results) for i in range(8)]
     nbytes = [sum(r.stats["prof_bytes"][i] for r in results) for i in range(8)]
@@ -429,7 +459,13 @@ def roofline_of(results, workload):
     peak, peak_kind = measured_hbm_peak()
     achieved = nbytes[top] / secs[top] / 1e9 if secs[top] > 0 else 0.0
     traffic = TRAFFIC_PER_LAUNCH.get((workload, FAMILIES[top]))
+    fp64 = None
+    if elements_per_sweep and top in (0, 2) and secs[top] > 0:
+        gadds = elements_per_sweep * nlaunch[top] / secs[top] / 1e9
+        fp64 = {"adds_per_launch": elements_per_sweep, "achieved_gadds_per_s": gadds,
+                "peak_gadds_per_s_nominal": FP64_ADDS_PEAK_NOMINAL, "frac": gadds / FP64_ADDS_PEAK_NOMINAL}
     return {"bound": "hbm", "kernel": FAMILIES[top], "achieved": achieved, "peak": peak, "peak_source": peak_kind,
+            "fp64_pipe": fp64,
             "unit": "GB/s", "frac": achieved / peak if peak else None, "traffic": traffic,
             "traffic_source": ("ncu dram__bytes_read.sum + dram__bytes_write.sum per launch, "
                                "profiles/cg_rows_worker_firm_20M.md") if traffic is not None else None,

@@ -493,7 +493,7 @@ int build_problem(Problem& P, long long n_in, int k, int l, int n_fe, const doub
                 FEGB_LAUNCH_CHECK("counts");
                 FEGB_TRY(dalloc(scr, &D.long_list, (size_t)D.G, "long groups"));
                 FEGB_TRY(find_long_groups(D.off, D.G, CHUNK_R, D.long_list, &D.n_long, s));
-                if (cg_sorted[d]) {
+                if (sorted_all && (cg_sorted[d] || d == P.primary)) {  // the dimensions the CG operator sweeps
                     FEGB_TRY(dalloc(scr, &D.long_list_cg, (size_t)D.G, "long groups (cg)"));
                     FEGB_TRY(find_long_groups(D.off, D.G, CG_CHUNK, D.long_list_cg, &D.n_long_cg, s));
                     FEGB_TRY(dalloc(scr, &D.multi_list_cg, (size_t)D.G, "multi-chunk groups (cg)"));
@@ -1064,29 +1064,51 @@ int cg_streams(Problem& P, CGBuffers<T>& B) {
 }
 
 // Schur form: Jacobi preconditioner from the diagonal of
-// S = D_R'(I - P_P)D_R, S_gg = n_g - sum_w n_{w,g}^2 / n_w (only groups of the
-// primary spread over several groups of the dimension contribute), instead of
-// the group counts n_g. Needs each (group, primary group) pair as one
-// position of the dimension's stream (compressed streams over the primary and
-// at most one other many-group dimension); otherwise the counts stay.
+// S = D_R'(I - P_P)D_R, S_gg = n_g - sum_w n_{w,g}^2 / n_w over the (group,
+// primary group) pairs, instead of the group counts n_g (which overstate S_gg
+// by up to n_g / S_gg: the inner solve's max |z| stop would then end it early).
+// The pairs come from the dimension's compressed stream when its positions are
+// exactly those pairs (one other swept dimension), from a sort of the rows by
+// pair otherwise, and from the count matrices for the small dimensions.
 template <typename T>
 int cg_schur_precond(Problem& P, CGBuffers<T>& B) {
     const int pd = B.prim;
     std::vector<int> swept;
     for (int d = 0; d < P.n_fe; ++d)
         if (d != pd && P.dims[d].G > 0 && !B.dense[d]) swept.push_back(d);
-    if (swept.size() > 1 || (swept.size() == 1 && !B.compressed)) return 0;
     Scratch tmp(P.s);
     unsigned long long* acc = nullptr;
     FEGB_TRY(tmp.alloc(&acc, (size_t)std::max(1LL, B.Gv), "schur diagonal"));
     FEGB_CUDA(cudaMemsetAsync(acc, 0, sizeof(unsigned long long) * std::max(1LL, B.Gv), P.s), "schur diagonal zero");
+    const bool stream_pairs = swept.size() == 1 && B.compressed;
+    std::vector<int> by_counts;  // dimensions whose pair key does not fit 62 bits keep 1 / n_g
     for (int e : swept) {
         const auto& st = B.stream[e];
         const int32_t* pid = nullptr;
         for (int i = 0; i < st.n_src; ++i)
             if (st.src_dim[i] == pd) pid = st.src_gid[i];
-        if (!pid) return 0;
-        FEGB_TRY(launch_schur_diag_stream(st.gseq, st.m, st.weight, pid, P.dims[pd].counts, acc + B.off[e], P.s));
+        if (stream_pairs && pid) {
+            FEGB_TRY(launch_schur_diag_stream(st.gseq, st.m, st.weight, pid, P.dims[pd].counts, acc + B.off[e], P.s));
+            continue;
+        }
+        // the rows sorted by (group of e, primary group): one segment per pair
+        const int32_t* ptrs[2] = {P.dims[pd].gid, P.dims[e].gid};
+        const unsigned long long Gp = (unsigned long long)std::max(1, P.dims[pd].G);
+        const unsigned long long strides[2] = {1ULL, Gp};
+        if (Gp > (1ULL << 62) / (unsigned long long)P.dims[e].G) {
+            by_counts.push_back(e);
+            continue;
+        }
+        Scratch sub(P.s);
+        int32_t *perm = nullptr, *off = nullptr;
+        int npairs = 0;
+        FEGB_TRY(sub.alloc(&perm, (size_t)P.n, "pair perm"));
+        FEGB_TRY(sub.alloc(&off, (size_t)P.n + 1, "pair offsets"));
+        FEGB_TRY(cluster_ids_by_key(ptrs, strides, 2, P.n, bits_for(Gp * (unsigned long long)P.dims[e].G), nullptr,
+                                    &npairs, perm, off, P.s, sub, true, nullptr));
+        FEGB_TRY(launch_schur_diag_pairs(perm, off, npairs, P.dims[e].gid, P.dims[pd].gid, P.dims[pd].counts,
+                                         acc + B.off[e], P.s));
+        FEGB_CUDA(cudaStreamSynchronize(P.s), "schur pairs sync");  // sub is released here
     }
     for (int sd = 0; sd < P.n_fe; ++sd) {
         if (!B.dense[sd] || sd == pd || P.dims[sd].G <= 0) continue;
@@ -1099,6 +1121,8 @@ int cg_schur_precond(Problem& P, CGBuffers<T>& B) {
                                                        acc + B.off[sd], P.s));
     }
     FEGB_TRY(launch_inv_diag<T>(acc, B.counts_v, B.Gv, B.inv, P.s));
+    for (int e : by_counts)
+        FEGB_TRY(launch_inv_counts_t<T>(B.counts_v + B.off[e], P.dims[e].G, B.inv + B.off[e], P.s));
     FEGB_CUDA(cudaStreamSynchronize(P.s), "schur diagonal sync");
     return 0;
 }

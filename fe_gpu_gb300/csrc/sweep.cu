@@ -1801,6 +1801,32 @@ __global__ void schur_diag_stream_kernel(const int32_t* __restrict__ gseq, long 
     if (a) atomicAdd(acc + g, a);
 }
 
+// Pair form: the rows sorted by (group of the dimension, primary group) give
+// the pairs as segments off[p] .. off[p+1] of perm; acc[group] += term(segment
+// length, n_P[primary group]), SCHUR_RUN consecutive pairs per thread.
+__global__ void schur_diag_pairs_kernel(const int32_t* __restrict__ perm, const int32_t* __restrict__ off,
+                                        long long npairs, const int32_t* __restrict__ gid_e,
+                                        const int32_t* __restrict__ gid_p, const int32_t* __restrict__ nP,
+                                        unsigned long long* __restrict__ acc) {
+    const long long p0 = ((long long)blockIdx.x * blockDim.x + threadIdx.x) * SCHUR_RUN;
+    if (p0 >= npairs) return;
+    const long long p1 = min(npairs, p0 + SCHUR_RUN);
+    int g = gid_e[perm[off[p0]]];
+    unsigned long long a = 0;
+    for (long long p = p0; p < p1; ++p) {
+        const int s = off[p];
+        const int row = perm[s];
+        const int gp = gid_e[row];
+        if (gp != g) {
+            if (a) atomicAdd(acc + g, a);
+            g = gp;
+            a = 0;
+        }
+        a += schur_term_fixed((float)(off[p + 1] - s), nP[gid_p[row]]);
+    }
+    if (a) atomicAdd(acc + g, a);
+}
+
 // acc[t] += term(N[g][t], n[g]) over the Ge x Gs count matrix: thread i of the
 // first S = (threads / Gs) * Gs takes elements i, i + S, ... (one column each),
 // folded per block in shared memory, one global atomic per column per block.
@@ -1844,6 +1870,16 @@ int launch_schur_diag_stream(const int32_t* gseq, long long m, const float* w, c
     const long long threads = (m + SCHUR_RUN - 1) / SCHUR_RUN;
     schur_diag_stream_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(gseq, m, w, pid, nP, acc);
     FEGB_LAUNCH_CHECK("schur diagonal (stream)");
+    return 0;
+}
+
+int launch_schur_diag_pairs(const int32_t* perm, const int32_t* off, long long npairs, const int32_t* gid_e,
+                            const int32_t* gid_p, const int32_t* nP, unsigned long long* acc, cudaStream_t s) {
+    if (npairs <= 0) return 0;
+    const long long threads = (npairs + SCHUR_RUN - 1) / SCHUR_RUN;
+    schur_diag_pairs_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(perm, off, npairs, gid_e, gid_p, nP,
+                                                                             acc);
+    FEGB_LAUNCH_CHECK("schur diagonal (pairs)");
     return 0;
 }
 

@@ -283,6 +283,11 @@ int launch_alpha_primary(const double* mu, const T* table, long long G, int C, i
 // group order (gseq), weight w (null = 1), primary group pid, primary counts nP.
 int launch_schur_diag_stream(const int32_t* gseq, long long m, const float* w, const int32_t* pid, const int32_t* nP,
                              unsigned long long* acc, cudaStream_t s);
+// Pair form: perm and off (npairs + 1) are the rows sorted by (group of the
+// dimension, primary group) and the segments of equal pairs; gid_e and gid_p
+// the two dimensions' group ids by row.
+int launch_schur_diag_pairs(const int32_t* perm, const int32_t* off, long long npairs, const int32_t* gid_e,
+                            const int32_t* gid_p, const int32_t* nP, unsigned long long* acc, cudaStream_t s);
 // Dense form: N is the Ge x Gs count matrix (primary groups x the dimension's
 // Gs <= DENSE_SMALL_MAX_G groups), n the primary counts; adds into acc[0..Gs).
 template <typename CT>

@@ -467,8 +467,8 @@ def roofline_of(results, workload, elements_per_sweep=None):
     return {"bound": "hbm", "kernel": FAMILIES[top], "achieved": achieved, "peak": peak, "peak_source": peak_kind,
             "fp64_pipe": fp64,
             "unit": "GB/s", "frac": achieved / peak if peak else None, "traffic": traffic,
-            "traffic_source": ("ncu dram__bytes_read.sum + dram__bytes_write.sum per launch, "
-                               "profiles/cg_rows_worker_firm_20M.md") if traffic is not None else None,
+            "traffic_source": ("ncu dram__bytes_read.sum + dram__bytes_write.sum per launch, " +
+                               TRAFFIC_SOURCE[FAMILIES[top]]) if traffic is not None else None,
             "alg_bytes_definition": ALG_BYTES["segment" if top < 4 else ("cg" if top < 6 else "dense")],
             "launches": nlaunch[top], "avg_launch_ms": secs[top] / max(1, nlaunch[top]) * 1e3,
             "alg_bytes_per_launch": nbytes[top] / max(1, nlaunch[top]),
@@ -810,13 +810,19 @@ def formula_cpu_baseline(threads):
 
 
 # DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of the
-# dominant kernel family, from the ncu capture summarised in
-# profiles/cg_rows_worker_firm_20M.md (mean of the worker and firm operator
-# sweeps of one fit). Other workloads were not captured: the gathered tables
-# change size with the FE group counts, so the traffic does not scale with the
-# rows.
+# dominant kernel family, from the ncu captures summarised in profiles/:
+# - CG operator sweep: cg_rows_worker_firm_20M.md (mean of the worker and firm
+#   operator sweeps of one fit);
+# - FP64 segment sweep: fp64_sweeps_worker_firm_5M.md (mean of the worker and
+#   firm sweeps at 5M rows, times 4: the traffic is row data).
+# Other workloads were not captured.
 TRAFFIC_PER_LAUNCH: dict = {
     ("worker_firm_20M", "CG operator segment sweep fp32"): 1.027e+08,
+    ("worker_firm_20M", "segment sweep fp64"): 1.722e+09,
+}
+TRAFFIC_SOURCE = {
+    "CG operator segment sweep fp32": "profiles/cg_rows_worker_firm_20M.md",
+    "segment sweep fp64": "profiles/fp64_sweeps_worker_firm_5M.md (5M-row capture scaled by rows)",
 }
 
 

@@ -929,6 +929,26 @@ struct CGBuffers {
     double* mu_v = nullptr;       // FP64 group means in the CG layout (Schur form)
 };
 
+// flags[i] = 1 where the pair (ga, gb) changes along an ordered list of rows
+__global__ void pair_flags_kernel(const int32_t* __restrict__ ga, const int32_t* __restrict__ gb, long long n,
+                                  uint32_t* __restrict__ flags) {
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long st = (long long)gridDim.x * blockDim.x;
+    for (; i < n; i += st) flags[i] = (i == 0 || ga[i] != ga[i - 1] || gb[i] != gb[i - 1]) ? 1u : 0u;
+}
+
+// rank[i] = the run of position i; off[run] = its first position
+__global__ void run_ranks_kernel(const uint32_t* __restrict__ flags, const uint32_t* __restrict__ excl, long long n,
+                                 int32_t* __restrict__ off, int32_t* __restrict__ rank) {
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long st = (long long)gridDim.x * blockDim.x;
+    for (; i < n; i += st) {
+        const int32_t r = (int32_t)(excl[i] + flags[i]) - 1;
+        rank[i] = r;
+        if (flags[i]) off[r] = (int32_t)i;
+    }
+}
+
 // Position streams of the CG operator sweeps (see CGBuffers::Stream). The
 // rows are compressed into distinct id tuples of the many-group dimensions
 // when that removes at least a quarter of the positions: the operator carries
@@ -973,15 +993,41 @@ int cg_streams(Problem& P, CGBuffers<T>& B) {
     }
     int m = 0;
     int32_t *perm = nullptr, *toff = nullptr, *tseq = nullptr;
+    // the swept dimension whose group order the tuples come in: the primary (the
+    // most significant key part) after a key sort; with one other swept
+    // dimension e, e itself: its own row sort is stable over the storage order,
+    // which is the primary's, so it already lists the rows in (group of e,
+    // primary group) order and the tuples are its runs of equal pairs
+    int in_order = P.primary;
+    const int32_t n32 = (int32_t)n;
     {
         Scratch tmp(s);  // the sort's work arrays, released once the tuples are built
         // the row permutation, offsets and tuple ranks outlive the operator: the
         // cluster subset over the same dimensions reuses them
-        FEGB_TRY(dalloc(scr, &perm, (size_t)n, "tuple perm"));
         FEGB_TRY(dalloc(scr, &toff, (size_t)n + 1, "tuple offsets"));
         FEGB_TRY(dalloc(scr, &tseq, (size_t)n, "tuple ranks"));
-        FEGB_TRY(cluster_ids_by_key(ptrs.data(), strides.data(), (int)sw.size(), n, bits_for(stride), nullptr, &m,
-                                    perm, toff, s, tmp, true, tseq));
+        const Dim* E = (sw.size() == 2 && sw[1] == P.primary) ? &P.dims[sw[0]] : nullptr;
+        if (E && E->perm && E->gseq && E->gid_at_perm.size() > (size_t)P.primary && E->gid_at_perm[P.primary]) {
+            in_order = sw[0];
+            perm = E->perm;
+            uint32_t *flags = nullptr, *excl = nullptr, *total = nullptr;
+            FEGB_TRY(tmp.alloc(&flags, (size_t)n, "pair run flags"));
+            FEGB_TRY(tmp.alloc(&excl, (size_t)n, "pair run scan"));
+            FEGB_TRY(tmp.alloc(&total, 1, "pair run count"));
+            pair_flags_kernel<<<grid_stride_blocks(n, 256), 256, 0, s>>>(E->gseq, E->gid_at_perm[P.primary], n, flags);
+            FEGB_LAUNCH_CHECK("pair run flags");
+            FEGB_TRY(scan_exclusive_u32(flags, excl, n, total, s, tmp));
+            run_ranks_kernel<<<grid_stride_blocks(n, 256), 256, 0, s>>>(flags, excl, n, toff, tseq);
+            FEGB_LAUNCH_CHECK("pair run ranks");
+            uint32_t hm = 0;
+            FEGB_TRY(d2h_sync(&hm, total, sizeof(hm), s, "pair run count copy"));
+            m = (int)hm;
+            FEGB_TRY(h2d_sync(toff + m, &n32, sizeof(int32_t), s, "pair run end"));
+        } else {
+            FEGB_TRY(dalloc(scr, &perm, (size_t)n, "tuple perm"));
+            FEGB_TRY(cluster_ids_by_key(ptrs.data(), strides.data(), (int)sw.size(), n, bits_for(stride), nullptr,
+                                        &m, perm, toff, s, tmp, true, tseq));
+        }
         if (m > 0) {
             P.tuple_dims.assign(sw.begin(), sw.end());
             std::sort(P.tuple_dims.begin(), P.tuple_dims.end());
@@ -1017,8 +1063,8 @@ int cg_streams(Problem& P, CGBuffers<T>& B) {
             st = typename CGBuffers<T>::Stream();
             st.m = m;
             int32_t* order = nullptr;  // tuple index at each position (null: identity)
-            if (d == P.primary) {
-                st.gseq = tg[jd];  // the primary is the most significant key part: already in order
+            if (d == in_order) {
+                st.gseq = tg[jd];  // the tuples are already in this dimension's group order
                 st.weight = w;
             } else {
                 uint32_t* sorted = nullptr;

@@ -3029,6 +3029,74 @@ int fegb_estimate_device(const fegb_config* cfg, long long n, int k, int l, int 
                                 sh.get());
 }
 
+// Host-to-device upload over several copy streams: one cudaMemcpyAsync per
+// piece (pieces of at least 32 MB, round-robin over the streams), so several
+// copy engines run at once; the fit's stream waits on each copy stream's event.
+// The streams and events are created once per host thread.
+class Uploader {
+  public:
+    static constexpr int NS = 4;
+    explicit Uploader(cudaStream_t s) : s_(s) {
+        thread_local struct Pool {
+            cudaStream_t st[NS] = {};
+            cudaEvent_t ev[NS] = {};
+            bool ok = false;
+            Pool() {
+                ok = true;
+                for (int i = 0; i < NS; ++i) {
+                    ok = ok && cudaStreamCreateWithFlags(&st[i], cudaStreamNonBlocking) == cudaSuccess;
+                    ok = ok && cudaEventCreateWithFlags(&ev[i], cudaEventDisableTiming) == cudaSuccess;
+                }
+            }
+        } pool;
+        pool_ok_ = pool.ok;
+        for (int i = 0; i < NS; ++i) {
+            st_[i] = pool.st[i];
+            ev_[i] = pool.ev[i];
+        }
+    }
+    // copy streams start after the work already queued on s
+    int begin() {
+        if (!pool_ok_) return 0;
+        FEGB_CUDA(cudaEventRecord(ev_[0], s_), "upload start");
+        for (int i = 0; i < NS; ++i) FEGB_CUDA(cudaStreamWaitEvent(st_[i], ev_[0], 0), "upload start wait");
+        return 0;
+    }
+    int copy(void* dst, const void* src, size_t bytes, const char* what) {
+        if (!pool_ok_) {
+            FEGB_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, s_), what);
+            return 0;
+        }
+        constexpr size_t PIECE = 32u << 20;
+        const size_t pieces = std::max<size_t>(1, std::min<size_t>(NS, bytes / PIECE));
+        const size_t per = (bytes + pieces - 1) / pieces;
+        for (size_t o = 0; o < bytes; o += per) {
+            const size_t b = std::min(per, bytes - o);
+            FEGB_CUDA(cudaMemcpyAsync(static_cast<char*>(dst) + o, static_cast<const char*>(src) + o, b,
+                                      cudaMemcpyHostToDevice, st_[next_]),
+                      what);
+            next_ = (next_ + 1) % NS;
+        }
+        return 0;
+    }
+    // s waits for every piece
+    int join() {
+        if (!pool_ok_) return 0;
+        for (int i = 0; i < NS; ++i) {
+            FEGB_CUDA(cudaEventRecord(ev_[i], st_[i]), "upload done");
+            FEGB_CUDA(cudaStreamWaitEvent(s_, ev_[i], 0), "upload join");
+        }
+        return 0;
+    }
+
+  private:
+    cudaStream_t s_;
+    cudaStream_t st_[NS];
+    cudaEvent_t ev_[NS];
+    bool pool_ok_ = false;
+    int next_ = 0;
+};
+
 int fegb_estimate_host(const fegb_config* cfg, long long n, int k, int l, int n_fe, const double* y,
                        const double* W, const double* Z, const int* fe_ids, const int* group_sizes, double* beta,
                        double* se, fegb_result* result) {
@@ -3047,11 +3115,14 @@ int fegb_estimate_host(const fegb_config* cfg, long long n, int k, int l, int n_
     FEGB_TRY(scr.alloc(&dint, nn * std::max(1, n_fe), "ids upload"));
     FEGB_TRY(scr.alloc(&dids, nn * std::max(1, n_fe), "ids"));
     if (n > 0) {
-        FEGB_CUDA(cudaMemcpyAsync(dy, y, sizeof(double) * n, cudaMemcpyHostToDevice, s), "y H2D");
-        if (k > 0) FEGB_CUDA(cudaMemcpyAsync(dW, W, sizeof(double) * n * k, cudaMemcpyHostToDevice, s), "W H2D");
-        if (l > 0) FEGB_CUDA(cudaMemcpyAsync(dZ, Z, sizeof(double) * n * l, cudaMemcpyHostToDevice, s), "Z H2D");
+        Uploader up(s);
+        FEGB_TRY(up.begin());
+        if (n_fe > 0) FEGB_TRY(up.copy(dint, fe_ids, sizeof(int32_t) * n * n_fe, "ids H2D"));
+        FEGB_TRY(up.copy(dy, y, sizeof(double) * n, "y H2D"));
+        if (k > 0) FEGB_TRY(up.copy(dW, W, sizeof(double) * n * k, "W H2D"));
+        if (l > 0) FEGB_TRY(up.copy(dZ, Z, sizeof(double) * n * l, "Z H2D"));
+        FEGB_TRY(up.join());
         if (n_fe > 0) {
-            FEGB_CUDA(cudaMemcpyAsync(dint, fe_ids, sizeof(int32_t) * n * n_fe, cudaMemcpyHostToDevice, s), "ids H2D");
             deinterleave_ids_kernel<<<grid_stride_blocks(n * n_fe, 256), 256, 0, s>>>(dint, n_fe, n, dids);
             FEGB_LAUNCH_CHECK("ids deinterleave");
         }

@@ -118,6 +118,9 @@ struct Problem {
     std::vector<int> tuple_sw;                 // swept dimensions of the tuples
     std::vector<const int32_t*> tuple_ids;     // m ids per swept dimension
     double* inc_tab = nullptr;                 // m x C
+    // recorded after the host upload of y, W and Z (null: already resident);
+    // the data block waits for it, the id preparation does not
+    cudaEvent_t data_ready = nullptr;
     // largest row count of a (group of d, group of e) pair, from the CG's count
     // matrices (-1: not counted); at most 1 means the pairs are unique
     std::vector<std::vector<int>> pair_max;
@@ -437,14 +440,9 @@ int build_problem(Problem& P, long long n_in, int k, int l, int n_fe, const doub
         row_of = const_cast<int32_t*>(rows);
     }
     P.row_of = row_of;
-    // AoS data block
+    // the AoS data block is built last: everything before it reads only the ids,
+    // so it overlaps an upload of y, W and Z still in flight (P.data_ready)
     FEGB_TRY(dalloc(scr, &P.X, (size_t)n * C, "data block"));
-    if (n > 0) {
-        int TR = std::max(1, std::min(64, 24576 / (8 * C)));
-        size_t smem = sizeof(double) * (size_t)TR * C;
-        build_x_kernel<<<(unsigned)((n + TR - 1) / TR), 256, smem, s>>>(y, W, Z, k, l, n_in, row_of, n, C, TR, P.X);
-        FEGB_LAUNCH_CHECK("build data block");
-    }
     if (mixed) FEGB_TRY(dalloc(scr, &P.Xc, (size_t)n * C, "correction block"));
     // per-dimension structures; group-indexed tables are slices of concatenated arrays
     P.goff.assign(n_fe + 1, 0);
@@ -558,6 +556,13 @@ int build_problem(Problem& P, long long n_in, int k, int l, int n_fe, const doub
     for (int a = 0; a < n_fe - 1; ++a)
         for (int b = a + 1; b < n_fe; ++b)
             if (G[P.order[b]] < G[P.order[a]]) std::swap(P.order[a], P.order[b]);
+    if (P.data_ready) FEGB_CUDA(cudaStreamWaitEvent(s, P.data_ready, 0), "data upload wait");
+    if (n > 0) {
+        int TR = std::max(1, std::min(64, 24576 / (8 * C)));
+        size_t smem = sizeof(double) * (size_t)TR * C;
+        build_x_kernel<<<(unsigned)((n + TR - 1) / TR), 256, smem, s>>>(y, W, Z, k, l, n_in, row_of, n, C, TR, P.X);
+        FEGB_LAUNCH_CHECK("build data block");
+    }
     return 0;
 }
 
@@ -2520,7 +2525,8 @@ class StreamHolder {
 int estimate_device_impl(const fegb_config* cfg_in, long long n, int k, int l, int n_fe, const double* y,
                          const double* W, const double* Z, const int32_t* const* ids, const int* group_sizes,
                          double* beta, double* se, fegb_result* result, double t_h2d, cudaStream_t s,
-                         const PreDemeaned* pre = nullptr, const double* y_raw = nullptr) {
+                         const PreDemeaned* pre = nullptr, const double* y_raw = nullptr,
+                         cudaEvent_t data_ready = nullptr) {
     auto t_start = Clock::now();
     fegb_config cfg;
     if (cfg_in)
@@ -2541,6 +2547,7 @@ int estimate_device_impl(const fegb_config* cfg_in, long long n, int k, int l, i
     P.s = s;
     P.scr = &scr;
     P.profile = cfg.profile != 0;
+    P.data_ready = data_ready;
     FitTimes tm;
     auto t0 = Clock::now();
     long long n_single = 0;
@@ -3079,13 +3086,26 @@ class Uploader {
         }
         return 0;
     }
-    // s waits for every piece
+    // s waits for every piece issued so far
     int join() {
         if (!pool_ok_) return 0;
         for (int i = 0; i < NS; ++i) {
             FEGB_CUDA(cudaEventRecord(ev_[i], st_[i]), "upload done");
             FEGB_CUDA(cudaStreamWaitEvent(s_, ev_[i], 0), "upload join");
         }
+        return 0;
+    }
+    // one event recorded once every piece issued so far is done (s does not wait):
+    // stream 0 waits for the others, then records it
+    int done_event(cudaEvent_t* out) {
+        *out = nullptr;
+        if (!pool_ok_) return 0;
+        for (int i = 1; i < NS; ++i) {
+            FEGB_CUDA(cudaEventRecord(ev_[i], st_[i]), "upload done");
+            FEGB_CUDA(cudaStreamWaitEvent(st_[0], ev_[i], 0), "upload gather");
+        }
+        FEGB_CUDA(cudaEventRecord(ev_[0], st_[0]), "upload done");
+        *out = ev_[0];
         return 0;
     }
 
@@ -3114,24 +3134,28 @@ int fegb_estimate_host(const fegb_config* cfg, long long n, int k, int l, int n_
     FEGB_TRY(scr.alloc(&dZ, nn * std::max(1, l), "Z upload"));
     FEGB_TRY(scr.alloc(&dint, nn * std::max(1, n_fe), "ids upload"));
     FEGB_TRY(scr.alloc(&dids, nn * std::max(1, n_fe), "ids"));
+    // the ids first: the preparation starts on them while y, W and Z are in flight
+    cudaEvent_t data_ready = nullptr;
+    Uploader up(s);
     if (n > 0) {
-        Uploader up(s);
         FEGB_TRY(up.begin());
         if (n_fe > 0) FEGB_TRY(up.copy(dint, fe_ids, sizeof(int32_t) * n * n_fe, "ids H2D"));
-        FEGB_TRY(up.copy(dy, y, sizeof(double) * n, "y H2D"));
-        if (k > 0) FEGB_TRY(up.copy(dW, W, sizeof(double) * n * k, "W H2D"));
-        if (l > 0) FEGB_TRY(up.copy(dZ, Z, sizeof(double) * n * l, "Z H2D"));
         FEGB_TRY(up.join());
         if (n_fe > 0) {
             deinterleave_ids_kernel<<<grid_stride_blocks(n * n_fe, 256), 256, 0, s>>>(dint, n_fe, n, dids);
             FEGB_LAUNCH_CHECK("ids deinterleave");
         }
+        FEGB_TRY(up.copy(dy, y, sizeof(double) * n, "y H2D"));
+        if (k > 0) FEGB_TRY(up.copy(dW, W, sizeof(double) * n * k, "W H2D"));
+        if (l > 0) FEGB_TRY(up.copy(dZ, Z, sizeof(double) * n * l, "Z H2D"));
+        FEGB_TRY(up.done_event(&data_ready));
+        if (!data_ready) FEGB_CUDA(cudaStreamSynchronize(s), "H2D sync");
     }
-    FEGB_CUDA(cudaStreamSynchronize(s), "H2D sync");
-    double t_h2d = seconds_since(t0);
+    double t_h2d = seconds_since(t0);  // issue time only: the copies overlap the preparation
     std::vector<const int32_t*> ids(n_fe);
     for (int d = 0; d < n_fe; ++d) ids[d] = dids + (size_t)d * n;
-    return estimate_device_impl(cfg, n, k, l, n_fe, dy, dW, dZ, ids.data(), group_sizes, beta, se, result, t_h2d, s);
+    return estimate_device_impl(cfg, n, k, l, n_fe, dy, dW, dZ, ids.data(), group_sizes, beta, se, result, t_h2d, s,
+                                nullptr, nullptr, data_ready);
 }
 
 int fegb_within_transform(const fegb_config* cfg_in, long long n, int k, int l, int n_fe, double* d_y, double* d_W,

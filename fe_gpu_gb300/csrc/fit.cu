@@ -212,6 +212,15 @@ __global__ void gather_gid_kernel(const int32_t* __restrict__ ids, const int32_t
     for (; i < n; i += st) out[i] = ids[rows ? rows[i] : i] - 1;
 }
 
+// *flag = 1 when keys is not non-decreasing (every writer stores the same value)
+__global__ void order_check_kernel(const uint32_t* __restrict__ keys, long long n, int* __restrict__ flag) {
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x + 1;
+    const long long st = (long long)gridDim.x * blockDim.x;
+    bool bad = false;
+    for (; i < n; i += st) bad = bad || keys[i] < keys[i - 1];
+    if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) *flag = 1;
+}
+
 __global__ void gather_keys_kernel(const int32_t* __restrict__ ids, const int32_t* __restrict__ rows, long long n,
                                    uint32_t* __restrict__ keys, int32_t* __restrict__ vals) {
     long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -434,8 +443,22 @@ int build_problem(Problem& P, long long n_in, int k, int l, int n_fe, const doub
         FEGB_TRY(dalloc(scr, &row_of, (size_t)n, "row_of"));
         gather_keys_kernel<<<grid_stride_blocks(n, 256), 256, 0, s>>>(ids[P.primary], rows, n, keys, vals);
         FEGB_LAUNCH_CHECK("primary keys");
-        FEGB_TRY(radix_sort_u32(keys, vals, sorted, row_of, n, bits_for((unsigned long long)G[P.primary]), s, scr));
-        P.dims[P.primary].gid = reinterpret_cast<int32_t*>(sorted);
+        // rows already in primary order (a panel stored id by id) keep their order: no sort
+        int* unsorted = nullptr;
+        FEGB_TRY(dalloc(scr, &unsorted, 1, "order flag"));
+        FEGB_CUDA(cudaMemsetAsync(unsorted, 0, sizeof(int), s), "order flag");
+        order_check_kernel<<<grid_stride_blocks(n, 256), 256, 0, s>>>(keys, n, unsorted);
+        FEGB_LAUNCH_CHECK("primary order check");
+        int h_unsorted = 1;
+        FEGB_TRY(d2h_sync(&h_unsorted, unsorted, sizeof(int), s, "order flag copy"));
+        if (!h_unsorted) {
+            row_of = rows ? vals : nullptr;
+            P.dims[P.primary].gid = reinterpret_cast<int32_t*>(keys);
+        } else {
+            FEGB_TRY(radix_sort_u32(keys, vals, sorted, row_of, n, bits_for((unsigned long long)G[P.primary]), s,
+                                    scr));
+            P.dims[P.primary].gid = reinterpret_cast<int32_t*>(sorted);
+        }
     } else if (rows) {
         row_of = const_cast<int32_t*>(rows);
     }

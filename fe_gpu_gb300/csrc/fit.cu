@@ -117,6 +117,9 @@ struct Problem {
     int32_t* row_tuple = nullptr;
     std::vector<int> tuple_sw;                 // swept dimensions of the tuples
     std::vector<const int32_t*> tuple_ids;     // m ids per swept dimension
+    // per FE dimension of the tuples: the tuples in its group order (order:
+    // tuple at each position, null = identity), their group ids and offsets
+    std::vector<const int32_t*> tuple_dim_order, tuple_dim_gseq, tuple_dim_off;
     double* inc_tab = nullptr;                 // m x C
     // recorded after the host upload of y, W and Z (null: already resident);
     // the data block waits for it, the id preparation does not
@@ -1147,6 +1150,9 @@ int cg_streams(Problem& P, CGBuffers<T>& B) {
         FEGB_LAUNCH_CHECK("tuple of each row");
         P.tuple_sw.assign(sw.begin(), sw.end());
         P.tuple_ids.assign(tg.begin(), tg.end());
+        P.tuple_dim_order.assign(P.n_fe, nullptr);
+        P.tuple_dim_gseq.assign(P.n_fe, nullptr);
+        P.tuple_dim_off.assign(P.n_fe, nullptr);
         FEGB_CUDA(cudaStreamSynchronize(s), "tuple build sync");  // host tables above are stack arrays
         // per swept dimension: the tuples in its group order
         for (size_t jd = 0; jd < sw.size(); ++jd) {
@@ -1163,7 +1169,7 @@ int cg_streams(Problem& P, CGBuffers<T>& B) {
                 uint32_t* sorted = nullptr;
                 float* wd = nullptr;
                 FEGB_TRY(dalloc(scr, &sorted, (size_t)m, "tuple gseq"));
-                FEGB_TRY(tmp.alloc(&order, (size_t)m, "tuple order"));
+                FEGB_TRY(dalloc(scr, &order, (size_t)m, "tuple order"));
                 FEGB_TRY(radix_sort_u32(reinterpret_cast<const uint32_t*>(tg[jd]), nullptr, sorted, order, m,
                                         bits_for((unsigned long long)G), s, tmp));
                 FEGB_TRY(dalloc(scr, &wd, (size_t)m, "tuple weights (sorted)"));
@@ -1195,6 +1201,10 @@ int cg_streams(Problem& P, CGBuffers<T>& B) {
             st.off = off;
             st.long_list = ll;
             st.multi_list = ml;
+            // the SEs sum the scores of this dimension's clusters from the tuples' sums
+            P.tuple_dim_order[d] = order;
+            P.tuple_dim_gseq[d] = st.gseq;
+            P.tuple_dim_off[d] = off;
         }
         FEGB_CUDA(cudaStreamSynchronize(s), "tuple streams sync");
     }
@@ -2018,19 +2028,19 @@ inline int ia_mask_bit(const std::vector<int>& cdims, int d) {
 }
 
 int cluster_score_sums(Problem& P, const double* S, int ns, const int32_t* perm, const int32_t* gseq,
-                       const int32_t* off, int n_cl, double* Sc, Scratch& scr) {
+                       const int32_t* off, int n_cl, double* Sc, Scratch& scr, long long npos = -1) {
     SegSweepParams<double> sp{};
     sp.X = const_cast<double*>(S);
     sp.rs = ns;
     sp.cs = 1;
     sp.C = ns;
-    sp.n = P.n;
+    sp.n = npos >= 0 ? npos : P.n;
     sp.perm = perm;
     sp.gseq = gseq;
     sp.pend.n = 0;
     sp.writeback = 0;
     sp.R = CHUNK_R;
-    long long nchunks = std::max(1LL, seg_nchunks(P.n, CHUNK_R));
+    long long nchunks = std::max(1LL, seg_nchunks(sp.n, CHUNK_R));
     double *sums = nullptr, *head = nullptr, *tail = nullptr;
     FEGB_TRY(scr.alloc(&sums, (size_t)std::max(1, n_cl) * ns, "score sums"));
     FEGB_TRY(scr.alloc(&head, (size_t)nchunks * ns, "score heads"));
@@ -2315,6 +2325,17 @@ int estimate_on_problem(Problem& P, const fegb_config& cfg, const int* G_all, lo
         // subsets whose clusters are single rows, and the meat S'S they all share
         std::vector<int> row_masks;
         double* meat_rows = nullptr;
+        // score sums per CG tuple (m x ns), formed once when a subset needs them
+        double* tuple_scores = nullptr;
+        auto tuple_sums = [&]() -> int {
+            if (tuple_scores) return 0;
+            FEGB_TRY(scr.alloc(&tuple_scores, (size_t)P.tuple_m * ns, "tuple scores"));
+            Scratch ts(s);
+            FEGB_TRY(cluster_score_sums(P, S, ns, P.tuple_perm, P.tuple_gseq, P.tuple_off, P.tuple_m, tuple_scores,
+                                        ts));
+            FEGB_CUDA(cudaStreamSynchronize(s), "tuple scores sync");
+            return 0;
+        };
         for (int mask = 1; mask < (1 << ncd) && cluster_ok; ++mask) {
             std::vector<int> sd;
             for (int j = 0; j < ncd; ++j)
@@ -2365,8 +2386,14 @@ int estimate_on_problem(Problem& P, const fegb_config& cfg, const int* G_all, lo
                 for (size_t j = 0; j < sds.size() && tuples; ++j)
                     tuples = sds[j] == P.tuple_dims[j] && P.dims[sds[j]].gid == P.tuple_gid[j];
             }
+            // a single dimension of the tuples: its clusters' sums from the tuples' sums
+            const bool tuple_single = m == 1 && !rows && !smallg_single && P.tuple_m > 0 && P.tuple_n == n &&
+                                      (size_t)sd[0] < P.tuple_dim_gseq.size() && P.tuple_dim_gseq[sd[0]] &&
+                                      P.tuple_dim_off[sd[0]];
             if (rows && m > 1) {
                 n_cl = (int)n;  // a refinement of single-row clusters: no sort needed
+            } else if (tuple_single) {
+                n_cl = P.dims[sd[0]].G;
             } else if (tuples) {
                 // the clusters are the CG operator's id tuples: its row sort serves
                 perm = P.tuple_perm;
@@ -2452,8 +2479,18 @@ int estimate_on_problem(Problem& P, const fegb_config& cfg, const int* G_all, lo
                           "meat copy");
             } else {
                 double* Sc = nullptr;
-                FEGB_TRY(sub.alloc(&Sc, (size_t)n_cl * ns, "cluster scores"));
-                if (smallg_single) {
+                if (tuples || tuple_single) FEGB_TRY(tuple_sums());
+                if (tuples)
+                    Sc = tuple_scores;  // the clusters are the tuples
+                else
+                    FEGB_TRY(sub.alloc(&Sc, (size_t)n_cl * ns, "cluster scores"));
+                if (tuples) {
+                } else if (tuple_single) {
+                    // n rows -> m tuple sums -> G cluster sums: the second pass reads m positions
+                    FEGB_TRY(cluster_score_sums(P, tuple_scores, ns, P.tuple_dim_order[sd[0]],
+                                                P.tuple_dim_gseq[sd[0]], P.tuple_dim_off[sd[0]], n_cl, Sc, sub,
+                                                P.tuple_m));
+                } else if (smallg_single) {
                     const Dim& D = P.dims[sd[0]];
                     SmallGParams<double> sp{};
                     sp.X = S;

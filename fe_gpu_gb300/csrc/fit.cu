@@ -121,6 +121,15 @@ struct Problem {
     // tuple at each position, null = identity), their group ids and offsets
     std::vector<const int32_t*> tuple_dim_order, tuple_dim_gseq, tuple_dim_off;
     double* inc_tab = nullptr;                 // m x C
+    // long-group lists of persistent offset arrays (the tuple streams), found
+    // once: offsets array, group count -> list, list length
+    struct LongCache {
+        const int32_t* off;
+        int G;
+        int32_t* list;
+        int n;
+    };
+    std::vector<LongCache> long_cache;
     // recorded after the host upload of y, W and Z (null: already resident);
     // the data block waits for it, the id preparation does not
     cudaEvent_t data_ready = nullptr;
@@ -843,9 +852,21 @@ __global__ void tuple_increments_kernel(TupleInc ti, long long m, int C, double*
     }
 }
 
+// Sums of the ns columns of S (row-major, stride ns) over the clusters of a
+// traversal (perm: storage row at each position, null = storage order; gseq:
+// cluster at each position; off: n_cl + 1 offsets) into Sc (n_cl x ns), over
+// npos positions (-1: all rows). timed_kind >= 0 records the sweep launch in
+// that profile family.
+int cluster_score_sums(Problem& P, const double* S, int ns, const int32_t* perm, const int32_t* gseq,
+                       const int32_t* off, int n_cl, double* Sc, Scratch& scr, long long npos = -1,
+                       int timed_kind = -1, bool persistent_off = false, const FinalizeParams* outputs = nullptr);
+
 // FP64 group means of the current FP64 residual for every dimension, after
 // subtracting the FE increments of the previous refinement round from the rows
-// (apply_alpha; one element pass, then read-only sweeps). Returns max |mean|.
+// (apply_alpha; one element pass, then read-only sweeps). With compressed CG
+// streams the swept dimensions' sums come from one row sweep into per-tuple
+// sums and short sweeps of those (n C + sum_d m C additions instead of
+// n C per dimension). Returns max |mean|.
 int fp64_mean_pass(Problem& P, bool apply_alpha, double* mu_max) {
     if (apply_alpha && P.n > 0) {
         PendingSet<double> ps{};
@@ -877,9 +898,36 @@ int fp64_mean_pass(Problem& P, bool apply_alpha, double* mu_max) {
         P.demean_bytes += (double)P.n * (4.0 * ps.n + 16.0 * P.C);
     }
     FEGB_CUDA(cudaMemsetAsync(P.max_bits + 1, 0, sizeof(unsigned long long), P.s), "reset mu max");
+    std::vector<char> via_tuples(P.n_fe, 0);
+    Scratch ts(P.s);
+    if (P.n > 0 && P.tuple_m > 0 && P.tuple_n == P.n && P.tuple_sw.size() > 1 &&
+        (double)P.tuple_m <= 0.75 * (double)P.n) {
+        bool all = true;
+        for (int d : P.tuple_sw) all = all && P.tuple_dim_gseq.size() > (size_t)d && P.tuple_dim_gseq[d];
+        if (all) {
+            double* tsum = nullptr;
+            FEGB_TRY(ts.alloc(&tsum, (size_t)P.tuple_m * P.C, "tuple sums"));
+            FEGB_TRY(cluster_score_sums(P, P.X, P.C, P.tuple_perm, P.tuple_gseq, P.tuple_off, P.tuple_m, tsum, ts,
+                                        -1, 0, true));
+            P.demean_bytes += (double)P.n * (8.0 + 8.0 * P.C);
+            for (int d : P.tuple_sw) {
+                Dim& D = P.dims[d];
+                FinalizeParams f{};
+                f.counts = D.counts;
+                f.inv_counts = P.inv_counts_all + P.goff[d];
+                f.mean_out = D.mu;
+                f.max_partials = P.max_partials;
+                f.change_bits = P.max_bits + 1;
+                FEGB_TRY(cluster_score_sums(P, tsum, P.C, P.tuple_dim_order[d], P.tuple_dim_gseq[d],
+                                            P.tuple_dim_off[d], D.G, nullptr, ts, P.tuple_m, -1, true, &f));
+                P.demean_bytes += (double)P.tuple_m * ((P.tuple_dim_order[d] ? 8.0 : 4.0) + 8.0 * P.C);
+                via_tuples[d] = 1;
+            }
+        }
+    }
     for (int d = 0; d < P.n_fe; ++d) {
         Dim& D = P.dims[d];
-        if (D.G <= 0 || P.n <= 0) continue;
+        if (D.G <= 0 || P.n <= 0 || via_tuples[d]) continue;
         FEGB_TRY(sweep_sums<double>(P, d, P.X, PendingSet<double>{}, false));
         FinalizeParams f = finalize_base(P, d);
         f.mean_out = D.mu;
@@ -2028,7 +2076,8 @@ inline int ia_mask_bit(const std::vector<int>& cdims, int d) {
 }
 
 int cluster_score_sums(Problem& P, const double* S, int ns, const int32_t* perm, const int32_t* gseq,
-                       const int32_t* off, int n_cl, double* Sc, Scratch& scr, long long npos = -1) {
+                       const int32_t* off, int n_cl, double* Sc, Scratch& scr, long long npos, int timed_kind,
+                       bool persistent_off, const FinalizeParams* outputs) {
     SegSweepParams<double> sp{};
     sp.X = const_cast<double*>(S);
     sp.rs = ns;
@@ -2050,9 +2099,22 @@ int cluster_score_sums(Problem& P, const double* S, int ns, const int32_t* perm,
     sp.tail = tail;
     int32_t* long_list = nullptr;
     int n_long = 0;
-    FEGB_TRY(scr.alloc(&long_list, (size_t)std::max(1, n_cl), "score long groups"));
-    FEGB_TRY(find_long_groups(off, n_cl, CHUNK_R, long_list, &n_long, P.s));
-    FinalizeParams f{};
+    bool cached = false;
+    if (persistent_off)
+        for (const auto& c : P.long_cache)
+            if (c.off == off && c.G == n_cl) {
+                long_list = c.list;
+                n_long = c.n;
+                cached = true;
+            }
+    if (!cached) {
+        Scratch& where = persistent_off ? *P.scr : scr;
+        FEGB_TRY(where.alloc(&long_list, (size_t)std::max(1, n_cl), "score long groups"));
+        FEGB_TRY(find_long_groups(off, n_cl, CHUNK_R, long_list, &n_long, P.s));
+        if (persistent_off) P.long_cache.push_back({off, n_cl, long_list, n_long});
+    }
+    // outputs: the finalize's other outputs (means, maxima), its sources set here
+    FinalizeParams f = outputs ? *outputs : FinalizeParams{};
     f.G = n_cl;
     f.C = ns;
     f.off = off;
@@ -2060,8 +2122,13 @@ int cluster_score_sums(Problem& P, const double* S, int ns, const int32_t* perm,
     f.head = head;
     f.tail = tail;
     f.R = CHUNK_R;
+    f.partials = nullptr;
     f.sum_out = Sc;
+    CGTimer tm(P);
+    if (timed_kind >= 0)
+        FEGB_TRY(tm.begin(timed_kind, (double)sp.n * (4.0 + (perm ? 4.0 : 0.0) + 8.0 * ns)));
     FEGB_TRY(launch_seg_sweep<double>(sp, P.s));
+    FEGB_TRY(tm.end());
     FEGB_TRY(launch_long_sums(off, head, tail, CHUNK_R, ns, long_list, n_long, sums, P.s));
     return launch_finalize(f, P.s);
 }
@@ -2332,7 +2399,7 @@ int estimate_on_problem(Problem& P, const fegb_config& cfg, const int* G_all, lo
             FEGB_TRY(scr.alloc(&tuple_scores, (size_t)P.tuple_m * ns, "tuple scores"));
             Scratch ts(s);
             FEGB_TRY(cluster_score_sums(P, S, ns, P.tuple_perm, P.tuple_gseq, P.tuple_off, P.tuple_m, tuple_scores,
-                                        ts));
+                                        ts, -1, -1, true));
             FEGB_CUDA(cudaStreamSynchronize(s), "tuple scores sync");
             return 0;
         };
@@ -2489,7 +2556,7 @@ int estimate_on_problem(Problem& P, const fegb_config& cfg, const int* G_all, lo
                     // n rows -> m tuple sums -> G cluster sums: the second pass reads m positions
                     FEGB_TRY(cluster_score_sums(P, tuple_scores, ns, P.tuple_dim_order[sd[0]],
                                                 P.tuple_dim_gseq[sd[0]], P.tuple_dim_off[sd[0]], n_cl, Sc, sub,
-                                                P.tuple_m));
+                                                P.tuple_m, -1, true));
                 } else if (smallg_single) {
                     const Dim& D = P.dims[sd[0]];
                     SmallGParams<double> sp{};

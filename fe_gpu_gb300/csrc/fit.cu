@@ -128,6 +128,8 @@ struct Problem {
         int G;
         int32_t* list;
         int n;
+        int32_t* multi = nullptr;  // groups crossing 1..SEG_LONG_SPAN chunk edges (null: not found yet)
+        int n_multi = 0;
     };
     std::vector<LongCache> long_cache;
     // recorded after the host upload of y, W and Z (null: already resident);
@@ -861,6 +863,8 @@ int cluster_score_sums(Problem& P, const double* S, int ns, const int32_t* perm,
                        const int32_t* off, int n_cl, double* Sc, Scratch& scr, long long npos = -1,
                        int timed_kind = -1, bool persistent_off = false, const FinalizeParams* outputs = nullptr);
 
+int tuple_row_sums(Problem& P, const double* X, int C, double* out, Scratch& scr, int timed_kind);
+
 // FP64 group means of the current FP64 residual for every dimension, after
 // subtracting the FE increments of the previous refinement round from the rows
 // (apply_alpha; one element pass, then read-only sweeps). With compressed CG
@@ -907,8 +911,7 @@ int fp64_mean_pass(Problem& P, bool apply_alpha, double* mu_max) {
         if (all) {
             double* tsum = nullptr;
             FEGB_TRY(ts.alloc(&tsum, (size_t)P.tuple_m * P.C, "tuple sums"));
-            FEGB_TRY(cluster_score_sums(P, P.X, P.C, P.tuple_perm, P.tuple_gseq, P.tuple_off, P.tuple_m, tsum, ts,
-                                        -1, 0, true));
+            FEGB_TRY(tuple_row_sums(P, P.X, P.C, tsum, ts, 0));
             P.demean_bytes += (double)P.n * (8.0 + 8.0 * P.C);
             for (int d : P.tuple_sw) {
                 Dim& D = P.dims[d];
@@ -2133,6 +2136,48 @@ int cluster_score_sums(Problem& P, const double* S, int ns, const int32_t* perm,
     return launch_finalize(f, P.s);
 }
 
+// Complete per-tuple sums of the rows (m x C) written in place: runs inside a
+// chunk come straight from the sweep, the chunk-crossing ones are completed by
+// the group-sum pass (no finalize copy). The tuples' offsets are persistent,
+// so their group lists are found once.
+int tuple_row_sums(Problem& P, const double* X, int C, double* out, Scratch& scr, int timed_kind) {
+    const int G = P.tuple_m;
+    const int32_t* off = P.tuple_off;
+    Problem::LongCache* c = nullptr;
+    for (auto& e : P.long_cache)
+        if (e.off == off && e.G == G) c = &e;
+    if (!c) {
+        Problem::LongCache e{off, G, nullptr, 0};
+        FEGB_TRY(P.scr->alloc(&e.list, (size_t)std::max(1, G), "tuple long groups"));
+        FEGB_TRY(find_long_groups(off, G, CHUNK_R, e.list, &e.n, P.s));
+        P.long_cache.push_back(e);
+        c = &P.long_cache.back();
+    }
+    if (!c->multi) {
+        FEGB_TRY(P.scr->alloc(&c->multi, (size_t)std::max(1, G), "tuple multi-chunk groups"));
+        FEGB_TRY(find_multi_groups(off, G, CHUNK_R, c->multi, &c->n_multi, P.s));
+    }
+    SegSweepParams<double> sp{};
+    sp.X = const_cast<double*>(X);
+    sp.rs = C;
+    sp.cs = 1;
+    sp.C = C;
+    sp.n = P.n;
+    sp.perm = P.tuple_perm;
+    sp.gseq = P.tuple_gseq;
+    sp.R = CHUNK_R;
+    const long long nchunks = std::max(1LL, seg_nchunks(P.n, CHUNK_R));
+    FEGB_TRY(scr.alloc(&sp.head, (size_t)nchunks * C, "tuple heads"));
+    FEGB_TRY(scr.alloc(&sp.tail, (size_t)nchunks * C, "tuple tails"));
+    sp.sums = out;
+    CGTimer tm(P);
+    if (timed_kind >= 0) FEGB_TRY(tm.begin(timed_kind, (double)P.n * (8.0 + 8.0 * C)));
+    FEGB_TRY(launch_seg_sweep<double>(sp, P.s));
+    FEGB_TRY(tm.end());
+    return launch_group_sums<double>(off, sp.head, sp.tail, CHUNK_R, C, c->list, c->n, c->multi, c->n_multi, out,
+                                     P.s);
+}
+
 struct FitTimes {
     double prep = 0, demean = 0, regression = 0, se = 0;
 };
@@ -2398,8 +2443,7 @@ int estimate_on_problem(Problem& P, const fegb_config& cfg, const int* G_all, lo
             if (tuple_scores) return 0;
             FEGB_TRY(scr.alloc(&tuple_scores, (size_t)P.tuple_m * ns, "tuple scores"));
             Scratch ts(s);
-            FEGB_TRY(cluster_score_sums(P, S, ns, P.tuple_perm, P.tuple_gseq, P.tuple_off, P.tuple_m, tuple_scores,
-                                        ts, -1, -1, true));
+            FEGB_TRY(tuple_row_sums(P, S, ns, tuple_scores, ts, -1));
             FEGB_CUDA(cudaStreamSynchronize(s), "tuple scores sync");
             return 0;
         };

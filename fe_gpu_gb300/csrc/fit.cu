@@ -3213,7 +3213,7 @@ int fegb_estimate_device(const fegb_config* cfg, long long n, int k, int l, int 
 // The streams and events are created once per host thread.
 class Uploader {
   public:
-    static constexpr int NS = 4;
+    static constexpr int NS = 8;
     explicit Uploader(cudaStream_t s) : s_(s) {
         thread_local struct Pool {
             cudaStream_t st[NS] = {};

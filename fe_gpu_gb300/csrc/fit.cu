@@ -2631,7 +2631,6 @@ int estimate_on_problem(Problem& P, const fegb_config& cfg, const int* G_all, lo
             }
             double w = (m % 2 == 1) ? 1.0 : -1.0;
             FEGB_TRY(dense_sandwich_acc(kk, Qinv, Mk, ldm, idx_dev, w, acc, work, s));
-            FEGB_CUDA(cudaStreamSynchronize(s), "subset sync");
         }
         if (cluster_ok) {
             double scalar;

@@ -813,12 +813,12 @@ def formula_cpu_baseline(threads):
 # dominant kernel family, from the ncu captures summarised in profiles/:
 # - CG operator sweep: cg_rows_worker_firm_20M.md (mean of the worker and firm
 #   operator sweeps of one fit);
-# - FP64 segment sweep: fp64_sweeps_worker_firm_5M.md (mean of the worker and
-#   firm sweeps at 5M rows, times 4: the traffic is row data).
+# - FP64 segment sweep: fp64_sweeps_worker_firm_5M.md (the tuple row sweep at
+#   5M rows, times 4: the traffic is row data).
 # Other workloads were not captured.
 TRAFFIC_PER_LAUNCH: dict = {
     ("worker_firm_20M", "CG operator segment sweep fp32"): 1.027e+08,
-    ("worker_firm_20M", "segment sweep fp64"): 1.722e+09,
+    ("worker_firm_20M", "segment sweep fp64"): 2.027e+09,
 }
 TRAFFIC_SOURCE = {
     "CG operator segment sweep fp32": "profiles/cg_rows_worker_firm_20M.md",

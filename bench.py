@@ -26,6 +26,8 @@ import time
 
 import numpy as np
 
+from fe_gpu_gb300 import replicas
+
 ROOT = os.path.dirname(os.path.abspath(__file__))
 if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
@@ -74,8 +76,7 @@ BATCH_WORKLOADS = {
 
 
 def dist_env():
-    return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(
-        os.environ.get("LOCAL_RANK", "0"))
+    return replicas.dist_env()
 
 
 def make_panel(name, scale=1):
@@ -249,10 +250,7 @@ def main():
 
     rank, world, local = dist_env()
     torch.cuda.set_device(local)
-    if world > 1:
-        import torch.distributed as dist
-
-        dist.init_process_group("nccl")
+    replicas.init(world)
     _native.check(_native.lib().fe_gpu_runtime_is_available(), "no CUDA device")
     stream = torch.cuda.Stream()
 
@@ -284,10 +282,7 @@ def main():
         return 0
 
     def barrier():
-        if world > 1:
-            import torch.distributed as dist
-
-            dist.barrier()
+        replicas.barrier(world)
 
     def timed(precision, steps, profile, method=None):
         res = None
@@ -306,12 +301,7 @@ def main():
         barrier()
         launches = _native.lib().fegb_kernel_launches() - launches0
         ms = ev0.elapsed_time(ev1) / steps
-        if world > 1:
-            import torch.distributed as dist
-
-            t = torch.tensor([ms], device=dev)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            ms = float(t.item())
+        ms = replicas.max_over_ranks(ms, world, dev)
         return ms, results, launches
 
     for _ in range(args.warmup):
@@ -348,12 +338,7 @@ def main():
         er = fe_gpu_estimate(cfg_for(args.precision), hdr, hp, stream=stream.cuda_stream)
     torch.cuda.synchronize()
     e2e_s = (time.perf_counter() - t0) / args.e2e_steps
-    if world > 1:
-        import torch.distributed as dist
-
-        t = torch.tensor([e2e_s], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_s = replicas.max_over_ranks(e2e_s, world, dev)
     h2d = pin_y.nbytes + n * k * 8 + n * n_fe * 4
     d2h = 2 * k * 8
 
@@ -424,10 +409,7 @@ def main():
                                 if k2 != "seconds"}
     if rank == 0:
         print(json.dumps(line), flush=True)
-    if world > 1:
-        import torch.distributed as dist
-
-        dist.destroy_process_group()
+    replicas.finish(world)
     return 0
 
 
@@ -490,10 +472,7 @@ def run_formula(args):
 
     rank, world, local = dist_env()
     torch.cuda.set_device(local)
-    if world > 1:
-        import torch.distributed as dist
-
-        dist.init_process_group("nccl")
+    replicas.init(world)
     w = FORMULA_WORKLOADS[args.workload]
     hdr, host, formula = iv_formula_panel(n=w["n"], g=w["g"], seed=w["seed"])
     n = host.y.shape[0]
@@ -513,10 +492,7 @@ def run_formula(args):
         return res
 
     def barrier():
-        if world > 1:
-            import torch.distributed as dist
-
-            dist.barrier()
+        replicas.barrier(world)
 
     def timed(precision, method, steps, profile):
         barrier()
@@ -529,12 +505,7 @@ def run_formula(args):
         torch.cuda.synchronize()
         barrier()
         ms = ev0.elapsed_time(ev1) / steps
-        if world > 1:
-            import torch.distributed as dist
-
-            t = torch.tensor([ms], device=torch.device("cuda", local))
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            ms = float(t.item())
+        ms = replicas.max_over_ranks(ms, world, torch.device("cuda", local))
         return ms, results, _native.lib().fegb_kernel_launches() - l0
 
     if args.profile_case:
@@ -581,7 +552,7 @@ def run_formula(args):
     for _ in range(args.e2e_steps):
         er = fe_gpu_estimate_formula(formula, hdr, hp, cfg_for(args.precision, args.method), stream.cuda_stream)
     torch.cuda.synchronize()
-    e2e_s = (time.perf_counter() - t0) / args.e2e_steps
+    e2e_s = replicas.max_over_ranks((time.perf_counter() - t0) / args.e2e_steps, world, torch.device("cuda", local))
     k = len(last.beta)
     line = {
         "metric": METRIC, "value": world * n / (ms / 1e3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -612,10 +583,7 @@ def run_formula(args):
         line["cpu_baseline"] = formula_cpu_baseline(os.cpu_count() or 1)
     if rank == 0:
         print(json.dumps(line), flush=True)
-    if world > 1:
-        import torch.distributed as dist
-
-        dist.destroy_process_group()
+    replicas.finish(world)
     return 0
 
 
@@ -633,10 +601,7 @@ def run_batch(args):
 
     rank, world, local = dist_env()
     torch.cuda.set_device(local)
-    if world > 1:
-        import torch.distributed as dist
-
-        dist.init_process_group("nccl")
+    replicas.init(world)
     w = BATCH_WORKLOADS[args.workload]
     specs = batch_specs(n_specs=w["n_specs"], total_rows=w["total_rows"], seed=w["seed"])
     stream = torch.cuda.Stream()
@@ -661,10 +626,7 @@ def run_batch(args):
                             demean_cg=(args.method == "cg"))
 
     def barrier():
-        if world > 1:
-            import torch.distributed as dist
-
-            dist.barrier()
+        replicas.barrier(world)
 
     def timed(fn, steps):
         barrier()
@@ -677,12 +639,7 @@ def run_batch(args):
         torch.cuda.synchronize()
         barrier()
         ms = ev0.elapsed_time(ev1) / steps
-        if world > 1:
-            import torch.distributed as dist
-
-            t = torch.tensor([ms], device=torch.device("cuda", local))
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            ms = float(t.item())
+        ms = replicas.max_over_ranks(ms, world, torch.device("cuda", local))
         return ms, out, _native.lib().fegb_kernel_launches() - l0
 
     def batch_fit(profile=False):
@@ -746,7 +703,7 @@ def run_batch(args):
     for _ in range(args.e2e_steps):
         e2e_step()
     torch.cuda.synchronize()
-    e2e_s = (time.perf_counter() - t0) / args.e2e_steps
+    e2e_s = replicas.max_over_ranks((time.perf_counter() - t0) / args.e2e_steps, world, torch.device("cuda", local))
     ktot = sum(h.W.shape[1] for h, _ in specs)
     diffs_b = [float(np.max(np.abs(a.beta - b.beta) / np.maximum(np.abs(b.beta), 1e-300))) for a, b in zip(last, seq)] \
         if seq else []
@@ -775,10 +732,7 @@ def run_batch(args):
     }
     if rank == 0:
         print(json.dumps(line), flush=True)
-    if world > 1:
-        import torch.distributed as dist
-
-        dist.destroy_process_group()
+    replicas.finish(world)
     return 0
 
 

@@ -12,7 +12,7 @@ ROOT = Path(__file__).resolve().parents[1]
 
 
 @pytest.mark.timeout(300)
-def test_reference_arm_json_line():
+def test_reference_arm_json_line(built):
     env = dict(os.environ, OMP_NUM_THREADS="2")
     out = subprocess.run([sys.executable, str(ROOT / "bench.py"), "--impl", "reference", "--workload", "nls_panel",
                           "--steps", "1", "--warmup", "0"], cwd=ROOT, env=env, capture_output=True, text=True,

@@ -3,15 +3,24 @@
 
 One step = one whole fit (FE preparation, within-transform to fe-tol 1e-8,
 normal equations, 3-way clustered SEs) of the workload below, with its inputs
-already resident in HBM. The default workload is the 20M-row worker-firm panel
-(1,000,000 workers x 20 periods, 100,000 firms with Pareto(1.5) sizes, 10%
-switching per period, 8 regressors, FEs worker/firm/time, 3-way clustering),
-fitted in the mixed-precision form; the plain FP64 form is timed beside it.
+already resident in HBM. The default workload is the 150M-row worker-firm
+panel (5,000,000 workers x 30 periods, 1,000,000 firms with Pareto(1.5) sizes,
+5% mobility per period, tenure + sick + 6 regressors, FEs worker/firm/time,
+3-way clustering), fitted in the mixed-precision form; the plain FP64 forms
+are timed beside it.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--workload NAME]
 
 Prints one JSON line (rank 0). Under torchrun each rank fits its own replica
 of the panel (weak scaling, no collective on the data path).
+
+The CPU legs (cpu_baseline, and --impl reference) fit a bounded sample of the
+workload: the same panel design with the workers and firms divided by the
+workload's sample divisor (1/200 of the 150M panel: 25,000 workers x 30
+periods over 5,000 firms, 750k rows). The GPU fits the same sample too, so the
+line carries a like-for-like rate and the per-coefficient errors of the GPU
+fit against the CPU oracle on identical inputs.
 """
 from __future__ import annotations
 
@@ -37,18 +46,19 @@ UNIT = "rows/s"
 
 WORKLOADS = {
     "worker_firm_20M": dict(n_workers=1_000_000, n_firms=100_000, n_periods=20, switch_prob=0.1, n_reg=8,
-                            seed=20261204, desc="1M workers x 20 periods, 100k Pareto(1.5) firms, 10% switching, "
-                                               "8 regressors, FEs worker/firm/time, 3-way clustered SEs"),
+                            seed=20261204, cpu_sample_div=20,
+                            desc="1M workers x 20 periods, 100k Pareto(1.5) firms, 10% switching, "
+                                 "8 regressors, FEs worker/firm/time, 3-way clustered SEs"),
     "worker_firm_150M": dict(n_workers=5_000_000, n_firms=1_000_000, n_periods=30, switch_prob=0.05, n_reg=8,
-                             tenure_sick=True, seed=20261206,
+                             tenure_sick=True, seed=20261206, cpu_sample_div=200,
                              desc="5M workers x 30 periods, 1M Pareto(1.5) firms, 5% mobility, tenure/sick + 6 "
                                   "regressors, FEs worker/firm/time, 3-way clustered SEs"),
     "worker_firm_2M": dict(n_workers=100_000, n_firms=10_000, n_periods=20, switch_prob=0.1, n_reg=8,
-                           seed=20261204, desc="small case of the 20M panel for profiling"),
+                           seed=20261204, cpu_sample_div=2, desc="small case of the 20M panel for profiling"),
     "worker_firm_5M": dict(n_workers=250_000, n_firms=25_000, n_periods=20, switch_prob=0.1, n_reg=8,
-                           seed=20261204, desc="quarter-size case of the 20M panel for ncu captures (360 MB of "
+                           seed=20261204, cpu_sample_div=5, desc="quarter-size case of the 20M panel for ncu captures (360 MB of "
                                                 "FP64 rows, above L2)"),
-    "nls_panel": dict(generator="nls", seed=20261203,
+    "nls_panel": dict(generator="nls", seed=20261203, cpu_sample_div=1,
                       desc="nlswork-shaped unbalanced panel: 4,700 ids with U{1..15} consecutive years of 15, "
                            "13 Zipf(1.1) occupations, 5 regressors, FEs id/occupation/year, 3-way clustered SEs"),
 }
@@ -87,12 +97,35 @@ def make_panel(name, scale=1):
 
     w = dict(WORKLOADS[name])
     w.pop("desc")
+    w.pop("cpu_sample_div", None)
     if w.pop("generator", None) == "nls":
         return nls_panel(seed=w["seed"])
     if scale > 1:
         w["n_workers"] = max(1000, w["n_workers"] // scale)
         w["n_firms"] = max(100, w["n_firms"] // scale)
     return worker_firm_panel(**w)
+
+
+def sample_of(name):
+    """(header, host arrays, description) of the bounded CPU sample of a
+    workload: the same design with the workers and firms divided by the
+    workload's sample divisor; the nls panel whole."""
+    w = WORKLOADS[name]
+    div = w.get("cpu_sample_div", 1)
+    hdr, host = make_panel(name, scale=div)
+    if w.get("generator") == "nls" or div == 1:
+        what = "the whole panel"
+    else:
+        what = (f"1/{div} of the panel: {max(1000, w['n_workers'] // div)} workers x {w['n_periods']} periods, "
+                f"{max(100, w['n_firms'] // div)} firms, same design and seed")
+    return hdr, host, what
+
+
+def workload_rows(name):
+    w = WORKLOADS[name]
+    if w.get("generator") == "nls":
+        return make_panel(name)[1].y.shape[0]
+    return w["n_workers"] * w["n_periods"]
 
 
 class ClockSampler:
@@ -160,60 +193,72 @@ def measured_hbm_peak():
     return 6800.0, "fallback"
 
 
-def cpu_baseline(name, threads):
-    """The oracle (C restatement of the reference CPU estimator) on a bounded
-    sample of the workload: the same panel design with 1/5 of the workers and
-    firms (4M rows of the 20M panel), fitted with the CPU path's conventions;
-    the nls panel whole."""
+def oracle_fit(host, threads):
+    """The oracle (C restatement of the reference CPU estimator) on one panel,
+    with the CPU path's conventions; returns (result, seconds)."""
     from oracle import oracle as O
 
-    w = WORKLOADS[name]
-    nls = w.get("generator") == "nls"
-    hdr, host = make_panel(name, scale=1 if nls else 5)
     os.environ["OMP_NUM_THREADS"] = str(threads)
     t0 = time.perf_counter()
     r = O.cpu_estimate(host.y, host.W, host.fe_ids, tol=1e-8, max_iter=100000, cluster_dims=[1, 2, 3])
-    dt = time.perf_counter() - t0
+    return r, time.perf_counter() - t0
+
+
+def cpu_baseline(name, threads, sample=None):
+    """The oracle on the workload's bounded sample (about 10-20 s of CPU work
+    on the host's cores). Returns the baseline entry and the oracle result."""
+    hdr, host, what = sample if sample is not None else sample_of(name)
+    r, dt = oracle_fit(host, threads)
     n = host.y.shape[0]
-    what = ("the whole panel" if nls else
-            f"{w['n_workers'] // 5} workers x {w['n_periods']} periods, {w['n_firms'] // 5} firms")
-    return {"value": n / dt, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"{n} rows ({what}), whole fit with the reference CPU conventions, "
-                      f"{r.stats['fe_iterations']} AP iterations, {dt:.2f} s", "seconds": dt}
-
-
-def workload_rows(name):
-    w = WORKLOADS[name]
-    if w.get("generator") == "nls":
-        return make_panel(name)[1].y.shape[0]
-    return w["n_workers"] * w["n_periods"]
+    entry = {"value": n / dt, "unit": UNIT, "cores": threads, "kind": "port",
+             "sample": f"{n} rows ({what}), whole fit with the reference CPU conventions, "
+                       f"{r.stats['fe_iterations']} AP iterations, {dt:.2f} s on {threads} host threads",
+             "rows": n, "seconds": dt}
+    return entry, r
 
 
 def run_reference(args):
+    """The reference's CPU path (the oracle port: the reference itself needs a
+    Fortran compiler and LAPACK) on the workload's bounded sample, with all
+    host threads. Each step fits the whole sample; ms_per_step is the measured
+    time of one such fit, and config.rows the rows it fitted."""
     rank, world, _ = dist_env()
     if rank != 0:
         return 0
     threads = os.cpu_count() or 1
     os.environ["OMP_NUM_THREADS"] = str(threads)
-    vals = []
-    cb = None
+    sample = sample_of(args.workload)
+    hdr, host, what = sample
+    n = host.y.shape[0]
+    secs = []
+    r = None
     for i in range(args.warmup + args.steps):
-        cb = cpu_baseline(args.workload, threads)
+        r, dt = oracle_fit(host, threads)
         if i >= args.warmup:
-            vals.append(cb["value"])
-    value = float(np.median(vals)) if vals else cb["value"]
+            secs.append(dt)
+    step_s = float(np.median(secs)) if secs else float("nan")
+    value = n / step_s
     w = WORKLOADS[args.workload]
-    rows = workload_rows(args.workload)
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": rows / value * 1e3, "higher_is_better": True,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_s * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
-        "config": {"workload": args.workload, "description": w["desc"], "rows": rows, "fe_tol": 1e-8},
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": cb["sample"]},
+        "config": {"workload": f"{args.workload} sample ({what})", "description": w["desc"], "rows": n,
+                   "full_workload_rows": workload_rows(args.workload), "fe_tol": 1e-8,
+                   "sampled": True, "step_seconds_all": secs},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"{n} rows ({what}), whole fit with the reference CPU conventions, "
+                                   f"{r.stats['fe_iterations'] if r else 0} AP iterations per fit, "
+                                   f"median {step_s:.2f} s per fit on {threads} host threads"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
     return 0
+
+
+def rel_errors(got, ref):
+    got, ref = np.asarray(got, dtype=np.float64), np.asarray(ref, dtype=np.float64)
+    return [float(v) for v in np.abs(got - ref) / np.maximum(np.abs(ref), 1e-300)]
 
 
 def main():
@@ -223,15 +268,17 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=sorted(WORKLOADS) + sorted(FORMULA_WORKLOADS) + sorted(BATCH_WORKLOADS),
-                    default="worker_firm_20M")
+                    default="worker_firm_150M")
     ap.add_argument("--precision", choices=["mixed", "fp64"], default="mixed")
     ap.add_argument("--method", choices=["cg", "ap"], default="cg",
                     help="within-transform of the headline form (the FP64 comparison always uses AP)")
-    ap.add_argument("--fp64-steps", type=int, default=2, help="timed steps of the plain FP64 form")
+    ap.add_argument("--fp64-steps", type=int, default=1,
+                    help="timed steps of each plain FP64 form (AP and CG; no warm-up of their own)")
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--no-file", action="store_true",
-                    help="skip the .bin file leg (write the panel once, load it to the device, fit)")
+    ap.add_argument("--file", choices=["auto", "on", "off"], default="auto",
+                    help=".bin file leg (write the panel once, load it to the device, fit); auto: panels up to "
+                         "50M rows")
     ap.add_argument("--profile-case", action="store_true",
                     help="one fit per (precision, method) and exit (for ncu captures)")
     ap.add_argument("--case", default="all", help="with --profile-case: mixed-cg, fp64-cg, mixed-ap, fp64-ap or all")
@@ -312,11 +359,14 @@ def main():
     clocks = sampler.stop()
     last = results[-1]
 
-    # plain FP64 form beside it
-    fp64_ms = None
-    fp64_res = None
+    # plain FP64 forms beside it (the reference's AP scheme, and CG), timed
+    # without warm-up fits of their own: one FP64 AP fit of the 150M panel
+    # takes about a minute
+    fp64_ms = fp64cg_ms = None
+    fp64_res = fp64cg_res = None
     if args.fp64_steps > 0:
-        fit("fp64", method="ap")
+        fp64cg_ms, fr, _ = timed("fp64", args.fp64_steps, False, method="cg")
+        fp64cg_res = fr[-1]
         fp64_ms, fr, _ = timed("fp64", args.fp64_steps, False, method="ap")
         fp64_res = fr[-1]
 
@@ -345,7 +395,8 @@ def main():
     # .bin file leg: the panel written once in the fe_gpu format, then loaded
     # straight to the device (fegb_load_bin) and fitted from there
     file_leg = None
-    if not args.no_file and rank == 0:
+    file_on = args.file == "on" or (args.file == "auto" and n <= 50_000_000)
+    if file_on and rank == 0:
         import tempfile
 
         from fe_gpu_gb300.bin_io import DeviceDataset, write_dataset
@@ -393,10 +444,16 @@ def main():
         "fp64_ap_fit_time_s": fp64_ms / 1e3 if fp64_ms else None,
         "fp64_fe_iterations": fp64_res.fe_iterations if fp64_res else None,
         "speedup_vs_plain_fp64_ap": (fp64_ms / ms) if fp64_ms else None,
-        "beta_max_rel_diff_mixed_vs_fp64": (float(np.max(np.abs(last.beta - fp64_res.beta) /
-                                                         np.abs(fp64_res.beta))) if fp64_res else None),
-        "se_max_rel_diff_mixed_vs_fp64": (float(np.max(np.abs(last.se - fp64_res.se) / np.abs(fp64_res.se)))
-                                          if fp64_res else None),
+        "fp64_cg_fit_time_s": fp64cg_ms / 1e3 if fp64cg_ms else None,
+        "fp64_cg_fe_iterations": fp64cg_res.fe_iterations if fp64cg_res else None,
+        "speedup_vs_plain_fp64_cg": (fp64cg_ms / ms) if fp64cg_ms else None,
+        "fp64_timed_steps": args.fp64_steps,
+        "beta_max_rel_diff_mixed_vs_fp64": (max(rel_errors(last.beta, fp64_res.beta)) if fp64_res else None),
+        "se_max_rel_diff_mixed_vs_fp64": (max(rel_errors(last.se, fp64_res.se)) if fp64_res else None),
+        "coefficients_vs_fp64_ap": ({"names": last.coef_names, "beta": [float(b) for b in last.beta],
+                                     "se": [float(v) for v in last.se],
+                                     "beta_rel_err": rel_errors(last.beta, fp64_res.beta),
+                                     "se_rel_err": rel_errors(last.se, fp64_res.se)} if fp64_res else None),
         "e2e": {"value": world * n / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "seconds_per_step": e2e_s},
         "gpu_launches": int(launches / args.steps) * args.steps,
@@ -405,12 +462,52 @@ def main():
         "clocks": clocks,
     }
     if rank == 0 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = {k2: v for k2, v in cpu_baseline(args.workload, os.cpu_count() or 1).items()
-                                if k2 != "seconds"}
+        # the CPU oracle and the GPU on the same bounded sample: a like-for-like
+        # rate, and the GPU fit's per-coefficient errors against the oracle
+        # (CPU conventions on both sides)
+        sample = sample_of(args.workload)
+        entry, oref = cpu_baseline(args.workload, os.cpu_count() or 1, sample)
+        line["cpu_baseline"] = {k2: v for k2, v in entry.items() if k2 not in ("seconds", "rows")}
+        line["parity_vs_oracle"] = parity_on_sample(sample, oref, entry, stream)
     if rank == 0:
         print(json.dumps(line), flush=True)
     replicas.finish(world)
     return 0
+
+
+def parity_on_sample(sample, oref, cpu_entry, stream):
+    """Fits the CPU baseline's sample on the GPU (headline mixed CG form and
+    plain FP64 AP, CPU SE conventions, from pinned-free host arrays through
+    fegb_estimate_host) and compares every coefficient and SE with the
+    oracle's, and the integer outputs exactly."""
+    import torch
+
+    from fe_gpu_gb300.estimator import fe_gpu_estimate, fe_runtime_config
+
+    hdr, host, what = sample
+    n = host.y.shape[0]
+    out = {"sample": what, "rows": n, "tolerance": {"beta_rel": 1e-6, "se_rel": 1e-5},
+           "oracle": "C restatement of the reference CPU estimator (fe_pipeline.f90:71-513)",
+           "oracle_fe_iterations": oref.stats["fe_iterations"]}
+    for label, precision, cg in (("mixed_cg", "mixed", True), ("fp64_ap", "fp64", False)):
+        cfg = fe_runtime_config(fe_tolerance=1e-8, fe_max_iterations=100000, cluster_fe_dims=[1, 2, 3],
+                                precision=precision, demean_cg=cg, se_convention="cpu")
+        fe_gpu_estimate(cfg, hdr, host, stream=stream.cuda_stream)  # warm-up
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r = fe_gpu_estimate(cfg, hdr, host, stream=stream.cuda_stream)
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        be = rel_errors(r.beta, oref.beta)
+        sv = rel_errors(r.se, oref.se)
+        out[label] = {"beta_rel_err": be, "se_rel_err": sv, "max_beta_rel": max(be), "max_se_rel": max(sv),
+                      "dof_resid_equal": int(r.dof_resid) == int(oref.stats["dof_resid"]),
+                      "converged": bool(r.converged), "fe_iterations": r.fe_iterations,
+                      "fit_s_host_arrays": dt, "rows_per_s_host_arrays": n / dt,
+                      "vs_cpu_baseline_same_sample": (n / dt) / cpu_entry["value"]}
+    out["pass"] = all(out[lb]["max_beta_rel"] < 1e-6 and out[lb]["max_se_rel"] < 1e-5 and out[lb]["dof_resid_equal"]
+                      for lb in ("mixed_cg", "fp64_ap"))
+    return out
 
 
 FAMILIES = ["segment sweep fp64", "segment sweep fp32", "small-G sweep fp64", "small-G sweep fp32",

@@ -1,0 +1,541 @@
+// Tensor-core (tcgen05) form of the dense count-matrix pass of the CG operator.
+//
+// One pass over the count matrix M (Ge x Gs, uint8, row g = the rows of each
+// group t of a small dimension s inside group g of a dimension e) forms two
+// small products per tile of UT = 128 groups of e:
+//
+//   E = M_tile . S            (128 x Gs by Gs x C)   the e side / Schur u
+//   D2 += U_tile' . M_tile    (C x 128 by 128 x Gs)  the small side
+//
+// where S holds the small dimension's rows ps and U the tile's rows of pe (or,
+// in the Schur form, u = (sums - E) / counts, which the pass also writes to the
+// primary's table). Both products run on the 5th-generation tensor cores:
+// tcgen05.mma kind::f16 with BF16 operands and FP32 accumulation in tensor
+// memory, issued by one thread of the CTA.
+//
+// Exactness of the operands: counts up to 255 are exact in BF16 (8 significant
+// bits). Every FP32 value v of S and U is split into three BF16 pieces
+// h = bf16(v), m = bf16(v - h), l = bf16(v - h - m) with v = h + m + l exactly,
+// so every product of a count and a piece is exact in FP32 and the three
+// pieces are accumulated as separate columns (E) or rows (D2) and added in the
+// order l + m + h afterwards. The result carries FP32 accumulation rounding
+// only, as the FP32 CUDA-core form does.
+//
+// Data movement: the tile's count bytes and row data are contiguous runs in
+// global memory and are fetched by cp.async.bulk (the TMA's bulk copy engine)
+// into a double-buffered stage, completing on an mbarrier; the next tile's
+// copies are in flight while this tile is processed. A 2-D tensor map does not
+// apply: its row strides must be multiples of 16 bytes, and these rows are Gs
+// bytes (30 at the 150M-row panel) and C floats (36 bytes) long. The CUDA cores
+// convert the counts to BF16 in the MMA operand layout, form u and its pieces,
+// and read the accumulators back from tensor memory with tcgen05.ld.
+//
+// Shared-memory operand layout: the canonical no-swizzle layout of tcgen05
+// descriptors, built of 8 x 16-byte core matrices. A core matrix holds 8 rows
+// of 8 BF16 values; LBO is the byte distance between core matrices adjacent in
+// the contraction (K) direction and SBO between those adjacent in the M or N
+// direction. The count tile (128 groups x KT small groups, KT = Gs padded to
+// 32 or 64) is stored once as core matrices (g/8, t/8) and read both as the
+// K-major A operand of E (M = g, K = t) and as the MN-major B operand of D2
+// (K = g, N = t).
+//
+// Every wait (mbarrier phases of the copies and of the MMAs) is bounded by a
+// globaltimer limit; a CTA that runs out of time records it in an error word
+// that the host reads after the within-transform, releases its tensor memory
+// and returns.
+#include "common.cuh"
+#include "sweep.cuh"
+
+#include <cuda_bf16.h>
+
+#include <algorithm>
+#include <cstdint>
+
+namespace fegb {
+
+namespace {
+
+constexpr int UT = 128;        // groups per tile (= threads per CTA: thread r owns row r of the tile)
+constexpr int UCP = 16;        // columns per piece block (C <= 16)
+constexpr int UNP = 3;         // BF16 pieces per FP32 value
+constexpr int UN1 = UNP * UCP; // N of the e-side product
+constexpr int UM2 = 128;       // M of the small-side product (rows p * 16 + c; 48 used)
+constexpr int TMEM_COLS = 128; // tensor-memory columns per CTA: E at [0, 48), D2 at [64, 64 + KT)
+constexpr int D2_COL = 64;
+constexpr unsigned long long WAIT_LIMIT_NS = 2000000000ull;  // 2 s per wait
+
+__device__ int g_umma_error;  // nonzero: a wait of the tensor-core pass ran out of time
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ unsigned long long globaltimer() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+    return t;
+}
+
+// tcgen05 shared-memory matrix descriptor, no swizzle: start address, LBO and
+// SBO in 16-byte units, fixed version bits 0b001 at 46-48.
+__device__ __forceinline__ uint64_t umma_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+    return (uint64_t)((saddr & 0x3FFFFu) >> 4) | ((uint64_t)(lbo >> 4) << 16) | ((uint64_t)(sbo >> 4) << 32) |
+           (1ull << 46);
+}
+
+// Instruction descriptor of kind::f16: FP32 accumulator, BF16 A and B, the
+// majorness of each operand (0 = K-major, 1 = MN-major), N >> 3 and M >> 4.
+__host__ __device__ constexpr uint32_t umma_idesc(int M, int N, int a_mn, int b_mn) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)a_mn << 15) | ((uint32_t)b_mn << 16) |
+           ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void umma_bf16(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc, int acc) {
+    asm volatile(
+        "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
+        "l"(a), "l"(b), "r"(idesc), "r"(acc)
+        : "memory");
+}
+
+__device__ __forceinline__ void umma_commit(uint64_t* bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+                 : "memory");
+}
+
+__device__ __forceinline__ void fence_before_sync() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_after_sync() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, int count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+// true once the phase of the given parity has completed, false after the time limit
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+    const uint32_t a = smem_u32(bar);
+    const unsigned long long t0 = globaltimer();
+    while (true) {
+        uint32_t ok;
+        asm volatile(
+            "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.b32 %0, 1, 0, p;\n}\n"
+            : "=r"(ok)
+            : "r"(a), "r"(parity)
+            : "memory");
+        if (ok) return true;
+        if (globaltimer() - t0 > WAIT_LIMIT_NS) return false;
+    }
+}
+
+// bulk global -> shared copy completing on bar (16-byte aligned, size a multiple of 16)
+__device__ __forceinline__ void bulk_copy(void* sdst, const void* gsrc, uint32_t bytes, uint64_t* bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_u32(sdst)),
+                 "l"(gsrc), "r"(bytes), "r"(smem_u32(bar))
+                 : "memory");
+}
+
+template <int N>
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[N], int base) {
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+#pragma unroll
+    for (int j = 0; j < 16; ++j) v[base + j] = __uint_as_float(r[j]);
+}
+__device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
+// v = h + m + l with BF16 pieces (exact for finite FP32 v)
+__device__ __forceinline__ void split3(float v, __nv_bfloat16& h, __nv_bfloat16& m, __nv_bfloat16& l) {
+    h = __float2bfloat16_rn(v);
+    const float r1 = v - __bfloat162float(h);
+    m = __float2bfloat16_rn(r1);
+    const float r2 = r1 - __bfloat162float(m);
+    l = __float2bfloat16_rn(r2);
+}
+
+__device__ __forceinline__ uint32_t pack2(__nv_bfloat16 a, __nv_bfloat16 b) {
+    return (uint32_t)__bfloat16_as_ushort(a) | ((uint32_t)__bfloat16_as_ushort(b) << 16);
+}
+
+struct UmmaArgs {
+    const uint8_t* M;
+    long long Ge;
+    int Gs;
+    const float* pe;
+    const float* ps;
+    int ld;
+    int C;
+    long long per;        // groups per CTA (a multiple of UT)
+    double* partials;     // [block][Gs][C] small-side sums, or null
+    float* extra;         // plain form: Ge x C (+)= M ps, or null
+    int accumulate;
+    const float* sums;    // Schur form: Ge x C, the primary's stream sums
+    const int32_t* counts;
+    float* table;         // Schur form: u rows (stride ld)
+    int bulk_counts;      // counts are 16-byte aligned: copied in bulk
+    uint32_t raw_bytes;   // stage sizes (multiples of 128)
+    uint32_t row_bytes;
+};
+
+// Shared-memory plan (bytes from the 1024-aligned dynamic base).
+struct UmmaSmem {
+    uint32_t b1, cnt0, cnt1, u, raw0, raw1, row0, row1, total;
+};
+__host__ __device__ inline UmmaSmem umma_smem_plan(int KT, uint32_t raw_bytes, uint32_t row_bytes) {
+    UmmaSmem s;
+    s.b1 = 0;
+    s.cnt0 = (uint32_t)(UN1 * KT * 2);
+    s.cnt1 = s.cnt0 + (uint32_t)(UT * KT * 2);
+    s.u = s.cnt1 + (uint32_t)(UT * KT * 2);
+    s.raw0 = s.u + (uint32_t)(UM2 * UT * 2);
+    s.raw1 = s.raw0 + raw_bytes;
+    s.row0 = s.raw1 + raw_bytes;
+    s.row1 = s.row0 + row_bytes;
+    s.total = s.row1 + row_bytes;
+    return s;
+}
+
+template <int KT, bool SCHUR>
+__global__ void __launch_bounds__(UT) dense_umma_kernel(UmmaArgs a) {
+    extern __shared__ __align__(1024) unsigned char sm[];
+    __shared__ __align__(8) uint64_t bars[4];  // 0, 1: tile copies; 2: e-side MMA; 3: small-side MMA
+    __shared__ uint32_t tmem_base_s;
+    __shared__ int abort_s;
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const long long g0 = (long long)blockIdx.x * a.per;
+    const long long g1 = min(a.Ge, g0 + a.per);
+    const int Gs = a.Gs, C = a.C, ld = a.ld;
+    const bool small = a.partials != nullptr;
+    const bool need_e = SCHUR || a.extra != nullptr;
+    double* const part = small ? a.partials + (long long)blockIdx.x * Gs * C : nullptr;
+    if (g0 >= g1) {  // no groups: zero partials
+        if (small)
+            for (int i = tid; i < Gs * C; i += UT) part[i] = 0.0;
+        return;
+    }
+    const UmmaSmem L = umma_smem_plan(KT, a.raw_bytes, a.row_bytes);
+    constexpr uint32_t CORE_ROW = (uint32_t)(KT / 8) * 128;  // bytes of one 8-group row of count cores
+    constexpr uint32_t U_LBO = (uint32_t)(UM2 / 8) * 128;    // bytes between 8-group blocks of the U tile
+    const uint32_t sbase = smem_u32(sm);
+
+    // tensor memory, barriers, U tile zeroed (rows 48.. stay zero), S pieces
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base_s)),
+                     "r"(TMEM_COLS));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    if (tid == 0) {
+        for (int i = 0; i < 4; ++i) mbar_init(&bars[i], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        abort_s = 0;
+    }
+    for (uint32_t o = tid * 16; o < (uint32_t)(UM2 * UT * 2); o += UT * 16)
+        *reinterpret_cast<uint4*>(sm + L.u + o) = make_uint4(0, 0, 0, 0);
+    if (need_e) {
+        // S pieces, K-major: B operand n = p * 16 + c (48 rows), k = t; core (n/8, t/8)
+        for (int i = tid; i < UN1 * KT; i += UT) {
+            const int n = i / KT, t = i - (i / KT) * KT;
+            const int p = n / UCP, c = n - p * UCP;
+            const float v = (t < Gs && c < C) ? a.ps[(long long)t * ld + c] : 0.0f;
+            __nv_bfloat16 h, m, l;
+            split3(v, h, m, l);
+            const __nv_bfloat16 piece = p == 0 ? h : (p == 1 ? m : l);
+            const uint32_t off = (uint32_t)(n / 8) * CORE_ROW + (uint32_t)(t / 8) * 128 + (uint32_t)(n % 8) * 16 +
+                                 (uint32_t)(t % 8) * 2;
+            *reinterpret_cast<__nv_bfloat16*>(sm + L.b1 + off) = piece;
+        }
+    }
+    fence_async_smem();
+    fence_before_sync();
+    __syncthreads();
+    fence_after_sync();
+    const uint32_t tmem = tmem_base_s;
+    const uint32_t t_lane = (uint32_t)(warp * 32) << 16;
+
+    const int ntiles = (int)((g1 - g0 + UT - 1) / UT);
+    auto full_tile = [&](long long tile) { return tile + UT <= g1; };
+    // the elected thread starts the copies of a tile into a stage (or, for a
+    // ragged tile, completes the stage's phase without copies: the threads
+    // then load it with plain loads)
+    auto issue = [&](int stg, long long tile) {
+        uint64_t* bar = &bars[stg];
+        unsigned char* raw = sm + (stg ? L.raw1 : L.raw0);
+        unsigned char* row = sm + (stg ? L.row1 : L.row0);
+        if (!full_tile(tile)) {
+            mbar_arrive(bar);
+            return;
+        }
+        const uint32_t cb = (uint32_t)(UT * Gs);
+        uint32_t rb;
+        if (SCHUR)
+            rb = (uint32_t)(UT * C * 4) + (a.bulk_counts ? (uint32_t)(UT * 4) : 0u);
+        else
+            rb = small ? (uint32_t)(UT * ld * 4) : 0u;
+        mbar_arrive_tx(bar, cb + rb);
+        bulk_copy(raw, a.M + tile * Gs, cb, bar);
+        if (SCHUR) {
+            bulk_copy(row, a.sums + tile * C, (uint32_t)(UT * C * 4), bar);
+            if (a.bulk_counts) bulk_copy(row + ((UT * C * 4 + 15) / 16) * 16, a.counts + tile, UT * 4, bar);
+        } else if (small) {
+            bulk_copy(row, a.pe + tile * ld, (uint32_t)(UT * ld * 4), bar);
+        }
+    };
+    if (tid == 0) issue(0, g0);
+
+    bool failed = false;
+    for (int i = 0; i < ntiles; ++i) {
+        const long long tile = g0 + (long long)i * UT;
+        const int nt = (int)min((long long)UT, g1 - tile);
+        const int stg = i & 1;
+        unsigned char* const raw = sm + (stg ? L.raw1 : L.raw0);
+        unsigned char* const row = sm + (stg ? L.row1 : L.row0);
+        const uint32_t cnt_off = stg ? L.cnt1 : L.cnt0;
+        if (tid == 0 && i + 1 < ntiles) issue(stg ^ 1, tile + UT);
+        bool ok = mbar_wait(&bars[stg], (uint32_t)((i >> 1) & 1));
+        if (__syncthreads_or(!ok)) {
+            failed = true;
+            break;
+        }
+        float* const srow = reinterpret_cast<float*>(row);
+        const int32_t* cnt_row = reinterpret_cast<const int32_t*>(row + ((UT * C * 4 + 15) / 16) * 16);
+        const bool ragged = !full_tile(tile);
+        if (ragged) {
+            // plain loads of the ragged tile (the stage's copy phase completed empty)
+            for (int j = tid; j < nt * Gs; j += UT) raw[j] = a.M[tile * Gs + j];
+            if (SCHUR) {
+                for (int j = tid; j < nt * C; j += UT) srow[j] = a.sums[tile * C + j];
+            } else if (small) {
+                for (int j = tid; j < nt * ld; j += UT) srow[j] = a.pe[tile * ld + j];
+            }
+        }
+        if (SCHUR && (ragged || !a.bulk_counts)) {
+            if (tid < nt) const_cast<int32_t*>(cnt_row)[tid] = a.counts[tile + tid];
+        }
+        if (ragged || (SCHUR && !a.bulk_counts)) __syncthreads();
+
+        // counts row tid -> BF16 core matrices (tid/8, t/8), row tid % 8
+        {
+            const unsigned char* src = raw + tid * Gs;
+#pragma unroll
+            for (int tb = 0; tb < KT / 8; ++tb) {
+                uint32_t w[4];
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    const int t0 = tb * 8 + 2 * q;
+                    const float x0 = (tid < nt && t0 < Gs) ? (float)src[t0] : 0.0f;
+                    const float x1 = (tid < nt && t0 + 1 < Gs) ? (float)src[t0 + 1] : 0.0f;
+                    w[q] = pack2(__float2bfloat16_rn(x0), __float2bfloat16_rn(x1));
+                }
+                *reinterpret_cast<uint4*>(sm + cnt_off + (uint32_t)(tid / 8) * CORE_ROW + (uint32_t)tb * 128 +
+                                          (uint32_t)(tid % 8) * 16) = make_uint4(w[0], w[1], w[2], w[3]);
+            }
+        }
+        fence_async_smem();
+        fence_before_sync();
+        __syncthreads();
+        fence_after_sync();
+
+        float e[UN1];
+        if (need_e) {
+            if (tid == 0) {
+                const uint32_t id = umma_idesc(UT, UN1, 0, 0);
+#pragma unroll
+                for (int s = 0; s < KT / 16; ++s)
+                    umma_bf16(tmem, umma_desc(sbase + cnt_off + s * 256, 128, CORE_ROW),
+                              umma_desc(sbase + L.b1 + s * 256, 128, CORE_ROW), id, s > 0);
+                umma_commit(&bars[2]);
+            }
+            ok = mbar_wait(&bars[2], (uint32_t)(i & 1));
+            if (__syncthreads_or(!ok)) {
+                failed = true;
+                break;
+            }
+            fence_after_sync();
+            tmem_ld16(tmem + t_lane + 0, e, 0);
+            tmem_ld16(tmem + t_lane + 16, e, 16);
+            tmem_ld16(tmem + t_lane + 32, e, 32);
+            tmem_wait_ld();
+        }
+        float v[UCP];
+#pragma unroll
+        for (int c = 0; c < UCP; ++c) v[c] = 0.0f;
+        if (SCHUR) {
+            const int n = tid < nt ? cnt_row[tid] : 0;
+            const float rn = n > 0 ? 1.0f / (float)n : 0.0f;
+#pragma unroll
+            for (int c = 0; c < UCP; ++c) {
+                if (c < C && tid < nt) {
+                    const float ec = (e[32 + c] + e[16 + c]) + e[c];
+                    v[c] = n > 0 ? (srow[tid * C + c] - ec) * rn : 0.0f;
+                }
+            }
+            if (tid < nt) {
+                float* trow = a.table + (tile + tid) * ld;
+#pragma unroll
+                for (int c = 0; c < UCP; ++c)
+                    if (c < C) trow[c] = v[c];
+            }
+        } else {
+            if (a.extra && tid < nt) {
+                float* xr = a.extra + (tile + tid) * C;
+#pragma unroll
+                for (int c = 0; c < UCP; ++c) {
+                    if (c < C) {
+                        const float ec = (e[32 + c] + e[16 + c]) + e[c];
+                        xr[c] = a.accumulate ? xr[c] + ec : ec;
+                    }
+                }
+            }
+            if (small && tid < nt) {
+#pragma unroll
+                for (int c = 0; c < UCP; ++c)
+                    if (c < C) v[c] = srow[tid * ld + c];
+            }
+        }
+        if (small) {
+            // the previous tile's small-side MMA must be done with the U tile
+            ok = i == 0 || mbar_wait(&bars[3], (uint32_t)((i - 1) & 1));
+            if (__syncthreads_or(!ok)) {
+                failed = true;
+                break;
+            }
+            // U pieces, MN-major: row m = p * 16 + c, core (m/8, tid/8), row tid % 8
+#pragma unroll
+            for (int p = 0; p < UNP; ++p) {
+#pragma unroll
+                for (int hb = 0; hb < 2; ++hb) {
+                    uint32_t w[4];
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) {
+                        __nv_bfloat16 pc[2];
+#pragma unroll
+                        for (int z = 0; z < 2; ++z) {
+                            __nv_bfloat16 h, m, l;
+                            split3(v[hb * 8 + 2 * q + z], h, m, l);
+                            pc[z] = p == 0 ? h : (p == 1 ? m : l);
+                        }
+                        w[q] = pack2(pc[0], pc[1]);
+                    }
+                    const uint32_t mb = (uint32_t)(p * 2 + hb);
+                    *reinterpret_cast<uint4*>(sm + L.u + mb * 128 + (uint32_t)(tid / 8) * U_LBO +
+                                              (uint32_t)(tid % 8) * 16) = make_uint4(w[0], w[1], w[2], w[3]);
+                }
+            }
+            fence_async_smem();
+        }
+        fence_before_sync();
+        __syncthreads();
+        fence_after_sync();
+        if (small && tid == 0) {
+            const uint32_t id = umma_idesc(UM2, KT, 1, 1);
+#pragma unroll
+            for (int s = 0; s < UT / 16; ++s)
+                umma_bf16(tmem + D2_COL, umma_desc(sbase + L.u + s * 2 * U_LBO, U_LBO, 128),
+                          umma_desc(sbase + cnt_off + s * 2 * CORE_ROW, CORE_ROW, 128), id, (i > 0 || s > 0) ? 1 : 0);
+            umma_commit(&bars[3]);
+        }
+    }
+    if (failed) {
+        if (tid == 0) {
+            atomicExch(&g_umma_error, 1);
+            abort_s = 1;
+        }
+    } else if (small) {
+        const bool ok = mbar_wait(&bars[3], (uint32_t)((ntiles - 1) & 1));
+        if (__syncthreads_or(!ok)) {
+            failed = true;
+            if (tid == 0) atomicExch(&g_umma_error, 1);
+        } else {
+            fence_after_sync();
+            // D2 row m (TMEM lane m) -> shared [m][t] (floats, over the U tile)
+            float* d2s = reinterpret_cast<float*>(sm + L.u);
+            __syncthreads();
+            if (warp < 2) {
+                float d[KT];
+#pragma unroll
+                for (int c0 = 0; c0 < KT; c0 += 16) tmem_ld16(tmem + t_lane + D2_COL + c0, d, c0);
+                tmem_wait_ld();
+                if (tid < UN1)
+#pragma unroll
+                    for (int t = 0; t < KT; ++t) d2s[tid * KT + t] = d[t];
+            }
+            __syncthreads();
+            for (int j = tid; j < Gs * C; j += UT) {
+                const int t = j / C, c = j - t * C;
+                part[j] = ((double)d2s[(32 + c) * KT + t] + (double)d2s[(16 + c) * KT + t]) + (double)d2s[c * KT + t];
+            }
+        }
+    }
+    fence_before_sync();
+    __syncthreads();
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS));
+}
+
+template <int KT, bool SCHUR>
+int launch_umma(const UmmaArgs& a, int nb, cudaStream_t s) {
+    const UmmaSmem L = umma_smem_plan(KT, a.raw_bytes, a.row_bytes);
+    static const cudaError_t attr = cudaFuncSetAttribute(dense_umma_kernel<KT, SCHUR>,
+                                                         cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    if (attr != cudaSuccess) return set_cuda_error(attr, "dense tensor-core pass attr");
+    dense_umma_kernel<KT, SCHUR><<<nb, UT, L.total, s>>>(a);
+    FEGB_LAUNCH_CHECK("dense small-G pair product (tcgen05)");
+    return 0;
+}
+
+bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
+
+}  // namespace
+
+int launch_dense_pair_umma(const uint8_t* M, long long Ge, int Gs, const float* pe, const float* ps, int ld, int C,
+                           double* partials, float* extra, int accumulate, const DenseSchur<float>& sch,
+                           cudaStream_t s, bool* launched) {
+    *launched = false;
+    const bool schur = sch.sums != nullptr;
+    if (Ge <= 0 || Gs <= 0 || Gs > 64 || C <= 0 || C > UCP || ld < C || ld % 4 != 0) return 0;
+    if (!aligned16(M) || !aligned16(ps) || (pe && !aligned16(pe)) || (schur && !aligned16(sch.sums))) return 0;
+    if (!schur && partials && !pe) return 0;
+    UmmaArgs a{};
+    a.M = M;
+    a.Ge = Ge;
+    a.Gs = Gs;
+    a.pe = pe;
+    a.ps = ps;
+    a.ld = ld;
+    a.C = C;
+    const int nb = dense_chunks(Ge);
+    long long per = (Ge + nb - 1) / nb;
+    a.per = (per + UT - 1) / UT * UT;
+    a.partials = partials;
+    a.extra = schur ? nullptr : extra;
+    a.accumulate = accumulate;
+    a.sums = sch.sums;
+    a.counts = sch.counts;
+    a.table = sch.table;
+    a.bulk_counts = schur && aligned16(sch.counts) ? 1 : 0;
+    a.raw_bytes = (uint32_t)((UT * Gs + 127) / 128 * 128);
+    const uint32_t rb = schur ? (uint32_t)(((UT * C * 4 + 15) / 16) * 16 + UT * 4) : (uint32_t)(UT * ld * 4);
+    a.row_bytes = (rb + 127) / 128 * 128;
+    *launched = true;
+    if (Gs <= 32) return schur ? launch_umma<32, true>(a, nb, s) : launch_umma<32, false>(a, nb, s);
+    return schur ? launch_umma<64, true>(a, nb, s) : launch_umma<64, false>(a, nb, s);
+}
+
+int dense_umma_error(int* flag, bool reset, cudaStream_t s) {
+    void* p = nullptr;
+    FEGB_CUDA(cudaGetSymbolAddress(&p, g_umma_error), "tensor-core pass error word");
+    int h = 0;
+    FEGB_CUDA(cudaMemcpyAsync(&h, p, sizeof(int), cudaMemcpyDeviceToHost, s), "tensor-core pass error read");
+    FEGB_CUDA(cudaStreamSynchronize(s), "tensor-core pass error sync");
+    if (reset && h) FEGB_CUDA(cudaMemsetAsync(p, 0, sizeof(int), s), "tensor-core pass error reset");
+    *flag = h;
+    return 0;
+}
+
+}  // namespace fegb

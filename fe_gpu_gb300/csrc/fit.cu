@@ -1985,6 +1985,12 @@ int demean_cg(Problem& P, double tol, int max_iter, int* iterations, int* conver
         total += it;
         apply_alpha = true;
     }
+    if (sizeof(T) == 4 && B.any_dense) {
+        // the tensor-core count-matrix passes record a wait that ran out of time
+        int umma_err = 0;
+        FEGB_TRY(dense_umma_error(&umma_err, true, P.s));
+        if (umma_err) return set_error("CG operator: a tensor-core count-matrix pass timed out waiting on its copies");
+    }
     *iterations = total;
     *converged = hit;
     *max_update = mu;

@@ -925,12 +925,16 @@ int dense_finalize_cov(int k, double* acc, double scalar, int do_psd, double* se
 // by every GPU that loads the library until the process exits), which bounds
 // the input to at most NOALLOC_MAX_COLS = 32 columns.
 //
-// The device address of the array is looked up once per device with
-// cudaGetSymbolAddress, by the first call made while that device is current;
-// make that first call before capturing any stream. Every call shares the
-// one array: calls whose kernels overlap on the GPU (other host threads, or
-// other streams) race on it. Each launch overwrites every partial it later
-// reads, so nothing has to be cleared between calls.
+// The device address of the array is looked up with cudaGetSymbolAddress by
+// the first call made while a device is current, and cached with the identity
+// of that device's CUDA context (cuCtxGetId). A later call in a new context
+// (after cudaDeviceReset, or a primary context that was released and created
+// again) finds a different identity and looks the address up again. Make the
+// first call on each device, and the first after a reset, before capturing
+// any stream. Every call shares the one array: calls whose kernels overlap on
+// the GPU (other host threads, or other streams) race on it. Each launch
+// overwrites every partial it later reads, so nothing has to be cleared
+// between calls.
 // ---------------------------------------------------------------------------
 namespace fegb {
 
@@ -945,18 +949,59 @@ __device__ __align__(256) double g_syrk_noalloc_partials[NOALLOC_BLOCKS * NOALLO
 constexpr int NOALLOC_MAX_DEVICES = 64;
 std::mutex g_noalloc_mu;
 double* g_noalloc_partials[NOALLOC_MAX_DEVICES] = {};
+unsigned long long g_noalloc_ctx_id[NOALLOC_MAX_DEVICES] = {};
 
-// Device address of the partials array for the current device (set-up on the
-// first call per device).
+// Driver entry points for the current context's identity, fetched through the
+// runtime so the library needs no link against libcuda.
+typedef int (*ctx_get_current_fn)(void** ctx);
+typedef int (*ctx_get_id_fn)(void* ctx, unsigned long long* id);
+
+// Identity of the calling thread's current context; *have = false when no
+// context is current or its identity cannot be read (a context destroyed by a
+// reset), so that the caller runs the set-up again.
+int current_context_id(unsigned long long* id, bool* have) {
+    static ctx_get_current_fn get_current = nullptr;
+    static ctx_get_id_fn get_id = nullptr;
+    *have = false;
+    if (!get_current || !get_id) {
+        void* f1 = nullptr;
+        void* f2 = nullptr;
+        cudaDriverEntryPointQueryResult q1{}, q2{};
+        FEGB_CUDA(cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 12000, cudaEnableDefault, &q1),
+                  "cudaGetDriverEntryPointByVersion (cuCtxGetCurrent)");
+        FEGB_CUDA(cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000, cudaEnableDefault, &q2),
+                  "cudaGetDriverEntryPointByVersion (cuCtxGetId)");
+        if (q1 != cudaDriverEntryPointSuccess || q2 != cudaDriverEntryPointSuccess || !f1 || !f2)
+            return set_error("fe_gpu_syrk_noalloc: the driver does not provide cuCtxGetCurrent/cuCtxGetId");
+        get_current = reinterpret_cast<ctx_get_current_fn>(f1);
+        get_id = reinterpret_cast<ctx_get_id_fn>(f2);
+    }
+    void* ctx = nullptr;
+    if (get_current(&ctx) != 0 || !ctx) return 0;
+    if (get_id(ctx, id) != 0) return 0;
+    *have = true;
+    return 0;
+}
+
+// Device address of the partials array in the current device's context
+// (looked up on the first call per device and again whenever the context
+// changed since).
 int noalloc_partials(double** out) {
     int dev = 0;
     FEGB_CUDA(cudaGetDevice(&dev), "cudaGetDevice");
     if (dev < 0 || dev >= NOALLOC_MAX_DEVICES) return set_error("fe_gpu_syrk_noalloc: device %d out of range", dev);
     std::lock_guard<std::mutex> lk(g_noalloc_mu);
-    if (!g_noalloc_partials[dev]) {
+    unsigned long long ctx_id = 0;
+    bool have = false;
+    FEGB_TRY(current_context_id(&ctx_id, &have));
+    if (!have || !g_noalloc_partials[dev] || g_noalloc_ctx_id[dev] != ctx_id) {
+        // set-up: the lookup also makes the device's primary context current
         void* p = nullptr;
         FEGB_CUDA(cudaGetSymbolAddress(&p, g_syrk_noalloc_partials), "cudaGetSymbolAddress (syrk scratch)");
+        FEGB_TRY(current_context_id(&ctx_id, &have));
+        if (!have) return set_error("fe_gpu_syrk_noalloc: no current CUDA context after set-up");
         g_noalloc_partials[dev] = static_cast<double*>(p);
+        g_noalloc_ctx_id[dev] = ctx_id;
     }
     *out = g_noalloc_partials[dev];
     return 0;
@@ -974,6 +1019,8 @@ extern "C" int fe_gpu_syrk_noalloc(int n_rows, int n_cols, double alpha, const d
     if (n_cols > NOALLOC_MAX_COLS)
         return set_error("fe_gpu_syrk_noalloc: n_cols=%d exceeds the %d-column limit of its fixed scratch", n_cols,
                          NOALLOC_MAX_COLS);
+    if (ldW < std::max(1, n_rows))
+        return set_error("fe_gpu_syrk_noalloc: ldW=%d is below max(1, n_rows=%d)", ldW, n_rows);
     double* partials = nullptr;
     FEGB_TRY(noalloc_partials(&partials));
     const cudaStream_t s = 0;  // legacy default stream, as the rest of the kernel-level ABI

@@ -12,6 +12,7 @@
 #include <atomic>
 #include <cstdarg>
 #include <cstring>
+#include <memory>
 #include <mutex>
 #include <vector>
 
@@ -89,38 +90,46 @@ constexpr cudaStream_t kLegacy = 0;  // the reference ABI runs on the legacy def
 // --------------------------- sorted-id cache ------------------------------
 // The reference host calls fe_gpu_fe_accumulate with the same id buffer four
 // times per dimension and iteration. The group-sorted permutation of that
-// buffer is kept, keyed by (pointer, n, n_groups) and validated against an
-// order-sensitive hash of the ids computed on every call.
+// buffer is kept, keyed by (device, pointer, n, n_groups), together with a
+// device copy of the ids it was built from. Every call compares the buffer
+// with that copy element by element (one read of 2n ints and a one-int
+// readback), so an entry is reused only when the ids are exactly the same.
+// Entries are shared: a caller keeps its entry alive while it uses it, even if
+// another thread evicts it from the cache meanwhile.
 struct SortedIds {
     const int* ids = nullptr;
     size_t n = 0;
     int n_groups = 0;
-    unsigned long long hash = 0;
     int device = -1;
+    int32_t* ids_copy = nullptr;  // the ids the permutation was built from
     int32_t* perm = nullptr;
     int32_t* gseq = nullptr;
     int32_t* off = nullptr;     // n_groups + 2 (last group collects invalid ids)
     int32_t* counts = nullptr;  // n_groups + 1
+    SortedIds() = default;
+    SortedIds(const SortedIds&) = delete;
+    SortedIds& operator=(const SortedIds&) = delete;
+    ~SortedIds() {
+        cudaFree(ids_copy);
+        cudaFree(perm);
+        cudaFree(gseq);
+        cudaFree(off);
+        cudaFree(counts);
+    }
 };
 
 std::mutex g_cache_mu;
-std::vector<SortedIds> g_cache;
-unsigned long long g_tick = 0;
+std::vector<std::shared_ptr<SortedIds>> g_cache;
 
-__global__ void ids_hash_kernel(const int* __restrict__ ids, long long n, unsigned long long* out) {
-    unsigned long long h = 0;
+// mismatch[0] = 1 when a[i] != b[i] for some i (a plain store of 1: every
+// writer writes the same value, so the outcome is order-independent)
+__global__ void ids_differ_kernel(const int* __restrict__ a, const int* __restrict__ b, long long n,
+                                  int* __restrict__ mismatch) {
     long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const long long st = (long long)gridDim.x * blockDim.x;
-    for (; i < n; i += st) {
-        unsigned long long x = (unsigned long long)(unsigned)ids[i] + 0x9e3779b97f4a7c15ull * (unsigned long long)(i + 1);
-        x ^= x >> 31;
-        x *= 0xbf58476d1ce4e5b9ull;
-        x ^= x >> 29;
-        h += x;
-    }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) h += __shfl_xor_sync(0xffffffffu, h, o);
-    if ((threadIdx.x & 31) == 0) atomicAdd(out, h);
+    bool diff = false;
+    for (; i < n; i += st) diff |= (a[i] != b[i]);
+    if (__any_sync(0xffffffffu, diff) && (threadIdx.x & 31) == 0) *mismatch = 1;
 }
 
 __global__ void sort_keys_kernel(const int* __restrict__ ids, long long n, int n_groups, uint32_t* __restrict__ keys) {
@@ -137,58 +146,78 @@ __global__ void counts_kernel(const int32_t* __restrict__ off, int G, int32_t* _
     if (g < G) counts[g] = off[g + 1] - off[g];
 }
 
-void free_entry(SortedIds& e) {
-    cudaFree(e.perm);
-    cudaFree(e.gseq);
-    cudaFree(e.off);
-    cudaFree(e.counts);
-    e = SortedIds();
+// True when the device buffer ids holds exactly the values cached in e.
+int same_ids(const int* ids, const SortedIds& e, Scratch& scr, bool* same) {
+    *same = false;
+    if (e.n == 0) {
+        *same = true;
+        return 0;
+    }
+    int* flag = nullptr;
+    FEGB_TRY(scr.alloc(&flag, 1, "id compare flag"));
+    FEGB_CUDA(cudaMemsetAsync(flag, 0, sizeof(int), kLegacy), "id compare reset");
+    ids_differ_kernel<<<grid_stride_blocks((long long)e.n, 256), 256, 0, kLegacy>>>(ids, e.ids_copy, (long long)e.n,
+                                                                                   flag);
+    FEGB_LAUNCH_CHECK("id compare");
+    int h = 1;
+    FEGB_CUDA(cudaMemcpy(&h, flag, sizeof(h), cudaMemcpyDeviceToHost), "id compare copy");
+    *same = (h == 0);
+    return 0;
 }
 
-int sorted_ids(const int* ids, size_t n, int n_groups, SortedIds** out) {
+int sorted_ids(const int* ids, size_t n, int n_groups, std::shared_ptr<SortedIds>* out) {
     int dev = 0;
     cudaGetDevice(&dev);
     configure_mem_pool();
     Scratch scr(kLegacy);
-    unsigned long long* hd = nullptr;
-    FEGB_TRY(scr.alloc(&hd, 1, "id hash"));
-    FEGB_CUDA(cudaMemsetAsync(hd, 0, sizeof(unsigned long long), kLegacy), "id hash reset");
-    ids_hash_kernel<<<grid_stride_blocks((long long)n, 256), 256, 0, kLegacy>>>(ids, (long long)n, hd);
-    FEGB_LAUNCH_CHECK("id hash");
-    unsigned long long h = 0;
-    FEGB_CUDA(cudaMemcpy(&h, hd, sizeof(h), cudaMemcpyDeviceToHost), "id hash copy");
-    std::lock_guard<std::mutex> lk(g_cache_mu);
-    for (auto& e : g_cache)
-        if (e.ids == ids && e.n == n && e.n_groups == n_groups && e.hash == h && e.device == dev) {
-            *out = &e;
+    std::shared_ptr<SortedIds> hit;
+    {
+        std::lock_guard<std::mutex> lk(g_cache_mu);
+        for (auto& e : g_cache)
+            if (e->ids == ids && e->n == n && e->n_groups == n_groups && e->device == dev) {
+                hit = e;
+                break;
+            }
+    }
+    if (hit) {
+        bool same = false;
+        FEGB_TRY(same_ids(ids, *hit, scr, &same));
+        if (same) {
+            *out = hit;
             return 0;
         }
-    if (g_cache.size() >= 8) {
-        free_entry(g_cache.front());
-        g_cache.erase(g_cache.begin());
+        std::lock_guard<std::mutex> lk(g_cache_mu);
+        g_cache.erase(std::remove(g_cache.begin(), g_cache.end(), hit), g_cache.end());
     }
-    SortedIds e;
-    e.ids = ids;
-    e.n = n;
-    e.n_groups = n_groups;
-    e.hash = h;
-    e.device = dev;
-    FEGB_CUDA(cudaMalloc(&e.perm, sizeof(int32_t) * std::max<size_t>(1, n)), "sorted ids perm");
-    FEGB_CUDA(cudaMalloc(&e.gseq, sizeof(int32_t) * std::max<size_t>(1, n)), "sorted ids keys");
-    FEGB_CUDA(cudaMalloc(&e.off, sizeof(int32_t) * ((size_t)n_groups + 2)), "sorted ids offsets");
-    FEGB_CUDA(cudaMalloc(&e.counts, sizeof(int32_t) * ((size_t)n_groups + 1)), "sorted ids counts");
+    auto e = std::make_shared<SortedIds>();
+    e->ids = ids;
+    e->n = n;
+    e->n_groups = n_groups;
+    e->device = dev;
+    const size_t n1 = std::max<size_t>(1, n);
+    FEGB_CUDA(cudaMalloc(&e->ids_copy, sizeof(int32_t) * n1), "sorted ids copy");
+    FEGB_CUDA(cudaMalloc(&e->perm, sizeof(int32_t) * n1), "sorted ids perm");
+    FEGB_CUDA(cudaMalloc(&e->gseq, sizeof(int32_t) * n1), "sorted ids keys");
+    FEGB_CUDA(cudaMalloc(&e->off, sizeof(int32_t) * ((size_t)n_groups + 2)), "sorted ids offsets");
+    FEGB_CUDA(cudaMalloc(&e->counts, sizeof(int32_t) * ((size_t)n_groups + 1)), "sorted ids counts");
+    if (n > 0)
+        FEGB_CUDA(cudaMemcpyAsync(e->ids_copy, ids, sizeof(int32_t) * n, cudaMemcpyDeviceToDevice, kLegacy),
+                  "sorted ids copy");
     uint32_t* keys = nullptr;
-    FEGB_TRY(scr.alloc(&keys, std::max<size_t>(1, n), "sort keys"));
+    FEGB_TRY(scr.alloc(&keys, n1, "sort keys"));
     sort_keys_kernel<<<grid_stride_blocks((long long)n, 256), 256, 0, kLegacy>>>(ids, (long long)n, n_groups, keys);
     FEGB_LAUNCH_CHECK("sort keys");
-    FEGB_TRY(radix_sort_u32(keys, nullptr, reinterpret_cast<uint32_t*>(e.gseq), e.perm, (long long)n,
+    FEGB_TRY(radix_sort_u32(keys, nullptr, reinterpret_cast<uint32_t*>(e->gseq), e->perm, (long long)n,
                             bits_for((unsigned long long)n_groups + 1), kLegacy, scr));
-    FEGB_TRY(segment_offsets(reinterpret_cast<const uint32_t*>(e.gseq), (long long)n, n_groups + 1, e.off, kLegacy));
-    counts_kernel<<<(n_groups + 1 + 255) / 256, 256, 0, kLegacy>>>(e.off, n_groups + 1, e.counts);
+    FEGB_TRY(segment_offsets(reinterpret_cast<const uint32_t*>(e->gseq), (long long)n, n_groups + 1, e->off, kLegacy));
+    counts_kernel<<<(n_groups + 1 + 255) / 256, 256, 0, kLegacy>>>(e->off, n_groups + 1, e->counts);
     FEGB_LAUNCH_CHECK("sorted ids counts");
-    ++g_tick;
-    g_cache.push_back(e);
-    *out = &g_cache.back();
+    {
+        std::lock_guard<std::mutex> lk(g_cache_mu);
+        if (g_cache.size() >= 8) g_cache.erase(g_cache.begin());
+        g_cache.push_back(e);
+    }
+    *out = e;
     return 0;
 }
 
@@ -340,6 +369,23 @@ extern "C" {
 
 long long fegb_kernel_launches(void) { return fegb::launches(); }
 
+int fegb_pool_usage(int reset_high, unsigned long long* used, unsigned long long* used_high,
+                    unsigned long long* reserved) {
+    int dev = 0;
+    FEGB_CUDA(cudaGetDevice(&dev), "cudaGetDevice");
+    cudaMemPool_t pool;
+    FEGB_CUDA(cudaDeviceGetDefaultMemPool(&pool, dev), "cudaDeviceGetDefaultMemPool");
+    if (reset_high) {
+        unsigned long long zero = 0;
+        FEGB_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrUsedMemHigh, &zero), "reset pool high-water mark");
+    }
+    if (used) FEGB_CUDA(cudaMemPoolGetAttribute(pool, cudaMemPoolAttrUsedMemCurrent, used), "pool used");
+    if (used_high) FEGB_CUDA(cudaMemPoolGetAttribute(pool, cudaMemPoolAttrUsedMemHigh, used_high), "pool used high");
+    if (reserved)
+        FEGB_CUDA(cudaMemPoolGetAttribute(pool, cudaMemPoolAttrReservedMemCurrent, reserved), "pool reserved");
+    return set_ok();
+}
+
 int fe_gpu_runtime_is_available(void) {
     int count = 0;
     cudaError_t err = cudaGetDeviceCount(&count);
@@ -372,7 +418,6 @@ int fe_gpu_runtime_init(int device_id, fe_gpu_device_info* info) {
 int fe_gpu_runtime_shutdown(void) {
     {
         std::lock_guard<std::mutex> lk(g_cache_mu);
-        for (auto& e : g_cache) free_entry(e);
         g_cache.clear();
     }
     return set_cuda_error(cudaDeviceReset(), "cudaDeviceReset");
@@ -392,14 +437,9 @@ int fe_gpu_runtime_free(void* ptr) {
     {
         // drop cached permutations of a buffer that is going away
         std::lock_guard<std::mutex> lk(g_cache_mu);
-        for (size_t i = 0; i < g_cache.size();) {
-            if ((const void*)g_cache[i].ids == ptr) {
-                free_entry(g_cache[i]);
-                g_cache.erase(g_cache.begin() + i);
-            } else {
-                ++i;
-            }
-        }
+        g_cache.erase(std::remove_if(g_cache.begin(), g_cache.end(),
+                                     [ptr](const std::shared_ptr<SortedIds>& e) { return (const void*)e->ids == ptr; }),
+                      g_cache.end());
     }
     return set_cuda_error(cudaFree(ptr), "cudaFree");
 }
@@ -445,6 +485,8 @@ int fe_gpu_linalg_shutdown(void) { return set_ok(); }
 int fe_gpu_syrk(int n_rows, int n_cols, double alpha, const double* W, int ldW, double beta, double* Q) {
     if (n_cols == 0) return set_ok();
     if (n_cols < 0 || n_rows < 0) return set_error("fe_gpu_syrk: negative dimension");
+    // the reference's cublasDsyrk rejects lda < max(1, k) with a nonzero status
+    if (ldW < std::max(1, n_rows)) return set_error("fe_gpu_syrk: ldW=%d is below max(1, n_rows=%d)", ldW, n_rows);
     configure_mem_pool();
     Scratch scr(kLegacy);
     MatView v{W, 1, ldW, n_cols};
@@ -515,7 +557,7 @@ int fe_gpu_cluster_scores(const double* residual, const double* W, const int* cl
                           int ldW, int n_clusters, double* scores) {
     if (n_cols == 0 || n_rows <= 0 || n_clusters <= 0) return set_ok();
     configure_mem_pool();
-    SortedIds* si = nullptr;
+    std::shared_ptr<SortedIds> si;
     FEGB_TRY(sorted_ids(cluster_ids, (size_t)n_rows, n_clusters, &si));
     Scratch scr(kLegacy);
     double *S = nullptr, *tmp = nullptr;
@@ -543,7 +585,7 @@ int fe_gpu_fe_accumulate(const double* y, const double* W, const double* Z, cons
     if (n_groups <= 0) return set_ok();
     if (n_obs > 0x7fffffffULL) return set_error("fe_gpu_fe_accumulate: n_obs exceeds the int32 index range");
     configure_mem_pool();
-    SortedIds* si = nullptr;
+    std::shared_ptr<SortedIds> si;
     FEGB_TRY(sorted_ids(fe_ids, n_obs, n_groups, &si));
     Scratch scr(kLegacy);
     const int width = std::max(1, std::max(n_reg, n_inst));
@@ -756,10 +798,11 @@ int fegb_test_dense_pair(const uint8_t* counts, long long Ge, int Gs, const floa
     DenseSchur<float> sch;
     if (schur) {
         FEGB_TRY(scr.alloc(&dsums, (size_t)Ge * C, "test sums"));
-        // the group counts start one element past an aligned address (a primary
-        // that is not the first dimension): the pass must not stage them asynchronously
+        // for odd Ge the group counts start one element past an aligned address
+        // (a primary that is not the first dimension): the pass must not stage
+        // them asynchronously; for even Ge they are aligned
         FEGB_TRY(scr.alloc(&dcnt, (size_t)Ge + 1, "test group counts"));
-        dcnt += 1;
+        if (Ge % 2 == 1) dcnt += 1;
         FEGB_TRY(scr.alloc(&dtab, (size_t)Ge * ld, "test table"));
         FEGB_CUDA(cudaMemcpy(dsums, sums, sizeof(float) * Ge * C, cudaMemcpyHostToDevice), "test sums copy");
         FEGB_CUDA(cudaMemcpy(dcnt, group_counts, sizeof(int32_t) * Ge, cudaMemcpyHostToDevice), "test counts copy");
@@ -782,6 +825,11 @@ int fegb_test_dense_pair(const uint8_t* counts, long long Ge, int Gs, const floa
                                                      accumulate, kLegacy, sch);
     dense_force_mode(-1);
     FEGB_TRY(st);
+    {
+        int umma_err = 0;
+        FEGB_TRY(dense_umma_error(&umma_err, true, kLegacy));
+        if (umma_err) return set_error("fegb_test_dense_pair: the tensor-core pass timed out waiting on its copies");
+    }
     if (out_small) FEGB_TRY(launch_fold_dense(dpart, nparts, Gs, C, dsmall, kLegacy));
     FEGB_CUDA(cudaDeviceSynchronize(), "test sync");
     if (out_small) FEGB_CUDA(cudaMemcpy(out_small, dsmall, sizeof(double) * Gs * C, cudaMemcpyDeviceToHost), "test out");

@@ -1387,238 +1387,18 @@ int dense_pair_two(const CT* M, long long Ge, int Gs, const T* pe, const T* ps, 
 }  // namespace
 
 namespace {
-thread_local int t_dense_mode = -1;  // -1 (default) and 0: the FP32 form; 1: the tensor-core form
+thread_local int t_dense_mode = -1;  // -1: the default form; 0: the FP32 CUDA-core form; 1: the tensor-core form
 }  // namespace
 
 bool dense_use_mma() {
     if (t_dense_mode >= 0) return t_dense_mode > 0;
-    static const bool env = [] {  // FEGB_DENSE_TENSOR=1: the tensor-core form by default
+    static const bool env = [] {  // FEGB_DENSE_TENSOR=1 selects the tensor-core form by default
         const char* v = std::getenv("FEGB_DENSE_TENSOR");
         return v && v[0] == '1';
     }();
     return env;
 }
 void dense_force_mode(int mode) { t_dense_mode = mode; }
-
-namespace {
-
-// ---- tensor-core form of the dense pair pass (FP32 storage, uint8 counts) ----
-// The two products of a tile of 64 groups of e are small matrix products:
-//   E = N S     (64 x Gs by Gs x C: the other side / the Schur u),
-//   acc += N' U (Gs x 64 by 64 x C: the small side, U = pe rows or u).
-// They run as mma.sync m16n8k8 TF32 products with FP32 accumulation. The
-// counts (< 256) are exact in TF32; S and U are split into two TF32 parts
-// (hi = rounded to TF32, lo = TF32 of the remainder), so each product is two
-// MMAs and keeps about 2^-22 relative precision. Warp w: phase A takes the
-// (m-tile, n-tile) pairs w, w + 8, ... of E; phase B the 8 groups 8w..8w+7 of
-// the tile for every (m-tile, n-tile) of acc. acc is folded across warps in
-// warp order at the end (FP64), as in the FP32 kernel.
-
-__device__ __forceinline__ uint32_t tf32_bits(float x) {
-    uint32_t r;
-    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
-    return r;
-}
-
-__device__ __forceinline__ void mma_tf32(float (&d)[4], uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a3,
-                                         uint32_t b0, uint32_t b1) {
-    asm volatile(
-        "mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-        "{%0,%1,%2,%3};"
-        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
-        : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
-}
-
-// hi/lo TF32 split of x
-__device__ __forceinline__ void tf32_split(float x, uint32_t& hi, uint32_t& lo) {
-    hi = tf32_bits(x);
-    lo = tf32_bits(x - __uint_as_float(hi));
-}
-
-template <int MT, int CN>
-__global__ void __launch_bounds__(256) dense_pair_mma_kernel(const uint8_t* __restrict__ M, long long Ge, int Gs,
-                                                             const float* __restrict__ pe,
-                                                             const float* __restrict__ ps, int ld, int C,
-                                                             long long per, double* __restrict__ partials,
-                                                             float* __restrict__ extra, int accumulate,
-                                                             DenseSchur<float> sch) {
-    constexpr int KP = MT * 16;  // padded small-dimension extent (k of phase A, m of phase B)
-    constexpr int NP = CN * 8;   // padded columns
-    extern __shared__ __align__(16) unsigned char dense_smem[];
-    uint32_t* sSh = reinterpret_cast<uint32_t*>(dense_smem);  // KP x NP: S hi (TF32 bits)
-    uint32_t* sSl = sSh + KP * NP;                              // KP x NP: S lo
-    float* sU = reinterpret_cast<float*>(sSl + KP * NP);       // DENSE_TILE x NP: u (Schur form)
-    const size_t fixed = sizeof(uint32_t) * 2 * KP * NP + sizeof(float) * DENSE_TILE * NP;
-    const size_t p_bytes = dense_slot_bytes<float>(ld, C);
-    const size_t m_bytes = (((size_t)DENSE_TILE * Gs + 15) / 16) * 16;
-    unsigned char* const buf0 = dense_smem + fixed;
-    unsigned char* const buf1 = buf0 + p_bytes + m_bytes;
-    double* red = reinterpret_cast<double*>(dense_smem);  // Gs x C (after the tiles)
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int gid = lane >> 2, tig = lane & 3;
-    const bool schur = sch.sums != nullptr;
-    const bool small_side = partials != nullptr;
-    const bool other = schur || extra != nullptr;
-    if (other)
-        for (int i = threadIdx.x; i < KP * NP; i += 256) {
-            const int k = i / NP, c = i - k * NP;
-            const float x = (k < Gs && c < C) ? ps[(long long)k * ld + c] : 0.f;
-            uint32_t h, l;
-            tf32_split(x, h, l);
-            sSh[i] = h;
-            sSl[i] = l;
-        }
-    float acc[MT][CN][4];
-#pragma unroll
-    for (int a = 0; a < MT; ++a)
-#pragma unroll
-        for (int b = 0; b < CN; ++b)
-#pragma unroll
-            for (int q = 0; q < 4; ++q) acc[a][b][q] = 0.f;
-    const long long g0 = (long long)blockIdx.x * per;
-    const long long g1 = min(Ge, g0 + per);
-    if (g0 < g1)
-        dense_issue<float, uint8_t>(M, small_side && !schur ? pe : nullptr, Gs, ld, g0,
-                                    (int)min((long long)DENSE_TILE, g1 - g0), reinterpret_cast<uint8_t*>(buf0 + p_bytes),
-                                    reinterpret_cast<float*>(buf0), sch.sums, sch.counts, C);
-    cp_async_commit();
-    bool odd = false;
-    for (long long tile = g0; tile < g1; tile += DENSE_TILE, odd = !odd) {
-        unsigned char* const cur = odd ? buf1 : buf0;
-        unsigned char* const nxt = odd ? buf0 : buf1;
-        const int nt = (int)min((long long)DENSE_TILE, g1 - tile);
-        const long long next = tile + DENSE_TILE;
-        if (next < g1)
-            dense_issue<float, uint8_t>(M, small_side && !schur ? pe : nullptr, Gs, ld, next,
-                                        (int)min((long long)DENSE_TILE, g1 - next),
-                                        reinterpret_cast<uint8_t*>(nxt + p_bytes), reinterpret_cast<float*>(nxt),
-                                        sch.sums, sch.counts, C);
-        cp_async_commit();
-        cp_async_wait_prev();
-        uint8_t* const m = reinterpret_cast<uint8_t*>(cur + p_bytes);
-        const float* const pt = reinterpret_cast<const float*>(cur);
-        dense_tail<float, uint8_t>(M, Gs, tile, nt, m, reinterpret_cast<float*>(cur), sch.sums, sch.counts, C);
-        __syncthreads();
-        const int32_t* const tcnt = reinterpret_cast<const int32_t*>(cur + dense_sums_bytes<float>(C));
-        auto cnt = [&](int row, int col) -> uint32_t {  // count (group row, small col) as TF32 bits
-            return (row < nt && col < Gs) ? __float_as_uint((float)m[row * Gs + col]) : 0u;
-        };
-        if (other) {
-            // phase A: E = N S for (m-tile, n-tile) pairs of this warp
-            for (int idx = warp; idx < 4 * CN; idx += 8) {
-                const int mt = idx & 3, j = idx >> 2;
-                float d[4] = {0.f, 0.f, 0.f, 0.f};
-                const int r0 = mt * 16 + gid;
-#pragma unroll
-                for (int ks = 0; ks < 2 * MT; ++ks) {
-                    const int k0 = ks * 8 + tig;
-                    const uint32_t a0 = cnt(r0, k0), a1 = cnt(r0 + 8, k0), a2 = cnt(r0, k0 + 4),
-                                   a3 = cnt(r0 + 8, k0 + 4);
-                    const int bi0 = k0 * NP + j * 8 + gid, bi1 = (k0 + 4) * NP + j * 8 + gid;
-                    mma_tf32(d, a0, a1, a2, a3, sSh[bi0], sSh[bi1]);
-                    mma_tf32(d, a0, a1, a2, a3, sSl[bi0], sSl[bi1]);
-                }
-#pragma unroll
-                for (int q = 0; q < 4; ++q) {
-                    const int row = r0 + (q >> 1) * 8;
-                    const int col = j * 8 + 2 * tig + (q & 1);
-                    const long long g = tile + row;
-                    if (schur) {
-                        float u = 0.f;
-                        if (row < nt && col < C) {
-                            const int n = tcnt[row];
-                            if (n > 0) u = (pt[row * C + col] - d[q]) / (float)n;
-                            sch.table[g * ld + col] = u;
-                        }
-                        sU[row * NP + col] = u;
-                    } else if (row < nt && col < C) {
-                        float* o = extra + g * C + col;
-                        *o = accumulate ? *o + d[q] : d[q];
-                    }
-                }
-            }
-            if (schur) __syncthreads();
-        }
-        if (small_side) {
-            // phase B: acc += N' U over this warp's 8 groups of the tile
-            const int kg0 = warp * 8 + tig;  // group rows of the B fragment / columns of the A fragment
-            uint32_t bh[CN][2], bl[CN][2];
-#pragma unroll
-            for (int j = 0; j < CN; ++j) {
-#pragma unroll
-                for (int h = 0; h < 2; ++h) {
-                    const int kg = kg0 + 4 * h;
-                    float x = 0.f;
-                    if (kg < nt) x = schur ? sU[kg * NP + j * 8 + gid] : pt[kg * ld + j * 8 + gid];
-                    tf32_split(x, bh[j][h], bl[j][h]);
-                }
-            }
-#pragma unroll
-            for (int mt2 = 0; mt2 < MT; ++mt2) {
-                const int t0 = mt2 * 16 + gid;
-                const uint32_t a0 = cnt(kg0, t0), a1 = cnt(kg0, t0 + 8), a2 = cnt(kg0 + 4, t0),
-                               a3 = cnt(kg0 + 4, t0 + 8);
-#pragma unroll
-                for (int j = 0; j < CN; ++j) {
-                    mma_tf32(acc[mt2][j], a0, a1, a2, a3, bh[j][0], bh[j][1]);
-                    mma_tf32(acc[mt2][j], a0, a1, a2, a3, bl[j][0], bl[j][1]);
-                }
-            }
-        }
-        __syncthreads();  // this buffer is refilled two tiles on; sU is rewritten
-    }
-    if (!small_side) return;
-    __syncthreads();  // red overlays the staging arrays
-    for (int w = 0; w < DENSE_WARPS; ++w) {
-        if (warp == w) {
-#pragma unroll
-            for (int mt2 = 0; mt2 < MT; ++mt2)
-#pragma unroll
-                for (int j = 0; j < CN; ++j)
-#pragma unroll
-                    for (int q = 0; q < 4; ++q) {
-                        const int t = mt2 * 16 + gid + (q >> 1) * 8;
-                        const int c = j * 8 + 2 * tig + (q & 1);
-                        if (t < Gs && c < C) red[t * C + c] = (w ? red[t * C + c] : 0.0) + (double)acc[mt2][j][q];
-                    }
-        }
-        __syncthreads();
-    }
-    for (int i = threadIdx.x; i < Gs * C; i += 256) partials[(long long)blockIdx.x * Gs * C + i] = red[i];
-}
-
-template <int MT, int CN>
-int dense_pair_mma(const uint8_t* M, long long Ge, int Gs, const float* pe, const float* ps, int ld, int C,
-                   double* partials, float* extra, int accumulate, const DenseSchur<float>& sch, cudaStream_t s) {
-    static const cudaError_t attr = cudaFuncSetAttribute(dense_pair_mma_kernel<MT, CN>,
-                                                         cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
-    if (attr != cudaSuccess) return set_cuda_error(attr, "dense pair (mma) attr");
-    const int nb = dense_chunks(Ge);
-    long long per = (Ge + nb - 1) / nb;
-    per = (per + DENSE_TILE - 1) / DENSE_TILE * DENSE_TILE;
-    constexpr int KP = MT * 16, NP = CN * 8;
-    const size_t fixed = sizeof(uint32_t) * 2 * KP * NP + sizeof(float) * DENSE_TILE * NP;
-    const size_t p_bytes = dense_slot_bytes<float>(ld, C);
-    const size_t m_bytes = (((size_t)DENSE_TILE * Gs + 15) / 16) * 16;
-    const size_t smem = std::max(fixed + 2 * (p_bytes + m_bytes), sizeof(double) * (size_t)Gs * C);
-    dense_pair_mma_kernel<MT, CN><<<nb, 256, smem, s>>>(M, Ge, Gs, pe, ps, ld, C, per, partials, extra, accumulate,
-                                                        sch);
-    FEGB_LAUNCH_CHECK("dense small-G pair product (mma)");
-    return 0;
-}
-
-template <int MT>
-int dense_pair_mma_cn(int CN, const uint8_t* M, long long Ge, int Gs, const float* pe, const float* ps, int ld, int C,
-                      double* partials, float* extra, int accumulate, const DenseSchur<float>& sch, cudaStream_t s) {
-    switch (CN) {
-        case 1: return dense_pair_mma<MT, 1>(M, Ge, Gs, pe, ps, ld, C, partials, extra, accumulate, sch, s);
-        case 2: return dense_pair_mma<MT, 2>(M, Ge, Gs, pe, ps, ld, C, partials, extra, accumulate, sch, s);
-        case 3: return dense_pair_mma<MT, 3>(M, Ge, Gs, pe, ps, ld, C, partials, extra, accumulate, sch, s);
-        default: return dense_pair_mma<MT, 4>(M, Ge, Gs, pe, ps, ld, C, partials, extra, accumulate, sch, s);
-    }
-}
-
-}  // namespace
 
 template <typename T, typename CT>
 int launch_dense_pair(const CT* M, long long Ge, int Gs, const T* pe, const T* ps, int ld, int C, double* partials,
@@ -1631,17 +1411,11 @@ int launch_dense_pair(const CT* M, long long Ge, int Gs, const T* pe, const T* p
         (sch.sums && (extra || !partials || !sch.counts || !sch.table)))
         return set_error("dense small-G product: invalid arguments (ld %d)", ld);
     if constexpr (std::is_same<T, float>::value && std::is_same<CT, uint8_t>::value) {
-        // tensor-core form: padded columns (multiple of 8) must fit the row stride
-        const int CN = (C + 7) / 8;
-        if (dense_use_mma() && CN * 8 <= ld) {
-            const int MT = (Gs + 15) / 16;
-            switch (MT) {
-                case 1: return dense_pair_mma_cn<1>(CN, M, Ge, Gs, pe, ps, ld, C, partials, extra, accumulate, sch, s);
-                case 2: return dense_pair_mma_cn<2>(CN, M, Ge, Gs, pe, ps, ld, C, partials, extra, accumulate, sch, s);
-                case 3: return dense_pair_mma_cn<3>(CN, M, Ge, Gs, pe, ps, ld, C, partials, extra, accumulate, sch, s);
-                default:
-                    return dense_pair_mma_cn<4>(CN, M, Ge, Gs, pe, ps, ld, C, partials, extra, accumulate, sch, s);
-            }
+        // tensor-core form (tcgen05, dense_umma.cu) where its shapes allow it
+        if (dense_use_mma()) {
+            bool launched = false;
+            FEGB_TRY(launch_dense_pair_umma(M, Ge, Gs, pe, ps, ld, C, partials, extra, accumulate, sch, s, &launched));
+            if (launched) return 0;
         }
     }
     if (C <= 4 && ld >= 4) return dense_pair_two<T, CT, 4>(M, Ge, Gs, pe, ps, ld, C, partials, extra, accumulate, sch, s);

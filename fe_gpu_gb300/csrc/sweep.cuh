@@ -256,13 +256,21 @@ template <typename T, typename CT>
 int launch_dense_pair(const CT* M, long long Ge, int Gs, const T* pe, const T* ps, int ld, int C, double* partials,
                       T* extra, int accumulate, cudaStream_t s, const DenseSchur<T>& sch = DenseSchur<T>());
 // Form of the uint8 / FP32 dense pair pass on the calling host thread: the
-// FP32 form by default (mode -1 or 0; FEGB_DENSE_TENSOR=1 in the environment
-// makes mode -1 the tensor-core form), the tensor-core (TF32 split) form with
-// mode 1. The TF32 split keeps about 2^-22 relative precision per product
-// against 2^-24 for FP32 FMAs, which cost the FP32 inner CG a few iterations
-// per solve on the worker-firm panels, so the FP32 form stays the default.
+// tensor-core form (tcgen05, BF16 pieces, FP32 accumulation; dense_umma.cu)
+// by default wherever its shapes allow it (C <= 16, Gs <= 64, 16-byte aligned
+// operands), else the FP32 CUDA-core form. mode 0 forces the CUDA-core form,
+// mode 1 the tensor-core form, -1 restores the default; FEGB_DENSE_TENSOR=0 in
+// the environment makes the CUDA-core form the default.
 bool dense_use_mma();
 void dense_force_mode(int mode);
+// The tensor-core form of launch_dense_pair for FP32 storage and uint8 counts.
+// *launched = false (status 0) when the shapes or alignments do not allow it.
+int launch_dense_pair_umma(const uint8_t* M, long long Ge, int Gs, const float* pe, const float* ps, int ld, int C,
+                           double* partials, float* extra, int accumulate, const DenseSchur<float>& sch,
+                           cudaStream_t s, bool* launched);
+// Reads (synchronising s) and optionally resets the error word of the
+// tensor-core pass: nonzero when one of its bounded waits ran out of time.
+int dense_umma_error(int* flag, bool reset, cudaStream_t s);
 // Schur-complement CG helpers (the primary dimension eliminated):
 // table[g * L + c] = (sums[g * C + c] - extra[g * C + c]) / counts[g] (extra optional)
 template <typename T>

@@ -66,9 +66,12 @@ int fe_gpu_syrk(int n_rows, int n_cols, double alpha, const double* W, int ldW, 
  * own allocator and budget, or a section that must not touch the allocator.
  * Its partial sums live in a fixed 642 KB device array held by every GPU that
  * loads the library; n_cols is limited to 32 (larger requests return a
- * nonzero status). The first call on each device (with that device current)
- * looks up the array's address; make it before any stream capture. All calls
- * share the array: calls that overlap on the GPU race. */
+ * nonzero status), and ldW below max(1, n_rows) is rejected as in
+ * fe_gpu_syrk. The first call on each device (with that device current)
+ * looks up the array's address and records the device's context; a call in a
+ * new context (after cudaDeviceReset) looks it up again. Make the first call,
+ * and the first after a reset, before any stream capture. All calls share the
+ * array: calls that overlap on the GPU race. */
 int fe_gpu_syrk_noalloc(int n_rows, int n_cols, double alpha, const double* W, int ldW, double beta, double* Q);
 /* b = alpha W^T y + beta b */
 int fe_gpu_gemv(int n_rows, int n_cols, double alpha, const double* W, int ldW, const double* y, double beta,

@@ -143,6 +143,14 @@ int fegb_group_sizes(const int* const* d_fe_ids, int n_fe, long long n, int* siz
 /* Number of kernel launches issued by this library since it was loaded. */
 long long fegb_kernel_launches(void);
 
+/* Memory of the current device's default stream-ordered pool, the pool this
+ * library's temporaries come from: bytes in use now, the high-water mark of
+ * bytes in use, and bytes reserved from the device. reset_high != 0 first
+ * resets the high-water mark to the bytes in use now. Any output may be null.
+ * A diagnostic for hosts that budget device memory. */
+int fegb_pool_usage(int reset_high, unsigned long long* used, unsigned long long* used_high,
+                    unsigned long long* reserved);
+
 /* Self-test of one dense count-matrix pass of the CG operator (FP32 storage,
  * uint8 counts), on host arrays. counts: Ge x Gs row-major (rows of each pair
  * of a group g of a many-group dimension and a group t of a small dimension);
@@ -152,8 +160,11 @@ long long fegb_kernel_launches(void);
  *                       accumulate = 1 adds to the values passed in)
  * Schur form (sums non-null, Ge x C; group_counts Ge; pe unused; out_extra
  * null): out_table[g*ld+c] = (sums[g][c] - sum_t counts[g][t] ps[t][c]) /
- * group_counts[g] and out_small uses those rows as pe. tensor_cores = 1: the
- * tensor-core (TF32 split) form, 0: the FP32 form. */
+ * group_counts[g] and out_small uses those rows as pe; for odd Ge the group
+ * counts are placed one element past a 16-byte boundary on the device (the
+ * pass then loads them with plain loads instead of bulk copies).
+ * tensor_cores = 1: the tensor-core (tcgen05, BF16 pieces) form where the
+ * shapes allow it (C <= 16, Gs <= 64), else the FP32 form; 0: the FP32 form. */
 int fegb_test_dense_pair(const unsigned char* counts, long long Ge, int Gs, const float* pe, const float* ps, int ld,
                          int C, const float* sums, const int* group_counts, int accumulate, int tensor_cores,
                          double* out_small, float* out_extra, float* out_table);

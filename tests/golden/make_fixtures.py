@@ -1,9 +1,8 @@
 """Regenerate the golden fixtures under tests/golden/ from the reference.
 
-Run in a container where the reference tree is mounted (default
-/root/reference, override with FE_GPU_REFERENCE):
+Run where the reference source tree is present, naming its root:
 
-    python tests/golden/make_fixtures.py
+    FE_GPU_REFERENCE=<reference tree> python tests/golden/make_fixtures.py
 
 reference_generator_small.npz: output of the reference's own synthetic panel
 generator (tools/generate_synthetic_data.py, build_panel) at a small size,
@@ -17,7 +16,9 @@ from pathlib import Path
 
 import numpy as np
 
-REF = Path(os.environ.get("FE_GPU_REFERENCE", "/root/reference"))
+if not os.environ.get("FE_GPU_REFERENCE"):
+    raise SystemExit("set FE_GPU_REFERENCE to the root of the reference source tree")
+REF = Path(os.environ["FE_GPU_REFERENCE"])
 OUT = Path(__file__).resolve().parent
 
 

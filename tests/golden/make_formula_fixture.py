@@ -1,14 +1,16 @@
 """Builds formula_expansion_log.json from the reference's own example run:
 the six fe_gpu formulas of Examples/01TESTS_fe_gpu_small.sh and, for each,
 the coefficient names, estimator line, endogenous columns and dof printed in
-Examples/01TESTS_fe_gpu_small_output.txt. Run in a container holding the
-reference tree (FE_GPU_REFERENCE, default /root/reference)."""
+Examples/01TESTS_fe_gpu_small_output.txt. Run where the reference source tree
+is present, with FE_GPU_REFERENCE naming its root."""
 import json
 import os
 import re
 from pathlib import Path
 
-REF = Path(os.environ.get("FE_GPU_REFERENCE", "/root/reference"))
+if not os.environ.get("FE_GPU_REFERENCE"):
+    raise SystemExit("set FE_GPU_REFERENCE to the root of the reference source tree")
+REF = Path(os.environ["FE_GPU_REFERENCE"])
 OUT = Path(__file__).resolve().parent / "formula_expansion_log.json"
 
 

@@ -1,7 +1,13 @@
 """The CG operator's dense count-matrix pass (fegb_test_dense_pair) against
-numpy in FP64: the FP32 form and the tensor-core (TF32 split) form, plain,
-accumulating and Schur forms, ragged sizes (partial tiles, small dimensions
-above 32 groups, columns that are not a multiple of 8)."""
+numpy in FP64: the FP32 CUDA-core form and the tensor-core form (tcgen05,
+BF16 pieces, FP32 accumulation in tensor memory), plain, accumulating and
+Schur forms, ragged sizes (partial tiles of 128 groups, blocks without
+groups, small dimensions above 32 groups, columns that are not a multiple of
+8, counts up to 255, group counts aligned or not). Shapes the tensor-core form
+does not take (C > 16) check its fallback to the CUDA-core form.
+
+Tolerance: 5e-6 of the largest magnitude, for FP32 accumulation of sums of up
+to a few hundred terms."""
 import ctypes as C
 
 import numpy as np
@@ -37,7 +43,9 @@ def rel(a, b):
 
 
 @pytest.mark.parametrize("tensor_cores", [1, 0])
-@pytest.mark.parametrize("ge,gs,cols,maxc", [(5000, 20, 9, 1), (3001, 33, 3, 7), (700, 7, 17, 255), (64, 64, 32, 3)])
+@pytest.mark.parametrize("ge,gs,cols,maxc", [(5000, 20, 9, 1), (3001, 33, 3, 7), (700, 7, 17, 255), (64, 64, 32, 3),
+                                             (200_000, 30, 9, 1), (100_003, 30, 16, 255), (129, 64, 1, 2),
+                                             (77_777, 64, 12, 40), (2, 1, 9, 3)])
 def test_dense_pair_matches_numpy(built, tensor_cores, ge, gs, cols, maxc):
     rng = np.random.default_rng(ge + gs + cols)
     ld = row_stride(cols)

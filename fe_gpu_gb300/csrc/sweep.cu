@@ -1392,9 +1392,9 @@ thread_local int t_dense_mode = -1;  // -1: the default form; 0: the FP32 CUDA-c
 
 bool dense_use_mma() {
     if (t_dense_mode >= 0) return t_dense_mode > 0;
-    static const bool env = [] {  // FEGB_DENSE_TENSOR=1 selects the tensor-core form by default
+    static const bool env = [] {  // FEGB_DENSE_TENSOR=0 selects the FP32 CUDA-core form by default
         const char* v = std::getenv("FEGB_DENSE_TENSOR");
-        return v && v[0] == '1';
+        return !(v && v[0] == '0');
     }();
     return env;
 }

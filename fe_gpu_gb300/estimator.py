@@ -40,6 +40,10 @@ class fe_runtime_config:  # src/core/fe_config.f90:16-46 (host-facing subset)
     precision: str = "fp64"          # "fp64" (plain) or "mixed" (FP32 sweeps + FP64 refinement)
     se_convention: str = "gpu"       # "gpu" (reference GPU estimator) or "cpu" (reference CPU estimator)
     drop_singletons: bool = False
+    # mixed precision: also fit the plain FP64 form (FP64 storage, the
+    # reference's AP scheme) on the same inputs and attach every coefficient's
+    # and SE's relative error against it to the result
+    verify_fp64: bool = False
 
 
 def init_default_config() -> fe_runtime_config:  # src/core/fe_config.f90:53-79
@@ -77,6 +81,12 @@ class fe_estimation_result:  # src/core/fe_pipeline.f90:37-64
     n_obs_used: int = 0
     n_singletons: int = 0
     stats: dict = field(default_factory=dict)
+    # with verify_fp64: |x - x_fp64| / |x_fp64| per coefficient and SE (0 where
+    # both are 0, e.g. a column the filter dropped), and the FP64 fit's values
+    beta_rel_err_vs_fp64: Optional[np.ndarray] = None
+    se_rel_err_vs_fp64: Optional[np.ndarray] = None
+    beta_fp64: Optional[np.ndarray] = None
+    se_fp64: Optional[np.ndarray] = None
 
 
 def _make_config(cfg: fe_runtime_config, stream: Optional[int] = None, profile: bool = False):
@@ -143,6 +153,27 @@ def _ptr(a: np.ndarray) -> int:
     return a.ctypes.data if a is not None and a.size else None
 
 
+def _rel_err(x: np.ndarray, ref: np.ndarray) -> np.ndarray:
+    x, ref = np.asarray(x, dtype=np.float64), np.asarray(ref, dtype=np.float64)
+    d = np.abs(x - ref)
+    return np.where(d == 0.0, 0.0, d / np.maximum(np.abs(ref), np.finfo(np.float64).tiny))
+
+
+def _attach_fp64_errors(res: fe_estimation_result, cfg: fe_runtime_config, refit) -> fe_estimation_result:
+    """verify_fp64: refit in the plain FP64 form (AP) and attach the errors."""
+    if not cfg.verify_fp64 or cfg.precision == "fp64":
+        return res
+    c64 = copy.copy(cfg)
+    c64.precision = "fp64"
+    c64.demean_cg = False
+    c64.verify_fp64 = False
+    ref = refit(c64)
+    res.beta_fp64, res.se_fp64 = ref.beta, ref.se
+    res.beta_rel_err_vs_fp64 = _rel_err(res.beta, ref.beta)
+    res.se_rel_err_vs_fp64 = _rel_err(res.se, ref.se)
+    return res
+
+
 def fe_gpu_estimate(cfg: fe_runtime_config, header: Optional[fe_dataset_header], host: fe_host_arrays,
                     group_sizes: Optional[Sequence[int]] = None, stream: Optional[int] = None,
                     profile: bool = False) -> fe_estimation_result:
@@ -168,7 +199,8 @@ def fe_gpu_estimate(cfg: fe_runtime_config, header: Optional[fe_dataset_header],
                                     se.ctypes.data_as(C.POINTER(C.c_double)), C.byref(res))
     N.check(st, "fegb_estimate_host")
     del keep
-    return _result_from(res, beta[:k].copy(), se[:k].copy(), cfg, header)
+    out = _result_from(res, beta[:k].copy(), se[:k].copy(), cfg, header)
+    return _attach_fp64_errors(out, cfg, lambda c64: fe_gpu_estimate(c64, header, host, group_sizes, stream))
 
 
 def fe_gpu_estimate_device(cfg: fe_runtime_config, n: int, k: int, l: int, d_y: int, d_W: Optional[int],
@@ -191,7 +223,9 @@ def fe_gpu_estimate_device(cfg: fe_runtime_config, n: int, k: int, l: int, d_y: 
                                       se.ctypes.data_as(C.POINTER(C.c_double)), C.byref(res))
     N.check(st, "fegb_estimate_device")
     del keep
-    return _result_from(res, beta[:k].copy(), se[:k].copy(), cfg, header)
+    out = _result_from(res, beta[:k].copy(), se[:k].copy(), cfg, header)
+    return _attach_fp64_errors(out, cfg, lambda c64: fe_gpu_estimate_device(c64, n, k, l, d_y, d_W, d_Z, d_fe_ids,
+                                                                            group_sizes, stream, header))
 
 
 @dataclass

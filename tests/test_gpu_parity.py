@@ -191,3 +191,22 @@ def test_cg_schur_two_swept_dimensions(built, precision, g, k):
     assert res.fe_iterations < 60
     assert rel(res.beta, ref.beta) < BETA_RTOL
     assert rel(res.se, ref.se) < SE_RTOL
+
+
+def test_verify_fp64_reports_per_coefficient_errors(built):
+    """verify_fp64: the mixed-precision fit carries, per coefficient and SE,
+    its relative error against the plain FP64 form on the same inputs; both
+    fits are within the parity bar of the oracle."""
+    hdr, host = worker_firm_panel(n_workers=20000, n_firms=2000, n_periods=10, switch_prob=0.1, seed=6)
+    cfg = fe_runtime_config(fe_tolerance=1e-8, fe_max_iterations=20000, cluster_fe_dims=[1, 2, 3],
+                            precision="mixed", demean_cg=True, verify_fp64=True)
+    res = fe_gpu_estimate(cfg, hdr, host)
+    assert res.beta_rel_err_vs_fp64 is not None and res.se_rel_err_vs_fp64 is not None
+    assert res.beta_rel_err_vs_fp64.shape == res.beta.shape and res.se_rel_err_vs_fp64.shape == res.se.shape
+    np.testing.assert_allclose(res.beta_rel_err_vs_fp64,
+                               np.abs(res.beta - res.beta_fp64) / np.abs(res.beta_fp64), rtol=1e-12, atol=0)
+    assert np.max(res.beta_rel_err_vs_fp64) < BETA_RTOL
+    assert np.max(res.se_rel_err_vs_fp64) < SE_RTOL
+    ref = O.gpu_estimate(host.y, host.W, host.fe_ids, tol=1e-11, max_iter=200000, cluster_dims=[1, 2, 3])
+    assert rel(res.beta_fp64, ref.beta) < BETA_RTOL
+    assert rel(res.se_fp64, ref.se) < SE_RTOL

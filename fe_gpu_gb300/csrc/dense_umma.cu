@@ -23,12 +23,24 @@
 //
 // Data movement: the tile's count bytes and row data are contiguous runs in
 // global memory and are fetched by cp.async.bulk (the TMA's bulk copy engine)
-// into a double-buffered stage, completing on an mbarrier; the next tile's
-// copies are in flight while this tile is processed. A 2-D tensor map does not
-// apply: its row strides must be multiples of 16 bytes, and these rows are Gs
-// bytes (30 at the 150M-row panel) and C floats (36 bytes) long. The CUDA cores
-// convert the counts to BF16 in the MMA operand layout, form u and its pieces,
-// and read the accumulators back from tensor memory with tcgen05.ld.
+// into double-buffered stages completing on mbarriers, the counts three tiles
+// and the rows two tiles ahead of their use. A 2-D tensor map does not apply:
+// its row strides must be multiples of 16 bytes, and these rows are Gs bytes
+// (30 at the 150M-row panel) and C floats (36 bytes) long. The CUDA cores
+// convert the counts to BF16 in the MMA operand layout (a byte placed in the
+// mantissa of 2^23 and 2^23 subtracted: exact, no conversion unit), form u and
+// its pieces, and read the accumulators back from tensor memory with
+// tcgen05.ld. E is double-buffered in tensor memory, so the MMA of tile i + 1
+// runs while the CUDA cores finish tile i.
+//
+// The small-side product uses M = 64 (48 rows used): its accumulator row r
+// sits in tensor-memory lane (r / 16) * 32 + r % 16, so piece p's 16 rows are
+// lanes 0..15 of warp p.
+//
+// Grid: one wave of persistent CTAs (4 per SM at these shared-memory sizes),
+// each over a contiguous range of whole tiles; the small-side partial sums are
+// one slot per CTA, and the slots past the grid are written as zeros, so the
+// fold that follows sees a fixed number of slots.
 //
 // Shared-memory operand layout: the canonical no-swizzle layout of tcgen05
 // descriptors, built of 8 x 16-byte core matrices. A core matrix holds 8 rows
@@ -59,10 +71,18 @@ constexpr int UT = 128;        // groups per tile (= threads per CTA: thread r o
 constexpr int UCP = 16;        // columns per piece block (C <= 16)
 constexpr int UNP = 3;         // BF16 pieces per FP32 value
 constexpr int UN1 = UNP * UCP; // N of the e-side product
-constexpr int UM2 = 128;       // M of the small-side product (rows p * 16 + c; 48 used)
-constexpr int TMEM_COLS = 128; // tensor-memory columns per CTA: E at [0, 48), D2 at [64, 64 + KT)
-constexpr int D2_COL = 64;
+constexpr int UM2 = 64;        // M of the small-side product (rows p * 16 + c; 48 used)
 constexpr unsigned long long WAIT_LIMIT_NS = 2000000000ull;  // 2 s per wait
+
+// Tensor-memory columns: two E buffers (tile i in buffer i & 1) and the D2
+// accumulator; 128 columns when the small dimension has at most 32 groups.
+template <int KT>
+struct TmemPlan {
+    static constexpr int E0 = 0;
+    static constexpr int E1 = UN1;
+    static constexpr int D2 = KT <= 32 ? 2 * UN1 : 128;
+    static constexpr int COLS = KT <= 32 ? 128 : 256;
+};
 
 __device__ int g_umma_error;  // nonzero: a wait of the tensor-core pass ran out of time
 
@@ -173,18 +193,20 @@ struct UmmaArgs {
     int ld;
     int C;
     long long per;        // groups per CTA (a multiple of UT)
-    double* partials;     // [block][Gs][C] small-side sums, or null
+    int nparts;           // partial slots (>= the grid); slots past the grid are zeroed
+    double* partials;     // [slot][Gs][C] small-side sums, or null
     float* extra;         // plain form: Ge x C (+)= M ps, or null
     int accumulate;
     const float* sums;    // Schur form: Ge x C, the primary's stream sums
     const int32_t* counts;
     float* table;         // Schur form: u rows (stride ld)
-    int bulk_counts;      // counts are 16-byte aligned: copied in bulk
+    int bulk_counts;      // counts are 16-byte aligned: copied in bulk with the sums
     uint32_t raw_bytes;   // stage sizes (multiples of 128)
     uint32_t row_bytes;
 };
 
-// Shared-memory plan (bytes from the 1024-aligned dynamic base).
+// Shared-memory plan (bytes from the dynamic base): S pieces, two count
+// tiles, the U tile, two raw-count stages and two row stages.
 struct UmmaSmem {
     uint32_t b1, cnt0, cnt1, u, raw0, raw1, row0, row1, total;
 };
@@ -202,44 +224,61 @@ __host__ __device__ inline UmmaSmem umma_smem_plan(int KT, uint32_t raw_bytes, u
     return s;
 }
 
+// exact float of the byte b of a 32-bit word (2^23 + b as an FP32 bit pattern, minus 2^23)
+__device__ __forceinline__ float byte_f32(uint32_t w, uint32_t sel) {
+    return __uint_as_float(__byte_perm(w, 0x4B000000u, sel)) - 8388608.0f;
+}
+
+// Persistent pass: CTA b covers groups [b per, (b + 1) per) tile by tile.
+// Per tile i (thread = group row of the tile):
+//   (a) counts of tile i + 1 -> BF16 count tile; S1; MMA E(i + 1) = counts . S
+//   (b) wait E(i); u or the e-side output of tile i; pieces of u / pe -> U; S2;
+//       MMA D2 += U' . counts(i)
+// with the raw counts fetched three tiles ahead and the rows two tiles ahead
+// (bulk copies on per-stage mbarriers), so that copies, E(i + 1) and D2(i)
+// overlap the CUDA-core work of tile i.
 template <int KT, bool SCHUR>
 __global__ void __launch_bounds__(UT) dense_umma_kernel(UmmaArgs a) {
+    using TP = TmemPlan<KT>;
     extern __shared__ __align__(1024) unsigned char sm[];
-    __shared__ __align__(8) uint64_t bars[4];  // 0, 1: tile copies; 2: e-side MMA; 3: small-side MMA
+    // 0, 1: raw-count stages; 2, 3: row stages; 4, 5: E buffers; 6: D2
+    __shared__ __align__(8) uint64_t bars[7];
     __shared__ uint32_t tmem_base_s;
-    __shared__ int abort_s;
-    const int tid = threadIdx.x, warp = tid >> 5;
-    const long long g0 = (long long)blockIdx.x * a.per;
-    const long long g1 = min(a.Ge, g0 + a.per);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int Gs = a.Gs, C = a.C, ld = a.ld;
     const bool small = a.partials != nullptr;
     const bool need_e = SCHUR || a.extra != nullptr;
+    // partial slots past the grid hold zeros
+    if (small)
+        for (long long slot = (long long)blockIdx.x + gridDim.x; slot < a.nparts; slot += gridDim.x)
+            for (int j = tid; j < Gs * C; j += UT) a.partials[slot * Gs * C + j] = 0.0;
     double* const part = small ? a.partials + (long long)blockIdx.x * Gs * C : nullptr;
-    if (g0 >= g1) {  // no groups: zero partials
+    const long long g0 = (long long)blockIdx.x * a.per;
+    const long long g1 = min(a.Ge, g0 + a.per);
+    if (g0 >= g1) {
         if (small)
-            for (int i = tid; i < Gs * C; i += UT) part[i] = 0.0;
+            for (int j = tid; j < Gs * C; j += UT) part[j] = 0.0;
         return;
     }
     const UmmaSmem L = umma_smem_plan(KT, a.raw_bytes, a.row_bytes);
     constexpr uint32_t CORE_ROW = (uint32_t)(KT / 8) * 128;  // bytes of one 8-group row of count cores
     constexpr uint32_t U_LBO = (uint32_t)(UM2 / 8) * 128;    // bytes between 8-group blocks of the U tile
     const uint32_t sbase = smem_u32(sm);
+    const uint32_t sums_bytes = (uint32_t)(((UT * C * 4) + 15) / 16 * 16);
 
-    // tensor memory, barriers, U tile zeroed (rows 48.. stay zero), S pieces
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base_s)),
-                     "r"(TMEM_COLS));
+                     "r"(TP::COLS));
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
     }
     if (tid == 0) {
-        for (int i = 0; i < 4; ++i) mbar_init(&bars[i], 1);
+        for (int i = 0; i < 7; ++i) mbar_init(&bars[i], 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-        abort_s = 0;
     }
+    // U tile zeroed once (rows 48..63 stay zero), S pieces (K-major: n = p * 16 + c, k = t)
     for (uint32_t o = tid * 16; o < (uint32_t)(UM2 * UT * 2); o += UT * 16)
         *reinterpret_cast<uint4*>(sm + L.u + o) = make_uint4(0, 0, 0, 0);
     if (need_e) {
-        // S pieces, K-major: B operand n = p * 16 + c (48 rows), k = t; core (n/8, t/8)
         for (int i = tid; i < UN1 * KT; i += UT) {
             const int n = i / KT, t = i - (i / KT) * KT;
             const int p = n / UCP, c = n - p * UCP;
@@ -258,132 +297,162 @@ __global__ void __launch_bounds__(UT) dense_umma_kernel(UmmaArgs a) {
     fence_after_sync();
     const uint32_t tmem = tmem_base_s;
     const uint32_t t_lane = (uint32_t)(warp * 32) << 16;
-
     const int ntiles = (int)((g1 - g0 + UT - 1) / UT);
-    auto full_tile = [&](long long tile) { return tile + UT <= g1; };
-    // the elected thread starts the copies of a tile into a stage (or, for a
-    // ragged tile, completes the stage's phase without copies: the threads
-    // then load it with plain loads)
-    auto issue = [&](int stg, long long tile) {
-        uint64_t* bar = &bars[stg];
-        unsigned char* raw = sm + (stg ? L.raw1 : L.raw0);
-        unsigned char* row = sm + (stg ? L.row1 : L.row0);
-        if (!full_tile(tile)) {
+    auto tile_of = [&](int j) { return g0 + (long long)j * UT; };
+    auto full = [&](int j) { return tile_of(j) + UT <= g1; };
+    // copy issue (elected thread): a ragged tile completes its stage's phase
+    // without copies; its threads read their rows from global memory
+    auto issue_raw = [&](int j) {
+        uint64_t* bar = &bars[j & 1];
+        if (!full(j)) {
             mbar_arrive(bar);
             return;
         }
         const uint32_t cb = (uint32_t)(UT * Gs);
-        uint32_t rb;
-        if (SCHUR)
-            rb = (uint32_t)(UT * C * 4) + (a.bulk_counts ? (uint32_t)(UT * 4) : 0u);
-        else
-            rb = small ? (uint32_t)(UT * ld * 4) : 0u;
-        mbar_arrive_tx(bar, cb + rb);
-        bulk_copy(raw, a.M + tile * Gs, cb, bar);
+        mbar_arrive_tx(bar, cb);
+        bulk_copy(sm + ((j & 1) ? L.raw1 : L.raw0), a.M + tile_of(j) * Gs, cb, bar);
+    };
+    const bool rows_needed = SCHUR || small;
+    auto issue_rows = [&](int j) {
+        uint64_t* bar = &bars[2 + (j & 1)];
+        if (!full(j) || !rows_needed) {
+            mbar_arrive(bar);
+            return;
+        }
+        unsigned char* row = sm + ((j & 1) ? L.row1 : L.row0);
         if (SCHUR) {
-            bulk_copy(row, a.sums + tile * C, (uint32_t)(UT * C * 4), bar);
-            if (a.bulk_counts) bulk_copy(row + ((UT * C * 4 + 15) / 16) * 16, a.counts + tile, UT * 4, bar);
-        } else if (small) {
-            bulk_copy(row, a.pe + tile * ld, (uint32_t)(UT * ld * 4), bar);
+            const uint32_t cbytes = a.bulk_counts ? (uint32_t)(UT * 4) : 0u;
+            mbar_arrive_tx(bar, (uint32_t)(UT * C * 4) + cbytes);
+            bulk_copy(row, a.sums + tile_of(j) * C, (uint32_t)(UT * C * 4), bar);
+            if (cbytes) bulk_copy(row + sums_bytes, a.counts + tile_of(j), cbytes, bar);
+        } else {
+            mbar_arrive_tx(bar, (uint32_t)(UT * ld * 4));
+            bulk_copy(row, a.pe + tile_of(j) * ld, (uint32_t)(UT * ld * 4), bar);
         }
     };
-    if (tid == 0) issue(0, g0);
-
     bool failed = false;
-    for (int i = 0; i < ntiles; ++i) {
-        const long long tile = g0 + (long long)i * UT;
+    // counts of tile j -> count tile j & 1 (BF16 core matrices (tid/8, t/8), row tid % 8)
+    auto convert = [&](int j) -> bool {
+        if (!mbar_wait(&bars[j & 1], (uint32_t)((j >> 1) & 1))) return false;
+        const long long tile = tile_of(j);
         const int nt = (int)min((long long)UT, g1 - tile);
-        const int stg = i & 1;
-        unsigned char* const raw = sm + (stg ? L.raw1 : L.raw0);
-        unsigned char* const row = sm + (stg ? L.row1 : L.row0);
-        const uint32_t cnt_off = stg ? L.cnt1 : L.cnt0;
-        if (tid == 0 && i + 1 < ntiles) issue(stg ^ 1, tile + UT);
-        bool ok = mbar_wait(&bars[stg], (uint32_t)((i >> 1) & 1));
+        const bool mine = tid < nt;
+        const unsigned char* src = full(j) ? sm + ((j & 1) ? L.raw1 : L.raw0) + tid * Gs : a.M + (tile + tid) * Gs;
+        const uint32_t cnt_off = (j & 1) ? L.cnt1 : L.cnt0;
+#pragma unroll
+        for (int tb = 0; tb < KT / 8; ++tb) {
+            uint32_t w[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const int t0 = tb * 8 + 2 * q;
+                uint32_t pair = 0;
+                if (mine && t0 < Gs) pair = src[t0] | ((t0 + 1 < Gs ? (uint32_t)src[t0 + 1] : 0u) << 8);
+                const float x0 = byte_f32(pair, 0x7540u), x1 = byte_f32(pair, 0x7541u);
+                w[q] = pack2(__float2bfloat16_rn(x0), __float2bfloat16_rn(x1));
+            }
+            *reinterpret_cast<uint4*>(sm + cnt_off + (uint32_t)(tid / 8) * CORE_ROW + (uint32_t)tb * 128 +
+                                      (uint32_t)(tid % 8) * 16) = make_uint4(w[0], w[1], w[2], w[3]);
+        }
+        fence_async_smem();
+        return true;
+    };
+    auto issue_e = [&](int j) {
+        const uint32_t cnt_off = (j & 1) ? L.cnt1 : L.cnt0;
+        const uint32_t id = umma_idesc(UT, UN1, 0, 0);
+        const uint32_t ecol = (j & 1) ? TP::E1 : TP::E0;
+#pragma unroll
+        for (int s = 0; s < KT / 16; ++s)
+            umma_bf16(tmem + ecol, umma_desc(sbase + cnt_off + s * 256, 128, CORE_ROW),
+                      umma_desc(sbase + L.b1 + s * 256, 128, CORE_ROW), id, s > 0);
+        umma_commit(&bars[4 + (j & 1)]);
+    };
+
+    // prologue: copies of tiles 0..1 (raw and rows); counts of tile 0 and its E
+    if (tid == 0) {
+        for (int j = 0; j < 2 && j < ntiles; ++j) issue_raw(j);
+        for (int j = 0; j < 2 && j < ntiles; ++j) issue_rows(j);
+    }
+    bool ok = convert(0);
+    fence_before_sync();
+    if (__syncthreads_or(!ok)) failed = true;
+    fence_after_sync();
+    if (!failed && tid == 0) {
+        if (need_e) issue_e(0);
+        if (ntiles > 2) issue_raw(2);  // raw stage 0 was consumed by the conversion of tile 0
+    }
+
+    int d2_waited = -1;  // the last tile whose D2 MMA is known complete
+    for (int i = 0; i < ntiles && !failed; ++i) {
+        const long long tile = tile_of(i);
+        const int nt = (int)min((long long)UT, g1 - tile);
+        const bool mine = tid < nt;
+        // (a) counts of tile i + 1 (its count tile was read by the MMAs of tile i - 1)
+        ok = true;
+        if (i + 1 < ntiles) {
+            if (small && i >= 1) {
+                ok = mbar_wait(&bars[6], (uint32_t)((i - 1) & 1));
+                d2_waited = i - 1;
+            }
+            ok = ok && convert(i + 1);
+        }
+        fence_before_sync();
         if (__syncthreads_or(!ok)) {
             failed = true;
             break;
         }
-        float* const srow = reinterpret_cast<float*>(row);
-        const int32_t* cnt_row = reinterpret_cast<const int32_t*>(row + ((UT * C * 4 + 15) / 16) * 16);
-        const bool ragged = !full_tile(tile);
-        if (ragged) {
-            // plain loads of the ragged tile (the stage's copy phase completed empty)
-            for (int j = tid; j < nt * Gs; j += UT) raw[j] = a.M[tile * Gs + j];
-            if (SCHUR) {
-                for (int j = tid; j < nt * C; j += UT) srow[j] = a.sums[tile * C + j];
-            } else if (small) {
-                for (int j = tid; j < nt * ld; j += UT) srow[j] = a.pe[tile * ld + j];
-            }
-        }
-        if (SCHUR && (ragged || !a.bulk_counts)) {
-            if (tid < nt) const_cast<int32_t*>(cnt_row)[tid] = a.counts[tile + tid];
-        }
-        if (ragged || (SCHUR && !a.bulk_counts)) __syncthreads();
-
-        // counts row tid -> BF16 core matrices (tid/8, t/8), row tid % 8
-        {
-            const unsigned char* src = raw + tid * Gs;
-#pragma unroll
-            for (int tb = 0; tb < KT / 8; ++tb) {
-                uint32_t w[4];
-#pragma unroll
-                for (int q = 0; q < 4; ++q) {
-                    const int t0 = tb * 8 + 2 * q;
-                    const float x0 = (tid < nt && t0 < Gs) ? (float)src[t0] : 0.0f;
-                    const float x1 = (tid < nt && t0 + 1 < Gs) ? (float)src[t0 + 1] : 0.0f;
-                    w[q] = pack2(__float2bfloat16_rn(x0), __float2bfloat16_rn(x1));
-                }
-                *reinterpret_cast<uint4*>(sm + cnt_off + (uint32_t)(tid / 8) * CORE_ROW + (uint32_t)tb * 128 +
-                                          (uint32_t)(tid % 8) * 16) = make_uint4(w[0], w[1], w[2], w[3]);
-            }
-        }
-        fence_async_smem();
-        fence_before_sync();
-        __syncthreads();
         fence_after_sync();
-
-        float e[UN1];
-        if (need_e) {
-            if (tid == 0) {
-                const uint32_t id = umma_idesc(UT, UN1, 0, 0);
+        if (tid == 0 && i + 1 < ntiles) {
+            if (need_e) issue_e(i + 1);
+            if (i + 3 < ntiles) issue_raw(i + 3);  // raw stage (i + 1) & 1 was just consumed
+        }
+        // (b) this tile: its rows, then E(i)
+        ok = mbar_wait(&bars[2 + (i & 1)], (uint32_t)((i >> 1) & 1));
+        float v[UCP];
 #pragma unroll
-                for (int s = 0; s < KT / 16; ++s)
-                    umma_bf16(tmem, umma_desc(sbase + cnt_off + s * 256, 128, CORE_ROW),
-                              umma_desc(sbase + L.b1 + s * 256, 128, CORE_ROW), id, s > 0);
-                umma_commit(&bars[2]);
+        for (int c = 0; c < UCP; ++c) v[c] = 0.0f;
+        int n_g = 0;
+        const float* srow = reinterpret_cast<const float*>(sm + ((i & 1) ? L.row1 : L.row0));
+        if (ok && mine) {
+            if (SCHUR) {
+                const bool f = full(i);
+#pragma unroll
+                for (int c = 0; c < UCP; ++c)
+                    if (c < C) v[c] = f ? srow[tid * C + c] : a.sums[(tile + tid) * C + c];
+                n_g = (f && a.bulk_counts) ? reinterpret_cast<const int32_t*>(sm + ((i & 1) ? L.row1 : L.row0) +
+                                                                             sums_bytes)[tid]
+                                           : a.counts[tile + tid];
+            } else if (small) {
+                const bool f = full(i);
+#pragma unroll
+                for (int c = 0; c < UCP; ++c)
+                    if (c < C) v[c] = f ? srow[tid * ld + c] : a.pe[(tile + tid) * ld + c];
             }
-            ok = mbar_wait(&bars[2], (uint32_t)(i & 1));
+        }
+        if (need_e) {
+            ok = ok && mbar_wait(&bars[4 + (i & 1)], (uint32_t)((i >> 1) & 1));
             if (__syncthreads_or(!ok)) {
                 failed = true;
                 break;
             }
             fence_after_sync();
-            tmem_ld16(tmem + t_lane + 0, e, 0);
-            tmem_ld16(tmem + t_lane + 16, e, 16);
-            tmem_ld16(tmem + t_lane + 32, e, 32);
+            float e[UN1];
+            const uint32_t ecol = (i & 1) ? TP::E1 : TP::E0;
+            tmem_ld16(tmem + t_lane + ecol + 0, e, 0);
+            tmem_ld16(tmem + t_lane + ecol + 16, e, 16);
+            tmem_ld16(tmem + t_lane + ecol + 32, e, 32);
             tmem_wait_ld();
-        }
-        float v[UCP];
-#pragma unroll
-        for (int c = 0; c < UCP; ++c) v[c] = 0.0f;
-        if (SCHUR) {
-            const int n = tid < nt ? cnt_row[tid] : 0;
-            const float rn = n > 0 ? 1.0f / (float)n : 0.0f;
-#pragma unroll
-            for (int c = 0; c < UCP; ++c) {
-                if (c < C && tid < nt) {
-                    const float ec = (e[32 + c] + e[16 + c]) + e[c];
-                    v[c] = n > 0 ? (srow[tid * C + c] - ec) * rn : 0.0f;
-                }
-            }
-            if (tid < nt) {
-                float* trow = a.table + (tile + tid) * ld;
+            if (SCHUR) {
+                const float rn = n_g > 0 ? 1.0f / (float)n_g : 0.0f;
 #pragma unroll
                 for (int c = 0; c < UCP; ++c)
-                    if (c < C) trow[c] = v[c];
-            }
-        } else {
-            if (a.extra && tid < nt) {
+                    if (c < C) v[c] = n_g > 0 ? (v[c] - ((e[32 + c] + e[16 + c]) + e[c])) * rn : 0.0f;
+                if (mine) {
+                    float* trow = a.table + (tile + tid) * ld;
+#pragma unroll
+                    for (int c = 0; c < UCP; ++c)
+                        if (c < C) trow[c] = v[c];
+                }
+            } else if (mine) {
                 float* xr = a.extra + (tile + tid) * C;
 #pragma unroll
                 for (int c = 0; c < UCP; ++c) {
@@ -393,79 +462,82 @@ __global__ void __launch_bounds__(UT) dense_umma_kernel(UmmaArgs a) {
                     }
                 }
             }
-            if (small && tid < nt) {
-#pragma unroll
-                for (int c = 0; c < UCP; ++c)
-                    if (c < C) v[c] = srow[tid * ld + c];
-            }
+        } else if (__syncthreads_or(!ok)) {
+            failed = true;
+            break;
         }
         if (small) {
-            // the previous tile's small-side MMA must be done with the U tile
-            ok = i == 0 || mbar_wait(&bars[3], (uint32_t)((i - 1) & 1));
+            // the U tile was read by D2(i - 1)
+            ok = true;
+            if (i >= 1 && d2_waited < i - 1) {
+                ok = mbar_wait(&bars[6], (uint32_t)((i - 1) & 1));
+                d2_waited = i - 1;
+            }
             if (__syncthreads_or(!ok)) {
                 failed = true;
                 break;
             }
             // U pieces, MN-major: row m = p * 16 + c, core (m/8, tid/8), row tid % 8
 #pragma unroll
-            for (int p = 0; p < UNP; ++p) {
+            for (int hb = 0; hb < 2; ++hb) {
+                if (hb * 8 >= C) break;
+                uint32_t w[UNP][4];
 #pragma unroll
-                for (int hb = 0; hb < 2; ++hb) {
-                    uint32_t w[4];
+                for (int q = 0; q < 4; ++q) {
+                    __nv_bfloat16 h0, m0, l0, h1, m1, l1;
+                    split3(v[hb * 8 + 2 * q], h0, m0, l0);
+                    split3(v[hb * 8 + 2 * q + 1], h1, m1, l1);
+                    w[0][q] = pack2(h0, h1);
+                    w[1][q] = pack2(m0, m1);
+                    w[2][q] = pack2(l0, l1);
+                }
 #pragma unroll
-                    for (int q = 0; q < 4; ++q) {
-                        __nv_bfloat16 pc[2];
-#pragma unroll
-                        for (int z = 0; z < 2; ++z) {
-                            __nv_bfloat16 h, m, l;
-                            split3(v[hb * 8 + 2 * q + z], h, m, l);
-                            pc[z] = p == 0 ? h : (p == 1 ? m : l);
-                        }
-                        w[q] = pack2(pc[0], pc[1]);
-                    }
+                for (int p = 0; p < UNP; ++p) {
                     const uint32_t mb = (uint32_t)(p * 2 + hb);
                     *reinterpret_cast<uint4*>(sm + L.u + mb * 128 + (uint32_t)(tid / 8) * U_LBO +
-                                              (uint32_t)(tid % 8) * 16) = make_uint4(w[0], w[1], w[2], w[3]);
+                                              (uint32_t)(tid % 8) * 16) =
+                        make_uint4(w[p][0], w[p][1], w[p][2], w[p][3]);
                 }
             }
             fence_async_smem();
         }
         fence_before_sync();
-        __syncthreads();
+        __syncthreads();  // S2
         fence_after_sync();
-        if (small && tid == 0) {
-            const uint32_t id = umma_idesc(UM2, KT, 1, 1);
+        if (tid == 0) {
+            if (small) {
+                const uint32_t id = umma_idesc(UM2, KT, 1, 1);
+                const uint32_t cnt_off = (i & 1) ? L.cnt1 : L.cnt0;
 #pragma unroll
-            for (int s = 0; s < UT / 16; ++s)
-                umma_bf16(tmem + D2_COL, umma_desc(sbase + L.u + s * 2 * U_LBO, U_LBO, 128),
-                          umma_desc(sbase + cnt_off + s * 2 * CORE_ROW, CORE_ROW, 128), id, (i > 0 || s > 0) ? 1 : 0);
-            umma_commit(&bars[3]);
+                for (int s = 0; s < UT / 16; ++s)
+                    umma_bf16(tmem + TP::D2, umma_desc(sbase + L.u + s * 2 * U_LBO, U_LBO, 128),
+                              umma_desc(sbase + cnt_off + s * 2 * CORE_ROW, CORE_ROW, 128), id,
+                              (i > 0 || s > 0) ? 1 : 0);
+                umma_commit(&bars[6]);
+            }
+            if (i + 2 < ntiles) issue_rows(i + 2);  // row stage i & 1 was read before S2
         }
     }
     if (failed) {
-        if (tid == 0) {
-            atomicExch(&g_umma_error, 1);
-            abort_s = 1;
-        }
+        if (tid == 0) atomicExch(&g_umma_error, 1);
     } else if (small) {
-        const bool ok = mbar_wait(&bars[3], (uint32_t)((ntiles - 1) & 1));
-        if (__syncthreads_or(!ok)) {
+        const bool okf = mbar_wait(&bars[6], (uint32_t)((ntiles - 1) & 1));
+        if (__syncthreads_or(!okf)) {
             failed = true;
             if (tid == 0) atomicExch(&g_umma_error, 1);
         } else {
             fence_after_sync();
-            // D2 row m (TMEM lane m) -> shared [m][t] (floats, over the U tile)
+            // D2 row m = p * 16 + c sits in TMEM lane p * 32 + c (M = 64 layout):
+            // warps 0..2, lanes 0..15 -> shared [m][t] floats over the U tile
             float* d2s = reinterpret_cast<float*>(sm + L.u);
-            __syncthreads();
-            if (warp < 2) {
-                float d[KT];
+            float d[KT];
 #pragma unroll
-                for (int c0 = 0; c0 < KT; c0 += 16) tmem_ld16(tmem + t_lane + D2_COL + c0, d, c0);
-                tmem_wait_ld();
-                if (tid < UN1)
+            for (int c0 = 0; c0 < KT; c0 += 16) tmem_ld16(tmem + t_lane + TP::D2 + c0, d, c0);
+            tmem_wait_ld();
+            __syncthreads();  // the U tile is free (D2 complete); reuse it for the readback
+            if (warp < UNP && lane < UCP)
 #pragma unroll
-                    for (int t = 0; t < KT; ++t) d2s[tid * KT + t] = d[t];
-            }
+                for (int t = 0; t < KT; ++t) d2s[(warp * UCP + lane) * KT + t] = d[t];
             __syncthreads();
             for (int j = tid; j < Gs * C; j += UT) {
                 const int t = j / C, c = j - t * C;
@@ -475,16 +547,38 @@ __global__ void __launch_bounds__(UT) dense_umma_kernel(UmmaArgs a) {
     }
     fence_before_sync();
     __syncthreads();
-    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS));
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TP::COLS));
 }
 
 template <int KT, bool SCHUR>
-int launch_umma(const UmmaArgs& a, int nb, cudaStream_t s) {
+int launch_umma(UmmaArgs a, cudaStream_t s) {
     const UmmaSmem L = umma_smem_plan(KT, a.raw_bytes, a.row_bytes);
     static const cudaError_t attr = cudaFuncSetAttribute(dense_umma_kernel<KT, SCHUR>,
                                                          cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     if (attr != cudaSuccess) return set_cuda_error(attr, "dense tensor-core pass attr");
-    dense_umma_kernel<KT, SCHUR><<<nb, UT, L.total, s>>>(a);
+    // one wave of persistent CTAs (at most the partial slots), each over a
+    // contiguous range of whole tiles. Resident CTAs per SM for this
+    // shared-memory size are cached per size, so the calls made during a
+    // stream capture make no runtime queries.
+    static thread_local uint32_t cached_bytes = 0;
+    static thread_local int cached_sms = 0, cached_occ = 0;
+    if (cached_bytes != L.total) {
+        int dev = 0;
+        FEGB_CUDA(cudaGetDevice(&dev), "cudaGetDevice");
+        FEGB_CUDA(cudaDeviceGetAttribute(&cached_sms, cudaDevAttrMultiProcessorCount, dev), "SM count");
+        FEGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&cached_occ, dense_umma_kernel<KT, SCHUR>, UT,
+                                                                L.total),
+                  "occupancy");
+        cached_bytes = L.total;
+    }
+    // tensor memory per SM: 512 columns
+    const int occ = std::max(1, std::min(cached_occ, 512 / TmemPlan<KT>::COLS));
+    const long long tiles = (a.Ge + UT - 1) / UT;
+    int grid = (int)std::min<long long>({(long long)a.nparts, (long long)occ * cached_sms, tiles});
+    grid = std::max(grid, 1);
+    const long long tiles_per = (tiles + grid - 1) / grid;
+    a.per = tiles_per * UT;
+    dense_umma_kernel<KT, SCHUR><<<grid, UT, L.total, s>>>(a);
     FEGB_LAUNCH_CHECK("dense small-G pair product (tcgen05)");
     return 0;
 }
@@ -509,9 +603,7 @@ int launch_dense_pair_umma(const uint8_t* M, long long Ge, int Gs, const float* 
     a.ps = ps;
     a.ld = ld;
     a.C = C;
-    const int nb = dense_chunks(Ge);
-    long long per = (Ge + nb - 1) / nb;
-    a.per = (per + UT - 1) / UT * UT;
+    a.nparts = dense_chunks(Ge);
     a.partials = partials;
     a.extra = schur ? nullptr : extra;
     a.accumulate = accumulate;
@@ -523,8 +615,8 @@ int launch_dense_pair_umma(const uint8_t* M, long long Ge, int Gs, const float* 
     const uint32_t rb = schur ? (uint32_t)(((UT * C * 4 + 15) / 16) * 16 + UT * 4) : (uint32_t)(UT * ld * 4);
     a.row_bytes = (rb + 127) / 128 * 128;
     *launched = true;
-    if (Gs <= 32) return schur ? launch_umma<32, true>(a, nb, s) : launch_umma<32, false>(a, nb, s);
-    return schur ? launch_umma<64, true>(a, nb, s) : launch_umma<64, false>(a, nb, s);
+    if (Gs <= 32) return schur ? launch_umma<32, true>(a, s) : launch_umma<32, false>(a, s);
+    return schur ? launch_umma<64, true>(a, s) : launch_umma<64, false>(a, s);
 }
 
 int dense_umma_error(int* flag, bool reset, cudaStream_t s) {

@@ -1831,13 +1831,17 @@ __device__ __forceinline__ void cg_sub_row(const T* __restrict__ row, int cw, T 
 }
 
 #ifndef CG_ROWS_MINB
-#define CG_ROWS_MINB 3
+#define CG_ROWS_MINB 4
 #endif
 
+// Run state of one lane. The lane's first run (its head, which may continue
+// the previous lane's last run) is parked in shared memory (head[i * 32], one
+// column per 32 consecutive words, no bank conflicts) once a second run starts,
+// so that only the current run is held in registers.
 template <typename T, int TILE>
 struct CGRun {
-    T head[TILE];
     T run[TILE];
+    T* head;  // this lane's head slot: head[i * 32] = column i
     int firstg;
     int cur;
     bool single;
@@ -1858,7 +1862,7 @@ __device__ __forceinline__ void cg_run_push(CGRun<T, TILE>& st, int g, const T (
     if (g != st.cur) {
         if (st.single) {
 #pragma unroll
-            for (int i = 0; i < TILE; ++i) st.head[i] = st.run[i];
+            for (int i = 0; i < TILE; ++i) st.head[i * 32] = st.run[i];
             st.single = false;
         } else {
             // a run that starts and ends inside this lane is complete
@@ -1900,12 +1904,11 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 && CGR_TILE <= 12) ? CG_R
     const int32_t* __restrict__ gseq = p.gseq;
     const unsigned long long keep = l2_policy_evict_last();
 
+    __shared__ T s_head[8][CGR_TILE * 32];  // one slot per lane of each of the block's 8 warps
     CGRun<T, CGR_TILE> st;
+    st.head = &s_head[threadIdx.x >> 5][lane];
 #pragma unroll
-    for (int i = 0; i < CGR_TILE; ++i) {
-        st.head[i] = T(0);
-        st.run[i] = T(0);
-    }
+    for (int i = 0; i < CGR_TILE; ++i) st.run[i] = T(0);
     st.firstg = -1;
     st.cur = -1;
     st.single = true;
@@ -1982,10 +1985,6 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 && CGR_TILE <= 12) ? CG_R
     const int firstg = st.firstg;
     const bool single = st.single;
     const int lastg = st.cur;
-    if (single) {
-#pragma unroll
-        for (int i = 0; i < CGR_TILE; ++i) st.head[i] = st.run[i];
-    }
     // empty lanes (only in the last chunk) are transparent: they continue the
     // previous lane's run with a zero contribution
     const unsigned full = 0xffffffffu;
@@ -2029,7 +2028,7 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 && CGR_TILE <= 12) ? CG_R
 #pragma unroll
     for (int i = 0; i < CGR_TILE; ++i) {
         if (i >= cw) continue;  // uniform across the warp
-        T b = empty ? T(0) : (single ? st.head[i] : st.run[i]);
+        T b = empty ? T(0) : st.run[i];  // a single-run lane's head is its run
 #pragma unroll
         for (int k = 0; k < 5; ++k) {
             const T b_up = __shfl_up_sync(full, b, 1 << k);
@@ -2041,7 +2040,7 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 && CGR_TILE <= 12) ? CG_R
         const long long col = c0 + i;
         if (!empty && !single) {
             // head run of a multi-run lane ends inside this lane
-            const T val = (cont ? in : T(0)) + st.head[i];
+            const T val = (cont ? in : T(0)) + st.head[i * 32];
             if (head_from_start && before)
                 p.head[q * C + col] = (double)val;
             else

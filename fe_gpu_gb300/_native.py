@@ -204,6 +204,9 @@ SIGNATURES = {
     "fegb_group_sizes": (_I, [C.POINTER(C.c_void_p), _I, _LL, _IP]),
     "fegb_drop_singletons": (_I, [C.POINTER(C.c_void_p), _IP, _I, _LL, _P, C.POINTER(C.c_longlong)]),
     "fegb_kernel_launches": (_LL, []),
+    "fegb_set_tuning": (_I, [C.c_char_p, _I]),
+    "fegb_get_tuning": (_I, [C.c_char_p, _IP]),
+    "fegb_reset_tuning": (_I, []),
     "fegb_pool_usage": (_I, [_I, C.POINTER(C.c_ulonglong), C.POINTER(C.c_ulonglong), C.POINTER(C.c_ulonglong)]),
     "fegb_test_dense_pair": (_I, [_P, _LL, _I, _P, _P, _I, _I, _P, _P, _I, _I, _P, _P, _P]),
     "fegb_test_group_sums": (_I, [_P, _LL, _I, _P, _I, _I, _P]),

@@ -98,6 +98,17 @@ class Scratch {
 // Keep the default memory pool's freed blocks cached across calls.
 void configure_mem_pool();
 
+// Launch-shape knobs (process-wide), set through fegb_set_tuning by the host
+// from the autotuner's table (fe_gpu_gb300/autotune.py):
+//   TUNE_DENSE_FORM       -1 default, 0 CUDA-core, 1 tensor-core count-matrix passes
+//   TUNE_CG_COLS_PER_PASS 0 all columns of a row in one pass of the operator
+//                         sweep, else at most 4 or 8 (more passes, fewer registers)
+//   TUNE_SPLIT_GRAM       output pairs per input column from which Gram
+//                         products use the split-FP32 form (>= 1)
+//   TUNE_CG_GRAPH         1 the CG loop runs as a CUDA graph, 0 host-driven
+enum TuneKey { TUNE_DENSE_FORM = 0, TUNE_CG_COLS_PER_PASS, TUNE_SPLIT_GRAM, TUNE_CG_GRAPH, TUNE_COUNT };
+int tuning(TuneKey key);
+
 // ---------------------------------------------------------------------------
 // Device helpers
 // ---------------------------------------------------------------------------

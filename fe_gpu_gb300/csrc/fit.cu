@@ -1950,7 +1950,7 @@ int demean_cg(Problem& P, double tol, int max_iter, int* iterations, int* conver
     FEGB_TRY(cg_alloc<T>(P, B));
     CGGraph<T> G;
     bool use_graph = false;
-    if (!P.profile) {
+    if (!P.profile && tuning(TUNE_CG_GRAPH)) {
         FEGB_TRY(dalloc(*P.scr, &G.ctl, 1, "cg loop state"));
         use_graph = cg_build_graph<T>(P, B, G) == 0;
         if (!use_graph) {

@@ -855,7 +855,7 @@ int crossprod_auto(const MatView& A, const MatView& B, long long n, bool gram, b
                    double beta, double* out, int ldo, cudaStream_t s, Scratch& scr) {
     const long long pairs = gram ? (long long)A.cols * (A.cols + 1) / 2 : (long long)A.cols * B.cols;
     const long long cols = gram ? A.cols : (long long)A.cols + B.cols;
-    if (pairs >= CROSSPROD_SPLIT_PAIRS_PER_COL * cols && n >= 4096)
+    if (pairs >= (long long)tuning(TUNE_SPLIT_GRAM) * cols && n >= 4096)
         return crossprod_split(A, B, n, gram, upper_only, alpha, beta, out, ldo, s, scr);
     return crossprod(A, B, n, gram, upper_only, alpha, beta, out, ldo, s, scr);
 }

@@ -29,7 +29,8 @@ int crossprod(const MatView& A, const MatView& B, long long n, bool gram, bool u
 // per output and folded into FP64 every tile of rows. Relative error per term
 // about 2^-47, against 2^-53 for FP64 products; GB300 issues FP32 at about 60x
 // its FP64 rate, so cross products whose FP64 form is bound by the FP64 pipe
-// (outputs at least CROSSPROD_SPLIT_PAIRS_PER_COL times the input columns)
+// (outputs at least "split_gram_pairs_per_col" times the input columns; the
+// knob's default is CROSSPROD_SPLIT_PAIRS_PER_COL)
 // run several times faster. The FP64 values are split while a tile is loaded;
 // a value beyond the split range sends the whole product to the FP64 path.
 constexpr long long CROSSPROD_SPLIT_PAIRS_PER_COL = 3;

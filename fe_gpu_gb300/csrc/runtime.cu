@@ -53,6 +53,22 @@ std::atomic<long long> g_launches{0};
 void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 long long launches() { return g_launches.load(std::memory_order_relaxed); }
 
+namespace {
+struct TuneSpec {
+    const char* name;
+    int def, lo, hi;
+};
+constexpr TuneSpec kTune[TUNE_COUNT] = {
+    {"dense_form", -1, -1, 1},
+    {"cg_cols_per_pass", 0, 0, 8},
+    {"split_gram_pairs_per_col", 3, 1, 1 << 20},
+    {"cg_graph", 1, 0, 1},
+};
+std::atomic<int> g_tune[TUNE_COUNT] = {{kTune[0].def}, {kTune[1].def}, {kTune[2].def}, {kTune[3].def}};
+}  // namespace
+
+int tuning(TuneKey key) { return g_tune[key].load(std::memory_order_relaxed); }
+
 int num_sms() {
     // per device, computed once; safe to call from several host threads
     static std::mutex mu;
@@ -368,6 +384,38 @@ using namespace fegb;
 extern "C" {
 
 long long fegb_kernel_launches(void) { return fegb::launches(); }
+
+int fegb_set_tuning(const char* key, int value) {
+    using namespace fegb;
+    if (!key) return set_error("fegb_set_tuning: null key");
+    for (int i = 0; i < TUNE_COUNT; ++i)
+        if (std::strcmp(key, kTune[i].name) == 0) {
+            if (value < kTune[i].lo || value > kTune[i].hi)
+                return set_error("fegb_set_tuning: %s = %d outside [%d, %d]", key, value, kTune[i].lo, kTune[i].hi);
+            if (i == TUNE_CG_COLS_PER_PASS && value != 0 && value != 4 && value != 8)
+                return set_error("fegb_set_tuning: cg_cols_per_pass must be 0, 4 or 8 (got %d)", value);
+            g_tune[i].store(value, std::memory_order_relaxed);
+            return set_ok();
+        }
+    return set_error("fegb_set_tuning: unknown key '%s'", key);
+}
+
+int fegb_get_tuning(const char* key, int* value) {
+    using namespace fegb;
+    if (!key || !value) return set_error("fegb_get_tuning: null argument");
+    for (int i = 0; i < TUNE_COUNT; ++i)
+        if (std::strcmp(key, kTune[i].name) == 0) {
+            *value = g_tune[i].load(std::memory_order_relaxed);
+            return set_ok();
+        }
+    return set_error("fegb_get_tuning: unknown key '%s'", key);
+}
+
+int fegb_reset_tuning(void) {
+    using namespace fegb;
+    for (int i = 0; i < TUNE_COUNT; ++i) g_tune[i].store(kTune[i].def, std::memory_order_relaxed);
+    return set_ok();
+}
 
 int fegb_pool_usage(int reset_high, unsigned long long* used, unsigned long long* used_high,
                     unsigned long long* reserved) {

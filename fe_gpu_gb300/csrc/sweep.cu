@@ -1392,6 +1392,8 @@ thread_local int t_dense_mode = -1;  // -1: the default form; 0: the FP32 CUDA-c
 
 bool dense_use_mma() {
     if (t_dense_mode >= 0) return t_dense_mode > 0;
+    const int knob = tuning(TUNE_DENSE_FORM);
+    if (knob >= 0) return knob > 0;
     static const bool env = [] {  // FEGB_DENSE_TENSOR=0 selects the FP32 CUDA-core form by default
         const char* v = std::getenv("FEGB_DENSE_TENSOR");
         return !(v && v[0] == '0');
@@ -2089,8 +2091,9 @@ int launch_cg_rows(const CGRowsParams<T>& p, cudaStream_t s) {
     if (p.ld % (32 / (int)sizeof(T)) != 0) return set_error("cg operator: row stride %d is not a 32-byte multiple", p.ld);
     for (int e = 0; e < p.n_src; ++e)
         if ((reinterpret_cast<uintptr_t>(p.src_tab[e]) & 31u) != 0) return set_error("cg operator: unaligned table");
-    if (p.C <= 4) return launch_cg_rows_nsrc<T, 4>(p, s);
-    if (p.C <= 8) return launch_cg_rows_nsrc<T, 8>(p, s);
+    const int cap = tuning(TUNE_CG_COLS_PER_PASS);  // columns per pass (0: all, up to 16)
+    if (p.C <= 4 || cap == 4) return launch_cg_rows_nsrc<T, 4>(p, s);
+    if (p.C <= 8 || cap == 8) return launch_cg_rows_nsrc<T, 8>(p, s);
     if (p.C == 9) return launch_cg_rows_nsrc<T, 9>(p, s);
     if (p.C <= 12) return launch_cg_rows_nsrc<T, 12>(p, s);
     return launch_cg_rows_nsrc<T, 16>(p, s);

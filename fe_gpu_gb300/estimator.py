@@ -174,9 +174,16 @@ def _attach_fp64_errors(res: fe_estimation_result, cfg: fe_runtime_config, refit
     return res
 
 
+def _tune(rows: int, columns: int, tune: bool) -> None:
+    if tune:
+        from . import autotune
+
+        autotune.apply_for_shape(int(rows), int(columns))
+
+
 def fe_gpu_estimate(cfg: fe_runtime_config, header: Optional[fe_dataset_header], host: fe_host_arrays,
                     group_sizes: Optional[Sequence[int]] = None, stream: Optional[int] = None,
-                    profile: bool = False) -> fe_estimation_result:
+                    profile: bool = False, tune: bool = True) -> fe_estimation_result:
     """fe_gpu_estimate (src/core/fe_pipeline.f90:516) over host arrays: the
     upload, within-transform, normal equations and SEs all run in libfegb.so."""
     y = np.ascontiguousarray(host.y, dtype=np.float64)
@@ -188,6 +195,7 @@ def fe_gpu_estimate(cfg: fe_runtime_config, header: Optional[fe_dataset_header],
     if fe.ndim != 2 or fe.shape[1] != n:
         raise ValueError("fe_ids must have shape (n_fe, n)")
     k, l, n_fe = W.shape[1], Z.shape[1], fe.shape[0]
+    _tune(n, 1 + k + l, tune)
     c, keep = _make_config(cfg, stream, profile)
     beta = np.zeros(max(k, 1))
     se = np.zeros(max(k, 1))
@@ -200,15 +208,18 @@ def fe_gpu_estimate(cfg: fe_runtime_config, header: Optional[fe_dataset_header],
     N.check(st, "fegb_estimate_host")
     del keep
     out = _result_from(res, beta[:k].copy(), se[:k].copy(), cfg, header)
-    return _attach_fp64_errors(out, cfg, lambda c64: fe_gpu_estimate(c64, header, host, group_sizes, stream))
+    return _attach_fp64_errors(out, cfg, lambda c64: fe_gpu_estimate(c64, header, host, group_sizes, stream,
+                                                                     tune=tune))
 
 
 def fe_gpu_estimate_device(cfg: fe_runtime_config, n: int, k: int, l: int, d_y: int, d_W: Optional[int],
                            d_Z: Optional[int], d_fe_ids: Sequence[int], group_sizes: Optional[Sequence[int]] = None,
                            stream: Optional[int] = None, header: Optional[fe_dataset_header] = None,
-                           profile: bool = False) -> fe_estimation_result:
+                           profile: bool = False, tune: bool = True) -> fe_estimation_result:
     """Same fit over device arrays (raw device pointers), e.g. from the
-    fe_gpu_dataset upload (src/gpu/fe_gpu_data.f90:41-120)."""
+    fe_gpu_dataset upload (src/gpu/fe_gpu_data.f90:41-120). tune: apply the
+    autotuner's knobs for this shape first."""
+    _tune(n, 1 + k + l, tune)
     c, keep = _make_config(cfg, stream, profile)
     n_fe = len(d_fe_ids)
     ptrs = (C.c_void_p * max(1, n_fe))(*[C.c_void_p(int(p)) for p in d_fe_ids])
@@ -225,7 +236,8 @@ def fe_gpu_estimate_device(cfg: fe_runtime_config, n: int, k: int, l: int, d_y: 
     del keep
     out = _result_from(res, beta[:k].copy(), se[:k].copy(), cfg, header)
     return _attach_fp64_errors(out, cfg, lambda c64: fe_gpu_estimate_device(c64, n, k, l, d_y, d_W, d_Z, d_fe_ids,
-                                                                            group_sizes, stream, header))
+                                                                            group_sizes, stream, header,
+                                                                            tune=tune))
 
 
 @dataclass

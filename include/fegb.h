@@ -143,6 +143,23 @@ int fegb_group_sizes(const int* const* d_fe_ids, int n_fe, long long n, int* siz
 /* Number of kernel launches issued by this library since it was loaded. */
 long long fegb_kernel_launches(void);
 
+/* Launch-shape knobs (process-wide integers), chosen per problem shape by the
+ * autotuner (fe_gpu_gb300/autotune.py, table fe_gpu_gb300/tuning_gb300.json)
+ * and set by the host before a fit. Keys:
+ *   "dense_form"                -1 default, 0 CUDA-core, 1 tensor-core form of
+ *                               the CG operator's count-matrix passes
+ *   "cg_cols_per_pass"          0: all columns of a table row in one pass of
+ *                               the CG operator sweep; 4 or 8: at most that many
+ *   "split_gram_pairs_per_col"  Gram products with at least this many output
+ *                               pairs per input column use the split-FP32 form
+ *   "cg_graph"                  1: the CG loop runs as a CUDA graph; 0: host loop
+ * No knob changes what is computed beyond rounding; unknown keys and values
+ * out of range return a nonzero status. */
+int fegb_set_tuning(const char* key, int value);
+int fegb_get_tuning(const char* key, int* value);
+/* Every knob back to its default. */
+int fegb_reset_tuning(void);
+
 /* Memory of the current device's default stream-ordered pool, the pool this
  * library's temporaries come from: bytes in use now, the high-water mark of
  * bytes in use, and bytes reserved from the device. reset_high != 0 first

@@ -24,7 +24,7 @@ ORACLE = ROOT / "oracle"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
               "--expt-relaxed-constexpr", "-diag-suppress", "177"]
-SOURCES = ["prep.cu", "sweep.cu", "dense_umma.cu", "linalg.cu", "fit.cu", "runtime.cu", "design.cu", "loader.cu"]
+SOURCES = ["prep.cu", "sweep.cu", "dense_umma.cu", "batch_est.cu", "linalg.cu", "fit.cu", "runtime.cu", "design.cu", "loader.cu"]
 LIB_NAME = "libfegb.so"
 
 

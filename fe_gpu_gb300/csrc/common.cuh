@@ -106,7 +106,16 @@ void configure_mem_pool();
 //   TUNE_SPLIT_GRAM       output pairs per input column from which Gram
 //                         products use the split-FP32 form (>= 1)
 //   TUNE_CG_GRAPH         1 the CG loop runs as a CUDA graph, 0 host-driven
-enum TuneKey { TUNE_DENSE_FORM = 0, TUNE_CG_COLS_PER_PASS, TUNE_SPLIT_GRAM, TUNE_CG_GRAPH, TUNE_COUNT };
+//   TUNE_BATCH_ESTIMATOR  1 batched specifications are estimated class by
+//                         class in one batched pass, 0 one by one
+enum TuneKey {
+    TUNE_DENSE_FORM = 0,
+    TUNE_CG_COLS_PER_PASS,
+    TUNE_SPLIT_GRAM,
+    TUNE_CG_GRAPH,
+    TUNE_BATCH_ESTIMATOR,
+    TUNE_COUNT
+};
 int tuning(TuneKey key);
 
 // ---------------------------------------------------------------------------

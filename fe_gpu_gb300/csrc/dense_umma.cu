@@ -134,16 +134,25 @@ __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
 __device__ __forceinline__ void mbar_arrive_tx(uint64_t* bar, uint32_t bytes) {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
 }
-// true once the phase of the given parity has completed, false after the time limit
+// true once the phase of the given parity has completed, false after the time
+// limit. Each try suspends the thread in hardware (up to the hint, or until
+// the phase completes), so waiting warps take no issue slots from the warps
+// that work.
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
     const uint32_t a = smem_u32(bar);
+    uint32_t ok;
+    asm volatile(
+        "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\nselp.b32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(a), "r"(parity), "r"(1000000u)
+        : "memory");
+    if (ok) return true;
     const unsigned long long t0 = globaltimer();
     while (true) {
-        uint32_t ok;
         asm volatile(
-            "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.b32 %0, 1, 0, p;\n}\n"
+            "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\nselp.b32 %0, 1, 0, p;\n}\n"
             : "=r"(ok)
-            : "r"(a), "r"(parity)
+            : "r"(a), "r"(parity), "r"(1000000u)
             : "memory");
         if (ok) return true;
         if (globaltimer() - t0 > WAIT_LIMIT_NS) return false;
@@ -553,8 +562,16 @@ __global__ void __launch_bounds__(UT) dense_umma_kernel(UmmaArgs a) {
 template <int KT, bool SCHUR>
 int launch_umma(UmmaArgs a, cudaStream_t s) {
     const UmmaSmem L = umma_smem_plan(KT, a.raw_bytes, a.row_bytes);
-    static const cudaError_t attr = cudaFuncSetAttribute(dense_umma_kernel<KT, SCHUR>,
-                                                         cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    // the largest shared-memory carveout, so that four CTAs fit on an SM (the
+    // default carveout leaves room for one)
+    static const cudaError_t attr = [] {
+        cudaError_t e = cudaFuncSetAttribute(dense_umma_kernel<KT, SCHUR>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             200 * 1024);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(dense_umma_kernel<KT, SCHUR>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                     cudaSharedmemCarveoutMaxShared);
+        return e;
+    }();
     if (attr != cudaSuccess) return set_cuda_error(attr, "dense tensor-core pass attr");
     // one wave of persistent CTAs (at most the partial slots), each over a
     // contiguous range of whole tiles. Resident CTAs per SM for this

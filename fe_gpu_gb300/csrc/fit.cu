@@ -10,6 +10,7 @@
 #include "linalg.cuh"
 #include "prep.cuh"
 #include "sweep.cuh"
+#include "batch_est.cuh"
 
 #include <algorithm>
 #include <thread>
@@ -3107,7 +3108,79 @@ int estimate_batch_impl(const fegb_config& cfg, int n_specs, const fegb_spec* sp
         std::vector<const int32_t*> ids_b(fe_b);
         for (int d = 0; d < fe_b; ++d) ids_b[d] = idsb + (size_t)d * N;
         PreDemeaned pre;
+        auto tc0 = Clock::now();
         FEGB_TRY(within_impl(cfg, N, kb, 0, fe_b, yb, Wb, nullptr, ids_b.data(), Gb.data(), s, &pre));
+        FEGB_CUDA(cudaStreamSynchronize(s), "batch demean sync");
+        const double t_within = seconds_since(tc0);
+        tc0 = Clock::now();
+        // the whole class at once (batch_est.cu) when the batched estimator takes it
+        {
+            std::vector<BeSpecHost> be(ns);
+            for (int t = 0; t < ns; ++t) {
+                const fegb_spec& S = specs[idx[t]];
+                BeSpecHost& B = be[t];
+                B.row0 = hs[t].row0;
+                B.n = S.n;
+                B.k = S.k;
+                B.l = S.l;
+                B.n_fe = S.n_fe;
+                for (int d = 0; d < fe_b && d < BE_MAX_FE; ++d) {
+                    B.G[d] = Gs[t][d];
+                    B.goff[d] = hs[t].goff[d];
+                }
+                // cluster dimensions: valid, unique, the first three (fe_pipeline.f90:1553-1599)
+                for (int i = 0; i < S.n_cluster_dims && B.n_cd < MAX_CLUSTER_DIMS; ++i) {
+                    const int v = S.cluster_dims[i];
+                    if (v < 1 || v > S.n_fe) continue;
+                    bool dup = false;
+                    for (int j = 0; j < B.n_cd; ++j) dup = dup || B.cd[j] == v - 1;
+                    if (!dup) B.cd[B.n_cd++] = v - 1;
+                }
+                if (S.n_iv_regressors > 0) B.endog.assign(S.iv_regressors, S.iv_regressors + S.n_iv_regressors);
+                if (S.n_iv_instruments > 0)
+                    B.instr.assign(S.iv_instruments, S.iv_instruments + S.n_iv_instruments);
+                B.y_raw = S.y;
+            }
+            if (fe_b <= BE_MAX_FE && batch_est_eligible(cfg, cb, be) && tuning(TUNE_BATCH_ESTIMATOR)) {
+                std::vector<double*> bp(ns), sp(ns);
+                std::vector<fegb_result*> rp(ns);
+                for (int t = 0; t < ns; ++t) {
+                    const int si = idx[t];
+                    bp[t] = beta + boff[si];
+                    sp[t] = se + boff[si];
+                    rp[t] = &results[si];
+                    fegb_result* r = rp[t];
+                    std::memset(r, 0, sizeof(*r));
+                    for (int j = 0; j < specs[si].k; ++j) bp[t][j] = sp[t][j] = 0.0;
+                    r->converged = pre.converged;
+                    r->fe_iterations = pre.iterations;
+                    r->max_update = pre.max_update;
+                    r->outer_iterations = pre.outer;
+                    r->projections = pre.projections;
+                    r->demean_bytes = pre.demean_bytes;
+                    r->time_demean = pre.seconds;
+                    if (t == 0)
+                        for (int f = 0; f < 8; ++f) {
+                            r->prof_launches[f] = pre.prof.prof_launches[f];
+                            r->prof_seconds[f] = pre.prof.prof_seconds[f];
+                            r->prof_bytes[f] = pre.prof.prof_bytes[f];
+                        }
+                }
+                FEGB_TRY(estimate_class_batched(cfg, be, N, cb, yb, Wb, ids_b.data(), fe_b, bp.data(), sp.data(),
+                                                rp.data(), s));
+                for (int t = 0; t < ns; ++t) {
+                    fegb_result* r = rp[t];
+                    if (r->solver_info == 0 && r->dof_model > 0) finalize_stats(r, specs[idx[t]].n);
+                    r->time_total = r->time_demean + r->time_regression + r->time_se;
+                }
+                if (trace_enabled())
+                    std::fprintf(stderr,
+                                 "fegb batch: class of %d columns: %d specs, %lld rows, within-transform %.1f ms "
+                                 "(%d CG), batched estimation %.1f ms\n",
+                                 cb, ns, N, t_within * 1e3, pre.iterations, seconds_since(tc0) * 1e3);
+                continue;
+            }
+        }
         // every specification on its own demeaned rows; the fits are
         // independent, so a few host threads run them on their own streams
         auto fit_one = [&](int t, cudaStream_t ws) -> int {
@@ -3180,6 +3253,10 @@ int estimate_batch_impl(const fegb_config& cfg, int n_specs, const fegb_spec* sp
         worker();
         for (auto& th : pool) th.join();
         if (err_status) return set_error("%s", err_msg.c_str());
+        if (trace_enabled())
+            std::fprintf(stderr, "fegb batch: class of %d columns: %d specs, %lld rows, within-transform %.1f ms (%d CG), "
+                                 "per-spec fits %.1f ms\n",
+                         cb, ns, N, t_within * 1e3, pre.iterations, seconds_since(tc0) * 1e3);
     }
     return set_ok();
 }

@@ -153,6 +153,8 @@ long long fegb_kernel_launches(void);
  *   "split_gram_pairs_per_col"  Gram products with at least this many output
  *                               pairs per input column use the split-FP32 form
  *   "cg_graph"                  1: the CG loop runs as a CUDA graph; 0: host loop
+ *   "batch_estimator"           1: fegb_estimate_batch estimates each column
+ *                               class in one batched pass; 0: spec by spec
  * No knob changes what is computed beyond rounding; unknown keys and values
  * out of range return a nonzero status. */
 int fegb_set_tuning(const char* key, int value);

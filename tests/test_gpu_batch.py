@@ -1,6 +1,8 @@
 """Batched specifications (fegb_estimate_batch) against the same fits run
 one by one and against the oracle: uneven sizes, 1-3 FE dimensions, 2-24
-regressors, OLS and 2SLS, 1-3-way clustering."""
+regressors, OLS and 2SLS, 1-3-way clustering; both the batched estimation of
+each column class (default) and the specification-by-specification path
+(knob batch_estimator = 0)."""
 import numpy as np
 import pytest
 
@@ -31,13 +33,21 @@ def rel(a, b):
     return float(np.max(np.abs(a - b) / np.maximum(np.abs(b), 1e-300)))
 
 
+@pytest.mark.parametrize("batched", [1, 0])
 @pytest.mark.parametrize("precision,cg", [("fp64", False), ("mixed", True)])
-def test_batch_matches_single_fits_and_oracle(built, precision, cg):
+def test_batch_matches_single_fits_and_oracle(built, precision, cg, batched):
+    from fe_gpu_gb300 import autotune as A
+
     specs = batch_specs(n_specs=12, total_rows=300_000, row_range=(2_000, 60_000), seed=1)
     assert sum(1 for _, e in specs if e["iv_regressors"]) >= 3
     bufs, dspecs = _upload(specs)
     cfg = fe_runtime_config(fe_tolerance=1e-8, fe_max_iterations=100000, precision=precision, demean_cg=cg)
-    batch = fe_gpu_estimate_batch(cfg, dspecs)
+    A.reset()
+    A.set_knob("batch_estimator", batched)
+    try:
+        batch = fe_gpu_estimate_batch(cfg, dspecs)
+    finally:
+        A.reset()
     assert len(batch) == len(specs)
     for (host, extra), sp, rb in zip(specs, dspecs, batch):
         c1 = fe_runtime_config(fe_tolerance=1e-8, fe_max_iterations=100000, precision=precision, demean_cg=cg,
@@ -54,6 +64,24 @@ def test_batch_matches_single_fits_and_oracle(built, precision, cg):
         assert rel(rb.beta, ref.beta) < 1e-6
         assert rel(rb.se, ref.se) < 1e-5
         assert abs(rb.r2 - rs.r2) < 1e-7 and abs(rb.r2_within - rs.r2_within) < 1e-7
+        assert rb.psd_fix_applied == r.psd_fix_applied
+        assert abs(rb.tss_total - rs.tss_total) <= 1e-9 * abs(rs.tss_total)
+        assert abs(rb.rss - rs.rss) <= 1e-7 * abs(rs.rss)
+
+
+def test_batch_64_specs_match_oracle(built):
+    """64 specifications (the batched estimator's path) against the oracle."""
+    specs = batch_specs(n_specs=64, total_rows=1_500_000, row_range=(2_000, 80_000), seed=3)
+    bufs, dspecs = _upload(specs)
+    cfg = fe_runtime_config(fe_tolerance=1e-8, fe_max_iterations=100000, precision="mixed", demean_cg=True)
+    batch = fe_gpu_estimate_batch(cfg, dspecs)
+    for (host, extra), rb in zip(specs, batch):
+        ref = O.gpu_estimate(host.y, host.W, host.fe_ids, Z=host.Z, tol=1e-12, max_iter=200000,
+                             cluster_dims=extra["cluster_fe_dims"], iv_regressors=extra["iv_regressors"])
+        assert rb.converged
+        assert rb.dof_resid == ref.stats["dof_resid"] and rb.dof_model == ref.stats["dof_model"]
+        assert rel(rb.beta, ref.beta) < 1e-6
+        assert rel(rb.se, ref.se) < 1e-5
 
 
 def test_batch_rejects_bad_specs(built):

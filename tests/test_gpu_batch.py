@@ -74,7 +74,14 @@ def test_batch_64_specs_match_oracle(built):
     specs = batch_specs(n_specs=64, total_rows=1_500_000, row_range=(2_000, 80_000), seed=3)
     bufs, dspecs = _upload(specs)
     cfg = fe_runtime_config(fe_tolerance=1e-8, fe_max_iterations=100000, precision="mixed", demean_cg=True)
-    batch = fe_gpu_estimate_batch(cfg, dspecs)
+    from fe_gpu_gb300 import autotune as A
+
+    A.reset()
+    A.set_knob("batch_estimator", 1)
+    try:
+        batch = fe_gpu_estimate_batch(cfg, dspecs)
+    finally:
+        A.reset()
     for (host, extra), rb in zip(specs, batch):
         ref = O.gpu_estimate(host.y, host.W, host.fe_ids, Z=host.Z, tol=1e-12, max_iter=200000,
                              cluster_dims=extra["cluster_fe_dims"], iv_regressors=extra["iv_regressors"])

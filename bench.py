@@ -256,6 +256,13 @@ def run_reference(args):
     return 0
 
 
+def knob_values():
+    """The launch-shape knobs in force (after the autotuner's table or --knob)."""
+    from fe_gpu_gb300 import autotune
+
+    return {k: autotune.get_knob(k) for k in list(autotune.KNOBS) + ["batch_estimator"]}
+
+
 def rel_errors(got, ref):
     got, ref = np.asarray(got, dtype=np.float64), np.asarray(ref, dtype=np.float64)
     return [float(v) for v in np.abs(got - ref) / np.maximum(np.abs(ref), 1e-300)]
@@ -282,7 +289,18 @@ def main():
     ap.add_argument("--profile-case", action="store_true",
                     help="one fit per (precision, method) and exit (for ncu captures)")
     ap.add_argument("--case", default="all", help="with --profile-case: mixed-cg, fp64-cg, mixed-ap, fp64-ap or all")
+    ap.add_argument("--knob", action="append", default=[],
+                    help="key=value: set a launch-shape knob (fegb_set_tuning) for every fit of the run; the "
+                         "autotuner's table is not applied then")
     args = ap.parse_args()
+    if args.knob and args.impl == "ours":
+        from fe_gpu_gb300 import autotune
+
+        os.environ["FEGB_TUNING"] = "off"
+        autotune.reset()
+        for kv in args.knob:
+            key, val = kv.split("=", 1)
+            autotune.set_knob(key.strip(), int(val))
     if args.impl == "reference":
         return run_reference(args)
     if args.workload in FORMULA_WORKLOADS:
@@ -432,7 +450,7 @@ def main():
         "config": {"workload": args.workload, "description": WORKLOADS[args.workload]["desc"], "rows": n,
                    "columns": 1 + k, "fe_tol": 1e-8, "precision": args.precision, "within_transform": args.method,
                    "l2": "inputs larger than L2 (%.2f GB of FP64 data per fit)" % (n * (1 + k) * 8 / 1e9),
-                   "parallelism": f"replicas x{world}"},
+                   "parallelism": f"replicas x{world}", "knobs": knob_values()},
         "fit_time_s": ms / 1e3,
         "fit_breakdown_s": {key: last.stats[key] for key in ("time_prep", "time_demean", "time_regression",
                                                               "time_se")},
@@ -812,7 +830,7 @@ def run_batch(args):
         "dtype": "f32-sweeps+f64" if args.precision == "mixed" else "f64", "data": "synthetic (seeded)",
         "config": {"workload": args.workload, "description": w["desc"], "specs": len(specs), "rows": rows,
                    "fe_tol": 1e-8, "precision": args.precision, "within_transform": args.method,
-                   "l2": "inputs larger than L2", "parallelism": f"replicas x{world}"},
+                   "l2": "inputs larger than L2", "parallelism": f"replicas x{world}", "knobs": knob_values()},
         "fit_time_s": ms / 1e3,
         "specs_per_s": len(specs) / (ms / 1e3),
         "iv_specs": sum(1 for r in last if r.is_iv),

@@ -580,12 +580,18 @@ int launch_umma(UmmaArgs a, cudaStream_t s) {
     static thread_local uint32_t cached_bytes = 0;
     static thread_local int cached_sms = 0, cached_occ = 0;
     if (cached_bytes != L.total) {
-        int dev = 0;
+        // CTAs per SM from the SM's shared memory (the occupancy API's answer
+        // does not follow the carveout set above), the per-block reserve and
+        // the kernel's static shared memory
+        int dev = 0, smem_sm = 0, reserved = 0;
         FEGB_CUDA(cudaGetDevice(&dev), "cudaGetDevice");
         FEGB_CUDA(cudaDeviceGetAttribute(&cached_sms, cudaDevAttrMultiProcessorCount, dev), "SM count");
-        FEGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&cached_occ, dense_umma_kernel<KT, SCHUR>, UT,
-                                                                L.total),
-                  "occupancy");
+        FEGB_CUDA(cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev), "SM smem");
+        FEGB_CUDA(cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev), "smem reserve");
+        cudaFuncAttributes fa{};
+        FEGB_CUDA(cudaFuncGetAttributes(&fa, dense_umma_kernel<KT, SCHUR>), "kernel attributes");
+        const size_t per_cta = (size_t)L.total + fa.sharedSizeBytes + (size_t)reserved;
+        cached_occ = (int)std::max<size_t>(1, (size_t)smem_sm / per_cta);
         cached_bytes = L.total;
     }
     // tensor memory per SM: 512 columns

@@ -30,6 +30,8 @@
 #include <chrono>
 #include <climits>
 #include <cmath>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 
 namespace fegb {
@@ -321,10 +323,10 @@ __device__ __forceinline__ int be_spec_of(const long long* __restrict__ row0, in
     return lo;
 }
 
-// Residual r = y - W beta and score columns S[t][row] = r * x_{score col t}
+// Residual r = y - W beta and score rows S[row][t] = r * x_{score col t}
 // (regressors for OLS, Z_aug for 2SLS; zeros past the specification's count),
-// one block per item; per-item RSS partials. Score columns are column-major
-// with leading dimension N.
+// one block per item; per-item RSS partials. Score rows are row-major with Sb
+// (even) values each.
 __global__ void __launch_bounds__(BE_THREADS)
     be_resid_kernel(ColMajorX X, const BeSpecDev* __restrict__ specs, const BeItem* __restrict__ items,
                     const double* __restrict__ beta_full, int Kb, int Sb, long long N, double* __restrict__ S,
@@ -344,8 +346,15 @@ __global__ void __launch_bounds__(BE_THREADS)
         double v = X(r, 0);
         for (int j = 0; j < k; ++j) v -= X(r, 1 + j) * s_beta[j];
         acc += v * v;
-        if (S)
-            for (int tcol = 0; tcol < Sb; ++tcol) S[(long long)tcol * N + r] = s_col[tcol] >= 0 ? v * X(r, s_col[tcol]) : 0.0;
+        if (S) {
+            // row-major rows of Sb scores (the cluster sums read whole rows)
+            double* srow = S + r * Sb;
+            for (int tcol = 0; tcol < Sb; tcol += 2) {
+                const double a = s_col[tcol] >= 0 ? v * X(r, s_col[tcol]) : 0.0;
+                const double b2 = (tcol + 1 < Sb && s_col[tcol + 1] >= 0) ? v * X(r, s_col[tcol + 1]) : 0.0;
+                *reinterpret_cast<double2*>(srow + tcol) = make_double2(a, b2);
+            }
+        }
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
@@ -460,17 +469,23 @@ __global__ void be_cluster_ranges_kernel(const int32_t* __restrict__ cl_spec, in
     }
 }
 
-// Sc[c][t] = sum over the rows of cluster c (in sorted order) of S[t][row]
-__global__ void be_cluster_sums_kernel(const double* __restrict__ S, long long N, int Sb,
-                                       const int32_t* __restrict__ perm, const int32_t* __restrict__ off, int n_cl,
-                                       double* __restrict__ Sc) {
-    long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    const long long st = (long long)gridDim.x * blockDim.x;
-    for (; e < (long long)n_cl * Sb; e += st) {
-        const int c = (int)(e / Sb), t = (int)(e - (long long)c * Sb);
-        double v = 0.0;
-        for (int p = off[c]; p < off[c + 1]; ++p) v += S[(long long)t * N + perm[p]];
-        Sc[e] = v;
+// Sc[c][t] = sum over the rows of cluster c (in sorted order) of S[row][t]:
+// one warp per cluster, lanes over the columns, so every row is one
+// contiguous read.
+__global__ void be_cluster_sums_kernel(const double* __restrict__ S, int Sb, const int32_t* __restrict__ perm,
+                                       const int32_t* __restrict__ off, int n_cl, double* __restrict__ Sc) {
+    const int lane = threadIdx.x & 31;
+    long long c = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const long long st = ((long long)gridDim.x * blockDim.x) >> 5;
+    for (; c < n_cl; c += st) {
+        double a0 = 0.0, a1 = 0.0;
+        for (int p = off[c]; p < off[c + 1]; ++p) {
+            const double* row = S + (long long)perm[p] * Sb;
+            if (lane < Sb) a0 += row[lane];
+            if (lane + 32 < Sb) a1 += row[lane + 32];
+        }
+        if (lane < Sb) Sc[c * Sb + lane] = a0;
+        if (lane + 32 < Sb) Sc[c * Sb + lane + 32] = a1;
     }
 }
 
@@ -668,6 +683,19 @@ int estimate_class_batched(const fegb_config& cfg, const std::vector<BeSpecHost>
     const int ns = (int)specs.size();
     if (ns == 0) return 0;
     Scratch scr(s);
+    // FEGB_TRACE=1: the stream is synchronised after each phase and its time printed
+    static const bool trace = [] {
+        const char* v = std::getenv("FEGB_TRACE");
+        return v && v[0] && v[0] != '0';
+    }();
+    auto tp = BeClock::now();
+    auto phase = [&](const char* what) -> int {
+        if (!trace) return 0;
+        FEGB_CUDA(cudaStreamSynchronize(s), "trace sync");
+        std::fprintf(stderr, "fegb batch est: %-28s %8.2f ms\n", what, be_seconds_since(tp) * 1e3);
+        tp = BeClock::now();
+        return 0;
+    };
     const int Kb = Cw;  // regressors and score columns per specification: at most Cw - 1
     const int P = Cw * (Cw + 1) / 2;
     auto t0 = BeClock::now();
@@ -745,6 +773,7 @@ int estimate_class_batched(const fegb_config& cfg, const std::vector<BeSpecHost>
     } else {
         FEGB_CUDA(cudaMemsetAsync(d_tss, 0, sizeof(double) * ns, s), "tss zero");
     }
+    FEGB_TRY(phase("records and tss"));
 
     // ---- Gram products and solves ----
     double *d_gram = nullptr, *d_scratch = nullptr, *d_beta = nullptr, *d_Qinv = nullptr, *d_Pi = nullptr;
@@ -755,6 +784,7 @@ int estimate_class_batched(const fegb_config& cfg, const std::vector<BeSpecHost>
     FEGB_TRY(scr.alloc(&d_Pi, (size_t)ns * Kb * Kb, "batch Pi"));
     ColMajorX X{yb, Wb, N};
     FEGB_TRY(be_gram(X, items, item0, item1, d_width, ns, Cw, d_gram, s, scr));
+    FEGB_TRY(phase("gram"));
     be_solve_kernel<<<ns, DN_THREADS, 0, s>>>(d_specs, d_gram, Cw, Kb, d_scratch, d_beta, d_Qinv, d_Pi);
     FEGB_LAUNCH_CHECK("batch solve");
     FEGB_CUDA(cudaStreamSynchronize(s), "batch solve sync");
@@ -764,7 +794,7 @@ int estimate_class_batched(const fegb_config& cfg, const std::vector<BeSpecHost>
     // ---- residuals, scores, RSS ----
     bool any_cluster = false;
     for (const BeSpecHost& S : specs) any_cluster = any_cluster || S.n_cd > 0;
-    const int Sb = Cw;  // score columns per row (at most Cw - 1 used)
+    const int Sb = (Cw + 1) / 2 * 2;  // score values per row (at most Cw - 1 used), even for 16-byte stores
     double* d_S = nullptr;
     double* d_rss = nullptr;
     if (any_cluster) FEGB_TRY(scr.alloc(&d_S, (size_t)N * Sb, "batch score columns"));
@@ -777,6 +807,7 @@ int estimate_class_batched(const fegb_config& cfg, const std::vector<BeSpecHost>
     } else {
         FEGB_CUDA(cudaMemsetAsync(d_rss, 0, sizeof(double) * ns, s), "rss zero");
     }
+    FEGB_TRY(phase("residuals and scores"));
     // solve outcomes (kept columns and dof) for the host
     std::vector<BeSpecDev> hs(ns);
     FEGB_TRY(be_sync_copy(hs.data(), d_specs, sizeof(BeSpecDev) * ns, cudaMemcpyDeviceToHost, s, "spec results copy"));
@@ -855,7 +886,9 @@ int estimate_class_batched(const fegb_config& cfg, const std::vector<BeSpecHost>
             be_key_kernel<<<grid_stride_blocks(N, 256), 256, 0, s>>>(kd, d_row0, ns, N, d_subdim, d_stride, d_goff,
                                                                     d_part_spec, LB, keys);
             FEGB_LAUNCH_CHECK("cluster keys");
+            FEGB_TRY(phase("cluster keys"));
             FEGB_TRY(radix_sort_u64(keys, nullptr, skeys, perm, N, LB + SB, s, scr));
+            FEGB_TRY(phase("cluster sort"));
             be_cluster_flags_kernel<<<grid_stride_blocks(N, 256), 256, 0, s>>>(skeys, N, ns, LB, flags);
             FEGB_LAUNCH_CHECK("cluster flags");
             FEGB_TRY(scan_exclusive_u32(flags, excl, N, total, s, scr));
@@ -871,8 +904,8 @@ int estimate_class_batched(const fegb_config& cfg, const std::vector<BeSpecHost>
             FEGB_CUDA(cudaMemsetAsync(d_c1, 0, sizeof(int) * ns, s), "cluster end zero");
             if (n_cl > 0) {
                 be_cluster_ranges_kernel<<<grid_stride_blocks(n_cl, 256), 256, 0, s>>>(cl_spec, n_cl, d_c0, d_c1);
-                be_cluster_sums_kernel<<<grid_stride_blocks((long long)n_cl * Sb, 256), 256, 0, s>>>(
-                    d_S, N, Sb, perm, off, n_cl, Sc);
+                be_cluster_sums_kernel<<<grid_stride_blocks((long long)n_cl * 32, 256), 256, 0, s>>>(d_S, Sb, perm,
+                                                                                                  off, n_cl, Sc);
                 FEGB_LAUNCH_CHECK("cluster score sums");
             }
             std::vector<int> c0(ns), c1(ns);
@@ -892,11 +925,14 @@ int estimate_class_batched(const fegb_config& cfg, const std::vector<BeSpecHost>
             FEGB_TRY(scr.alloc(&d_swidth, (size_t)ns, "score widths"));
             FEGB_CUDA(cudaMemcpyAsync(d_swidth, swidth.data(), sizeof(int) * ns, cudaMemcpyHostToDevice, s),
                       "score widths copy");
+            FEGB_TRY(phase("cluster sums"));
             RowMajor R{Sc, Sb};
             FEGB_TRY(be_gram(R, citems, ci0, ci1, d_swidth, ns, Cw, d_meat, s, scr));
+            FEGB_TRY(phase("meat gram"));
             be_sandwich_kernel<<<ns, DN_THREADS, 0, s>>>(d_specs, d_part_spec, d_meat, Cw, Kb, d_Qinv, d_Pi,
                                                          (m % 2 == 1) ? 1.0 : -1.0, d_acc, d_scratch);
             FEGB_LAUNCH_CHECK("batch sandwich");
+            FEGB_TRY(phase("sandwich"));
         }
     }
 
@@ -940,6 +976,7 @@ int estimate_class_batched(const fegb_config& cfg, const std::vector<BeSpecHost>
     FEGB_CUDA(cudaMemcpyAsync(hbeta.data(), d_beta, sizeof(double) * hbeta.size(), cudaMemcpyDeviceToHost, s), "beta");
     FEGB_CUDA(cudaMemcpyAsync(hse.data(), d_se, sizeof(double) * hse.size(), cudaMemcpyDeviceToHost, s), "se");
     FEGB_TRY(be_sync_copy(hpsd.data(), d_psd, sizeof(int) * ns, cudaMemcpyDeviceToHost, s, "psd copy"));
+    FEGB_TRY(phase("finalize"));
     const double t_se = be_seconds_since(t0);
     for (int i = 0; i < ns; ++i) {
         const BeSpecHost& S = specs[i];

@@ -238,35 +238,53 @@ __device__ __forceinline__ float byte_f32(uint32_t w, uint32_t sel) {
     return __uint_as_float(__byte_perm(w, 0x4B000000u, sel)) - 8388608.0f;
 }
 
+template <int N>
+__device__ __forceinline__ void tmem_ld4(uint32_t taddr, float (&v)[N], int base) {
+    uint32_t r0, r1, r2, r3;
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0,%1,%2,%3}, [%4];"
+                 : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3)
+                 : "r"(taddr));
+    v[base] = __uint_as_float(r0);
+    v[base + 1] = __uint_as_float(r1);
+    v[base + 2] = __uint_as_float(r2);
+    v[base + 3] = __uint_as_float(r3);
+}
+
 // Persistent pass: CTA b covers groups [b per, (b + 1) per) tile by tile.
-// Per tile i (thread = group row of the tile):
+// Two threads per group of the tile (g = tid % 128, half h = tid / 128): each
+// converts half of the group's counts and owns 8 of its 16 column slots,
+// c = 4h + j and 8 + 4h + j (j < 4), so that each writes whole 8-byte halves
+// of the U tile's 16-byte chunks. Per tile i:
 //   (a) counts of tile i + 1 -> BF16 count tile; S1; MMA E(i + 1) = counts . S
 //   (b) wait E(i); u or the e-side output of tile i; pieces of u / pe -> U; S2;
 //       MMA D2 += U' . counts(i)
 // with the raw counts fetched three tiles ahead and the rows two tiles ahead
 // (bulk copies on per-stage mbarriers), so that copies, E(i + 1) and D2(i)
 // overlap the CUDA-core work of tile i.
+constexpr int BT = 2 * UT;  // threads per CTA
+
 template <int KT, bool SCHUR>
-__global__ void __launch_bounds__(UT) dense_umma_kernel(UmmaArgs a) {
+__global__ void __launch_bounds__(BT, 4) dense_umma_kernel(UmmaArgs a) {
     using TP = TmemPlan<KT>;
     extern __shared__ __align__(1024) unsigned char sm[];
     // 0, 1: raw-count stages; 2, 3: row stages; 4, 5: E buffers; 6: D2
     __shared__ __align__(8) uint64_t bars[7];
     __shared__ uint32_t tmem_base_s;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int g = tid & (UT - 1), h = tid / UT;
     const int Gs = a.Gs, C = a.C, ld = a.ld;
     const bool small = a.partials != nullptr;
     const bool need_e = SCHUR || a.extra != nullptr;
     // partial slots past the grid hold zeros
     if (small)
         for (long long slot = (long long)blockIdx.x + gridDim.x; slot < a.nparts; slot += gridDim.x)
-            for (int j = tid; j < Gs * C; j += UT) a.partials[slot * Gs * C + j] = 0.0;
+            for (int j = tid; j < Gs * C; j += BT) a.partials[slot * Gs * C + j] = 0.0;
     double* const part = small ? a.partials + (long long)blockIdx.x * Gs * C : nullptr;
     const long long g0 = (long long)blockIdx.x * a.per;
     const long long g1 = min(a.Ge, g0 + a.per);
     if (g0 >= g1) {
         if (small)
-            for (int j = tid; j < Gs * C; j += UT) part[j] = 0.0;
+            for (int j = tid; j < Gs * C; j += BT) part[j] = 0.0;
         return;
     }
     const UmmaSmem L = umma_smem_plan(KT, a.raw_bytes, a.row_bytes);
@@ -274,6 +292,8 @@ __global__ void __launch_bounds__(UT) dense_umma_kernel(UmmaArgs a) {
     constexpr uint32_t U_LBO = (uint32_t)(UM2 / 8) * 128;    // bytes between 8-group blocks of the U tile
     const uint32_t sbase = smem_u32(sm);
     const uint32_t sums_bytes = (uint32_t)(((UT * C * 4) + 15) / 16 * 16);
+    // this thread's column slots: c = 4h + j (j < 4) and 8 + 4h + (j - 4) (j >= 4)
+    auto col_of = [&](int j) { return j < 4 ? 4 * h + j : 8 + 4 * h + (j - 4); };
 
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base_s)),
@@ -284,17 +304,18 @@ __global__ void __launch_bounds__(UT) dense_umma_kernel(UmmaArgs a) {
         for (int i = 0; i < 7; ++i) mbar_init(&bars[i], 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
-    // U tile zeroed once (rows 48..63 stay zero), S pieces (K-major: n = p * 16 + c, k = t)
-    for (uint32_t o = tid * 16; o < (uint32_t)(UM2 * UT * 2); o += UT * 16)
+    // U tile zeroed once (rows 48..63 and columns past C stay zero), S pieces
+    // (K-major: n = p * 16 + c, k = t)
+    for (uint32_t o = tid * 16; o < (uint32_t)(UM2 * UT * 2); o += BT * 16)
         *reinterpret_cast<uint4*>(sm + L.u + o) = make_uint4(0, 0, 0, 0);
     if (need_e) {
-        for (int i = tid; i < UN1 * KT; i += UT) {
+        for (int i = tid; i < UN1 * KT; i += BT) {
             const int n = i / KT, t = i - (i / KT) * KT;
             const int p = n / UCP, c = n - p * UCP;
             const float v = (t < Gs && c < C) ? a.ps[(long long)t * ld + c] : 0.0f;
-            __nv_bfloat16 h, m, l;
-            split3(v, h, m, l);
-            const __nv_bfloat16 piece = p == 0 ? h : (p == 1 ? m : l);
+            __nv_bfloat16 hh, mm, ll;
+            split3(v, hh, mm, ll);
+            const __nv_bfloat16 piece = p == 0 ? hh : (p == 1 ? mm : ll);
             const uint32_t off = (uint32_t)(n / 8) * CORE_ROW + (uint32_t)(t / 8) * 128 + (uint32_t)(n % 8) * 16 +
                                  (uint32_t)(t % 8) * 2;
             *reinterpret_cast<__nv_bfloat16*>(sm + L.b1 + off) = piece;
@@ -305,7 +326,7 @@ __global__ void __launch_bounds__(UT) dense_umma_kernel(UmmaArgs a) {
     __syncthreads();
     fence_after_sync();
     const uint32_t tmem = tmem_base_s;
-    const uint32_t t_lane = (uint32_t)(warp * 32) << 16;
+    const uint32_t t_lane = (uint32_t)((warp & 3) * 32) << 16;
     const int ntiles = (int)((g1 - g0 + UT - 1) / UT);
     auto tile_of = [&](int j) { return g0 + (long long)j * UT; };
     auto full = [&](int j) { return tile_of(j) + UT <= g1; };
@@ -340,16 +361,18 @@ __global__ void __launch_bounds__(UT) dense_umma_kernel(UmmaArgs a) {
         }
     };
     bool failed = false;
-    // counts of tile j -> count tile j & 1 (BF16 core matrices (tid/8, t/8), row tid % 8)
+    // counts of tile j -> count tile j & 1 (BF16 core matrices (g/8, t/8), row
+    // g % 8); half h converts the core blocks [h KT/16, (h + 1) KT/16)
     auto convert = [&](int j) -> bool {
         if (!mbar_wait(&bars[j & 1], (uint32_t)((j >> 1) & 1))) return false;
         const long long tile = tile_of(j);
         const int nt = (int)min((long long)UT, g1 - tile);
-        const bool mine = tid < nt;
-        const unsigned char* src = full(j) ? sm + ((j & 1) ? L.raw1 : L.raw0) + tid * Gs : a.M + (tile + tid) * Gs;
+        const bool mine = g < nt;
+        const unsigned char* src = full(j) ? sm + ((j & 1) ? L.raw1 : L.raw0) + g * Gs : a.M + (tile + g) * Gs;
         const uint32_t cnt_off = (j & 1) ? L.cnt1 : L.cnt0;
 #pragma unroll
-        for (int tb = 0; tb < KT / 8; ++tb) {
+        for (int tq = 0; tq < KT / 16; ++tq) {
+            const int tb = h * (KT / 16) + tq;
             uint32_t w[4];
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
@@ -359,8 +382,8 @@ __global__ void __launch_bounds__(UT) dense_umma_kernel(UmmaArgs a) {
                 const float x0 = byte_f32(pair, 0x7540u), x1 = byte_f32(pair, 0x7541u);
                 w[q] = pack2(__float2bfloat16_rn(x0), __float2bfloat16_rn(x1));
             }
-            *reinterpret_cast<uint4*>(sm + cnt_off + (uint32_t)(tid / 8) * CORE_ROW + (uint32_t)tb * 128 +
-                                      (uint32_t)(tid % 8) * 16) = make_uint4(w[0], w[1], w[2], w[3]);
+            *reinterpret_cast<uint4*>(sm + cnt_off + (uint32_t)(g / 8) * CORE_ROW + (uint32_t)tb * 128 +
+                                      (uint32_t)(g % 8) * 16) = make_uint4(w[0], w[1], w[2], w[3]);
         }
         fence_async_smem();
         return true;
@@ -394,7 +417,7 @@ __global__ void __launch_bounds__(UT) dense_umma_kernel(UmmaArgs a) {
     for (int i = 0; i < ntiles && !failed; ++i) {
         const long long tile = tile_of(i);
         const int nt = (int)min((long long)UT, g1 - tile);
-        const bool mine = tid < nt;
+        const bool mine = g < nt;
         // (a) counts of tile i + 1 (its count tile was read by the MMAs of tile i - 1)
         ok = true;
         if (i + 1 < ntiles) {
@@ -416,25 +439,28 @@ __global__ void __launch_bounds__(UT) dense_umma_kernel(UmmaArgs a) {
         }
         // (b) this tile: its rows, then E(i)
         ok = mbar_wait(&bars[2 + (i & 1)], (uint32_t)((i >> 1) & 1));
-        float v[UCP];
+        float v[8];
 #pragma unroll
-        for (int c = 0; c < UCP; ++c) v[c] = 0.0f;
+        for (int j = 0; j < 8; ++j) v[j] = 0.0f;
         int n_g = 0;
         const float* srow = reinterpret_cast<const float*>(sm + ((i & 1) ? L.row1 : L.row0));
         if (ok && mine) {
+            const bool f = full(i);
             if (SCHUR) {
-                const bool f = full(i);
 #pragma unroll
-                for (int c = 0; c < UCP; ++c)
-                    if (c < C) v[c] = f ? srow[tid * C + c] : a.sums[(tile + tid) * C + c];
+                for (int j = 0; j < 8; ++j) {
+                    const int c = col_of(j);
+                    if (c < C) v[j] = f ? srow[g * C + c] : a.sums[(tile + g) * C + c];
+                }
                 n_g = (f && a.bulk_counts) ? reinterpret_cast<const int32_t*>(sm + ((i & 1) ? L.row1 : L.row0) +
-                                                                             sums_bytes)[tid]
-                                           : a.counts[tile + tid];
+                                                                             sums_bytes)[g]
+                                           : a.counts[tile + g];
             } else if (small) {
-                const bool f = full(i);
 #pragma unroll
-                for (int c = 0; c < UCP; ++c)
-                    if (c < C) v[c] = f ? srow[tid * ld + c] : a.pe[(tile + tid) * ld + c];
+                for (int j = 0; j < 8; ++j) {
+                    const int c = col_of(j);
+                    if (c < C) v[j] = f ? srow[g * ld + c] : a.pe[(tile + g) * ld + c];
+                }
             }
         }
         if (need_e) {
@@ -444,29 +470,33 @@ __global__ void __launch_bounds__(UT) dense_umma_kernel(UmmaArgs a) {
                 break;
             }
             fence_after_sync();
-            float e[UN1];
+            // E columns of this thread's slots: piece p at p * 16 + c
+            float e[24];
             const uint32_t ecol = (i & 1) ? TP::E1 : TP::E0;
-            tmem_ld16(tmem + t_lane + ecol + 0, e, 0);
-            tmem_ld16(tmem + t_lane + ecol + 16, e, 16);
-            tmem_ld16(tmem + t_lane + ecol + 32, e, 32);
+#pragma unroll
+            for (int p = 0; p < UNP; ++p) {
+                tmem_ld4(tmem + t_lane + ecol + p * UCP + 4 * h, e, p * 8);
+                tmem_ld4(tmem + t_lane + ecol + p * UCP + 8 + 4 * h, e, p * 8 + 4);
+            }
             tmem_wait_ld();
             if (SCHUR) {
                 const float rn = n_g > 0 ? 1.0f / (float)n_g : 0.0f;
 #pragma unroll
-                for (int c = 0; c < UCP; ++c)
-                    if (c < C) v[c] = n_g > 0 ? (v[c] - ((e[32 + c] + e[16 + c]) + e[c])) * rn : 0.0f;
+                for (int j = 0; j < 8; ++j)
+                    if (col_of(j) < C) v[j] = n_g > 0 ? (v[j] - ((e[16 + j] + e[8 + j]) + e[j])) * rn : 0.0f;
                 if (mine) {
-                    float* trow = a.table + (tile + tid) * ld;
+                    float* trow = a.table + (tile + g) * ld;
 #pragma unroll
-                    for (int c = 0; c < UCP; ++c)
-                        if (c < C) trow[c] = v[c];
+                    for (int j = 0; j < 8; ++j)
+                        if (col_of(j) < C) trow[col_of(j)] = v[j];
                 }
             } else if (mine) {
-                float* xr = a.extra + (tile + tid) * C;
+                float* xr = a.extra + (tile + g) * C;
 #pragma unroll
-                for (int c = 0; c < UCP; ++c) {
+                for (int j = 0; j < 8; ++j) {
+                    const int c = col_of(j);
                     if (c < C) {
-                        const float ec = (e[32 + c] + e[16 + c]) + e[c];
+                        const float ec = (e[16 + j] + e[8 + j]) + e[j];
                         xr[c] = a.accumulate ? xr[c] + ec : ec;
                     }
                 }
@@ -486,16 +516,17 @@ __global__ void __launch_bounds__(UT) dense_umma_kernel(UmmaArgs a) {
                 failed = true;
                 break;
             }
-            // U pieces, MN-major: row m = p * 16 + c, core (m/8, tid/8), row tid % 8
+            // U pieces, MN-major: row m = p * 16 + c, core (m/8, g/8), row g % 8;
+            // this thread's 4 columns of each 8-column block are the chunk's half h
 #pragma unroll
             for (int hb = 0; hb < 2; ++hb) {
                 if (hb * 8 >= C) break;
-                uint32_t w[UNP][4];
+                uint32_t w[UNP][2];
 #pragma unroll
-                for (int q = 0; q < 4; ++q) {
+                for (int q = 0; q < 2; ++q) {
                     __nv_bfloat16 h0, m0, l0, h1, m1, l1;
-                    split3(v[hb * 8 + 2 * q], h0, m0, l0);
-                    split3(v[hb * 8 + 2 * q + 1], h1, m1, l1);
+                    split3(v[hb * 4 + 2 * q], h0, m0, l0);
+                    split3(v[hb * 4 + 2 * q + 1], h1, m1, l1);
                     w[0][q] = pack2(h0, h1);
                     w[1][q] = pack2(m0, m1);
                     w[2][q] = pack2(l0, l1);
@@ -503,9 +534,8 @@ __global__ void __launch_bounds__(UT) dense_umma_kernel(UmmaArgs a) {
 #pragma unroll
                 for (int p = 0; p < UNP; ++p) {
                     const uint32_t mb = (uint32_t)(p * 2 + hb);
-                    *reinterpret_cast<uint4*>(sm + L.u + mb * 128 + (uint32_t)(tid / 8) * U_LBO +
-                                              (uint32_t)(tid % 8) * 16) =
-                        make_uint4(w[p][0], w[p][1], w[p][2], w[p][3]);
+                    *reinterpret_cast<uint2*>(sm + L.u + mb * 128 + (uint32_t)(g / 8) * U_LBO + (uint32_t)(g % 8) * 16 +
+                                              (uint32_t)h * 8) = make_uint2(w[p][0], w[p][1]);
                 }
             }
             fence_async_smem();
@@ -539,16 +569,20 @@ __global__ void __launch_bounds__(UT) dense_umma_kernel(UmmaArgs a) {
             // D2 row m = p * 16 + c sits in TMEM lane p * 32 + c (M = 64 layout):
             // warps 0..2, lanes 0..15 -> shared [m][t] floats over the U tile
             float* d2s = reinterpret_cast<float*>(sm + L.u);
-            float d[KT];
-#pragma unroll
-            for (int c0 = 0; c0 < KT; c0 += 16) tmem_ld16(tmem + t_lane + TP::D2 + c0, d, c0);
-            tmem_wait_ld();
             __syncthreads();  // the U tile is free (D2 complete); reuse it for the readback
-            if (warp < UNP && lane < UCP)
+            if (warp < 4) {
 #pragma unroll
-                for (int t = 0; t < KT; ++t) d2s[(warp * UCP + lane) * KT + t] = d[t];
+                for (int c0 = 0; c0 < KT; c0 += 16) {
+                    float d[16];
+                    tmem_ld16(tmem + t_lane + TP::D2 + c0, d, 0);
+                    tmem_wait_ld();
+                    if (warp < UNP && lane < UCP)
+#pragma unroll
+                        for (int t = 0; t < 16; ++t) d2s[(warp * UCP + lane) * KT + c0 + t] = d[t];
+                }
+            }
             __syncthreads();
-            for (int j = tid; j < Gs * C; j += UT) {
+            for (int j = tid; j < Gs * C; j += BT) {
                 const int t = j / C, c = j - t * C;
                 part[j] = ((double)d2s[(32 + c) * KT + t] + (double)d2s[(16 + c) * KT + t]) + (double)d2s[c * KT + t];
             }
@@ -601,7 +635,7 @@ int launch_umma(UmmaArgs a, cudaStream_t s) {
     grid = std::max(grid, 1);
     const long long tiles_per = (tiles + grid - 1) / grid;
     a.per = tiles_per * UT;
-    dense_umma_kernel<KT, SCHUR><<<grid, UT, L.total, s>>>(a);
+    dense_umma_kernel<KT, SCHUR><<<grid, BT, L.total, s>>>(a);
     FEGB_LAUNCH_CHECK("dense small-G pair product (tcgen05)");
     return 0;
 }

@@ -45,7 +45,14 @@ double be_seconds_since(BeClock::time_point t0) {
 
 constexpr int BE_THREADS = 256;
 constexpr int BE_ITEM_ROWS = 16384;  // rows (or clusters) per work item
-constexpr int BE_TILE = 32;          // rows per shared-memory tile of the Gram
+// rows per shared-memory tile of the Gram: about 4096 values (32 KB as FP64),
+// a multiple of 32 between 32 and 256
+__host__ __device__ inline int be_tile_rows(int Cw) {
+    int tr = 4096 / (Cw > 0 ? Cw : 1);
+    tr = tr > 256 ? 256 : tr;
+    tr = tr / 32 * 32;
+    return tr < 32 ? 32 : tr;
+}
 constexpr int BE_PPT = 9;            // output pairs per thread at most (64 columns: 2080 pairs)
 
 struct BeItem {
@@ -124,11 +131,12 @@ __global__ void __launch_bounds__(BE_THREADS)
         double acc[BE_PPT];
 #pragma unroll
         for (int q = 0; q < BE_PPT; ++q) acc[q] = 0.0;
-        for (long long r0 = item.r0; r0 < item.r1; r0 += BE_TILE) {
-            const int rows = (int)min((long long)BE_TILE, item.r1 - r0);
+        const int TR = be_tile_rows(Cw);
+        for (long long r0 = item.r0; r0 < item.r1; r0 += TR) {
+            const int rows = (int)min((long long)TR, item.r1 - r0);
             __syncthreads();  // the previous tile is consumed
-            for (int e = t; e < BE_TILE * Cw; e += BE_THREADS) {
-                const int r = e % BE_TILE, c = e / BE_TILE;  // consecutive threads walk rows of a column
+            for (int e = t; e < TR * Cw; e += BE_THREADS) {
+                const int r = e % TR, c = e / TR;  // consecutive threads walk rows of a column
                 const double v = (r < rows && c < width) ? X(r0 + r, c) : 0.0;
                 if (SPLIT)
                     reinterpret_cast<float2*>(be_smem)[r * Cw + c] = split_f64<56>(v, oor);
@@ -629,15 +637,14 @@ int be_gram(Acc X, const std::vector<BeItem>& hitems, const std::vector<int>& it
     }();
     if (attr != cudaSuccess) return set_cuda_error(attr, "batch gram attr");
     const int grid = std::min(n_items, num_sms() * 4);
-    be_gram_kernel<Acc, true><<<grid, BE_THREADS, sizeof(float2) * BE_TILE * Cw, s>>>(X, d_items, n_items, d_width,
-                                                                                       Cw, part, d_q, d_bad);
+    const size_t smem = sizeof(double) * (size_t)be_tile_rows(Cw) * Cw;  // float2 and double are both 8 bytes
+    be_gram_kernel<Acc, true><<<grid, BE_THREADS, smem, s>>>(X, d_items, n_items, d_width, Cw, part, d_q, d_bad);
     FEGB_LAUNCH_CHECK("batch gram");
     int hbad = 0;
     FEGB_TRY(be_sync_copy(&hbad, d_bad, sizeof(int), cudaMemcpyDeviceToHost, s, "batch split flag copy"));
     if (hbad) {
-        be_gram_kernel<Acc, false><<<grid, BE_THREADS, sizeof(double) * BE_TILE * Cw, s>>>(X, d_items, n_items,
-                                                                                            d_width, Cw, part, d_q + 1,
-                                                                                            d_bad);
+        be_gram_kernel<Acc, false><<<grid, BE_THREADS, smem, s>>>(X, d_items, n_items, d_width, Cw, part, d_q + 1,
+                                                                   d_bad);
         FEGB_LAUNCH_CHECK("batch gram (fp64)");
     }
     be_fold_kernel<<<ns, 256, 0, s>>>(part, d_i0, d_i1, P, out);

@@ -53,7 +53,13 @@ __host__ __device__ inline int be_tile_rows(int Cw) {
     tr = tr / 32 * 32;
     return tr < 32 ? 32 : tr;
 }
-constexpr int BE_PPT = 9;            // output pairs per thread at most (64 columns: 2080 pairs)
+// output pairs per thread: 1 up to 22 columns (253 pairs), else 2, 4 or 9
+// (64 columns: 2080 pairs)
+inline int be_ppt(int Cw) {
+    const int P = Cw * (Cw + 1) / 2;
+    const int npt = (P + 255) / 256;
+    return npt <= 1 ? 1 : npt <= 2 ? 2 : npt <= 4 ? 4 : 9;
+}
 
 struct BeItem {
     int spec;
@@ -96,7 +102,7 @@ struct RowMajor {
 // stay busy whatever the items' sizes; the arithmetic of an item does not
 // depend on the block that takes it. SPLIT: double-single products on the
 // FP32 pipe (a value outside the split range sets *bad); else FP64.
-template <class Acc, bool SPLIT>
+template <class Acc, bool SPLIT, int BE_PPT>
 __global__ void __launch_bounds__(BE_THREADS)
     be_gram_kernel(Acc X, const BeItem* __restrict__ items, int n_items, const int* __restrict__ width_of,
                    int Cw, double* __restrict__ partials, int* __restrict__ queue, int* __restrict__ bad) {
@@ -105,15 +111,16 @@ __global__ void __launch_bounds__(BE_THREADS)
     __shared__ double s_fold[BE_THREADS];
     const int t = threadIdx.x;
     const int P = Cw * (Cw + 1) / 2;
-    // pair assignment: P <= 128: thread = (pair, row phase); else pairs t + j * BE_THREADS
-    const int phases = P <= 128 ? BE_THREADS / P : 1;
-    const int npt = P <= 128 ? 1 : (P + BE_THREADS - 1) / BE_THREADS;
+    // pair assignment: P <= BE_THREADS: thread = (pair, row phase); else pairs t + j * BE_THREADS
+    const bool one = P <= BE_THREADS;
+    const int phases = one ? BE_THREADS / P : 1;
+    const int npt = one ? 1 : (P + BE_THREADS - 1) / BE_THREADS;
     int pi[BE_PPT], pj[BE_PPT];
     bool pv[BE_PPT];
-    const int phase = P <= 128 ? t / P : 0;
+    const int phase = one ? t / P : 0;
 #pragma unroll
     for (int q = 0; q < BE_PPT; ++q) {
-        const int p = P <= 128 ? t % P : t + q * BE_THREADS;
+        const int p = one ? t % P : t + q * BE_THREADS;
         pv[q] = q < npt && p < P && phase < phases;
         int j = 0;
         while ((j + 1) * (j + 2) / 2 <= (pv[q] ? p : 0)) ++j;
@@ -145,17 +152,28 @@ __global__ void __launch_bounds__(BE_THREADS)
             }
             __syncthreads();
             if (SPLIT) {
+                // two rows per step into two sets of sums (independent chains)
                 const float2* x = reinterpret_cast<const float2*>(be_smem);
-                float sh[BE_PPT], sl[BE_PPT];
+                float sh[BE_PPT], sl[BE_PPT], sh2[BE_PPT], sl2[BE_PPT];
 #pragma unroll
-                for (int q = 0; q < BE_PPT; ++q) sh[q] = sl[q] = 0.f;
-                for (int r = phase; r < rows; r += phases) {
+                for (int q = 0; q < BE_PPT; ++q) sh[q] = sl[q] = sh2[q] = sl2[q] = 0.f;
+                int r = phase;
+                for (; r + phases < rows; r += 2 * phases) {
+                    const int r2 = r + phases;
+#pragma unroll
+                    for (int q = 0; q < BE_PPT; ++q)
+                        if (pv[q]) {
+                            ds_fma(x[r * Cw + pi[q]], x[r * Cw + pj[q]], sh[q], sl[q]);
+                            ds_fma(x[r2 * Cw + pi[q]], x[r2 * Cw + pj[q]], sh2[q], sl2[q]);
+                        }
+                }
+                if (r < rows) {
 #pragma unroll
                     for (int q = 0; q < BE_PPT; ++q)
                         if (pv[q]) ds_fma(x[r * Cw + pi[q]], x[r * Cw + pj[q]], sh[q], sl[q]);
                 }
 #pragma unroll
-                for (int q = 0; q < BE_PPT; ++q) acc[q] += (double)sh[q] + (double)sl[q];
+                for (int q = 0; q < BE_PPT; ++q) acc[q] += ((double)sh[q] + (double)sl[q]) + ((double)sh2[q] + (double)sl2[q]);
             } else {
                 const double* x = reinterpret_cast<const double*>(be_smem);
                 for (int r = phase; r < rows; r += phases) {
@@ -166,7 +184,7 @@ __global__ void __launch_bounds__(BE_THREADS)
             }
         }
         double* out = partials + (long long)it * P;
-        if (P <= 128) {
+        if (one) {
             s_fold[t] = pv[0] ? acc[0] : 0.0;
             __syncthreads();
             if (t < P) {
@@ -621,32 +639,31 @@ int be_gram(Acc X, const std::vector<BeItem>& hitems, const std::vector<int>& it
     FEGB_CUDA(cudaMemcpyAsync(d_i1, item1.data(), sizeof(int) * ns, cudaMemcpyHostToDevice, s), "batch item1 copy");
     FEGB_CUDA(cudaMemsetAsync(d_q, 0, sizeof(int) * 2, s), "batch queue reset");
     FEGB_CUDA(cudaMemsetAsync(d_bad, 0, sizeof(int), s), "batch flag reset");
-    static const cudaError_t attr = [] {
-        cudaError_t e = cudaFuncSetAttribute(be_gram_kernel<ColMajorX, true>,
-                                             cudaFuncAttributeMaxDynamicSharedMemorySize, 64 * 1024);
-        if (e == cudaSuccess)
-            e = cudaFuncSetAttribute(be_gram_kernel<ColMajorX, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     64 * 1024);
-        if (e == cudaSuccess)
-            e = cudaFuncSetAttribute(be_gram_kernel<RowMajor, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     64 * 1024);
-        if (e == cudaSuccess)
-            e = cudaFuncSetAttribute(be_gram_kernel<RowMajor, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     64 * 1024);
-        return e;
-    }();
-    if (attr != cudaSuccess) return set_cuda_error(attr, "batch gram attr");
     const int grid = std::min(n_items, num_sms() * 4);
     const size_t smem = sizeof(double) * (size_t)be_tile_rows(Cw) * Cw;  // float2 and double are both 8 bytes
-    be_gram_kernel<Acc, true><<<grid, BE_THREADS, smem, s>>>(X, d_items, n_items, d_width, Cw, part, d_q, d_bad);
-    FEGB_LAUNCH_CHECK("batch gram");
+    auto launch = [&](bool split, int* q) -> int {
+        const int ppt = be_ppt(Cw);
+#define BE_GRAM_CASE(NPT)                                                                                          \
+    if (ppt == NPT) {                                                                                              \
+        if (split)                                                                                                 \
+            be_gram_kernel<Acc, true, NPT><<<grid, BE_THREADS, smem, s>>>(X, d_items, n_items, d_width, Cw, part, q, \
+                                                                          d_bad);                                  \
+        else                                                                                                       \
+            be_gram_kernel<Acc, false, NPT><<<grid, BE_THREADS, smem, s>>>(X, d_items, n_items, d_width, Cw, part,   \
+                                                                           q, d_bad);                              \
+    }
+        BE_GRAM_CASE(1)
+        BE_GRAM_CASE(2)
+        BE_GRAM_CASE(4)
+        BE_GRAM_CASE(9)
+#undef BE_GRAM_CASE
+        FEGB_LAUNCH_CHECK("batch gram");
+        return 0;
+    };
+    FEGB_TRY(launch(true, d_q));
     int hbad = 0;
     FEGB_TRY(be_sync_copy(&hbad, d_bad, sizeof(int), cudaMemcpyDeviceToHost, s, "batch split flag copy"));
-    if (hbad) {
-        be_gram_kernel<Acc, false><<<grid, BE_THREADS, smem, s>>>(X, d_items, n_items, d_width, Cw, part, d_q + 1,
-                                                                   d_bad);
-        FEGB_LAUNCH_CHECK("batch gram (fp64)");
-    }
+    if (hbad) FEGB_TRY(launch(false, d_q + 1));
     be_fold_kernel<<<ns, 256, 0, s>>>(part, d_i0, d_i1, P, out);
     FEGB_LAUNCH_CHECK("batch gram fold");
     return 0;

@@ -364,7 +364,6 @@ __global__ void __launch_bounds__(BT, 4) dense_umma_kernel(UmmaArgs a) {
     // counts of tile j -> count tile j & 1 (BF16 core matrices (g/8, t/8), row
     // g % 8); half h converts the core blocks [h KT/16, (h + 1) KT/16)
     auto convert = [&](int j) -> bool {
-        if (!mbar_wait(&bars[j & 1], (uint32_t)((j >> 1) & 1))) return false;
         const long long tile = tile_of(j);
         const int nt = (int)min((long long)UT, g1 - tile);
         const bool mine = g < nt;
@@ -404,9 +403,14 @@ __global__ void __launch_bounds__(BT, 4) dense_umma_kernel(UmmaArgs a) {
         for (int j = 0; j < 2 && j < ntiles; ++j) issue_raw(j);
         for (int j = 0; j < 2 && j < ntiles; ++j) issue_rows(j);
     }
-    bool ok = convert(0);
-    fence_before_sync();
+    // one thread waits on each mbarrier and the block follows it at a barrier
+    // (the waiting thread's observation of the phase, then bar.sync, orders
+    // the copies' and the MMAs' results before every thread's reads)
+    bool ok = tid != 0 || mbar_wait(&bars[0], 0u);
     if (__syncthreads_or(!ok)) failed = true;
+    if (!failed) convert(0);
+    fence_before_sync();
+    __syncthreads();
     fence_after_sync();
     if (!failed && tid == 0) {
         if (need_e) issue_e(0);
@@ -421,30 +425,38 @@ __global__ void __launch_bounds__(BT, 4) dense_umma_kernel(UmmaArgs a) {
         // (a) counts of tile i + 1 (its count tile was read by the MMAs of tile i - 1)
         ok = true;
         if (i + 1 < ntiles) {
-            if (small && i >= 1) {
-                ok = mbar_wait(&bars[6], (uint32_t)((i - 1) & 1));
-                d2_waited = i - 1;
+            if (tid == 0) {
+                if (small && i >= 1) ok = mbar_wait(&bars[6], (uint32_t)((i - 1) & 1));
+                ok = ok && mbar_wait(&bars[(i + 1) & 1], (uint32_t)(((i + 1) >> 1) & 1));
             }
-            ok = ok && convert(i + 1);
+            if (small && i >= 1) d2_waited = i - 1;
+            if (__syncthreads_or(!ok)) {
+                failed = true;
+                break;
+            }
+            convert(i + 1);
         }
         fence_before_sync();
-        if (__syncthreads_or(!ok)) {
-            failed = true;
-            break;
-        }
+        __syncthreads();  // S1
         fence_after_sync();
         if (tid == 0 && i + 1 < ntiles) {
             if (need_e) issue_e(i + 1);
             if (i + 3 < ntiles) issue_raw(i + 3);  // raw stage (i + 1) & 1 was just consumed
         }
         // (b) this tile: its rows, then E(i)
-        ok = mbar_wait(&bars[2 + (i & 1)], (uint32_t)((i >> 1) & 1));
+        ok = tid != 0 || mbar_wait(&bars[2 + (i & 1)], (uint32_t)((i >> 1) & 1));
+        if (tid == 0 && ok && need_e) ok = mbar_wait(&bars[4 + (i & 1)], (uint32_t)((i >> 1) & 1));
+        if (__syncthreads_or(!ok)) {
+            failed = true;
+            break;
+        }
+        fence_after_sync();
         float v[8];
 #pragma unroll
         for (int j = 0; j < 8; ++j) v[j] = 0.0f;
         int n_g = 0;
         const float* srow = reinterpret_cast<const float*>(sm + ((i & 1) ? L.row1 : L.row0));
-        if (ok && mine) {
+        if (mine) {
             const bool f = full(i);
             if (SCHUR) {
 #pragma unroll
@@ -464,12 +476,6 @@ __global__ void __launch_bounds__(BT, 4) dense_umma_kernel(UmmaArgs a) {
             }
         }
         if (need_e) {
-            ok = ok && mbar_wait(&bars[4 + (i & 1)], (uint32_t)((i >> 1) & 1));
-            if (__syncthreads_or(!ok)) {
-                failed = true;
-                break;
-            }
-            fence_after_sync();
             // E columns of this thread's slots: piece p at p * 16 + c
             float e[24];
             const uint32_t ecol = (i & 1) ? TP::E1 : TP::E0;
@@ -501,20 +507,16 @@ __global__ void __launch_bounds__(BT, 4) dense_umma_kernel(UmmaArgs a) {
                     }
                 }
             }
-        } else if (__syncthreads_or(!ok)) {
-            failed = true;
-            break;
         }
         if (small) {
             // the U tile was read by D2(i - 1)
-            ok = true;
             if (i >= 1 && d2_waited < i - 1) {
-                ok = mbar_wait(&bars[6], (uint32_t)((i - 1) & 1));
+                ok = tid != 0 || mbar_wait(&bars[6], (uint32_t)((i - 1) & 1));
                 d2_waited = i - 1;
-            }
-            if (__syncthreads_or(!ok)) {
-                failed = true;
-                break;
+                if (__syncthreads_or(!ok)) {
+                    failed = true;
+                    break;
+                }
             }
             // U pieces, MN-major: row m = p * 16 + c, core (m/8, g/8), row g % 8;
             // this thread's 4 columns of each 8-column block are the chunk's half h
@@ -560,7 +562,7 @@ __global__ void __launch_bounds__(BT, 4) dense_umma_kernel(UmmaArgs a) {
     if (failed) {
         if (tid == 0) atomicExch(&g_umma_error, 1);
     } else if (small) {
-        const bool okf = mbar_wait(&bars[6], (uint32_t)((ntiles - 1) & 1));
+        const bool okf = tid != 0 || mbar_wait(&bars[6], (uint32_t)((ntiles - 1) & 1));
         if (__syncthreads_or(!okf)) {
             failed = true;
             if (tid == 0) atomicExch(&g_umma_error, 1);

@@ -63,7 +63,7 @@ constexpr TuneSpec kTune[TUNE_COUNT] = {
     {"cg_cols_per_pass", 0, 0, 8},
     {"split_gram_pairs_per_col", 3, 1, 1 << 20},
     {"cg_graph", 1, 0, 1},
-    {"batch_estimator", 0, 0, 1},
+    {"batch_estimator", 1, 0, 1},
 };
 std::atomic<int> g_tune[TUNE_COUNT] = {{kTune[0].def}, {kTune[1].def}, {kTune[2].def}, {kTune[3].def},
                                        {kTune[4].def}};

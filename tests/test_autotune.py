@@ -8,7 +8,7 @@ from fe_gpu_gb300 import autotune as A
 
 def test_knobs_set_get_reset(built):
     A.reset()
-    assert A.get_knob("dense_form") == -1 and A.get_knob("cg_graph") == 1
+    assert A.get_knob("dense_form") == -1 and A.get_knob("cg_graph") == 1 and A.get_knob("batch_estimator") == 1
     A.set_knob("cg_cols_per_pass", 8)
     assert A.get_knob("cg_cols_per_pass") == 8
     assert N.lib().fegb_set_tuning(b"cg_cols_per_pass", 5) != 0  # only 0, 4 or 8

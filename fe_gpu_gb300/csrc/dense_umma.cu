@@ -53,8 +53,9 @@
 //
 // Every wait (mbarrier phases of the copies and of the MMAs) is bounded by a
 // globaltimer limit; a CTA that runs out of time records it in an error word
-// that the host reads after the within-transform, releases its tensor memory
-// and returns.
+// that the host reads after the within-transform, waits (each wait bounded
+// again) for the copies and MMAs it still has in flight, releases its tensor
+// memory and returns.
 #include "common.cuh"
 #include "sweep.cuh"
 
@@ -269,6 +270,9 @@ __global__ void __launch_bounds__(BT, 4) dense_umma_kernel(UmmaArgs a) {
     extern __shared__ __align__(1024) unsigned char sm[];
     // 0, 1: raw-count stages; 2, 3: row stages; 4, 5: E buffers; 6: D2
     __shared__ __align__(8) uint64_t bars[7];
+    // phases armed (copies or MMA commits issued) and phases waited, per
+    // barrier; only the elected thread touches them
+    __shared__ uint32_t s_arm[7], s_done[7];
     __shared__ uint32_t tmem_base_s;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int g = tid & (UT - 1), h = tid / UT;
@@ -301,7 +305,11 @@ __global__ void __launch_bounds__(BT, 4) dense_umma_kernel(UmmaArgs a) {
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
     }
     if (tid == 0) {
-        for (int i = 0; i < 7; ++i) mbar_init(&bars[i], 1);
+        for (int i = 0; i < 7; ++i) {
+            mbar_init(&bars[i], 1);
+            s_arm[i] = 0;
+            s_done[i] = 0;
+        }
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     // U tile zeroed once (rows 48..63 and columns past C stay zero), S pieces
@@ -334,6 +342,7 @@ __global__ void __launch_bounds__(BT, 4) dense_umma_kernel(UmmaArgs a) {
     // without copies; its threads read their rows from global memory
     auto issue_raw = [&](int j) {
         uint64_t* bar = &bars[j & 1];
+        ++s_arm[j & 1];
         if (!full(j)) {
             mbar_arrive(bar);
             return;
@@ -345,6 +354,7 @@ __global__ void __launch_bounds__(BT, 4) dense_umma_kernel(UmmaArgs a) {
     const bool rows_needed = SCHUR || small;
     auto issue_rows = [&](int j) {
         uint64_t* bar = &bars[2 + (j & 1)];
+        ++s_arm[2 + (j & 1)];
         if (!full(j) || !rows_needed) {
             mbar_arrive(bar);
             return;
@@ -359,6 +369,13 @@ __global__ void __launch_bounds__(BT, 4) dense_umma_kernel(UmmaArgs a) {
             mbar_arrive_tx(bar, (uint32_t)(UT * ld * 4));
             bulk_copy(row, a.pe + tile_of(j) * ld, (uint32_t)(UT * ld * 4), bar);
         }
+    };
+    // waits for the next phase of barrier b (phases complete in issue order,
+    // so the parity of the next one is the count of phases waited so far)
+    auto bar_wait = [&](int b) -> bool {
+        const bool r = mbar_wait(&bars[b], s_done[b] & 1u);
+        if (r) ++s_done[b];
+        return r;
     };
     bool failed = false;
     // counts of tile j -> count tile j & 1 (BF16 core matrices (g/8, t/8), row
@@ -395,6 +412,7 @@ __global__ void __launch_bounds__(BT, 4) dense_umma_kernel(UmmaArgs a) {
         for (int s = 0; s < KT / 16; ++s)
             umma_bf16(tmem + ecol, umma_desc(sbase + cnt_off + s * 256, 128, CORE_ROW),
                       umma_desc(sbase + L.b1 + s * 256, 128, CORE_ROW), id, s > 0);
+        ++s_arm[4 + (j & 1)];
         umma_commit(&bars[4 + (j & 1)]);
     };
 
@@ -406,7 +424,7 @@ __global__ void __launch_bounds__(BT, 4) dense_umma_kernel(UmmaArgs a) {
     // one thread waits on each mbarrier and the block follows it at a barrier
     // (the waiting thread's observation of the phase, then bar.sync, orders
     // the copies' and the MMAs' results before every thread's reads)
-    bool ok = tid != 0 || mbar_wait(&bars[0], 0u);
+    bool ok = tid != 0 || bar_wait(0);
     if (__syncthreads_or(!ok)) failed = true;
     if (!failed) convert(0);
     fence_before_sync();
@@ -426,8 +444,8 @@ __global__ void __launch_bounds__(BT, 4) dense_umma_kernel(UmmaArgs a) {
         ok = true;
         if (i + 1 < ntiles) {
             if (tid == 0) {
-                if (small && i >= 1) ok = mbar_wait(&bars[6], (uint32_t)((i - 1) & 1));
-                ok = ok && mbar_wait(&bars[(i + 1) & 1], (uint32_t)(((i + 1) >> 1) & 1));
+                if (small && i >= 1) ok = bar_wait(6);
+                ok = ok && bar_wait((i + 1) & 1);
             }
             if (small && i >= 1) d2_waited = i - 1;
             if (__syncthreads_or(!ok)) {
@@ -444,8 +462,8 @@ __global__ void __launch_bounds__(BT, 4) dense_umma_kernel(UmmaArgs a) {
             if (i + 3 < ntiles) issue_raw(i + 3);  // raw stage (i + 1) & 1 was just consumed
         }
         // (b) this tile: its rows, then E(i)
-        ok = tid != 0 || mbar_wait(&bars[2 + (i & 1)], (uint32_t)((i >> 1) & 1));
-        if (tid == 0 && ok && need_e) ok = mbar_wait(&bars[4 + (i & 1)], (uint32_t)((i >> 1) & 1));
+        ok = tid != 0 || bar_wait(2 + (i & 1));
+        if (tid == 0 && ok && need_e) ok = bar_wait(4 + (i & 1));
         if (__syncthreads_or(!ok)) {
             failed = true;
             break;
@@ -511,7 +529,7 @@ __global__ void __launch_bounds__(BT, 4) dense_umma_kernel(UmmaArgs a) {
         if (small) {
             // the U tile was read by D2(i - 1)
             if (i >= 1 && d2_waited < i - 1) {
-                ok = tid != 0 || mbar_wait(&bars[6], (uint32_t)((i - 1) & 1));
+                ok = tid != 0 || bar_wait(6);
                 d2_waited = i - 1;
                 if (__syncthreads_or(!ok)) {
                     failed = true;
@@ -554,6 +572,7 @@ __global__ void __launch_bounds__(BT, 4) dense_umma_kernel(UmmaArgs a) {
                     umma_bf16(tmem + TP::D2, umma_desc(sbase + L.u + s * 2 * U_LBO, U_LBO, 128),
                               umma_desc(sbase + cnt_off + s * 2 * CORE_ROW, CORE_ROW, 128), id,
                               (i > 0 || s > 0) ? 1 : 0);
+                ++s_arm[6];
                 umma_commit(&bars[6]);
             }
             if (i + 2 < ntiles) issue_rows(i + 2);  // row stage i & 1 was read before S2
@@ -562,7 +581,7 @@ __global__ void __launch_bounds__(BT, 4) dense_umma_kernel(UmmaArgs a) {
     if (failed) {
         if (tid == 0) atomicExch(&g_umma_error, 1);
     } else if (small) {
-        const bool okf = tid != 0 || mbar_wait(&bars[6], (uint32_t)((ntiles - 1) & 1));
+        const bool okf = tid != 0 || bar_wait(6);
         if (__syncthreads_or(!okf)) {
             failed = true;
             if (tid == 0) atomicExch(&g_umma_error, 1);
@@ -590,6 +609,13 @@ __global__ void __launch_bounds__(BT, 4) dense_umma_kernel(UmmaArgs a) {
             }
         }
     }
+    // after a wait ran out of time: let every copy and MMA still in flight
+    // land (each wait bounded again) before the shared memory and the tensor
+    // memory are given back
+    if (failed && tid == 0)
+        for (int b = 0; b < 7; ++b)
+            while (s_done[b] < s_arm[b] && bar_wait(b)) {
+            }
     fence_before_sync();
     __syncthreads();
     if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TP::COLS));

@@ -1815,9 +1815,10 @@ __host__ __device__ constexpr int piece_width(int w) {
     return w >= W ? W : (w > W / 2 ? W : (w > 2 ? (W >= 4 ? 4 : W) : (w == 2 ? 2 : 1)));
 }
 
-// v[0..TILE) -= row[0..cw) of one source table (row already offset to column c0)
-template <typename T, int TILE, int K = 0>
-__device__ __forceinline__ void cg_sub_row(const T* __restrict__ row, int cw, T (&v)[TILE], unsigned long long pol) {
+// v[0..TILE) += row[0..cw) of one source table (row already offset to column
+// c0); FIRST: v = row instead (columns past cw keep their zeros)
+template <typename T, int TILE, bool FIRST, int K = 0>
+__device__ __forceinline__ void cg_add_row(const T* __restrict__ row, int cw, T (&v)[TILE], unsigned long long pol) {
     constexpr int W = 32 / (int)sizeof(T);  // elements per 256-bit load
     if constexpr (K * W < TILE) {
         if (K * W >= cw) return;
@@ -1827,8 +1828,13 @@ __device__ __forceinline__ void cg_sub_row(const T* __restrict__ row, int cw, T 
         ld_piece<NE>(row + W * K, w, pol);
 #pragma unroll
         for (int m = 0; m < NE; ++m)
-            if (W * K + m < TILE) v[W * K + m] -= w[m];
-        cg_sub_row<T, TILE, K + 1>(row, cw, v, pol);
+            if (W * K + m < TILE) {
+                if (FIRST)
+                    v[W * K + m] = w[m];
+                else
+                    v[W * K + m] += w[m];
+            }
+        cg_add_row<T, TILE, FIRST, K + 1>(row, cw, v, pol);
     }
 }
 
@@ -1850,15 +1856,17 @@ struct CGRun {
     bool started;
 };
 
-// Adds one position (group g, contribution v) to the lane's run state.
+// Adds one position (group g, contribution a * v) to the lane's run state: a
+// run that continues takes run += a * v as one fused multiply-add (a = -1
+// without weights: exactly run - v).
 template <typename T, int TILE>
-__device__ __forceinline__ void cg_run_push(CGRun<T, TILE>& st, int g, const T (&v)[TILE], T* __restrict__ sums,
+__device__ __forceinline__ void cg_run_push(CGRun<T, TILE>& st, int g, T a, const T (&v)[TILE], T* __restrict__ sums,
                                             int SC, int c0, int cw) {
     if (!st.started) {
         st.started = true;
         st.firstg = st.cur = g;
 #pragma unroll
-        for (int i = 0; i < TILE; ++i) st.run[i] = v[i];
+        for (int i = 0; i < TILE; ++i) st.run[i] = a * v[i];
         return;
     }
     if (g != st.cur) {
@@ -1875,10 +1883,10 @@ __device__ __forceinline__ void cg_run_push(CGRun<T, TILE>& st, int g, const T (
         }
         st.cur = g;
 #pragma unroll
-        for (int i = 0; i < TILE; ++i) st.run[i] = v[i];
+        for (int i = 0; i < TILE; ++i) st.run[i] = a * v[i];
     } else {
 #pragma unroll
-        for (int i = 0; i < TILE; ++i) st.run[i] += v[i];
+        for (int i = 0; i < TILE; ++i) st.run[i] = fma(a, v[i], st.run[i]);
     }
 }
 
@@ -1941,15 +1949,11 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 && CGR_TILE <= 12) ? CG_R
                     T v[CGR_TILE];
 #pragma unroll
                     for (int i = 0; i < CGR_TILE; ++i) v[i] = T(0);
+                    cg_add_row<T, CGR_TILE, true>(tabs[0] + (long long)sid[0][m] * LD, cw, v, keep);
 #pragma unroll
-                    for (int e = 0; e < NSRC; ++e)
-                        cg_sub_row<T, CGR_TILE>(tabs[e] + (long long)sid[e][m] * LD, cw, v, keep);
-                    if (p.weight) {
-                        const T w = (T)wq[m];
-#pragma unroll
-                        for (int i = 0; i < CGR_TILE; ++i) v[i] *= w;
-                    }
-                    cg_run_push(st, gq[m], v, p.sums, C, c0, cw);
+                    for (int e = 1; e < NSRC; ++e)
+                        cg_add_row<T, CGR_TILE, false>(tabs[e] + (long long)sid[e][m] * LD, cw, v, keep);
+                    cg_run_push(st, gq[m], p.weight ? -(T)wq[m] : T(-1), v, p.sums, C, c0, cw);
                 }
             } else {
                 // ragged end of the last chunk
@@ -1959,13 +1963,9 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 && CGR_TILE <= 12) ? CG_R
                     for (int i = 0; i < CGR_TILE; ++i) v[i] = T(0);
 #pragma unroll
                     for (int e = 0; e < NSRC; ++e)
-                        cg_sub_row<T, CGR_TILE>(tabs[e] + (long long)__ldg(sgid[e] + j) * LD, cw, v, keep);
-                    if (p.weight) {
-                        const T w = (T)__ldg(p.weight + j);
-#pragma unroll
-                        for (int i = 0; i < CGR_TILE; ++i) v[i] *= w;
-                    }
-                    cg_run_push(st, __ldg(gseq + j), v, p.sums, C, c0, cw);
+                        cg_add_row<T, CGR_TILE, false>(tabs[e] + (long long)__ldg(sgid[e] + j) * LD, cw, v, keep);
+                    cg_run_push(st, __ldg(gseq + j), p.weight ? -(T)__ldg(p.weight + j) : T(-1), v, p.sums, C, c0,
+                                cw);
                 }
             }
         }
@@ -1975,13 +1975,9 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 && CGR_TILE <= 12) ? CG_R
 #pragma unroll
             for (int i = 0; i < CGR_TILE; ++i) v[i] = T(0);
             for (int e = 0; e < p.n_src; ++e)
-                cg_sub_row<T, CGR_TILE>(p.src_tab[e] + (long long)__ldcs(p.src_gid[e] + j) * LD + c0, cw, v, keep);
-            if (p.weight) {
-                const T w = (T)__ldcs(p.weight + j);
-#pragma unroll
-                for (int i = 0; i < CGR_TILE; ++i) v[i] *= w;
-            }
-            cg_run_push(st, __ldcs(gseq + j), v, p.sums, C, c0, cw);
+                cg_add_row<T, CGR_TILE, false>(p.src_tab[e] + (long long)__ldcs(p.src_gid[e] + j) * LD + c0, cw, v,
+                                               keep);
+            cg_run_push(st, __ldcs(gseq + j), p.weight ? -(T)__ldcs(p.weight + j) : T(-1), v, p.sums, C, c0, cw);
         }
     }
     const int firstg = st.firstg;

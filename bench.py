@@ -565,7 +565,7 @@ def roofline_of(results, workload, elements_per_sweep=None):
             "fp64_pipe": fp64,
             "unit": "GB/s", "frac": achieved / peak if peak else None, "traffic": traffic,
             "traffic_source": ("ncu dram__bytes_read.sum + dram__bytes_write.sum per launch, " +
-                               TRAFFIC_SOURCE[FAMILIES[top]]) if traffic is not None else None,
+                               TRAFFIC_SOURCE[(workload, FAMILIES[top])]) if traffic is not None else None,
             "alg_bytes_definition": ALG_BYTES["segment" if top < 4 else ("cg" if top < 6 else "dense")],
             "launches": nlaunch[top], "avg_launch_ms": secs[top] / max(1, nlaunch[top]) * 1e3,
             "alg_bytes_per_launch": nbytes[top] / max(1, nlaunch[top]),
@@ -888,10 +888,13 @@ def formula_cpu_baseline(threads):
 TRAFFIC_PER_LAUNCH: dict = {
     ("worker_firm_20M", "CG operator segment sweep fp32"): 1.027e+08,
     ("worker_firm_20M", "segment sweep fp64"): 2.027e+09,
+    ("worker_firm_150M", "CG operator segment sweep fp32"): 1.0725e+09,
 }
 TRAFFIC_SOURCE = {
-    "CG operator segment sweep fp32": "profiles/cg_rows_worker_firm_20M.md",
-    "segment sweep fp64": "profiles/fp64_sweeps_worker_firm_5M.md (5M-row capture scaled by rows)",
+    ("worker_firm_20M", "CG operator segment sweep fp32"): "profiles/cg_rows_worker_firm_20M.md",
+    ("worker_firm_20M", "segment sweep fp64"): "profiles/fp64_sweeps_worker_firm_5M.md (5M-row capture scaled by rows)",
+    ("worker_firm_150M", "CG operator segment sweep fp32"):
+        "profiles/dram_cg_operator_worker_firm_150M.md (full-size one-pass capture, two iterations)",
 }
 
 

@@ -3,8 +3,9 @@
 The knobs select, for a problem shape, between equivalent forms of the hot
 kernels: the count-matrix pass on the tensor cores or the CUDA cores, the
 number of table columns one CG operator sweep carries per pass (4, 8 or all),
-the output size from which Gram products use the split-FP32 form, and whether
-the CG loop runs as a CUDA graph. None changes the result beyond rounding.
+the output size from which Gram products use the split-FP32 form, whether
+the CG loop runs as a CUDA graph, and whether operator sweeps of streams with
+short groups run one thread per group. None changes the result beyond rounding.
 
     python -m fe_gpu_gb300.autotune [--out PATH] [--repeats R] [--quick]
 
@@ -35,6 +36,7 @@ KNOBS = {
     "cg_cols_per_pass": [0, 8, 4],
     "split_gram_pairs_per_col": [3, 1, 8],
     "cg_graph": [1, 0],
+    "cg_short_groups": [1, 0],
 }
 
 

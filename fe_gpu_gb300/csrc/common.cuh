@@ -108,12 +108,15 @@ void configure_mem_pool();
 //   TUNE_CG_GRAPH         1 the CG loop runs as a CUDA graph, 0 host-driven
 //   TUNE_BATCH_ESTIMATOR  1 batched specifications are estimated class by
 //                         class in one batched pass, 0 one by one
+//   TUNE_CG_SHORT         1 operator sweeps of streams whose groups are all
+//                         short run one thread per group, 0 the chunked sweep
 enum TuneKey {
     TUNE_DENSE_FORM = 0,
     TUNE_CG_COLS_PER_PASS,
     TUNE_SPLIT_GRAM,
     TUNE_CG_GRAPH,
     TUNE_BATCH_ESTIMATOR,
+    TUNE_CG_SHORT,
     TUNE_COUNT
 };
 int tuning(TuneKey key);

@@ -1048,6 +1048,7 @@ struct CGBuffers {
         int n_long = 0;
         const int32_t* multi_list = nullptr;
         int n_multi = 0;
+        bool short_groups = false;  // every group short: the one-thread-per-group sweep applies
     };
     std::vector<Stream> stream;
     bool compressed = false;
@@ -1453,6 +1454,17 @@ int cg_alloc(Problem& P, CGBuffers<T>& B) {
         }
     }
     FEGB_TRY(cg_streams(P, B));
+    // streams whose groups are all short (a worker's few firms) take the
+    // one-thread-per-group sweep
+    for (int d = 0; d < P.n_fe; ++d) {
+        auto& st = B.stream[d];
+        st.short_groups = false;
+        if (st.n_src < 1 || st.n_src > 3 || !st.off || P.dims[d].G <= 0) continue;
+        if ((long long)P.dims[d].G * CG_SHORT_MEAN < st.m) continue;
+        int longest = 0;
+        FEGB_TRY(max_group_length(st.off, P.dims[d].G, &longest, P.s));
+        st.short_groups = longest <= CG_SHORT_MAX;
+    }
     if (B.schur) FEGB_TRY(cg_schur_precond(P, B));
     // the operator sweep's sums / head / tail, compact rows of C
     {
@@ -1520,9 +1532,13 @@ int cg_sweep(Problem& P, CGBuffers<T>& B, int d, int* n_src) {
         (double)st.m * (4.0 * (1 + rp.n_src) + (st.weight ? 4.0 : 0.0) + (double)rp.n_src * C * sizeof(T));
     CGTimer tm(P);
     FEGB_TRY(tm.begin(4 + (sizeof(T) == 4 ? 1 : 0), bytes));
-    FEGB_TRY(launch_cg_rows<T>(rp, P.s));
-    FEGB_TRY(launch_group_sums<T>(st.off, B.head, B.tail, CG_CHUNK, C, st.long_list, st.n_long, st.multi_list,
-                                  st.n_multi, B.sums, P.s));
+    if (st.short_groups && tuning(TUNE_CG_SHORT)) {
+        FEGB_TRY(launch_cg_short<T>(rp, st.off, P.dims[d].G, P.s));
+    } else {
+        FEGB_TRY(launch_cg_rows<T>(rp, P.s));
+        FEGB_TRY(launch_group_sums<T>(st.off, B.head, B.tail, CG_CHUNK, C, st.long_list, st.n_long, st.multi_list,
+                                      st.n_multi, B.sums, P.s));
+    }
     FEGB_TRY(tm.end());
     P.demean_bytes += bytes;
     return 0;

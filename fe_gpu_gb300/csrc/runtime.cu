@@ -64,9 +64,10 @@ constexpr TuneSpec kTune[TUNE_COUNT] = {
     {"split_gram_pairs_per_col", 3, 1, 1 << 20},
     {"cg_graph", 1, 0, 1},
     {"batch_estimator", 1, 0, 1},
+    {"cg_short_groups", 1, 0, 1},
 };
-std::atomic<int> g_tune[TUNE_COUNT] = {{kTune[0].def}, {kTune[1].def}, {kTune[2].def}, {kTune[3].def},
-                                       {kTune[4].def}};
+std::atomic<int> g_tune[TUNE_COUNT] = {{kTune[0].def}, {kTune[1].def}, {kTune[2].def},
+                                       {kTune[3].def}, {kTune[4].def}, {kTune[5].def}};
 }  // namespace
 
 int tuning(TuneKey key) { return g_tune[key].load(std::memory_order_relaxed); }

@@ -2095,6 +2095,128 @@ int launch_cg_rows(const CGRowsParams<T>& p, cudaStream_t s) {
     return launch_cg_rows_nsrc<T, 16>(p, s);
 }
 
+// Operator sweep of a stream whose groups are all short (every group at most
+// CG_SHORT_MAX positions, on average at most CG_SHORT_MEAN): thread t takes
+// column tile t / G of group t % G, so a warp covers 32 consecutive groups and
+// their contiguous positions. The thread sums its group's positions in order
+// (run = fma(a, v, run) from zero: the first step is the rounded product a * v,
+// as in a lane of the chunked sweep) and writes the complete sum; empty groups
+// get zeros. Two positions are
+// loaded ahead so that their row gathers are in flight together.
+template <typename T, int TILE, int NSRC>
+__global__ void __launch_bounds__(256) cg_short_kernel(CGRowsParams<T> p, const int32_t* __restrict__ off, int G,
+                                                       int ntiles) {
+    const long long t = (long long)blockIdx.x * 256 + threadIdx.x;
+    if (t >= (long long)G * ntiles) return;
+    const int tile = (int)(t / G);
+    const int g = (int)(t - (long long)tile * G);
+    const int c0 = tile * TILE;
+    const int cw = min(TILE, p.C - c0);
+    const int j0 = __ldg(off + g), j1 = __ldg(off + g + 1);
+    const unsigned long long keep = l2_policy_evict_last();
+    const T* tabs[NSRC];
+#pragma unroll
+    for (int e = 0; e < NSRC; ++e) tabs[e] = p.src_tab[e] + c0;
+    T run[TILE];
+#pragma unroll
+    for (int i = 0; i < TILE; ++i) run[i] = T(0);
+    int j = j0;
+    for (; j + 1 < j1; j += 2) {
+        T v0[TILE], v1[TILE];
+#pragma unroll
+        for (int i = 0; i < TILE; ++i) v0[i] = v1[i] = T(0);
+        int s0[NSRC], s1[NSRC];
+#pragma unroll
+        for (int e = 0; e < NSRC; ++e) {
+            s0[e] = __ldcs(p.src_gid[e] + j);
+            s1[e] = __ldcs(p.src_gid[e] + j + 1);
+        }
+        const T a0 = p.weight ? -(T)__ldcs(p.weight + j) : T(-1);
+        const T a1 = p.weight ? -(T)__ldcs(p.weight + j + 1) : T(-1);
+        cg_add_row<T, TILE, true>(tabs[0] + (long long)s0[0] * p.ld, cw, v0, keep);
+        cg_add_row<T, TILE, true>(tabs[0] + (long long)s1[0] * p.ld, cw, v1, keep);
+#pragma unroll
+        for (int e = 1; e < NSRC; ++e) {
+            cg_add_row<T, TILE, false>(tabs[e] + (long long)s0[e] * p.ld, cw, v0, keep);
+            cg_add_row<T, TILE, false>(tabs[e] + (long long)s1[e] * p.ld, cw, v1, keep);
+        }
+#pragma unroll
+        for (int i = 0; i < TILE; ++i) run[i] = fma(a0, v0[i], run[i]);
+#pragma unroll
+        for (int i = 0; i < TILE; ++i) run[i] = fma(a1, v1[i], run[i]);
+    }
+    if (j < j1) {
+        T v0[TILE];
+#pragma unroll
+        for (int i = 0; i < TILE; ++i) v0[i] = T(0);
+#pragma unroll
+        for (int e = 0; e < NSRC; ++e)
+            cg_add_row<T, TILE, false>(tabs[e] + (long long)__ldcs(p.src_gid[e] + j) * p.ld, cw, v0, keep);
+        const T a0 = p.weight ? -(T)__ldcs(p.weight + j) : T(-1);
+#pragma unroll
+        for (int i = 0; i < TILE; ++i) run[i] = fma(a0, v0[i], run[i]);
+    }
+    T* dst = p.sums + (long long)g * p.C + c0;
+#pragma unroll
+    for (int i = 0; i < TILE; ++i)
+        if (i < cw) dst[i] = run[i];
+}
+
+template <typename T, int TILE>
+int launch_cg_short_tile(const CGRowsParams<T>& p, const int32_t* off, int G, cudaStream_t s) {
+    const int ntiles = (p.C + TILE - 1) / TILE;
+    const long long threads = (long long)G * ntiles;
+    const long long blocks = (threads + 255) / 256;
+    if (p.n_src == 1)
+        cg_short_kernel<T, TILE, 1><<<(unsigned)blocks, 256, 0, s>>>(p, off, G, ntiles);
+    else if (p.n_src == 2)
+        cg_short_kernel<T, TILE, 2><<<(unsigned)blocks, 256, 0, s>>>(p, off, G, ntiles);
+    else
+        cg_short_kernel<T, TILE, 3><<<(unsigned)blocks, 256, 0, s>>>(p, off, G, ntiles);
+    FEGB_LAUNCH_CHECK("cg operator sweep (short groups)");
+    return 0;
+}
+
+template <typename T>
+int launch_cg_short(const CGRowsParams<T>& p, const int32_t* off, int G, cudaStream_t s) {
+    if (G <= 0) return 0;
+    if (p.n_src < 1 || p.n_src > 3) return set_error("cg short-group sweep: %d sources", p.n_src);
+    if (p.ld % (32 / (int)sizeof(T)) != 0) return set_error("cg operator: row stride %d is not a 32-byte multiple", p.ld);
+    for (int e = 0; e < p.n_src; ++e)
+        if ((reinterpret_cast<uintptr_t>(p.src_tab[e]) & 31u) != 0) return set_error("cg operator: unaligned table");
+    const int cap = tuning(TUNE_CG_COLS_PER_PASS);
+    if (p.C <= 4 || cap == 4) return launch_cg_short_tile<T, 4>(p, off, G, s);
+    if (p.C <= 8 || cap == 8) return launch_cg_short_tile<T, 8>(p, off, G, s);
+    if (p.C == 9) return launch_cg_short_tile<T, 9>(p, off, G, s);
+    if (p.C <= 12) return launch_cg_short_tile<T, 12>(p, off, G, s);
+    return launch_cg_short_tile<T, 16>(p, off, G, s);
+}
+
+__global__ void max_group_length_kernel(const int32_t* __restrict__ off, int G, int* __restrict__ out) {
+    int m = 0;
+    for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < G; g += gridDim.x * blockDim.x)
+        m = max(m, off[g + 1] - off[g]);
+    for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(out, m);
+}
+
+int max_group_length(const int32_t* off, int G, int* out, cudaStream_t s) {
+    *out = 0;
+    if (G <= 0) return 0;
+    int* d = nullptr;
+    FEGB_CUDA(cudaMallocAsync(&d, sizeof(int), s), "max group length");
+    FEGB_CUDA(cudaMemsetAsync(d, 0, sizeof(int), s), "max group length reset");
+    max_group_length_kernel<<<grid_stride_blocks(G, 256), 256, 0, s>>>(off, G, d);
+    FEGB_LAUNCH_CHECK("max group length");
+    FEGB_CUDA(cudaMemcpyAsync(out, d, sizeof(int), cudaMemcpyDeviceToHost, s), "max group length copy");
+    FEGB_CUDA(cudaFreeAsync(d, s), "max group length free");
+    FEGB_CUDA(cudaStreamSynchronize(s), "max group length sync");
+    return 0;
+}
+
+template int launch_cg_short<double>(const CGRowsParams<double>&, const int32_t*, int, cudaStream_t);
+template int launch_cg_short<float>(const CGRowsParams<float>&, const int32_t*, int, cudaStream_t);
+
 template int launch_cg_rows<double>(const CGRowsParams<double>&, cudaStream_t);
 template int launch_cg_rows<float>(const CGRowsParams<float>&, cudaStream_t);
 

@@ -192,6 +192,18 @@ struct CGRowsParams {
 template <typename T>
 int launch_cg_rows(const CGRowsParams<T>& p, cudaStream_t s);
 
+// Operator sweep of a stream whose groups all have few positions (at most
+// CG_SHORT_MAX, on average at most CG_SHORT_MEAN): one thread per (group,
+// column tile) writes the complete group sums into p.sums; the chunk heads,
+// tails and the group-sum pass are not used. off: G + 1 offsets of the groups'
+// positions; p.n_src from 1 to 3.
+constexpr int CG_SHORT_MAX = 64;
+constexpr int CG_SHORT_MEAN = 8;
+template <typename T>
+int launch_cg_short(const CGRowsParams<T>& p, const int32_t* off, int G, cudaStream_t s);
+// Largest off[g + 1] - off[g] over the G groups (host result, synchronises s).
+int max_group_length(const int32_t* off, int G, int* out, cudaStream_t s);
+
 // Row stride of the CG G-space vectors: rows padded to 32-byte multiples (a
 // multiple of 16 columns above 16) so that table rows load as 256-bit vectors.
 inline int cg_row_stride(int C, int elem_bytes) {

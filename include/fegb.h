@@ -155,6 +155,9 @@ long long fegb_kernel_launches(void);
  *   "cg_graph"                  1: the CG loop runs as a CUDA graph; 0: host loop
  *   "batch_estimator"           1: fegb_estimate_batch estimates each column
  *                               class in one batched pass; 0: spec by spec
+ *   "cg_short_groups"           1: a CG operator sweep whose groups all have
+ *                               few positions runs one thread per group; 0:
+ *                               the chunked sweep for every stream
  * No knob changes what is computed beyond rounding; unknown keys and values
  * out of range return a nonzero status. */
 int fegb_set_tuning(const char* key, int value);

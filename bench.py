@@ -281,7 +281,7 @@ def main():
                     help="within-transform of the headline form (the FP64 comparison always uses AP)")
     ap.add_argument("--fp64-steps", type=int, default=1,
                     help="timed steps of each plain FP64 form (AP and CG; no warm-up of their own)")
-    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--file", choices=["auto", "on", "off"], default="auto",
                     help=".bin file leg (write the panel once, load it to the device, fit); auto: panels up to "
@@ -886,12 +886,13 @@ def formula_cpu_baseline(threads):
 #   5M rows, times 4: the traffic is row data).
 # Other workloads were not captured.
 TRAFFIC_PER_LAUNCH: dict = {
-    ("worker_firm_20M", "CG operator segment sweep fp32"): 1.027e+08,
+    ("worker_firm_20M", "CG operator segment sweep fp32"): 7.65e+07,
     ("worker_firm_20M", "segment sweep fp64"): 2.027e+09,
     ("worker_firm_150M", "CG operator segment sweep fp32"): 1.0725e+09,
 }
 TRAFFIC_SOURCE = {
-    ("worker_firm_20M", "CG operator segment sweep fp32"): "profiles/cg_rows_worker_firm_20M.md",
+    ("worker_firm_20M", "CG operator segment sweep fp32"):
+        "profiles/dram_cg_operator_worker_firm_20M.md (full-size one-pass capture, two iterations)",
     ("worker_firm_20M", "segment sweep fp64"): "profiles/fp64_sweeps_worker_firm_5M.md (5M-row capture scaled by rows)",
     ("worker_firm_150M", "CG operator segment sweep fp32"):
         "profiles/dram_cg_operator_worker_firm_150M.md (full-size one-pass capture, two iterations)",

@@ -68,7 +68,7 @@ namespace fegb {
 
 namespace {
 
-constexpr int UT = 128;        // groups per tile (= threads per CTA: thread r owns row r of the tile)
+constexpr int UT = 128;        // groups per tile (two threads per group, each with half of its columns)
 constexpr int UCP = 16;        // columns per piece block (C <= 16)
 constexpr int UNP = 3;         // BF16 pieces per FP32 value
 constexpr int UN1 = UNP * UCP; // N of the e-side product
@@ -509,10 +509,13 @@ __global__ void __launch_bounds__(BT, 4) dense_umma_kernel(UmmaArgs a) {
                 for (int j = 0; j < 8; ++j)
                     if (col_of(j) < C) v[j] = n_g > 0 ? (v[j] - ((e[16 + j] + e[8 + j]) + e[j])) * rn : 0.0f;
                 if (mine) {
-                    float* trow = a.table + (tile + g) * ld;
-#pragma unroll
-                    for (int j = 0; j < 8; ++j)
-                        if (col_of(j) < C) trow[col_of(j)] = v[j];
+                    // this thread's two 16-byte column quads of the padded row
+                    // (zeros past C): whole 32-byte sectors are written, so
+                    // none has to be read back to merge a partial write
+                    float* trow = a.table + (tile + g) * ld + 4 * h;
+                    if (4 * h + 4 <= ld) *reinterpret_cast<float4*>(trow) = make_float4(v[0], v[1], v[2], v[3]);
+                    if (8 + 4 * h + 4 <= ld)
+                        *reinterpret_cast<float4*>(trow + 8) = make_float4(v[4], v[5], v[6], v[7]);
                 }
             } else if (mine) {
                 float* xr = a.extra + (tile + g) * C;
@@ -678,7 +681,9 @@ int launch_dense_pair_umma(const uint8_t* M, long long Ge, int Gs, const float* 
     *launched = false;
     const bool schur = sch.sums != nullptr;
     if (Ge <= 0 || Gs <= 0 || Gs > 64 || C <= 0 || C > UCP || ld < C || ld % 4 != 0) return 0;
-    if (!aligned16(M) || !aligned16(ps) || (pe && !aligned16(pe)) || (schur && !aligned16(sch.sums))) return 0;
+    if (!aligned16(M) || !aligned16(ps) || (pe && !aligned16(pe)) ||
+        (schur && (!aligned16(sch.sums) || !aligned16(sch.table))))
+        return 0;
     if (!schur && partials && !pe) return 0;
     UmmaArgs a{};
     a.M = M;

@@ -564,6 +564,10 @@ def roofline_of(results, workload, elements_per_sweep=None):
     return {"bound": "hbm", "kernel": FAMILIES[top], "achieved": achieved, "peak": peak, "peak_source": peak_kind,
             "fp64_pipe": fp64,
             "unit": "GB/s", "frac": achieved / peak if peak else None, "traffic": traffic,
+            # the captured DRAM bytes per launch over this run's average launch time
+            "traffic_gbs": (traffic / (secs[top] / max(1, nlaunch[top])) / 1e9) if traffic and secs[top] else None,
+            "traffic_frac": (traffic / (secs[top] / max(1, nlaunch[top])) / 1e9 / peak)
+                            if traffic and secs[top] and peak else None,
             "traffic_source": ("ncu dram__bytes_read.sum + dram__bytes_write.sum per launch, " +
                                TRAFFIC_SOURCE[(workload, FAMILIES[top])]) if traffic is not None else None,
             "alg_bytes_definition": ALG_BYTES["segment" if top < 4 else ("cg" if top < 6 else "dense")],

@@ -105,6 +105,40 @@ __device__ inline void chol_solve_inv_block(int k, const double* __restrict__ Q,
     }
 }
 
+// One block: whether the symmetric k x k matrix A (upper triangle read) has an
+// upper Cholesky factor with positive pivots, i.e. is positive definite; the
+// factor is formed in U (k^2 doubles). The answer is the same on every thread.
+__device__ inline bool block_cholesky_ok(int k, const double* __restrict__ A, double* __restrict__ U) {
+    __shared__ int s_fail;
+    __shared__ double s_d;
+    const int t = threadIdx.x;
+    for (int e = t; e < k * k; e += DN_THREADS) U[e] = A[e];
+    if (t == 0) s_fail = 0;
+    __syncthreads();
+    for (int j = 0; j < k; ++j) {
+        for (int c = j + t; c < k; c += DN_THREADS) {
+            double v = U[j + c * k];
+            for (int p = 0; p < j; ++p) v -= U[p + j * k] * U[p + c * k];
+            U[j + c * k] = v;
+        }
+        __syncthreads();
+        if (t == 0) {
+            const double d = U[j + j * k];
+            if (!(d > 0.0))
+                s_fail = 1;
+            else
+                s_d = sqrt(d);
+        }
+        __syncthreads();
+        if (s_fail) break;
+        for (int c = j + 1 + t; c < k; c += DN_THREADS) U[j + c * k] /= s_d;
+        __syncthreads();
+    }
+    const bool ok = s_fail == 0;
+    __syncthreads();
+    return ok;
+}
+
 // Parallel cyclic Jacobi on a k x k symmetric matrix A (in place; global
 // memory), eigenvectors accumulated in V; the round-robin pairing makes all
 // rotations of one round touch disjoint rows/columns.
@@ -237,6 +271,15 @@ __device__ inline void finalize_cov_block(int k, double* __restrict__ acc, doubl
     __syncthreads();
     for (int e = t; e < k * k; e += DN_THREADS) A[e] = acc[e];
     __syncthreads();
+    // A positive definite matrix has no negative eigenvalue to clamp, and its
+    // reconstruction V diag(lambda) V' is the matrix itself up to rounding:
+    // the eigensolver (about 24 ms at k = 90) runs only when the Cholesky
+    // factorisation fails
+    if (block_cholesky_ok(k, A, V)) {
+        for (int i = t; i < k; i += DN_THREADS) se[i] = sqrt(fmax(0.0, acc[i + i * k]));
+        if (t == 0) *psd_applied = 0;
+        return;
+    }
     block_jacobi(k, A, V);
     __syncthreads();
     // lambda_j = A[j,j]; scale eigenvector columns by sqrt(max(lambda,0))

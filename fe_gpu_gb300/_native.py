@@ -210,6 +210,7 @@ SIGNATURES = {
     "fegb_pool_usage": (_I, [_I, C.POINTER(C.c_ulonglong), C.POINTER(C.c_ulonglong), C.POINTER(C.c_ulonglong)]),
     "fegb_test_dense_pair": (_I, [_P, _LL, _I, _P, _P, _I, _I, _P, _P, _I, _I, _P, _P, _P]),
     "fegb_test_group_sums": (_I, [_P, _LL, _I, _P, _I, _I, _P]),
+    "fegb_test_gram": (_I, [_P, _LL, _I, _I, _P]),
     "fegb_reconstruct_fe": (_I, [C.POINTER(FegbConfig), _LL, _I, _I, _P, _P, _DP, C.POINTER(C.c_void_p), _IP, _DP,
                                  C.POINTER(C.c_longlong), _IP, _DP]),
     "fegb_load_bin": (_I, [C.c_char_p, C.POINTER(FegbDataset)]),

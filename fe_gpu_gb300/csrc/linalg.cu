@@ -432,6 +432,91 @@ __global__ void __launch_bounds__(CP_THREADS) crossprod_split_kernel(DSParams p)
     }
 }
 
+// Wide Gram products (more than DS_ROWS_MAX_A columns): thread q of the grid's
+// y range owns the 4 x 4 block (bi, bj), bi <= bj, of output entries
+// (4 bi + ii, 4 bj + jj), so per tile row it reads 4 + 4 split values from
+// shared memory (two 32-byte runs) for 16 double-single products, four
+// times fewer shared-memory reads per product than one pair per thread, whose
+// kernel the wide Grams saturated shared memory with. Columns past a are zero
+// in the tile; entries with i > j or past a are not written. Sums per tile in
+// double-single, folded into FP64 per tile, one partial per row block.
+constexpr int DSB_TR = 64;  // rows per tile
+
+__device__ __forceinline__ void pair_block(int q, int& bi, int& bj) {
+    int jj = (int)((sqrt(8.0 * (double)q + 1.0) - 1.0) * 0.5);
+    while ((jj + 1) * (jj + 2) / 2 <= q) ++jj;
+    while (jj * (jj + 1) / 2 > q) --jj;
+    bj = jj;
+    bi = q - jj * (jj + 1) / 2;
+}
+
+__global__ void __launch_bounds__(CP_THREADS)
+    crossprod_split_blocked_kernel(const double* __restrict__ A, long long rs, long long cs, int a, long long n,
+                                   long long rows_per_block, double* __restrict__ partials, int* __restrict__ bad) {
+    extern __shared__ float4 dsb[];
+    const int a4 = (a + 3) / 4 * 4;
+    float2* tile = reinterpret_cast<float2*>(dsb);  // [DSB_TR][a4]
+    const int nbk = a4 / 4;
+    const int nbp = nbk * (nbk + 1) / 2;
+    const int q = blockIdx.y * CP_THREADS + threadIdx.x;
+    const bool active = q < nbp;
+    int bi = 0, bj = 0;
+    if (active) pair_block(q, bi, bj);
+    double acc[16];
+#pragma unroll
+    for (int e = 0; e < 16; ++e) acc[e] = 0.0;
+    bool oor = false;
+    const long long r0 = (long long)blockIdx.x * rows_per_block;
+    const long long r1 = min(n, r0 + rows_per_block);
+    for (long long t0 = r0; t0 < r1; t0 += DSB_TR) {
+        const int rows = (int)min((long long)DSB_TR, r1 - t0);
+        for (int e = threadIdx.x; e < DSB_TR * a4; e += CP_THREADS) {
+            int r, c;
+            if (rs == 1) {  // column-major source: consecutive threads walk rows
+                r = e % DSB_TR;
+                c = e / DSB_TR;
+            } else {
+                r = e / a4;
+                c = e - r * a4;
+            }
+            tile[r * a4 + c] = (r < rows && c < a) ? split_bits(A[(t0 + r) * rs + (long long)c * cs], oor)
+                                                   : make_float2(0.f, 0.f);
+        }
+        __syncthreads();
+        if (active) {
+            float sh[16], sl[16];
+#pragma unroll
+            for (int e = 0; e < 16; ++e) sh[e] = sl[e] = 0.f;
+            const float4* row = reinterpret_cast<const float4*>(tile);
+            for (int r = 0; r < rows; ++r) {
+                const float4 i01 = row[(r * a4 + 4 * bi) / 2], i23 = row[(r * a4 + 4 * bi) / 2 + 1];
+                const float4 j01 = row[(r * a4 + 4 * bj) / 2], j23 = row[(r * a4 + 4 * bj) / 2 + 1];
+                const float2 xi[4] = {make_float2(i01.x, i01.y), make_float2(i01.z, i01.w), make_float2(i23.x, i23.y),
+                                      make_float2(i23.z, i23.w)};
+                const float2 xj[4] = {make_float2(j01.x, j01.y), make_float2(j01.z, j01.w), make_float2(j23.x, j23.y),
+                                      make_float2(j23.z, j23.w)};
+#pragma unroll
+                for (int ii = 0; ii < 4; ++ii)
+#pragma unroll
+                    for (int jj = 0; jj < 4; ++jj) ds_fma(xi[ii], xj[jj], sh[ii * 4 + jj], sl[ii * 4 + jj]);
+            }
+#pragma unroll
+            for (int e = 0; e < 16; ++e) acc[e] += (double)sh[e] + (double)sl[e];
+        }
+        __syncthreads();
+    }
+    if (__any_sync(0xffffffffu, oor) && (threadIdx.x & 31) == 0) atomicOr(bad, 1);
+    if (!active) return;
+    const long long np = (long long)a * (a + 1) / 2;
+#pragma unroll
+    for (int ii = 0; ii < 4; ++ii)
+#pragma unroll
+        for (int jj = 0; jj < 4; ++jj) {
+            const int i = 4 * bi + ii, j = 4 * bj + jj;
+            if (i <= j && j < a) partials[(long long)blockIdx.x * np + (long long)j * (j + 1) / 2 + i] = acc[ii * 4 + jj];
+        }
+}
+
 // Thin Gram products (A <= DS_ROWS_MAX_A columns): each row is handled by
 // SPLIT threads (one per warp of a warp group), thread part q holding the
 // pairs [q NPP, (q + 1) NPP) in registers as double-single sums; each thread
@@ -441,6 +526,7 @@ __global__ void __launch_bounds__(CP_THREADS) crossprod_split_kernel(DSParams p)
 constexpr int DS_ROWS_GROUPS = 2;        // row groups (of 32 rows) per block
 constexpr int DS_ROWS_PER_THREAD = 64;
 constexpr int DS_ROWS_MAX_A = 10;
+constexpr int DSB_MAX_A = 384;  // widest Gram of the blocked kernel (its 64-row tile: 196 KB of shared memory)
 
 __host__ __device__ constexpr int ds_rows_split(int A) { return A * (A + 1) / 2 <= 16 ? 1 : (A * (A + 1) / 2 + 15) / 16; }
 
@@ -566,6 +652,32 @@ int crossprod_split(const MatView& A, const MatView& B, long long n, bool gram, 
         FEGB_TRY(split_rows_dispatch(a, A.ptr, A.rs, n, partials, bad, (int)nb, s));
         crossprod_reduce_kernel<<<reduce_blocks(total_pairs), 256, 0, s>>>(
             partials, (int)nb, (int)total_pairs, 0, 1, upper_only, a, alpha, beta, out, ldo);
+        FEGB_LAUNCH_CHECK("split crossprod reduce");
+        int hbad = 0;
+        FEGB_CUDA(cudaMemcpyAsync(&hbad, bad, sizeof(int), cudaMemcpyDeviceToHost, s), "split flag copy");
+        FEGB_CUDA(cudaStreamSynchronize(s), "split flag sync");
+        if (hbad) return crossprod(A, B, n, gram, upper_only, alpha, beta, out, ldo, s, scr);
+        return 0;
+    }
+    if (gram && a > DS_ROWS_MAX_A && a <= DSB_MAX_A) {
+        const int a4 = (a + 3) / 4 * 4;
+        const int nbp = (a4 / 4) * (a4 / 4 + 1) / 2;
+        const int gy = (nbp + CP_THREADS - 1) / CP_THREADS;
+        const size_t bsmem = sizeof(float2) * (size_t)DSB_TR * a4;
+        static const cudaError_t battr = cudaFuncSetAttribute(
+            crossprod_split_blocked_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        if (battr != cudaSuccess) return set_cuda_error(battr, "split crossprod (blocked) attr");
+        long long nbr = std::min<long long>((n + DSB_TR - 1) / DSB_TR, std::max(1LL, (long long)num_sms() * 4 / gy));
+        long long rpb = (n + nbr - 1) / nbr;
+        rpb = ((rpb + DSB_TR - 1) / DSB_TR) * DSB_TR;
+        nbr = (n + rpb - 1) / rpb;
+        double* partials = nullptr;
+        FEGB_TRY(scr.alloc(&partials, (size_t)nbr * total_pairs, "split crossprod partials"));
+        crossprod_split_blocked_kernel<<<dim3((unsigned)nbr, (unsigned)gy), CP_THREADS, bsmem, s>>>(
+            A.ptr, A.rs, A.cs, a, n, rpb, partials, bad);
+        FEGB_LAUNCH_CHECK("split crossprod (blocked)");
+        crossprod_reduce_kernel<<<reduce_blocks(total_pairs), 256, 0, s>>>(
+            partials, (int)nbr, (int)total_pairs, 0, 1, upper_only, a, alpha, beta, out, ldo);
         FEGB_LAUNCH_CHECK("split crossprod reduce");
         int hbad = 0;
         FEGB_CUDA(cudaMemcpyAsync(&hbad, bad, sizeof(int), cudaMemcpyDeviceToHost, s), "split flag copy");

@@ -893,6 +893,23 @@ int fegb_test_dense_pair(const uint8_t* counts, long long Ge, int Gs, const floa
 
 // Self-test of the FP64 group-sum sweeps (segment and small-G forms) on host
 // data; see include/fegb.h.
+int fegb_test_gram(const double* X, long long n, int a, int split, double* out) {
+    using namespace fegb;
+    if (n <= 0 || a <= 0 || !X || !out) return set_error("fegb_test_gram: invalid sizes");
+    Scratch scr(kLegacy);
+    double *dX = nullptr, *dout = nullptr;
+    FEGB_TRY(scr.alloc(&dX, (size_t)n * a, "test data"));
+    FEGB_TRY(scr.alloc(&dout, (size_t)a * a, "test gram"));
+    FEGB_CUDA(cudaMemcpy(dX, X, sizeof(double) * n * a, cudaMemcpyHostToDevice), "test data copy");
+    MatView A{dX, (long long)a, 1, a};
+    if (split)
+        FEGB_TRY(crossprod_split(A, A, n, true, false, 1.0, 0.0, dout, a, kLegacy, scr));
+    else
+        FEGB_TRY(crossprod(A, A, n, true, false, 1.0, 0.0, dout, a, kLegacy, scr));
+    FEGB_CUDA(cudaMemcpy(out, dout, sizeof(double) * a * a, cudaMemcpyDeviceToHost), "test gram copy");
+    return set_ok();
+}
+
 int fegb_test_group_sums(const double* X, long long n, int C, const int32_t* gid, int G, int small_g,
                          double* out_sums) {
     using namespace fegb;

@@ -198,6 +198,13 @@ int fegb_test_dense_pair(const unsigned char* counts, long long Ge, int Gs, cons
  * tables). out_sums[g*C+c] = sum of X[i][c] over the rows of group g. */
 int fegb_test_group_sums(const double* X, long long n, int C, const int* gid, int G, int small_g, double* out_sums);
 
+/* Self-test of the Gram products behind the normal equations and the
+ * single-row cluster meats, on host arrays: X is n x a row-major; out (a x a,
+ * column-major, both triangles) = X'X. split = 1: the split-FP32
+ * (double-single) forms (rows kernel up to 10 columns, register-blocked
+ * kernel above); 0: the FP64 form. */
+int fegb_test_gram(const double* X, long long n, int a, int split, double* out);
+
 /* FE reconstruction of --save-fe (reconstruct_and_save_fixed_effects,
  * src/core/fe_pipeline.f90:1619-1733): forward Gauss-Seidel sweeps of the
  * residual y - W beta (beta: host, k values), dimension by dimension, each

@@ -178,12 +178,18 @@ int collect_profile(Problem& P, fegb_result* res) {
 // ----------------------------- small kernels ------------------------------
 
 // Row-major working copy X (n x C: y, then W, then Z) from the column-major
-// inputs, and back. A block moves a tile of XT_R rows x XT_C columns through
-// shared memory: it reads XT_R consecutive rows of each of its columns (1 KB
-// runs) and writes XT_C consecutive values of each row, so both sides are
-// contiguous runs whatever C is (at C = 111, 27-row tiles of every column
-// read 216-byte runs from 111 places at once and ran at 0.7 TB/s).
-constexpr int XT_R = 128, XT_C = 16;
+// inputs, and back. A block moves XT rows x all C columns through shared
+// memory (stride Cp = C rounded up to odd, so a warp reading down a column
+// does not conflict on banks): it reads XT consecutive values of each column
+// and writes (or reads) the XT rows as one contiguous run of XT x C values.
+// Whole rows per block matter: split by column tiles, every 32-byte sector of
+// a row was written by two blocks far apart in time and read back from DRAM
+// to merge the halves (25 ms at 10M x 111).
+inline int xt_rows(int C) {
+    const int cp = C | 1;
+    const int fit = (96 * 1024) / (8 * cp);
+    return fit >= 8 ? std::min(128, fit) / 8 * 8 : std::max(1, fit);
+}
 
 // column c of the (y, W, Z) inputs, each column-major with leading dimension ld
 template <typename P>
@@ -193,45 +199,39 @@ __device__ __forceinline__ P* x_column(P* y, P* W, P* Z, int k, long long ld, in
 
 __global__ void build_x_kernel(const double* __restrict__ y, const double* __restrict__ W,
                                const double* __restrict__ Z, int k, long long ld, const int32_t* __restrict__ row_of,
-                               long long n, int C, double* __restrict__ X) {
-    __shared__ double tile[XT_R][XT_C + 1];
-    const long long r0 = (long long)blockIdx.x * XT_R;
-    const int c0 = blockIdx.y * XT_C;
-    const int rows = (int)min((long long)XT_R, n - r0);
-    const int cols = min(XT_C, C - c0);
-    for (int e = threadIdx.x; e < XT_R * XT_C; e += blockDim.x) {
-        const int r = e % XT_R, cc = e / XT_R;
-        if (r < rows && cc < cols) {
-            const long long src = row_of ? (long long)row_of[r0 + r] : r0 + r;
-            tile[r][cc] = x_column(y, W, Z, k, ld, c0 + cc)[src];
-        }
+                               long long n, int C, int XT, double* __restrict__ X) {
+    extern __shared__ double tile[];
+    const int cp = C | 1;
+    const long long r0 = (long long)blockIdx.x * XT;
+    const int rows = (int)min((long long)XT, n - r0);
+    for (int e = threadIdx.x; e < rows * C; e += blockDim.x) {
+        const int r = e % rows, c = e / rows;
+        const long long src = row_of ? (long long)row_of[r0 + r] : r0 + r;
+        tile[r * cp + c] = x_column(y, W, Z, k, ld, c)[src];
     }
     __syncthreads();
-    for (int e = threadIdx.x; e < XT_R * XT_C; e += blockDim.x) {
-        const int r = e / XT_C, cc = e % XT_C;
-        if (r < rows && cc < cols) X[(r0 + r) * C + c0 + cc] = tile[r][cc];
+    for (int e = threadIdx.x; e < rows * C; e += blockDim.x) {
+        const int r = e / C, c = e - r * C;
+        X[r0 * C + e] = tile[r * cp + c];
     }
 }
 
 __global__ void scatter_x_kernel(const double* __restrict__ X, const int32_t* __restrict__ row_of, long long n, int C,
-                                 int k, long long ld, double* __restrict__ y, double* __restrict__ W,
+                                 int k, long long ld, int XT, double* __restrict__ y, double* __restrict__ W,
                                  double* __restrict__ Z) {
-    __shared__ double tile[XT_R][XT_C + 1];
-    const long long r0 = (long long)blockIdx.x * XT_R;
-    const int c0 = blockIdx.y * XT_C;
-    const int rows = (int)min((long long)XT_R, n - r0);
-    const int cols = min(XT_C, C - c0);
-    for (int e = threadIdx.x; e < XT_R * XT_C; e += blockDim.x) {
-        const int r = e / XT_C, cc = e % XT_C;
-        if (r < rows && cc < cols) tile[r][cc] = X[(r0 + r) * C + c0 + cc];
+    extern __shared__ double tile[];
+    const int cp = C | 1;
+    const long long r0 = (long long)blockIdx.x * XT;
+    const int rows = (int)min((long long)XT, n - r0);
+    for (int e = threadIdx.x; e < rows * C; e += blockDim.x) {
+        const int r = e / C, c = e - r * C;
+        tile[r * cp + c] = X[r0 * C + e];
     }
     __syncthreads();
-    for (int e = threadIdx.x; e < XT_R * XT_C; e += blockDim.x) {
-        const int r = e % XT_R, cc = e / XT_R;
-        if (r < rows && cc < cols) {
-            const long long dst = row_of ? (long long)row_of[r0 + r] : r0 + r;
-            x_column(y, W, Z, k, ld, c0 + cc)[dst] = tile[r][cc];
-        }
+    for (int e = threadIdx.x; e < rows * C; e += blockDim.x) {
+        const int r = e % rows, c = e / rows;
+        const long long dst = row_of ? (long long)row_of[r0 + r] : r0 + r;
+        x_column(y, W, Z, k, ld, c)[dst] = tile[r * cp + c];
     }
 }
 
@@ -611,8 +611,12 @@ int build_problem(Problem& P, long long n_in, int k, int l, int n_fe, const doub
             if (G[P.order[b]] < G[P.order[a]]) std::swap(P.order[a], P.order[b]);
     if (P.data_ready) FEGB_CUDA(cudaStreamWaitEvent(s, P.data_ready, 0), "data upload wait");
     if (n > 0) {
-        const dim3 grid((unsigned)((n + XT_R - 1) / XT_R), (unsigned)((C + XT_C - 1) / XT_C));
-        build_x_kernel<<<grid, 256, 0, s>>>(y, W, Z, k, n_in, row_of, n, C, P.X);
+        const int xt = xt_rows(C);
+        const size_t smem = sizeof(double) * (size_t)xt * (C | 1);
+        static const cudaError_t attr =
+            cudaFuncSetAttribute(build_x_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
+        if (attr != cudaSuccess) return set_cuda_error(attr, "build data block attr");
+        build_x_kernel<<<(unsigned)((n + xt - 1) / xt), 256, smem, s>>>(y, W, Z, k, n_in, row_of, n, C, xt, P.X);
         FEGB_LAUNCH_CHECK("build data block");
     }
     return 0;
@@ -2917,8 +2921,13 @@ int within_impl(const fegb_config& cfg, long long n, int k, int l, int n_fe, dou
         FEGB_TRY(demean_plain(P, cfg.fe_tol, cfg.fe_max_iter, &it, &conv, &mu));
     }
     if (n > 0) {
-        const dim3 grid((unsigned)((n + XT_R - 1) / XT_R), (unsigned)((P.C + XT_C - 1) / XT_C));
-        scatter_x_kernel<<<grid, 256, 0, s>>>(P.X, P.row_of, n, P.C, k, n, d_y, d_W, d_Z);
+        const int xt = xt_rows(P.C);
+        const size_t smem = sizeof(double) * (size_t)xt * (P.C | 1);
+        static const cudaError_t attr =
+            cudaFuncSetAttribute(scatter_x_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
+        if (attr != cudaSuccess) return set_cuda_error(attr, "scatter data block attr");
+        scatter_x_kernel<<<(unsigned)((n + xt - 1) / xt), 256, smem, s>>>(P.X, P.row_of, n, P.C, k, n, xt, d_y, d_W,
+                                                                          d_Z);
         FEGB_LAUNCH_CHECK("scatter data block");
     }
     FEGB_CUDA(cudaStreamSynchronize(s), "within sync");

@@ -194,6 +194,23 @@ __device__ __forceinline__ uint32_t pack2(__nv_bfloat16 a, __nv_bfloat16 b) {
     return (uint32_t)__bfloat16_as_ushort(a) | ((uint32_t)__bfloat16_as_ushort(b) << 16);
 }
 
+// the BF16 roundings of (a, b) packed as pack2 does (a in the low half), one
+// paired conversion
+__device__ __forceinline__ uint32_t bf16x2_bits(float a, float b) {
+    const __nv_bfloat162 v = __floats2bfloat162_rn(a, b);
+    return *reinterpret_cast<const uint32_t*>(&v);
+}
+
+// split3 of two values at once, the pieces already packed in pairs: the same
+// roundings, in paired conversions (the widening back to FP32 is exact)
+__device__ __forceinline__ void split3x2(float a, float b, uint32_t& h, uint32_t& m, uint32_t& l) {
+    h = bf16x2_bits(a, b);
+    const float ra = a - __uint_as_float(h << 16), rb = b - __uint_as_float(h & 0xffff0000u);
+    m = bf16x2_bits(ra, rb);
+    const float sa = ra - __uint_as_float(m << 16), sb = rb - __uint_as_float(m & 0xffff0000u);
+    l = bf16x2_bits(sa, sb);
+}
+
 struct UmmaArgs {
     const uint8_t* M;
     long long Ge;
@@ -396,7 +413,7 @@ __global__ void __launch_bounds__(BT, 4) dense_umma_kernel(UmmaArgs a) {
                 uint32_t pair = 0;
                 if (mine && t0 < Gs) pair = src[t0] | ((t0 + 1 < Gs ? (uint32_t)src[t0 + 1] : 0u) << 8);
                 const float x0 = byte_f32(pair, 0x7540u), x1 = byte_f32(pair, 0x7541u);
-                w[q] = pack2(__float2bfloat16_rn(x0), __float2bfloat16_rn(x1));
+                w[q] = bf16x2_bits(x0, x1);
             }
             *reinterpret_cast<uint4*>(sm + cnt_off + (uint32_t)(g / 8) * CORE_ROW + (uint32_t)tb * 128 +
                                       (uint32_t)(g % 8) * 16) = make_uint4(w[0], w[1], w[2], w[3]);
@@ -454,21 +471,20 @@ __global__ void __launch_bounds__(BT, 4) dense_umma_kernel(UmmaArgs a) {
             }
             convert(i + 1);
         }
+        // (b) this tile's rows and E(i), waited before the one barrier that
+        // also publishes the counts of tile i + 1 converted above
+        ok = tid != 0 || bar_wait(2 + (i & 1));
+        if (tid == 0 && ok && need_e) ok = bar_wait(4 + (i & 1));
         fence_before_sync();
-        __syncthreads();  // S1
+        if (__syncthreads_or(!ok)) {  // S1
+            failed = true;
+            break;
+        }
         fence_after_sync();
         if (tid == 0 && i + 1 < ntiles) {
             if (need_e) issue_e(i + 1);
             if (i + 3 < ntiles) issue_raw(i + 3);  // raw stage (i + 1) & 1 was just consumed
         }
-        // (b) this tile: its rows, then E(i)
-        ok = tid != 0 || bar_wait(2 + (i & 1));
-        if (tid == 0 && ok && need_e) ok = bar_wait(4 + (i & 1));
-        if (__syncthreads_or(!ok)) {
-            failed = true;
-            break;
-        }
-        fence_after_sync();
         float v[8];
 #pragma unroll
         for (int j = 0; j < 8; ++j) v[j] = 0.0f;
@@ -546,14 +562,8 @@ __global__ void __launch_bounds__(BT, 4) dense_umma_kernel(UmmaArgs a) {
                 if (hb * 8 >= C) break;
                 uint32_t w[UNP][2];
 #pragma unroll
-                for (int q = 0; q < 2; ++q) {
-                    __nv_bfloat16 h0, m0, l0, h1, m1, l1;
-                    split3(v[hb * 4 + 2 * q], h0, m0, l0);
-                    split3(v[hb * 4 + 2 * q + 1], h1, m1, l1);
-                    w[0][q] = pack2(h0, h1);
-                    w[1][q] = pack2(m0, m1);
-                    w[2][q] = pack2(l0, l1);
-                }
+                for (int q = 0; q < 2; ++q)
+                    split3x2(v[hb * 4 + 2 * q], v[hb * 4 + 2 * q + 1], w[0][q], w[1][q], w[2][q]);
 #pragma unroll
                 for (int p = 0; p < UNP; ++p) {
                     const uint32_t mb = (uint32_t)(p * 2 + hb);

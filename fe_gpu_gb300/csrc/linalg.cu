@@ -438,9 +438,12 @@ __global__ void __launch_bounds__(CP_THREADS) crossprod_split_kernel(DSParams p)
 // shared memory (two 32-byte runs) for 16 double-single products, four
 // times fewer shared-memory reads per product than one pair per thread, whose
 // kernel the wide Grams saturated shared memory with. Columns past a are zero
-// in the tile; entries with i > j or past a are not written. Sums per tile in
-// double-single, folded into FP64 per tile, one partial per row block.
-constexpr int DSB_TR = 64;  // rows per tile
+// in the tile; entries with i > j or past a are not written. The
+// double-single sums span DSB_FOLD rows (DSB_FOLD / DSB_TR tiles) and are then
+// folded into FP64 sums kept in shared memory, so that a thread holds only
+// its 32 FP32 sums in registers and three blocks fit on an SM.
+constexpr int DSB_TR = 32;    // rows per tile
+constexpr int DSB_FOLD = 128; // rows per double-single sum
 
 __device__ __forceinline__ void pair_block(int q, int& bi, int& bj) {
     int jj = (int)((sqrt(8.0 * (double)q + 1.0) - 1.0) * 0.5);
@@ -450,24 +453,28 @@ __device__ __forceinline__ void pair_block(int q, int& bi, int& bj) {
     bi = q - jj * (jj + 1) / 2;
 }
 
-__global__ void __launch_bounds__(CP_THREADS)
+__global__ void __launch_bounds__(CP_THREADS, 3)
     crossprod_split_blocked_kernel(const double* __restrict__ A, long long rs, long long cs, int a, long long n,
                                    long long rows_per_block, double* __restrict__ partials, int* __restrict__ bad) {
     extern __shared__ float4 dsb[];
     const int a4 = (a + 3) / 4 * 4;
-    float2* tile = reinterpret_cast<float2*>(dsb);  // [DSB_TR][a4]
+    double* acc = reinterpret_cast<double*>(dsb);                                  // [16][CP_THREADS]
+    float2* tile = reinterpret_cast<float2*>(acc + 16 * CP_THREADS);                // [DSB_TR][a4]
     const int nbk = a4 / 4;
     const int nbp = nbk * (nbk + 1) / 2;
     const int q = blockIdx.y * CP_THREADS + threadIdx.x;
     const bool active = q < nbp;
     int bi = 0, bj = 0;
     if (active) pair_block(q, bi, bj);
-    double acc[16];
 #pragma unroll
-    for (int e = 0; e < 16; ++e) acc[e] = 0.0;
+    for (int e = 0; e < 16; ++e) acc[e * CP_THREADS + threadIdx.x] = 0.0;
+    float sh[16], sl[16];
+#pragma unroll
+    for (int e = 0; e < 16; ++e) sh[e] = sl[e] = 0.f;
     bool oor = false;
     const long long r0 = (long long)blockIdx.x * rows_per_block;
     const long long r1 = min(n, r0 + rows_per_block);
+    int since_fold = 0;
     for (long long t0 = r0; t0 < r1; t0 += DSB_TR) {
         const int rows = (int)min((long long)DSB_TR, r1 - t0);
         for (int e = threadIdx.x; e < DSB_TR * a4; e += CP_THREADS) {
@@ -484,9 +491,6 @@ __global__ void __launch_bounds__(CP_THREADS)
         }
         __syncthreads();
         if (active) {
-            float sh[16], sl[16];
-#pragma unroll
-            for (int e = 0; e < 16; ++e) sh[e] = sl[e] = 0.f;
             const float4* row = reinterpret_cast<const float4*>(tile);
             for (int r = 0; r < rows; ++r) {
                 const float4 i01 = row[(r * a4 + 4 * bi) / 2], i23 = row[(r * a4 + 4 * bi) / 2 + 1];
@@ -500,8 +504,15 @@ __global__ void __launch_bounds__(CP_THREADS)
 #pragma unroll
                     for (int jj = 0; jj < 4; ++jj) ds_fma(xi[ii], xj[jj], sh[ii * 4 + jj], sl[ii * 4 + jj]);
             }
+            since_fold += DSB_TR;
+            if (since_fold >= DSB_FOLD || t0 + DSB_TR >= r1) {
 #pragma unroll
-            for (int e = 0; e < 16; ++e) acc[e] += (double)sh[e] + (double)sl[e];
+                for (int e = 0; e < 16; ++e) {
+                    acc[e * CP_THREADS + threadIdx.x] += (double)sh[e] + (double)sl[e];
+                    sh[e] = sl[e] = 0.f;
+                }
+                since_fold = 0;
+            }
         }
         __syncthreads();
     }
@@ -513,7 +524,9 @@ __global__ void __launch_bounds__(CP_THREADS)
 #pragma unroll
         for (int jj = 0; jj < 4; ++jj) {
             const int i = 4 * bi + ii, j = 4 * bj + jj;
-            if (i <= j && j < a) partials[(long long)blockIdx.x * np + (long long)j * (j + 1) / 2 + i] = acc[ii * 4 + jj];
+            if (i <= j && j < a)
+                partials[(long long)blockIdx.x * np + (long long)j * (j + 1) / 2 + i] =
+                    acc[(ii * 4 + jj) * CP_THREADS + threadIdx.x];
         }
 }
 
@@ -526,7 +539,7 @@ __global__ void __launch_bounds__(CP_THREADS)
 constexpr int DS_ROWS_GROUPS = 2;        // row groups (of 32 rows) per block
 constexpr int DS_ROWS_PER_THREAD = 64;
 constexpr int DS_ROWS_MAX_A = 10;
-constexpr int DSB_MAX_A = 384;  // widest Gram of the blocked kernel (its 64-row tile: 196 KB of shared memory)
+constexpr int DSB_MAX_A = 640;  // widest Gram of the blocked kernel (its 32-row tile and sums: 192 KB of shared memory)
 
 __host__ __device__ constexpr int ds_rows_split(int A) { return A * (A + 1) / 2 <= 16 ? 1 : (A * (A + 1) / 2 + 15) / 16; }
 
@@ -663,11 +676,11 @@ int crossprod_split(const MatView& A, const MatView& B, long long n, bool gram, 
         const int a4 = (a + 3) / 4 * 4;
         const int nbp = (a4 / 4) * (a4 / 4 + 1) / 2;
         const int gy = (nbp + CP_THREADS - 1) / CP_THREADS;
-        const size_t bsmem = sizeof(float2) * (size_t)DSB_TR * a4;
+        const size_t bsmem = sizeof(double) * 16 * CP_THREADS + sizeof(float2) * (size_t)DSB_TR * a4;
         static const cudaError_t battr = cudaFuncSetAttribute(
             crossprod_split_blocked_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
         if (battr != cudaSuccess) return set_cuda_error(battr, "split crossprod (blocked) attr");
-        long long nbr = std::min<long long>((n + DSB_TR - 1) / DSB_TR, std::max(1LL, (long long)num_sms() * 4 / gy));
+        long long nbr = std::min<long long>((n + DSB_TR - 1) / DSB_TR, std::max(1LL, (long long)num_sms() * 6 / gy));
         long long rpb = (n + nbr - 1) / nbr;
         rpb = ((rpb + DSB_TR - 1) / DSB_TR) * DSB_TR;
         nbr = (n + rpb - 1) / rpb;

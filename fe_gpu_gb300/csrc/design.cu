@@ -88,31 +88,70 @@ __global__ void level_distinct_kernel(const uint32_t* __restrict__ head, const u
 
 constexpr int DESIGN_COLS_PER_BLOCK = 16;
 
+// Order-preserving unsigned key of a double: -0 just below +0, NaNs beyond
+// the infinities, so an interval test on doubles becomes two integer
+// compares (no FP64 instruction, the slow pipe on this part).
+__device__ __forceinline__ unsigned long long order_key(double d) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(d);
+    return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
+}
+
+// Keys [lo, hi) of the values that round (half away from zero, as Fortran
+// nint) to the level L: [L - 0.5, L + 0.5) for L > 0, (L - 0.5, L + 0.5] for
+// L < 0, (-0.5, 0.5) for L = 0; L +- 0.5 are exact doubles.
+__device__ __forceinline__ void level_interval(int L, unsigned long long& lo, unsigned long long& hi) {
+    const unsigned long long kl = order_key((double)L - 0.5), kh = order_key((double)L + 0.5);
+    lo = L > 0 ? kl : kl + 1;
+    hi = L < 0 ? kh + 1 : kh;
+}
+
+struct DesignRecipe {
+    fegb_design_column col;
+    unsigned long long lo[FEGB_DESIGN_MAX_FACTORS], hi[FEGB_DESIGN_MAX_FACTORS];
+};
+
 // out[c * ld + i] = prod_f factor_f(i) for the columns of this block's column
-// chunk; factors multiply left to right as in the reference.
+// chunk; factors multiply left to right as in the reference. A dummy factor
+// is 1.0 when the value rounds to its level: an integer interval test on the
+// value's order key. A product of dummies is 1.0 or 0.0 with no FP64
+// multiply (1 x 1, 1 x 0, 0 x 0 are exact); a continuous value still
+// multiplies in FP64, so the result keeps its bits (signed zeros, NaN).
 __global__ void __launch_bounds__(256) build_design_kernel(const double* const* __restrict__ src,
                                                            const fegb_design_column* __restrict__ cols, int n_cols,
                                                            long long n, double* __restrict__ out, long long ld) {
-    __shared__ fegb_design_column sc[DESIGN_COLS_PER_BLOCK];
+    __shared__ DesignRecipe sc[DESIGN_COLS_PER_BLOCK];
     const int c0 = blockIdx.y * DESIGN_COLS_PER_BLOCK;
     const int nc = min(DESIGN_COLS_PER_BLOCK, n_cols - c0);
-    if (threadIdx.x < nc) sc[threadIdx.x] = cols[c0 + threadIdx.x];
+    if (threadIdx.x < nc) {
+        DesignRecipe& r = sc[threadIdx.x];
+        r.col = cols[c0 + threadIdx.x];
+        for (int f = 0; f < r.col.n_factors; ++f) level_interval(r.col.factors[f].level, r.lo[f], r.hi[f]);
+    }
     __syncthreads();
     long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const long long st = (long long)gridDim.x * blockDim.x;
     for (; i < n; i += st) {
         for (int c = 0; c < nc; ++c) {
-            const fegb_design_column& col = sc[c];
+            const DesignRecipe& r = sc[c];
             double v = 0.0;
-            for (int f = 0; f < col.n_factors; ++f) {
-                const fegb_design_factor& fa = col.factors[f];
+            bool dummies = true;  // v is the product of dummy factors so far: 1.0 iff hit
+            bool hit = true;
+            for (int f = 0; f < r.col.n_factors; ++f) {
+                const fegb_design_factor& fa = r.col.factors[f];
                 const double x = __ldg(src[fa.src] + i);
-                double fv = x;
                 if (fa.is_dummy) {
-                    int r = 0;
-                    fv = (nearest_int32(x, &r) && r == fa.level) ? 1.0 : 0.0;
+                    const unsigned long long k = order_key(x);
+                    const bool in = k >= r.lo[f] && k < r.hi[f];
+                    if (dummies) {
+                        hit = hit && in;
+                        v = hit ? 1.0 : 0.0;
+                    } else {
+                        v = v * (in ? 1.0 : 0.0);
+                    }
+                } else {
+                    v = (f == 0) ? x : v * x;
+                    dummies = false;
                 }
-                v = f == 0 ? fv : v * fv;
             }
             out[(long long)(c0 + c) * ld + i] = v;
         }

@@ -176,6 +176,42 @@ __global__ void __launch_bounds__(RS_THREADS)
     }
 }
 
+// The same for wide rows (many regressors): one warp per row, lanes over the
+// columns, so that reads of X and writes of S are contiguous runs (a thread
+// per row made every load and store instruction touch 32 rows); the lanes'
+// partial products are summed by a fixed xor tree.
+__global__ void __launch_bounds__(RS_THREADS)
+    residual_scores_wide_kernel(const double* __restrict__ X, int C, long long n, const double* __restrict__ beta,
+                                int k, const int* __restrict__ score_cols, int n_score, double* __restrict__ S,
+                                double* __restrict__ resid, double* __restrict__ partials) {
+    __shared__ double red[RS_THREADS / 32];
+    const int lane = threadIdx.x & 31;
+    double local = 0.0;
+    long long i = ((long long)blockIdx.x * RS_THREADS + threadIdx.x) >> 5;
+    const long long stride = ((long long)gridDim.x * RS_THREADS) >> 5;
+    for (; i < n; i += stride) {
+        const double* row = X + i * C;
+        double dot = 0.0;
+        for (int j = lane; j < k; j += 32) dot += row[1 + j] * beta[j];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) dot += __shfl_xor_sync(0xffffffffu, dot, o);
+        const double r = row[0] - dot;
+        if (resid && lane == 0) resid[i] = r;
+        if (S)
+            for (int t = lane; t < n_score; t += 32) S[i * n_score + t] = r * row[score_cols[t]];
+        if (lane == 0) local += r * r;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) local += __shfl_xor_sync(0xffffffffu, local, o);
+    if (lane == 0) red[threadIdx.x >> 5] = local;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double v = 0.0;
+        for (int w = 0; w < RS_THREADS / 32; ++w) v += red[w];
+        partials[blockIdx.x] = v;
+    }
+}
+
 __global__ void sum_partials_kernel(const double* __restrict__ partials, int nb, double* out) {
     if (threadIdx.x == 0 && blockIdx.x == 0) {
         double v = 0.0;
@@ -757,7 +793,12 @@ int residual_scores(const double* X, int C, long long n, const double* beta, int
     int nb = (int)std::min<long long>((long long)num_sms() * 8, std::max(1LL, (n + RS_THREADS - 1) / RS_THREADS));
     double* partials = nullptr;
     FEGB_TRY(scr.alloc(&partials, (size_t)nb, "rss partials"));
-    residual_scores_kernel<<<nb, RS_THREADS, 0, s>>>(X, C, n, beta, k, score_cols_dev, n_score, S, resid, partials);
+    if (C >= 32)
+        residual_scores_wide_kernel<<<nb, RS_THREADS, 0, s>>>(X, C, n, beta, k, score_cols_dev, n_score, S, resid,
+                                                              partials);
+    else
+        residual_scores_kernel<<<nb, RS_THREADS, 0, s>>>(X, C, n, beta, k, score_cols_dev, n_score, S, resid,
+                                                         partials);
     FEGB_LAUNCH_CHECK("residual/scores");
     sum_partials_kernel<<<1, 32, 0, s>>>(partials, nb, rss_dev);
     FEGB_LAUNCH_CHECK("rss sum");

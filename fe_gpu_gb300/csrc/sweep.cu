@@ -2095,13 +2095,15 @@ int launch_cg_rows(const CGRowsParams<T>& p, cudaStream_t s) {
     return launch_cg_rows_nsrc<T, 16>(p, s);
 }
 
+constexpr int CGS_U = 4;  // positions per step of the short-group sweep
+
 // Operator sweep of a stream whose groups are all short (every group at most
 // CG_SHORT_MAX positions, on average at most CG_SHORT_MEAN): thread t takes
 // column tile t / G of group t % G, so a warp covers 32 consecutive groups and
 // their contiguous positions. The thread sums its group's positions in order
 // (run = fma(a, v, run) from zero: the first step is the rounded product a * v,
 // as in a lane of the chunked sweep) and writes the complete sum; empty groups
-// get zeros. Two positions are
+// get zeros. CGS_U positions are
 // loaded ahead so that their row gathers are in flight together.
 template <typename T, int TILE, int NSRC>
 __global__ void __launch_bounds__(256) cg_short_kernel(CGRowsParams<T> p, const int32_t* __restrict__ off, int G,
@@ -2120,41 +2122,34 @@ __global__ void __launch_bounds__(256) cg_short_kernel(CGRowsParams<T> p, const 
     T run[TILE];
 #pragma unroll
     for (int i = 0; i < TILE; ++i) run[i] = T(0);
-    int j = j0;
-    for (; j + 1 < j1; j += 2) {
-        T v0[TILE], v1[TILE];
+    // CGS_U positions a step, all their row gathers issued before the first
+    // is consumed; positions past the group's end add zero
+    for (int j = j0; j < j1; j += CGS_U) {
+        T v[CGS_U][TILE];
+        T a[CGS_U];
+        int sid[CGS_U][NSRC];
 #pragma unroll
-        for (int i = 0; i < TILE; ++i) v0[i] = v1[i] = T(0);
-        int s0[NSRC], s1[NSRC];
+        for (int u = 0; u < CGS_U; ++u) {
+            const bool ok = j + u < j1;
 #pragma unroll
-        for (int e = 0; e < NSRC; ++e) {
-            s0[e] = __ldcs(p.src_gid[e] + j);
-            s1[e] = __ldcs(p.src_gid[e] + j + 1);
-        }
-        const T a0 = p.weight ? -(T)__ldcs(p.weight + j) : T(-1);
-        const T a1 = p.weight ? -(T)__ldcs(p.weight + j + 1) : T(-1);
-        cg_add_row<T, TILE, true>(tabs[0] + (long long)s0[0] * p.ld, cw, v0, keep);
-        cg_add_row<T, TILE, true>(tabs[0] + (long long)s1[0] * p.ld, cw, v1, keep);
+            for (int i = 0; i < TILE; ++i) v[u][i] = T(0);
 #pragma unroll
-        for (int e = 1; e < NSRC; ++e) {
-            cg_add_row<T, TILE, false>(tabs[e] + (long long)s0[e] * p.ld, cw, v0, keep);
-            cg_add_row<T, TILE, false>(tabs[e] + (long long)s1[e] * p.ld, cw, v1, keep);
+            for (int e = 0; e < NSRC; ++e) sid[u][e] = ok ? __ldcs(p.src_gid[e] + j + u) : 0;
+            a[u] = ok ? (p.weight ? -(T)__ldcs(p.weight + j + u) : T(-1)) : T(0);
         }
 #pragma unroll
-        for (int i = 0; i < TILE; ++i) run[i] = fma(a0, v0[i], run[i]);
+        for (int u = 0; u < CGS_U; ++u) {
+            if (j + u < j1) {
+                cg_add_row<T, TILE, true>(tabs[0] + (long long)sid[u][0] * p.ld, cw, v[u], keep);
 #pragma unroll
-        for (int i = 0; i < TILE; ++i) run[i] = fma(a1, v1[i], run[i]);
-    }
-    if (j < j1) {
-        T v0[TILE];
+                for (int e = 1; e < NSRC; ++e)
+                    cg_add_row<T, TILE, false>(tabs[e] + (long long)sid[u][e] * p.ld, cw, v[u], keep);
+            }
+        }
 #pragma unroll
-        for (int i = 0; i < TILE; ++i) v0[i] = T(0);
+        for (int u = 0; u < CGS_U; ++u)
 #pragma unroll
-        for (int e = 0; e < NSRC; ++e)
-            cg_add_row<T, TILE, false>(tabs[e] + (long long)__ldcs(p.src_gid[e] + j) * p.ld, cw, v0, keep);
-        const T a0 = p.weight ? -(T)__ldcs(p.weight + j) : T(-1);
-#pragma unroll
-        for (int i = 0; i < TILE; ++i) run[i] = fma(a0, v0[i], run[i]);
+            for (int i = 0; i < TILE; ++i) run[i] = fma(a[u], v[u][i], run[i]);
     }
     T* dst = p.sums + (long long)g * p.C + c0;
 #pragma unroll

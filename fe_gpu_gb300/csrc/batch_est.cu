@@ -202,6 +202,98 @@ __global__ void __launch_bounds__(BE_THREADS)
     if (SPLIT && __any_sync(0xffffffffu, oor) && (t & 31) == 0) atomicOr(bad, 1);
 }
 
+// The double-single Gram in 4 x 4 output blocks: thread t takes block
+// q = t % NB (bi <= bj over the class's Cw columns padded to Cw4) and row phase
+// t / NB, so each tile row costs it 4 + 4 shared-memory reads (two 32-byte
+// runs) for 16 products instead of two reads per product. Per item the
+// blocks' sums are folded over the phases in phase order. Same items, queue
+// and partial layout as be_gram_kernel.
+template <class Acc>
+__global__ void __launch_bounds__(BE_THREADS)
+    be_gram_blocked_kernel(Acc X, const BeItem* __restrict__ items, int n_items, const int* __restrict__ width_of,
+                           int Cw, double* __restrict__ partials, int* __restrict__ queue, int* __restrict__ bad) {
+    extern __shared__ __align__(16) unsigned char be_smem[];
+    __shared__ int s_item;
+    __shared__ double s_fold[BE_THREADS][17];  // a thread's 16 sums (odd stride: no bank conflicts)
+    const int t = threadIdx.x;
+    const int Cw4 = (Cw + 3) / 4 * 4;
+    const int nbk = Cw4 / 4;
+    const int NB = nbk * (nbk + 1) / 2;
+    const int phases = BE_THREADS / NB;
+    const int q = t % NB, phase = t / NB;
+    const bool active = phase < phases;
+    int bi = 0, bj = 0;
+    {
+        int j = 0;
+        while ((j + 1) * (j + 2) / 2 <= q) ++j;
+        bj = j;
+        bi = q - j * (j + 1) / 2;
+    }
+    const int P = Cw * (Cw + 1) / 2;
+    bool oor = false;
+    float2* tile = reinterpret_cast<float2*>(be_smem);  // [TR][Cw4]
+    while (true) {
+        if (t == 0) s_item = atomicAdd(queue, 1);
+        __syncthreads();
+        const int it = s_item;
+        if (it >= n_items) break;
+        const BeItem item = items[it];
+        const int width = min(Cw, width_of[item.spec]);
+        double acc[16];
+#pragma unroll
+        for (int e = 0; e < 16; ++e) acc[e] = 0.0;
+        const int TR = be_tile_rows(Cw);
+        for (long long r0 = item.r0; r0 < item.r1; r0 += TR) {
+            const int rows = (int)min((long long)TR, item.r1 - r0);
+            __syncthreads();  // the previous tile is consumed
+            for (int e = t; e < TR * Cw4; e += BE_THREADS) {
+                const int r = e % TR, c = e / TR;  // consecutive threads walk rows of a column
+                const double v = (r < rows && c < width) ? X(r0 + r, c) : 0.0;
+                tile[r * Cw4 + c] = split_f64<56>(v, oor);
+            }
+            __syncthreads();
+            if (active) {
+                float sh[16], sl[16];
+#pragma unroll
+                for (int e = 0; e < 16; ++e) sh[e] = sl[e] = 0.f;
+                const float4* row = reinterpret_cast<const float4*>(tile);
+                for (int r = phase; r < rows; r += phases) {
+                    const float4 i01 = row[(r * Cw4 + 4 * bi) / 2], i23 = row[(r * Cw4 + 4 * bi) / 2 + 1];
+                    const float4 j01 = row[(r * Cw4 + 4 * bj) / 2], j23 = row[(r * Cw4 + 4 * bj) / 2 + 1];
+                    const float2 xi[4] = {make_float2(i01.x, i01.y), make_float2(i01.z, i01.w),
+                                          make_float2(i23.x, i23.y), make_float2(i23.z, i23.w)};
+                    const float2 xj[4] = {make_float2(j01.x, j01.y), make_float2(j01.z, j01.w),
+                                          make_float2(j23.x, j23.y), make_float2(j23.z, j23.w)};
+#pragma unroll
+                    for (int ii = 0; ii < 4; ++ii)
+#pragma unroll
+                        for (int jj = 0; jj < 4; ++jj) ds_fma(xi[ii], xj[jj], sh[ii * 4 + jj], sl[ii * 4 + jj]);
+                }
+#pragma unroll
+                for (int e = 0; e < 16; ++e) acc[e] += (double)sh[e] + (double)sl[e];
+            }
+        }
+#pragma unroll
+        for (int e = 0; e < 16; ++e) s_fold[t][e] = active ? acc[e] : 0.0;
+        __syncthreads();
+        double* out = partials + (long long)it * P;
+        for (int w = t; w < NB * 16; w += BE_THREADS) {
+            const int qq = w / 16, e = w % 16;
+            int jb = 0;
+            while ((jb + 1) * (jb + 2) / 2 <= qq) ++jb;
+            const int ib = qq - jb * (jb + 1) / 2;
+            const int i = 4 * ib + e / 4, j = 4 * jb + e % 4;
+            if (i <= j && j < Cw) {
+                double v = 0.0;
+                for (int ph = 0; ph < phases; ++ph) v += s_fold[ph * NB + qq][e];
+                out[j * (j + 1) / 2 + i] = v;
+            }
+        }
+        __syncthreads();  // s_item and s_fold are reused
+    }
+    if (__any_sync(0xffffffffu, oor) && (t & 31) == 0) atomicOr(bad, 1);
+}
+
 // out[s][p] = sum over the items of specification s (in order) of partials[item][p]
 __global__ void be_fold_kernel(const double* __restrict__ partials, const int* __restrict__ item0,
                                const int* __restrict__ item1, int P, double* __restrict__ out) {
@@ -660,7 +752,22 @@ int be_gram(Acc X, const std::vector<BeItem>& hitems, const std::vector<int>& it
         FEGB_LAUNCH_CHECK("batch gram");
         return 0;
     };
-    FEGB_TRY(launch(true, d_q));
+    if (Cw >= 16) {
+        // the blocked double-single form (16 products per 8 shared-memory reads);
+        // below 16 columns there are too few 4 x 4 blocks per row and the
+        // phases' folds cost more than the reads saved (8 columns: 25 -> 30 ms)
+        const int cw4 = (Cw + 3) / 4 * 4;
+        const size_t bsmem = sizeof(float2) * (size_t)be_tile_rows(Cw) * cw4;
+        // the tile (up to 64 KB) beside the 35 KB of static fold space
+        static const cudaError_t attr = cudaFuncSetAttribute(be_gram_blocked_kernel<Acc>,
+                                                             cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024);
+        if (attr != cudaSuccess) return set_cuda_error(attr, "batch gram (blocked) attr");
+        be_gram_blocked_kernel<Acc><<<grid, BE_THREADS, bsmem, s>>>(X, d_items, n_items, d_width, Cw, part, d_q,
+                                                                    d_bad);
+        FEGB_LAUNCH_CHECK("batch gram (blocked)");
+    } else {
+        FEGB_TRY(launch(true, d_q));
+    }
     int hbad = 0;
     FEGB_TRY(be_sync_copy(&hbad, d_bad, sizeof(int), cudaMemcpyDeviceToHost, s, "batch split flag copy"));
     if (hbad) FEGB_TRY(launch(false, d_q + 1));

@@ -204,12 +204,14 @@ int launch_cg_short(const CGRowsParams<T>& p, const int32_t* off, int G, cudaStr
 // Largest off[g + 1] - off[g] over the G groups (host result, synchronises s).
 int max_group_length(const int32_t* off, int G, int* out, cudaStream_t s);
 
-// Row stride of the CG G-space vectors: rows padded to 32-byte multiples (a
-// multiple of 16 columns above 16) so that table rows load as 256-bit vectors.
+// Row stride of the CG G-space vectors: rows padded to 32-byte multiples so
+// that table rows load as 256-bit vectors (a tile of 16 columns starts at a
+// multiple of 64 bytes, its last piece ends inside the padded row). No more
+// padding than that: every padded byte is gathered with the row (24 FP32
+// columns: 96-byte rows, not 128).
 inline int cg_row_stride(int C, int elem_bytes) {
     const int vec = 32 / elem_bytes;
-    if (C <= 16) return ((C + vec - 1) / vec) * vec;
-    return ((C + 15) / 16) * 16;
+    return ((C + vec - 1) / vec) * vec;
 }
 
 // ---- conjugate gradients on the FE normal equations (D'D a = D'e) ----

@@ -1,8 +1,8 @@
 """Parity of the CUDA estimator (through the C ABI) with the CPU oracle.
 
-Tolerances (spec parity bar, at fe-tol 1e-8 on both sides unless
-stated): coefficients 1e-6 relative, standard errors 1e-5 relative; ids,
-degrees of freedom and cluster counts exactly equal.
+Tolerances (the parity bar of the estimation path, at fe-tol 1e-8 on both
+sides unless stated): coefficients 1e-6 relative, standard errors 1e-5
+relative; ids, degrees of freedom and cluster counts exactly equal.
 """
 import numpy as np
 import pytest

@@ -402,8 +402,11 @@ def main():
     barrier()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
+    e2e_each = []
     for _ in range(args.e2e_steps):
+        t1 = time.perf_counter()
         er = fe_gpu_estimate(cfg_for(args.precision), hdr, hp, stream=stream.cuda_stream)
+        e2e_each.append(time.perf_counter() - t1)
     torch.cuda.synchronize()
     e2e_s = (time.perf_counter() - t0) / args.e2e_steps
     e2e_s = replicas.max_over_ranks(e2e_s, world, dev)
@@ -473,7 +476,9 @@ def main():
                                      "beta_rel_err": rel_errors(last.beta, fp64_res.beta),
                                      "se_rel_err": rel_errors(last.se, fp64_res.se)} if fp64_res else None),
         "e2e": {"value": world * n / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                "seconds_per_step": e2e_s},
+                "seconds_per_step": e2e_s, "seconds_each": e2e_each,
+                "last_breakdown_s": {key: er.stats[key] for key in ("time_h2d", "time_prep", "time_demean",
+                                                                     "time_regression", "time_se", "time_total")}},
         "gpu_launches": int(launches / args.steps) * args.steps,
         "bin_file": file_leg,
         "roofline": roofline,

@@ -48,6 +48,16 @@ inline int trace_level() {
 }
 inline bool trace_enabled() { return trace_level() > 0; }
 
+// FEGB_TRACE >= 2: the stream drained and the time since t0 printed at a
+// point of the preparation. The sync is taken only when tracing; it holds
+// back the work issued after it, so a traced fit overlaps less.
+inline void trace_phase(cudaStream_t s, Clock::time_point t0, const char* what) {
+    if (trace_level() < 2) return;
+    cudaStreamSynchronize(s);
+    std::fprintf(stderr, "fegb prep: %-28s %8.2f ms\n", what,
+                 1e3 * std::chrono::duration<double>(Clock::now() - t0).count());
+}
+
 constexpr int MODE_SMALLG = 2;
 constexpr int CHUNK_R = 256;
 constexpr int MAX_CLUSTER_DIMS = 3;  // src/core/fe_pipeline.f90:20
@@ -421,6 +431,7 @@ int build_problem(Problem& P, long long n_in, int k, int l, int n_fe, const doub
                   bool sorted_all = false) {
     cudaStream_t s = P.s;
     Scratch& scr = *P.scr;
+    const auto t_bp = Clock::now();
     P.k = k;
     P.l = l;
     P.C = 1 + k + l;
@@ -439,6 +450,7 @@ int build_problem(Problem& P, long long n_in, int k, int l, int n_fe, const doub
             G[d] = G_in[d];
         }
     }
+    trace_phase(s, t_bp, "id ranges");
     // rows kept (singleton removal) in original order
     const int32_t* rows = nullptr;
     long long n = n_in;
@@ -623,7 +635,9 @@ int build_problem(Problem& P, long long n_in, int k, int l, int n_fe, const doub
     for (int a = 0; a < n_fe - 1; ++a)
         for (int b = a + 1; b < n_fe; ++b)
             if (G[P.order[b]] < G[P.order[a]]) std::swap(P.order[a], P.order[b]);
+    trace_phase(s, t_bp, "id preparation");
     if (P.data_ready) FEGB_CUDA(cudaStreamWaitEvent(s, P.data_ready, 0), "data upload wait");
+    trace_phase(s, t_bp, "data upload");
     if (n > 0) {
         const int xt = xt_rows(C);
         const size_t smem = sizeof(double) * (size_t)xt * (C | 1);
@@ -659,6 +673,7 @@ int build_problem(Problem& P, long long n_in, int k, int l, int n_fe, const doub
             build_x_kernel<<<(unsigned)((n + xt - 1) / xt), 256, smem, s>>>(y, W, Z, k, n_in, row_of, n, C, xt, P.X);
             FEGB_LAUNCH_CHECK("build data block");
         }
+        trace_phase(s, t_bp, two_pass ? "data block (two passes)" : "data block (one pass)");
     }
     return 0;
 }
@@ -2824,6 +2839,7 @@ int estimate_device_impl(const fegb_config* cfg_in, long long n, int k, int l, i
         }
         FEGB_TRY(compute_tss_dev(ycol, P.n, &tss, s, scr));
     }
+    trace_phase(s, t0, "problem and tss");
     FEGB_CUDA(cudaStreamSynchronize(s), "prep sync");
     tm.prep = seconds_since(t0);
     res->n_obs_used = P.n;
@@ -3465,6 +3481,7 @@ int fegb_estimate_host(const fegb_config* cfg, long long n, int k, int l, int n_
     FEGB_TRY(scr.alloc(&dZ, nn * std::max(1, l), "Z upload"));
     FEGB_TRY(scr.alloc(&dint, nn * std::max(1, n_fe), "ids upload"));
     FEGB_TRY(scr.alloc(&dids, nn * std::max(1, n_fe), "ids"));
+    trace_phase(s, t0, "upload buffers");
     // the ids first: the preparation starts on them while y, W and Z are in flight
     cudaEvent_t data_ready = nullptr;
     Uploader up(s);
@@ -3476,6 +3493,7 @@ int fegb_estimate_host(const fegb_config* cfg, long long n, int k, int l, int n_
             deinterleave_ids_kernel<<<grid_stride_blocks(n * n_fe, 256), 256, 0, s>>>(dint, n_fe, n, dids);
             FEGB_LAUNCH_CHECK("ids deinterleave");
         }
+        trace_phase(s, t0, "ids upload (alone)");
         FEGB_TRY(up.copy(dy, y, sizeof(double) * n, "y H2D"));
         if (k > 0) FEGB_TRY(up.copy(dW, W, sizeof(double) * n * k, "W H2D"));
         if (l > 0) FEGB_TRY(up.copy(dZ, Z, sizeof(double) * n * l, "Z H2D"));

@@ -50,7 +50,7 @@ struct SegSweepParams {
     const int32_t* gseq;   // 0-based group id at each traversal position (non-decreasing)
     PendingSet<T> pend;    // gid arrays indexed by traversal position
     int writeback;         // write the pending-adjusted rows back (storage order only)
-    int no_data;           // 1: rows are not read (value = 0 - pending), used by the CG operator
+    int no_data;           // 1: rows are not read (value = 0 - pending); the fits leave it 0
     int R;                 // positions per chunk
     double* sums;          // G x C, runs complete inside one chunk
     double* head;          // nchunks x C

@@ -47,3 +47,21 @@ def test_tuning_off_leaves_knobs(built, monkeypatch, value):
     assert A.apply_for_shape(1000, 9) is None
     assert A.get_knob("cg_graph") == 0
     A.reset()
+
+
+def test_every_listed_knob_value_is_accepted_and_the_table_names_known_knobs(built):
+    """The autotuner's knob list and the library's agree: every value the
+    tuner tries is accepted, and the committed table names only known knobs."""
+    import json
+
+    A.reset()
+    for key, values in A.KNOBS.items():
+        for v in values:
+            A.set_knob(key, v)
+            assert A.get_knob(key) == v
+        A.reset()
+    table = json.loads(A.TABLE.read_text())
+    for e in table["entries"]:
+        for key in e.get("best", {}):
+            assert key in A.KNOBS, key
+            A.get_knob(key)  # known to the library as well
